@@ -1,0 +1,210 @@
+"""Python front end of the C ABI, mirroring the reference's module interface.
+
+``Discharge`` owns one fs_ctx and exposes the reference's subroutines under
+their own names: ``ptcl_step`` (ptcl_lib.F90:32-97), ``lapl_solve``
+(lapl_lib.F90:57-121), ``accept``/``reject`` (main.F90:83-121) and ``step``,
+one iteration of the main.F90:68-121 loop.  State crosses the boundary as the
+reference's Fortran-ordered arrays (nx+2, ny+2[, 3]).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_NAME = "libfluidsim_gb300.so"
+_lib = None
+
+
+class FluidsimError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (abi.ERROR_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+def lib_path():
+    return os.path.join(_HERE, LIB_NAME)
+
+
+def load_library():
+    """Load the in-tree CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not os.path.exists(p):
+        raise FluidsimError(abi.FS_ERR_NO_DEVICE,
+                            "%s not built; run __graft_entry__.build() first" % p)
+    lib = C.CDLL(p)
+    abi.declare_api(lib, "fs_")
+    lib.fs_create.argtypes = [C.POINTER(abi.FsConfig), C.POINTER(abi.FsMesh),
+                              C.POINTER(C.c_void_p)]
+    lib.fs_create.restype = C.c_int
+    lib.fs_abi_version.restype = C.c_int32
+    lib.fs_max_ne.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.fs_max_ne.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def constants(cfg, lib=None, prefix="fs_"):
+    lib = lib or load_library()
+    out = abi.FsConstants()
+    c = cfg.c_struct()
+    rc = getattr(lib, prefix + "get_constants")(C.byref(c), C.byref(out))
+    if rc:
+        raise FluidsimError(rc, "get_constants failed")
+    return out.as_dict()
+
+
+def coefficient_table(cfg, lib=None, prefix="fs_"):
+    lib = lib or load_library()
+    out = np.zeros(8 * cfg.table_n)
+    c = cfg.c_struct()
+    rc = getattr(lib, prefix + "build_table")(C.byref(c), abi.dptr(out))
+    if rc:
+        raise FluidsimError(rc, "build_table failed")
+    return out.reshape(8, cfg.table_n)
+
+
+class Handle:
+    """One simulation context behind an fs_* style C interface."""
+
+    prefix = "fs_"
+
+    def __init__(self, lib, ctx, cfg, mesh):
+        self._lib = lib
+        self.ctx = ctx
+        self.cfg = cfg
+        self.mesh = mesh
+        self.nx, self.ny = cfg.nx, cfg.ny
+        self.dt = cfg.dt0
+        self.t = 0.0
+        self.ts = 0
+
+    def _f(self, name):
+        return getattr(self._lib, self.prefix + name)
+
+    def last_error(self):
+        m = self._f("last_error")(self.ctx)
+        return m.decode() if m else ""
+
+    def check(self, rc):
+        if rc != abi.FS_OK:
+            raise FluidsimError(rc, self.last_error())
+
+    def close(self):
+        if self.ctx:
+            self._f("destroy")(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ---------------------------------------------------------------
+    def set_time(self, t, dt):
+        self.t, self.dt = float(t), float(dt)
+        self.check(self._f("set_time")(self.ctx, self.t, self.dt))
+
+    def upload(self, state):
+        """state: dict with ni, ne, nt[, nm], ph as (nx+2, ny+2) or (nx+2, ny+2, 3)."""
+        ni = np.asfortranarray(state["ni"], dtype=np.float64)
+        nlev = 3 if ni.ndim == 3 else 1
+        arrs = [np.asfortranarray(state[k], dtype=np.float64) if state.get(k) is not None else None
+                for k in ("ni", "ne", "nt", "nm", "ph")]
+        self._keep = arrs
+        self.check(self._f("upload_state")(self.ctx, *[abi.dptr(a) for a in arrs],
+                                           self.nx + 2, nlev))
+
+    def download(self, nlev=1):
+        shp = (self.nx + 2, self.ny + 2) + ((3,) if nlev == 3 else ())
+        out = {k: np.zeros(shp, order="F") for k in ("ni", "ne", "nt")}
+        out["nm"] = np.zeros(shp, order="F") if self.cfg.nspecies == 4 else None
+        out["ph"] = np.zeros((self.nx + 2, self.ny + 2), order="F")
+        self.check(self._f("download_state")(
+            self.ctx, abi.dptr(out["ni"]), abi.dptr(out["ne"]), abi.dptr(out["nt"]),
+            abi.dptr(out["nm"]), abi.dptr(out["ph"]), self.nx + 2, nlev))
+        return out
+
+    # -- the reference's subroutines -----------------------------------------
+    def ptcl_step(self):
+        dt = C.c_double(self.dt)
+        tm, ida, idc = C.c_double(), C.c_double(), C.c_double()
+        att = C.c_int32()
+        self.check(self._f("ptcl_step")(self.ctx, C.byref(dt), C.byref(tm), C.byref(ida),
+                                        C.byref(idc), C.byref(att)))
+        self.dt = dt.value
+        return dict(dt=dt.value, t_m=tm.value, ida=ida.value, idc=idc.value,
+                    attempts=att.value)
+
+    def lapl_solve(self):
+        lerr, it, rr = C.c_int32(), C.c_int32(), C.c_double()
+        self.check(self._f("lapl_solve")(self.ctx, self.dt, C.byref(lerr), C.byref(it),
+                                         C.byref(rr)))
+        return dict(lerr=lerr.value, iters=it.value, relres=rr.value)
+
+    def accept(self):
+        self.check(self._f("accept")(self.ctx))
+        self.ts += 1
+        self.t += self.dt
+
+    def reject(self):
+        self.check(self._f("reject")(self.ctx))
+        self.dt = self.dt / 2.0
+
+    def step(self):
+        """One iteration of the main.F90:68-121 loop through the separate calls."""
+        info = {}
+        if self.ts > 1:
+            info.update(self.ptcl_step())
+        info.update(self.lapl_solve())
+        if info["lerr"] == 0:
+            self.accept()
+        else:
+            self.reject()
+        return info
+
+    def run(self, nsteps):
+        """nsteps main-loop iterations inside the library (fs_run)."""
+        st = abi.FsStats()
+        self.check(self._f("run")(self.ctx, int(nsteps), C.byref(st)))
+        d = st.as_dict()
+        self.t, self.dt, self.ts = d["t"], d["dt"], d["steps"]
+        return d
+
+    def stats(self):
+        st = abi.FsStats()
+        self.check(self._f("get_stats")(self.ctx, C.byref(st)))
+        return st.as_dict()
+
+
+class Discharge(Handle):
+    """A discharge simulated by the CUDA library: lapl_init + ptcl_init +
+    circ_init on construction, state in device memory until downloaded."""
+
+    prefix = "fs_"
+
+    def __init__(self, cfg, mesh=None, state=None):
+        lib = load_library()
+        mesh = mesh or cfg.mesh()
+        self._c_cfg = cfg.c_struct()
+        self._c_mesh = mesh.c_struct()
+        ctx = C.c_void_p()
+        rc = lib.fs_create(C.byref(self._c_cfg), C.byref(self._c_mesh), C.byref(ctx))
+        if rc != abi.FS_OK:
+            msg = lib.fs_last_error(None)
+            raise FluidsimError(rc, msg.decode() if msg else "fs_create failed")
+        super().__init__(lib, ctx, cfg, mesh)
+        self.set_time(0.0, cfg.dt0)
+        if state is not None:
+            self.upload(state)
+
+    def max_ne(self):
+        v = C.c_double()
+        self.check(self._lib.fs_max_ne(self.ctx, C.byref(v)))
+        return v.value

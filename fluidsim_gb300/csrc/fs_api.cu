@@ -1,0 +1,459 @@
+// fs_api.cu -- C ABI of the CUDA implementation (include/fluidsim_gpu.h):
+// context creation (lapl_init + ptcl_init + circ_init), state transfer, the
+// per-step entry points and the main-loop rotation of main.F90:83-121.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "fs_internal.h"
+
+static thread_local std::string g_err;
+
+int fs_set_error(fs_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_err = buf;
+    return code;
+}
+
+int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return FS_OK;
+    int code = (e == cudaErrorMemoryAllocation) ? FS_ERR_NOMEM : FS_ERR_CUDA;
+    return fs_set_error(c, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int fs_sync_ctrl(fs_ctx *c) {
+    cudaError_t e = cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return fs_cuda_check(c, e, "stream");
+}
+
+namespace {
+
+__global__ void k_fill(double *p, size_t n, double v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void k_set_dt(Ctrl *c, double dt) { c->dt = dt; }
+
+__global__ void k_max3(const double *a, const double *b, const double *d, int nx, int ny, int P, double *out) {
+    __shared__ double s[1024];
+    double m = -INFINITY;
+    const double *arr[3] = {a, b, d};
+    for (int l = 0; l < 3; l++)
+        for (int q = threadIdx.x; q < (nx + 2) * (ny + 2); q += blockDim.x) {
+            int gi = q % (nx + 2), gj = q / (nx + 2);
+            m = fmax(m, arr[l][(size_t)gj * P + gi]);
+        }
+    s[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+int validate(const fs_config *cfg, const fs_mesh *m) {
+    if (!cfg || !m) return fs_set_error(nullptr, FS_ERR_INVALID, "null config or mesh");
+    if (cfg->abi_version != FS_ABI_VERSION)
+        return fs_set_error(nullptr, FS_ERR_INVALID, "ABI version %d, library %d", cfg->abi_version, FS_ABI_VERSION);
+    if (cfg->nx < 3 || cfg->ny < 2)
+        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "grid must have nx >= 3 and ny >= 2 (got %d x %d)", cfg->nx, cfg->ny);
+    if ((long)cfg->nx * cfg->ny > (1L << 28))
+        return fs_set_error(nullptr, FS_ERR_INVALID, "grid too large");
+    if (cfg->nspecies != 3 && cfg->nspecies != 4) return fs_set_error(nullptr, FS_ERR_INVALID, "nspecies must be 3 or 4");
+    if (cfg->coef_mode != FS_COEF_TABLE)
+        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the tabulated coefficient mode runs on the GPU");
+    if (cfg->table_n < 2 || !(cfg->table_emax_ev > cfg->table_emin_ev) || !(cfg->table_emin_ev > 0))
+        return fs_set_error(nullptr, FS_ERR_INVALID, "bad coefficient table range");
+    if (cfg->rf != 0) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the DC source (rf = 0) is implemented");
+    if (cfg->precision != FS_PREC_FP64) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "precision mode not built");
+    if (cfg->mg_smooth < 1 || cfg->mg_smooth > 8) return fs_set_error(nullptr, FS_ERR_INVALID, "mg_smooth must be 1..8");
+    if (cfg->lapl_maxit < 1) return fs_set_error(nullptr, FS_ERR_INVALID, "lapl_maxit must be positive");
+    for (long q = 0; q < (long)cfg->nx * cfg->ny; q++) {
+        int tx = m->type_x[q], ty = m->type_y[q];
+        if (tx < -2 || tx > 2 || ty < -2 || ty > 2)
+            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "node type (%d,%d) at %ld not supported "
+                                "(dielectric walls need the surface-charge model)", tx, ty, q);
+    }
+    return FS_OK;
+}
+
+void free_ctx(fs_ctx *c) {
+    if (!c) return;
+    fs_lapl_free(c);
+    for (int s = 0; s < FS_MAX_SPECIES; s++) {
+        for (int b = 0; b < FS_NBUF; b++) cudaFree(c->sp[s].buf[b]);
+        for (int k = 0; k < 3; k++) cudaFree(c->sp[s].k[k]);
+    }
+    cudaFree(c->ph);
+    cudaFree(c->ph_mi);
+    cudaFree(c->d_part);
+    cudaFree(c->d_rows);
+    cudaFree(c->d_ctrl);
+    cudaFree(c->d_mesh_blob);
+    cudaFree(c->d_types);
+    cudaFree(c->d_tab);
+    if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int set_dt_dev(fs_ctx *c, double dt) {
+    c->dt = dt;
+    k_set_dt<<<1, 1, 0, c->stream>>>(c->d_ctrl, dt);
+    return fs_cuda_check(c, cudaGetLastError(), "set dt");
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fs_abi_version(void) { return FS_ABI_VERSION; }
+
+int fs_get_constants(const fs_config *cfg, fs_constants *out) {
+    if (!cfg || !out) return FS_ERR_INVALID;
+    fs_host_constants(*cfg, *out);
+    return FS_OK;
+}
+
+int fs_build_table(const fs_config *cfg, double *out) {
+    if (!cfg || !out || cfg->table_n < 2) return FS_ERR_INVALID;
+    fs_constants k;
+    fs_host_constants(*cfg, k);
+    std::vector<double> rows;
+    fs_host_table(*cfg, k, rows);
+    memcpy(out, rows.data(), rows.size() * sizeof(double));
+    return FS_OK;
+}
+
+const char *fs_last_error(const fs_ctx *c) { return c ? c->err.c_str() : g_err.c_str(); }
+
+int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
+    if (!out) return fs_set_error(nullptr, FS_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    int rc = validate(cfg, m);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fs_set_error(nullptr, FS_ERR_NO_DEVICE, "no CUDA device");
+    fs_ctx *c = new fs_ctx();
+    memset(&c->st, 0, sizeof(c->st));
+    c->cfg = *cfg;
+    c->nx = cfg->nx;
+    c->ny = cfg->ny;
+    c->pitch = ((cfg->nx + 2 + 31) / 32) * 32;
+    c->field_elems = (size_t)(cfg->ny + 2) * c->pitch;
+    cudaGetDevice(&c->device);
+    fs_host_constants(*cfg, c->k);
+    const fs_constants &k = c->k;
+    const int nx = c->nx, ny = c->ny;
+#define CK(call, what)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) {                            \
+            rc = fs_cuda_check(nullptr, e_, what);          \
+            free_ctx(c);                                    \
+            return rc;                                      \
+        }                                                   \
+    } while (0)
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+
+    // physics parameters
+    PhysParams &pp = c->pp;
+    memset(&pp, 0, sizeof(pp));
+    pp.nx = nx; pp.ny = ny; pp.pitch = c->pitch; pp.nspecies = cfg->nspecies; pp.cyl = cfg->cyl;
+    pp.ntab = cfg->table_n;
+    pp.ph0 = k.ph0; pp.e = k.e; pp.pi = k.pi; pp.me = k.me; pp.t0 = k.t0; pp.x0 = k.x0;
+    pp.mui = k.mui; pp.Di = k.Di; pp.vi = k.vi; pp.Dm = k.Dm; pp.gam = k.gam; pp.ninf = k.ninf;
+    pp.tg = k.tg; pp.kb = k.kb; pp.mi = k.mi;
+    pp.h_ir = k.h_ir; pp.h_ex = k.h_ex; pp.h_si = k.h_si;
+    pp.k_mp = k.k_mp; pp.k_r = k.k_r; pp.k_2q = k.k_2q; pp.k_3q = k.k_3q;
+    pp.nmin[0] = k.n_zero; pp.nmin[1] = k.n_zero; pp.nmin[2] = k.nmin_nt; pp.nmin[3] = k.n_zero;
+    pp.abs_tol = cfg->abs_tol; pp.rel_tol = cfg->rel_tol;
+    pp.lemin = std::log(cfg->table_emin_ev);
+    pp.inv_h = (double)(cfg->table_n - 1) / (std::log(cfg->table_emax_ev) - pp.lemin);
+    pp.ve_coef = (16.0 * k.e * k.ph0) / (3.0 * k.pi * k.me);
+    pp.tg_term = k.tg * k.kb / k.e / k.ph0;
+    pp.e100 = std::exp(-100.0);
+
+    // mesh blob: dx, inv_dx (nx+1), dy, inv_dy (ny+1), dlx, inv_dlx (nx), dly, inv_dly (ny),
+    // r (ny+2), dr_a, dr_c (ny+2)
+    std::vector<double> blob;
+    auto push = [&](const double *p, int n) { size_t o = blob.size(); blob.insert(blob.end(), p, p + n); return o; };
+    std::vector<double> inv_dx(nx + 1), inv_dy(ny + 1), inv_dlx(nx), inv_dly(ny);
+    for (int i = 0; i <= nx; i++) inv_dx[i] = 1.0 / m->dx[i];
+    for (int j = 0; j <= ny; j++) inv_dy[j] = 1.0 / m->dy[j];
+    for (int i = 0; i < nx; i++) inv_dlx[i] = 1.0 / m->dlx[i];
+    for (int j = 0; j < ny; j++) inv_dly[j] = 1.0 / m->dly[j];
+    // circ_step current weights per row (circ_lib.F90:87-151)
+    c->h_dr_a.assign(ny + 2, 0.0);
+    c->h_dr_c.assign(ny + 2, 0.0);
+    for (int gj = 1; gj <= ny; gj++) {
+        double dr = cfg->cyl ? m->dy[gj - 1] * m->r[gj - 1] * 2.0 * k.pi : m->dy[gj - 1] * cfg->w;
+        if (m->r[gj] < cfg->ew) dr = 0.0;
+        if (m->type_x[(size_t)(gj - 1) * nx + 0] == -2) c->h_dr_a[gj] = dr;
+        if (m->type_x[(size_t)(gj - 1) * nx + nx - 1] == 2) c->h_dr_c[gj] = dr;
+    }
+    size_t o_dx = push(m->dx, nx + 1), o_idx = push(inv_dx.data(), nx + 1);
+    size_t o_dy = push(m->dy, ny + 1), o_idy = push(inv_dy.data(), ny + 1);
+    size_t o_dlx = push(m->dlx, nx), o_idlx = push(inv_dlx.data(), nx);
+    size_t o_dly = push(m->dly, ny), o_idly = push(inv_dly.data(), ny);
+    size_t o_r = push(m->r, ny + 2), o_dra = push(c->h_dr_a.data(), ny + 2), o_drc = push(c->h_dr_c.data(), ny + 2);
+    CK(cudaMalloc(&c->d_mesh_blob, blob.size() * sizeof(double)), "cudaMalloc mesh");
+    CK(cudaMemcpy(c->d_mesh_blob, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice), "mesh upload");
+    std::vector<int8_t> types((size_t)2 * nx * ny);
+    for (size_t q = 0; q < (size_t)nx * ny; q++) {
+        types[q] = (int8_t)m->type_x[q];
+        types[(size_t)nx * ny + q] = (int8_t)m->type_y[q];
+    }
+    CK(cudaMalloc(&c->d_types, types.size()), "cudaMalloc types");
+    CK(cudaMemcpy(c->d_types, types.data(), types.size(), cudaMemcpyHostToDevice), "types upload");
+    MeshDev &md = c->mesh;
+    double *B = c->d_mesh_blob;
+    md.dx = B + o_dx; md.inv_dx = B + o_idx; md.dy = B + o_dy; md.inv_dy = B + o_idy;
+    md.dlx = B + o_dlx; md.inv_dlx = B + o_idlx; md.dly = B + o_dly; md.inv_dly = B + o_idly;
+    md.r = B + o_r; md.dr_a = B + o_dra; md.dr_c = B + o_drc;
+    md.tx = c->d_types;
+    md.ty = c->d_types + (size_t)nx * ny;
+
+    // coefficient table, node-major: 8 values then 8 slopes f(k+1)-f(k)
+    {
+        std::vector<double> rows;
+        fs_host_table(*cfg, k, rows);
+        const int n = cfg->table_n;
+        std::vector<double> t((size_t)n * FS_TAB_STRIDE, 0.0);
+        for (int i = 0; i < n; i++)
+            for (int r = 0; r < 8; r++) {
+                t[(size_t)i * FS_TAB_STRIDE + r] = rows[(size_t)r * n + i];
+                t[(size_t)i * FS_TAB_STRIDE + 8 + r] = i + 1 < n ? rows[(size_t)r * n + i + 1] - rows[(size_t)r * n + i] : 0.0;
+            }
+        CK(cudaMalloc(&c->d_tab, t.size() * sizeof(double)), "cudaMalloc table");
+        CK(cudaMemcpy(c->d_tab, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice), "table upload");
+    }
+
+    // fields, ptcl_init (ptcl_lib.F90:22-29) and lapl_init (lapl_lib.F90:27-28)
+    const size_t n = c->field_elems;
+    const double nt0 = cfg->n_init * k.tg * k.kb / k.e / k.ph0;
+    for (int s = 0; s < cfg->nspecies; s++) {
+        double v0 = s == 2 ? nt0 : cfg->n_init;
+        for (int b = 0; b < FS_NBUF; b++) {
+            CK(cudaMalloc(&c->sp[s].buf[b], n * sizeof(double)), "cudaMalloc species");
+            k_fill<<<256, 256, 0, c->stream>>>(c->sp[s].buf[b], n, v0);
+        }
+        for (int q = 0; q < 3; q++) {
+            CK(cudaMalloc(&c->sp[s].k[q], n * sizeof(double)), "cudaMalloc k");
+            CK(cudaMemsetAsync(c->sp[s].k[q], 0, n * sizeof(double), c->stream), "memset k");
+        }
+    }
+    c->lev[0] = c->lev[1] = c->lev[2] = 0;
+    CK(cudaMalloc(&c->ph, n * sizeof(double)), "cudaMalloc ph");
+    CK(cudaMalloc(&c->ph_mi, n * sizeof(double)), "cudaMalloc ph_mi");
+    CK(cudaMemsetAsync(c->ph, 0, n * sizeof(double), c->stream), "memset ph");
+    CK(cudaMemsetAsync(c->ph_mi, 0, n * sizeof(double), c->stream), "memset ph_mi");
+    CK(cudaMalloc(&c->d_ctrl, sizeof(Ctrl)), "cudaMalloc ctrl");
+    CK(cudaMallocHost(&c->h_ctrl, sizeof(Ctrl)), "cudaMallocHost ctrl");
+    memset(c->h_ctrl, 0, sizeof(Ctrl));
+    c->h_ctrl->err_prev = 1.0;
+    c->h_ctrl->t_m = 1e9;
+    CK(cudaMemcpyAsync(c->d_ctrl, c->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream), "ctrl init");
+    if ((rc = fs_ptcl_alloc(c)) || (rc = fs_lapl_alloc(c))) {
+        g_err = c->err;
+        free_ctx(c);
+        return rc;
+    }
+    // circ_init (circ_lib.F90:213-223)
+    c->Vmax = c->Vsrc = c->Vd_pl = c->Vd_mi = c->Vd_or = cfg->vl;
+    c->t = 0.0;
+    c->dt = 0.0;
+    c->ts = 0;
+    CK(cudaStreamSynchronize(c->stream), "create");
+#undef CK
+    *out = c;
+    return FS_OK;
+}
+
+void fs_destroy(fs_ctx *c) {
+    if (!c) return;
+    cudaStreamSynchronize(c->stream);
+    free_ctx(c);
+}
+
+int fs_set_time(fs_ctx *c, double t, double dt) {
+    if (!c) return FS_ERR_INVALID;
+    c->t = t;
+    return set_dt_dev(c, dt);
+}
+
+int fs_upload_state(fs_ctx *c, const double *ni, const double *ne, const double *nt, const double *nm,
+                    const double *ph, int32_t ld, int32_t nlev) {
+    if (!c) return FS_ERR_INVALID;
+    if (ld < c->nx + 2 || (nlev != 1 && nlev != 3))
+        return fs_set_error(c, FS_ERR_INVALID, "upload: ld %d < nx+2 or nlev %d not 1/3", ld, nlev);
+    const double *src[FS_MAX_SPECIES] = {ni, ne, nt, nm};
+    const size_t w = (size_t)(c->nx + 2) * sizeof(double), hp = (size_t)ld * sizeof(double),
+                 dp = (size_t)c->pitch * sizeof(double);
+    const int rows = c->ny + 2;
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < c->cfg.nspecies && e == cudaSuccess; s++) {
+        if (!src[s]) continue;
+        for (int l = 0; l < nlev && e == cudaSuccess; l++)
+            e = cudaMemcpy2DAsync(c->sp[s].buf[l], dp, src[s] + (size_t)l * ld * rows, hp, w, rows,
+                                  cudaMemcpyHostToDevice, c->stream);
+        // the remaining buffers start as copies of level 1, ghost ring included
+        for (int b = nlev; b < FS_NBUF && e == cudaSuccess; b++)
+            e = cudaMemcpyAsync(c->sp[s].buf[b], c->sp[s].buf[0], c->field_elems * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream);
+    }
+    if (e == cudaSuccess) {
+        if (nlev == 1) { c->lev[0] = c->lev[1] = c->lev[2] = 0; }
+        else { c->lev[0] = 0; c->lev[1] = 1; c->lev[2] = 2; }
+    }
+    if (ph && e == cudaSuccess) {
+        e = cudaMemcpy2DAsync(c->ph, dp, ph, hp, w, rows, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->ph_mi, c->ph, c->field_elems * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "upload_state");
+}
+
+int fs_download_state(fs_ctx *c, double *ni, double *ne, double *nt, double *nm, double *ph,
+                      int32_t ld, int32_t nlev) {
+    if (!c) return FS_ERR_INVALID;
+    if (ld < c->nx + 2 || (nlev != 1 && nlev != 3))
+        return fs_set_error(c, FS_ERR_INVALID, "download: ld %d < nx+2 or nlev %d not 1/3", ld, nlev);
+    double *dst[FS_MAX_SPECIES] = {ni, ne, nt, nm};
+    const size_t w = (size_t)(c->nx + 2) * sizeof(double), hp = (size_t)ld * sizeof(double),
+                 dp = (size_t)c->pitch * sizeof(double);
+    const int rows = c->ny + 2;
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < c->cfg.nspecies && e == cudaSuccess; s++) {
+        if (!dst[s]) continue;
+        for (int l = 0; l < nlev && e == cudaSuccess; l++)
+            e = cudaMemcpy2DAsync(dst[s] + (size_t)l * ld * rows, hp, c->sp[s].buf[c->lev[l]], dp, w, rows,
+                                  cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (ph && e == cudaSuccess)
+        e = cudaMemcpy2DAsync(ph, hp, c->ph, dp, w, rows, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "download_state");
+}
+
+int fs_ptcl_step(fs_ctx *c, double *dt_inout, double *t_m_out, double *ida_out, double *idc_out,
+                 int32_t *attempts_out) {
+    if (!c) return FS_ERR_INVALID;
+    int rc;
+    if (dt_inout && (rc = set_dt_dev(c, *dt_inout))) return rc;
+    int attempts = 0;
+    rc = fs_ptcl_step_impl(c, &attempts);
+    if (dt_inout) *dt_inout = c->h_ctrl->dt;
+    if (t_m_out) *t_m_out = c->h_ctrl->t_m;
+    if (ida_out) *ida_out = c->h_ctrl->ida;
+    if (idc_out) *idc_out = c->h_ctrl->idc;
+    if (attempts_out) *attempts_out = attempts;
+    return rc;
+}
+
+int fs_lapl_solve(fs_ctx *c, double dt, int32_t *lerr_out, int32_t *iters_out, double *relres_out) {
+    if (!c) return FS_ERR_INVALID;
+    int rc = set_dt_dev(c, dt);
+    if (rc) return rc;
+    int lerr = 1, iters = 0;
+    double relres = 0;
+    rc = fs_lapl_solve_impl(c, &lerr, &iters, &relres);
+    c->st.lapl_iters += iters;
+    c->st.last_lapl_iters = iters;
+    c->st.lapl_relres = relres;
+    c->st.lerr = lerr;
+    if (lerr_out) *lerr_out = lerr;
+    if (iters_out) *iters_out = iters;
+    if (relres_out) *relres_out = relres;
+    return rc;
+}
+
+int fs_accept(fs_ctx *c) {
+    if (!c) return FS_ERR_INVALID;
+    c->ts++;
+    c->t = c->t + c->dt;
+    c->lev[2] = c->lev[1];   // n3 <- n2
+    c->lev[1] = c->lev[0];   // n2 <- n1
+    c->Vd_or = c->Vd_mi;
+    c->Vd_mi = c->Vd_pl;
+    return FS_OK;
+}
+
+int fs_reject(fs_ctx *c) {
+    if (!c) return FS_ERR_INVALID;
+    c->lev[0] = c->lev[2];   // n1 <- n3
+    c->lev[1] = c->lev[2];   // n2 <- n3
+    c->Vd_pl = c->Vd_or;
+    c->Vd_mi = c->Vd_or;
+    return set_dt_dev(c, c->dt / 2.0);
+}
+
+int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out) {
+    if (!c) return FS_ERR_INVALID;
+    for (int s = 0; s < nsteps; s++) {
+        int rc;
+        if (c->ts > 1) {
+            int att = 0;
+            if ((rc = fs_ptcl_step_impl(c, &att))) return rc;
+        }
+        int lerr = 1, iters = 0;
+        double relres = 0;
+        if ((rc = fs_lapl_solve_impl(c, &lerr, &iters, &relres))) return rc;
+        c->st.lapl_iters += iters;
+        c->st.last_lapl_iters = iters;
+        c->st.lapl_relres = relres;
+        c->st.lerr = lerr;
+        if (lerr == 0) fs_accept(c);
+        else {
+            c->st.lapl_rejects++;
+            if ((rc = fs_reject(c))) return rc;
+        }
+    }
+    return fs_get_stats(c, out);
+}
+
+int fs_get_stats(fs_ctx *c, fs_stats *out) {
+    if (!c) return FS_ERR_INVALID;
+    if (!out) return FS_OK;
+    c->st.t = c->t;
+    c->st.dt = c->dt;
+    c->st.t_m = c->h_ctrl->t_m;
+    c->st.ida = c->h_ctrl->ida;
+    c->st.idc = c->h_ctrl->idc;
+    c->st.err_cur = c->h_ctrl->err_cur;
+    c->st.steps = c->ts;
+    *out = c->st;
+    return FS_OK;
+}
+
+// maxval(ne) over the whole module array, every level and the ghost ring
+// included (main.F90:131).
+int fs_max_ne(fs_ctx *c, double *out) {
+    if (!c || !out) return FS_ERR_INVALID;
+    double *d;
+    cudaError_t e = cudaMallocAsync((void **)&d, sizeof(double), c->stream);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "max_ne");
+    const SpeciesBufs &b = c->sp[1];
+    k_max3<<<1, 1024, 0, c->stream>>>(b.buf[c->lev[0]], b.buf[c->lev[1]], b.buf[c->lev[2]], c->nx, c->ny,
+                                       c->pitch, d);
+    e = cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(d, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "max_ne");
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// fs_internal.h -- device layout, kernel parameters and context of the CUDA
+// implementation behind include/fluidsim_gpu.h.
+//
+// Device field layout: every 2D field is an FP64 (or FP32) array of
+// (ny+2) rows of `pitch` elements; element (gi, gj) -- 0-based, ghost ring
+// included, gi = Fortran i-1 -- lives at gj*pitch + gi.  pitch is nx+2
+// rounded up to 32 elements so rows start on 256-byte boundaries.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/fluidsim_gpu.h"
+
+#define FS_MAX_SPECIES 4
+#define FS_NBUF 5            // level/stage buffers per species
+#define FS_TAB_STRIDE 16     // doubles per table node: 8 values + 8 slopes
+#define FS_MG_MAX_LEVELS 16
+
+// status bits raised by kernels (Ctrl::status)
+#define FS_ST_NEG_DENSITY 1u
+#define FS_ST_NAN 2u
+#define FS_ST_DFDPH_NAN 4u
+#define FS_ST_BNAN 8u
+
+// Physics and mesh constants passed by value to the particle and assembly kernels.
+struct PhysParams {
+    int nx, ny, pitch, nspecies, cyl;
+    int ntab;
+    double ph0, e, pi, me, t0, x0;
+    double mui, Di, vi, Dm, gam, ninf, tg, kb, mi;
+    double h_ir, h_ex, h_si, k_mp, k_r, k_2q, k_3q;
+    double nmin[FS_MAX_SPECIES];   // floors: n_zero, n_zero, n_zero/ph0/1e2, n_zero
+    double abs_tol, rel_tol;
+    double lemin, inv_h;           // table abscissa: ln(emin), (n-1)/ln(emax/emin)
+    double ve_coef;                // (16 e ph0)/(3 pi me): ve = sqrt(ve_coef*Te)*t0/x0
+    double tg_term;                // Tg*kb/e/ph0 (ptcl_lib.F90:508)
+    double e100;                   // exp(-100): the SG exponent clamp
+};
+
+// Mesh arrays on the device (all FP64, 0-based).
+struct MeshDev {
+    const double *dx, *dy;         // nx+1, ny+1: face spacings (Fortran dx(1..nx+1))
+    const double *inv_dx, *inv_dy;
+    const double *dlx, *dly;       // nx, ny: control-volume widths of interior nodes 1..n
+    const double *inv_dlx, *inv_dly;
+    const double *r;               // ny+2
+    const int8_t *tx, *ty;         // (nx, ny) row-major by gj: tx[(gj-1)*nx + gi-1]
+    const double *dr_a, *dr_c;     // per row gj (ny+2): current weights of circ_step
+};
+
+// Device-resident control block (one per context).
+struct Ctrl {
+    double dt;            // g%dt
+    double err_prev;      // ptcl_lib.F90:11
+    double err_cur;
+    double t_m;           // running min over stage-5 cells
+    double ida, idc;
+    double scfac;
+    unsigned int status;  // FS_ST_* bits
+    int rejected;         // last attempt rejected by the error norm
+    int min_dt;           // dt fell to dt_min
+    int pad;
+    // Krylov scalars
+    double rz, rz_old, pq, alpha, beta, rnorm2, bnorm2, relres;
+    int cg_done, cg_iters, cg_fail, pad2;
+    unsigned int counter[8];   // last-block-done counters of grid reductions
+};
+
+// One species' buffers.
+struct SpeciesBufs {
+    double *buf[FS_NBUF];
+    double *k[3];           // k1, k3, k4
+};
+
+// Multigrid level (FP64 plain path).
+struct MGLevel {
+    int nx, ny, pitch;      // interior size; fields are (ny+2) x pitch with ghost ring
+    double *mc, *ce, *cn, *extra, *inv_mc;
+    double *rhs, *x, *res;
+};
+
+struct fs_ctx {
+    fs_config cfg;
+    fs_constants k;
+    PhysParams pp;
+    int nx, ny, pitch;
+    size_t field_elems;          // (ny+2)*pitch
+    int device;
+    cudaStream_t stream;
+    std::string err;
+
+    // mesh
+    double *d_mesh_blob;
+    int8_t *d_types;
+    MeshDev mesh;
+    std::vector<double> h_dr_a, h_dr_c;
+    std::vector<int32_t> h_tx, h_ty;
+    std::vector<double> h_r;
+
+    // table
+    double *d_tab;
+
+    // fields
+    SpeciesBufs sp[FS_MAX_SPECIES];
+    int lev[3];                  // buffer index holding Fortran level 1,2,3 (same for all species)
+    double *ph, *ph_mi;
+    double *d_part;              // per-block partial sums (4 species)
+    int nblk_stage;              // blocks of one stage launch
+    double *d_rows;              // per-row current contributions (2*(ny+2))
+    Ctrl *d_ctrl;
+    Ctrl *h_ctrl;                // pinned mirror
+
+    // Poisson
+    MGLevel mg[FS_MG_MAX_LEVELS];
+    int mg_nlev;
+    double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D
+    double *d_cg_part;
+    int cg_nblk;
+
+    // host mirrors of scalar state
+    double t, dt;
+    double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or;
+    int64_t ts;
+    fs_stats st;
+};
+
+// ---------------------------------------------------------------- host helpers
+int fs_set_error(fs_ctx *c, int code, const char *fmt, ...);
+void fs_host_constants(const fs_config &cfg, fs_constants &k);
+void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<double> &rows);
+
+// particle kernels (fs_ptcl.cu)
+int fs_ptcl_step_impl(fs_ctx *c, int *attempts);
+int fs_ptcl_alloc(fs_ctx *c);
+// Poisson (fs_lapl.cu)
+int fs_lapl_alloc(fs_ctx *c);
+void fs_lapl_free(fs_ctx *c);
+int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
+// misc device helpers (fs_api.cu)
+int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
+int fs_sync_ctrl(fs_ctx *c);

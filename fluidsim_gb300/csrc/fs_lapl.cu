@@ -1,0 +1,766 @@
+// fs_lapl.cu -- the semi-implicit Poisson solve on the GPU (plain FP64 path).
+//
+// lapl_solve (lapl_lib.F90:57-121) assembles A d = -b every step (laplEqn
+// :123-379 for b, laplJ :381-609 and dFdPh :611-636 for A) and hands it to
+// PETSc KSP.  Here:
+//   * k_assemble evaluates, per face once, the Scharfetter-Gummel fluxes of
+//     laplEqn and the flux derivatives of dFdPh, and writes the system in
+//     its row-scaled symmetric form M d = D b with D = diag(dlx*dly),
+//     M = -D A: per node the diagonal M_c, the east and north face
+//     conductances c_e*dly and c_n*dlx (each face conductance
+//     1/dx + dt (dFi - dFe) is shared by the two rows of the face, so M is
+//     symmetric), and the Dirichlet/boundary remainder of the diagonal;
+//   * the preconditioner is a geometric multigrid V-cycle on 2x2 node
+//     aggregates: coarse face conductances are the series (along the face
+//     normal) and parallel (across it) combination of the fine ones, red-black
+//     Gauss-Seidel smoothing (red-black before, black-red after, so the cycle
+//     is symmetric), restriction by summation and prolongation by injection;
+//     levels with at most 32x32 nodes are handled by one CTA;
+//   * CG runs to ||A d + b||_2 / ||b||_2 <= lapl_rtol on the unscaled rows,
+//     the residual PETSc reports with -ksp_norm_type unpreconditioned;
+//   * phi += d and ph_mi = phi (lapl_lib.F90:112-119).
+// All reductions are two-level and fixed-order: per-CTA partials, then the
+// last CTA to finish sums them in index order.
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "fs_internal.h"
+
+#define LBX 32
+#define LBY 8
+#define LNT (LBX * LBY)
+#define BOTTOM_N 32
+#define BOTTOM_THREADS 1024
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of v, then deterministic grid sum by the last CTA.  Returns true
+// in the last CTA (all threads), with *out written.
+template <int NTH>
+__device__ bool grid_sum(double v, double *part, unsigned int *counter, int nblk, double *out) {
+    __shared__ double s_w[NTH / 32];
+    __shared__ bool s_last;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int bid = blockIdx.x + blockIdx.y * gridDim.x;
+    v = warp_sum_d(v);
+    if ((tid & 31) == 0) s_w[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NTH / 32; w++) s += s_w[w];
+        part[bid] = s;
+        __threadfence();
+        unsigned int prev = atomicAdd(counter, 1u);
+        s_last = (prev == (unsigned int)nblk - 1u);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    __shared__ double s_r[NTH];
+    double s = 0.0;
+    for (int b = tid; b < nblk; b += NTH) s += ((volatile double *)part)[b];
+    s_r[tid] = s;
+    __syncthreads();
+    for (int w = NTH / 2; w > 0; w >>= 1) {
+        if (tid < w) s_r[tid] += s_r[tid + w];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *out = s_r[0];
+        *counter = 0u;
+    }
+    __syncthreads();
+    return true;
+}
+
+// ----------------------------------------------------------------- assembly
+struct AsmArgs {
+    PhysParams pp;
+    MeshDev m;
+    const double *tab;
+    const double *ni, *ne, *nt, *ph, *phm;
+    const Ctrl *ctrl;
+    Ctrl *ctrl_w;
+    double *mc, *ce, *cn, *extra, *inv_mc, *rhs, *dinv;
+};
+
+__device__ __forceinline__ void tab_index(const PhysParams &pp, double T, int &k, double &w) {
+    double x = log(T * pp.ph0);
+    double u = (x - pp.lemin) * pp.inv_h;
+    if (!(u >= 0.0)) u = 0.0;
+    if (u > (double)(pp.ntab - 1)) u = (double)(pp.ntab - 1);
+    int i = (int)u;
+    if (i > pp.ntab - 2) i = pp.ntab - 2;
+    k = i;
+    w = u - (double)i;
+}
+__device__ __forceinline__ double tab_val(const double *tab, int k, double w, int row) {
+    const double *t = tab + (size_t)k * FS_TAB_STRIDE;
+    return __ldg(t + row) + w * __ldg(t + 8 + row);
+}
+
+// SG flux (get_Flux, ptcl_props.F90:142-165) for charge q, and dFdPh of the
+// same face at E_mi (lapl_lib.F90:611-636); the exponential is shared when
+// the two fields agree, which they do for every interior face because
+// ph_mi equals ph on the interior.
+__device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double dh, double mu,
+                                             double D, double nl, double nr, double &flux,
+                                             double &df, unsigned int &st) {
+    const double tolf = 9.9999999600419720025e-13;   // REAL(4) 1e-12 of get_Flux
+    double v = (double)q * mu * E;
+    double arg = v * dh / D;
+    double exa = exp(-fabs(arg));
+    if (fabs((double)q * E) < tolf) {
+        flux = D * (nl - nr) / dh;
+    } else {
+        double ex = fabs(arg) > 100.0 ? exp(-100.0) : exa;
+        if (arg > 0) flux = v * (nl - nr * ex) / (1.0 - ex);
+        else flux = v * (nr - nl * ex) / (1.0 - ex);
+    }
+    double vm = (double)q * mu * Emi;
+    double am = vm * dh / D;
+    if (fabs(vm) < 1e-12) {
+        df = 0.0;
+    } else {
+        double ex = (Emi == E) ? exa : exp(-fabs(am));
+        double one = 1.0 - ex;
+        if (am > 0) df = (nl - nr * ex) / one + vm * ex * (nr - nl) / (one * one) * dh / D;
+        else df = (nr - nl * ex) / one + vm * ex * (nr - nl) / (one * one) * dh / D;
+    }
+    if (isnan(df)) st |= FS_ST_DFDPH_NAN;
+}
+
+__global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
+    __shared__ double s_ni[LBY + 2][LBX + 2], s_ne[LBY + 2][LBX + 2], s_nt[LBY + 2][LBX + 2];
+    __shared__ double s_ph[LBY + 2][LBX + 2], s_pm[LBY + 2][LBX + 2];
+    __shared__ double s_te[LBY + 2][LBX + 2], s_mu[LBY + 2][LBX + 2], s_de[LBY + 2][LBX + 2];
+    // per face: ion flux, electron flux, field (as used by dfdx), conductance c, boundary g
+    __shared__ double s_xfi[LBY][LBX + 1], s_xfe[LBY][LBX + 1], s_xe[LBY][LBX + 1], s_xc[LBY][LBX + 1];
+    __shared__ double s_yfi[LBY + 1][LBX], s_yfe[LBY + 1][LBX], s_ye[LBY + 1][LBX], s_yc[LBY + 1][LBX];
+    const PhysParams &pp = a.pp;
+    const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
+    const int tid = threadIdx.x;
+    const int gx0 = blockIdx.x * LBX + 1, gy0 = blockIdx.y * LBY + 1;
+    const double dt = a.ctrl->dt;
+    unsigned int st = 0;
+    for (int q = tid; q < (LBX + 2) * (LBY + 2); q += LNT) {
+        int lx = q % (LBX + 2), ly = q / (LBX + 2);
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        bool in = gi <= nx + 1 && gj <= ny + 1;
+        size_t o = (size_t)gj * P + gi;
+        s_ni[ly][lx] = in ? a.ni[o] : 0.0;
+        s_ne[ly][lx] = in ? a.ne[o] : 0.0;
+        s_nt[ly][lx] = in ? a.nt[o] : 0.0;
+        s_ph[ly][lx] = in ? a.ph[o] : 0.0;
+        s_pm[ly][lx] = in ? a.phm[o] : 0.0;
+    }
+    __syncthreads();
+    for (int q = tid; q < (LBX + 2) * (LBY + 2); q += LNT) {
+        int lx = q % (LBX + 2), ly = q / (LBX + 2);
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        double te = 0, mu = 0, de = 0;
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
+            double nte = s_nt[ly][lx], nee = s_ne[ly][lx];
+            if ((nte >= 0.0) && (nee >= 0.0)) te = nte / nee;
+            else { st |= FS_ST_NEG_DENSITY; te = 1e-8; }
+            int k; double w;
+            tab_index(pp, te, k, w);
+            mu = tab_val(a.tab, k, w, 0);
+            de = tab_val(a.tab, k, w, 1);
+        }
+        s_te[ly][lx] = te; s_mu[ly][lx] = mu; s_de[ly][lx] = de;
+    }
+    __syncthreads();
+    // x faces between gi and gi+1
+    for (int q = tid; q < LBY * (LBX + 1); q += LNT) {
+        int c = q % (LBX + 1), r = q / (LBX + 1);
+        int gi = gx0 - 1 + c, gj = gy0 + r;
+        if (gj > ny || gi > nx) continue;
+        int lx = c, ly = r + 1;
+        double dh = a.m.dx[gi];
+        double E = -(s_ph[ly][lx + 1] - s_ph[ly][lx]) / dh;
+        double Emi = -(s_pm[ly][lx + 1] - s_pm[ly][lx]) / dh;
+        int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;
+        int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;
+        double fi = 0, fe = 0, eu = E, cf = 0;
+        if (gi == 0 && tr == -1) {
+            eu = 0.0;
+        } else if (gi == nx && tl == 1) {
+            eu = 0.0;
+        } else if (gi == 0 && tr == -2) {           // cathode-side electrode row
+            int lc = lx + 1;
+            double te = s_te[ly][lc], ni = s_ni[ly][lc], ne = s_ne[ly][lc], mue = s_mu[ly][lc];
+            double aa = (s_ph[ly][lx] > s_ph[ly][lc]) ? 1.0 : 0.0;
+            double ve = sqrt(pp.ve_coef * te) * pp.t0 / pp.x0;
+            fi = (1.0 - aa) * pp.mui * E * ni - 2.5e-1 * pp.vi * ni;
+            fe = -(aa * mue * E * ne) - 2.5e-1 * ve * ne - pp.gam * fi;
+            int ac = (s_ph[ly][lx] > s_ph[ly][lc]) ? 1 : 0;
+            double dfi = (double)(1 - ac) * pp.mui * ni / dh;
+            double dfe = -((double)ac * mue * ne / dh) - pp.gam * dfi;
+            cf = 1.0 / dh + dt * (dfi - dfe);         // Dirichlet conductance of the row
+        } else if (gi == nx && tl == 2) {          // anode-side electrode row
+            int lc = lx;
+            double te = s_te[ly][lc], ni = s_ni[ly][lc], ne = s_ne[ly][lc], mue = s_mu[ly][lc];
+            double aa = (s_ph[ly][lx + 1] > s_ph[ly][lc]) ? 1.0 : 0.0;
+            double ve = sqrt(pp.ve_coef * te) * pp.t0 / pp.x0;
+            fi = (1.0 - aa) * pp.mui * E * ni + 2.5e-1 * pp.vi * ni;
+            fe = -(aa * mue * E * ne) + 2.5e-1 * ve * ne - pp.gam * fi;
+            int ac = (s_ph[ly][lx + 1] > s_ph[ly][lc]) ? 1 : 0;
+            double dfi = (double)(ac - 1) * pp.mui * ni / dh;
+            double dfe = (double)ac * mue * ne / dh - pp.gam * dfi;
+            cf = 1.0 / dh - dt * (dfi - dfe);
+        } else {
+            double mue = 5e-1 * (s_mu[ly][lx] + s_mu[ly][lx + 1]);
+            double De = 5e-1 * (s_de[ly][lx] + s_de[ly][lx + 1]);
+            double dFi, dFe;
+            sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, s_ni[ly][lx], s_ni[ly][lx + 1], fi, dFi, st);
+            sg_and_dfdph(-1, E, Emi, dh, mue, De, s_ne[ly][lx], s_ne[ly][lx + 1], fe, dFe, st);
+            double dfi_mi = pp.mui / dh * dFi;
+            double dfe_mi = -(mue / dh * dFe);
+            cf = 1.0 / dh + dt * (dfi_mi - dfe_mi);
+        }
+        s_xfi[r][c] = fi; s_xfe[r][c] = fe; s_xe[r][c] = eu; s_xc[r][c] = cf;
+    }
+    // y faces between gj and gj+1
+    for (int q = tid; q < (LBY + 1) * LBX; q += LNT) {
+        int c = q % LBX, r = q / LBX;
+        int gi = gx0 + c, gj = gy0 - 1 + r;
+        if (gi > nx || gj > ny) continue;
+        int lx = c + 1, ly = r;
+        double dh = a.m.dy[gj];
+        double E = -(s_ph[ly + 1][lx] - s_ph[ly][lx]) / dh;
+        double Emi = -(s_pm[ly + 1][lx] - s_pm[ly][lx]) / dh;
+        int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
+        int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
+        double fi = 0, fe = 0, eu = E, cf = 0;
+        if (gj == 0 && tt == -1) {
+            eu = 0.0;
+        } else if (gj == 0 && tt == -2) {
+            // laplEqn has no lower y electrode flux (zero); laplJ has its derivative
+            int lc = ly + 1;
+            double ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
+            int ac = (s_ph[ly][lx] > s_ph[lc][lx]) ? 1 : 0;
+            double dfi = (double)(1 - ac) * pp.mui * ni / dh;
+            double dfe = -((double)ac * mue * ne / dh) - pp.gam * dfi;
+            cf = 1.0 / dh + dt * (dfi - dfe);
+        } else if (gj == ny && tb == 1) {
+            eu = 0.0;
+        } else if (gj == ny && tb == 2) {
+            int lc = ly;
+            double te = s_te[lc][lx], ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
+            double aa = (s_ph[ly + 1][lx] > s_ph[lc][lx]) ? 1.0 : 0.0;
+            double ve = sqrt(pp.ve_coef * te) * pp.t0 / pp.x0;
+            fi = (1.0 - aa) * pp.mui * E * ni + 2.5e-1 * pp.vi * ni;
+            fe = -(aa * mue * E * ne) + 2.5e-1 * ve * ne - pp.gam * fi;
+            int ac = (s_ph[ly + 1][lx] > s_ph[lc][lx]) ? 1 : 0;
+            double dfi = (double)(ac - 1) * pp.mui * ni / dh;
+            double dfe = (double)ac * mue * ne / dh - pp.gam * dfi;
+            cf = 1.0 / dh - dt * (dfi - dfe);
+        } else {
+            double mue = 5e-1 * (s_mu[ly][lx] + s_mu[ly + 1][lx]);
+            double De = 5e-1 * (s_de[ly][lx] + s_de[ly + 1][lx]);
+            double dFi, dFe;
+            sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, s_ni[ly][lx], s_ni[ly + 1][lx], fi, dFi, st);
+            sg_and_dfdph(-1, E, Emi, dh, mue, De, s_ne[ly][lx], s_ne[ly + 1][lx], fe, dFe, st);
+            double dfi_mi = pp.mui / dh * dFi;
+            double dfe_mi = -(mue / dh * dFe);
+            cf = 1.0 / dh + dt * (dfi_mi - dfe_mi);
+        }
+        s_yfi[r][c] = fi; s_yfe[r][c] = fe; s_ye[r][c] = eu; s_yc[r][c] = cf;
+    }
+    __syncthreads();
+    const int lx = tid % LBX, ly = tid / LBX;
+    const int gi = gx0 + lx, gj = gy0 + ly;
+    if (gi <= nx && gj <= ny) {
+        const size_t o = (size_t)gj * P + gi;
+        const double dlx = a.m.dlx[gi - 1], dly = a.m.dly[gj - 1];
+        const int tx = a.m.tx[(gj - 1) * nx + gi - 1], ty = a.m.ty[(gj - 1) * nx + gi - 1];
+        // cylindrical weights: r(j) of the row, face radii of the y faces
+        const double wr = pp.cyl ? a.m.r[gj] : 1.0;
+        const double wn = pp.cyl ? (a.m.r[gj + 1] + a.m.r[gj]) / 2.0 : 1.0;
+        const double ws = pp.cyl ? (a.m.r[gj] + a.m.r[gj - 1]) / 2.0 : 1.0;
+        // b of laplEqn (lapl_lib.F90:250-375)
+        double dfdx = -(s_xe[ly][lx + 1] - s_xe[ly][lx]) / dlx;
+        double dflxe_x = (s_xfe[ly][lx + 1] - s_xfe[ly][lx]) / dlx;
+        double dflxi_x = (s_xfi[ly][lx + 1] - s_xfi[ly][lx]) / dlx;
+        double dfdy, dflxi_y, dflxe_y;
+        if (pp.cyl) {
+            dfdy = -(s_ye[ly + 1][lx] * wn - s_ye[ly][lx] * ws) / dly / wr;
+            dflxi_y = (s_yfi[ly + 1][lx] * wn - s_yfi[ly][lx] * ws) / dly / wr;
+            dflxe_y = (s_yfe[ly + 1][lx] * wn - s_yfe[ly][lx] * ws) / dly / wr;
+        } else {
+            dfdy = -(s_ye[ly + 1][lx] - s_ye[ly][lx]) / dly;
+            dflxi_y = (s_yfi[ly + 1][lx] - s_yfi[ly][lx]) / dly;
+            dflxe_y = (s_yfe[ly + 1][lx] - s_yfe[ly][lx]) / dly;
+        }
+        double b = dfdx + dfdy + s_ni[ly + 1][lx + 1] - s_ne[ly + 1][lx + 1]
+                 - dt * (dflxi_x + dflxi_y - dflxe_x - dflxe_y);
+        if (isnan(b)) st |= FS_ST_BNAN;
+        // Row of M = -D A with D = dlx*dly*r: a face shared with an interior
+        // neighbour is an off-diagonal conductance; a boundary face enters the
+        // diagonal only (laplJ, lapl_lib.F90:566-607).
+        const double cw = s_xc[ly][lx], cee = s_xc[ly][lx + 1], cs = s_yc[ly][lx], cnn = s_yc[ly + 1][lx];
+        const double offw = gi > 1 ? cw : 0.0, offe = gi < nx ? cee : 0.0;
+        const double offs = gj > 1 ? cs : 0.0, offn = gj < ny ? cnn : 0.0;
+        double gx = 0.0, gys = 0.0, gyn = 0.0;
+        // electrode rows: Dirichlet conductance of the boundary face
+        if (gi == 1 && tx == -2) gx += cw;
+        if (gi == nx && tx == 2) gx += cee;
+        if (gj == 1 && ty == -2) gys += cs;
+        if (gj == ny && ty == 2) gyn += cnn;
+        // lower Neumann rows: the reference's diagonal takes the ghost spacing
+        // dx(i-1) / dy(j-1) where the off-diagonal takes dx(i) / dy(j)
+        if (gi == 1 && tx == -1) gx += 1.0 / a.m.dx[0] - 1.0 / a.m.dx[1];
+        if (gj == 1 && ty == -1) gyn += 1.0 / a.m.dy[0] - 1.0 / a.m.dy[1];
+        const double sx = dly * wr;
+        const double extra = gx * sx + (gys * ws + gyn * wn) * dlx;
+        const double mc = (offw + offe) * sx + (offs * ws + offn * wn) * dlx + extra;
+        const double D = dlx * dly * wr;
+        a.mc[o] = mc;
+        a.inv_mc[o] = 1.0 / mc;
+        a.extra[o] = extra;
+        a.ce[o] = offe * sx;
+        a.cn[o] = offn * wn * dlx;
+        a.rhs[o] = b * D;
+        a.dinv[o] = 1.0 / D;
+    }
+    if (st) atomicOr(&a.ctrl_w->status, st);
+}
+
+// ---------------------------------------------------------------- multigrid
+struct LevelDev {
+    int nx, ny, P;
+    double *mc, *ce, *cn, *extra, *inv_mc, *rhs, *x, *res;
+};
+
+__device__ __forceinline__ double inv_or_big(double c) { return c > 1e-300 ? 1.0 / c : 1e300; }
+
+// coarse operator of one aggregate level (series along, parallel across faces)
+__device__ void coarsen_cell(const LevelDev &f, const LevelDev &c, int I, int J) {
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    const size_t oc = (size_t)J * c.P + I;
+    double ce = 0.0, cn = 0.0, ex = 0.0;
+    if (I < c.nx) {
+        const int gx0 = fx1 + 1, gx1 = min(fx1 + 2, f.nx);
+        for (int fy = fy0; fy <= fy1; fy++) {
+            double R = inv_or_big(f.ce[(size_t)fy * f.P + fx1]);
+            if (fx1 > fx0) R += 0.5 * inv_or_big(f.ce[(size_t)fy * f.P + fx0]);
+            if (gx1 > gx0) R += 0.5 * inv_or_big(f.ce[(size_t)fy * f.P + gx0]);
+            ce += 1.0 / R;
+        }
+    }
+    if (J < c.ny) {
+        const int gy0 = fy1 + 1, gy1 = min(fy1 + 2, f.ny);
+        for (int fx = fx0; fx <= fx1; fx++) {
+            double R = inv_or_big(f.cn[(size_t)fy1 * f.P + fx]);
+            if (fy1 > fy0) R += 0.5 * inv_or_big(f.cn[(size_t)fy0 * f.P + fx]);
+            if (gy1 > gy0) R += 0.5 * inv_or_big(f.cn[(size_t)gy0 * f.P + fx]);
+            cn += 1.0 / R;
+        }
+    }
+    for (int fy = fy0; fy <= fy1; fy++)
+        for (int fx = fx0; fx <= fx1; fx++) {
+            double e = f.extra[(size_t)fy * f.P + fx];
+            if (e > 0.0 && fx1 > fx0) {
+                double ci = f.ce[(size_t)fy * f.P + fx0];
+                e = 1.0 / (1.0 / e + 0.5 * inv_or_big(ci));
+            }
+            ex += e;
+        }
+    c.ce[oc] = ce;
+    c.cn[oc] = cn;
+    c.extra[oc] = ex;
+}
+
+__device__ void coarsen_diag(const LevelDev &c, int I, int J) {
+    const size_t oc = (size_t)J * c.P + I;
+    double mc = c.ce[oc] + c.ce[oc - 1] + c.cn[oc] + c.cn[oc - c.P] + c.extra[oc];
+    c.mc[oc] = mc;
+    c.inv_mc[oc] = mc > 0.0 ? 1.0 / mc : 0.0;
+}
+
+__global__ void k_coarsen(const LevelDev f, const LevelDev c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I <= c.nx && J <= c.ny) coarsen_cell(f, c, I, J);
+}
+__global__ void k_coarsen_diag(const LevelDev c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I <= c.nx && J <= c.ny) coarsen_diag(c, I, J);
+}
+
+// Gauss-Seidel update of one node
+__device__ __forceinline__ double gs_node(const LevelDev &L, size_t o) {
+    return (L.rhs[o] + L.ce[o] * L.x[o + 1] + L.ce[o - 1] * L.x[o - 1] + L.cn[o] * L.x[o + L.P]
+            + L.cn[o - L.P] * L.x[o - L.P]) * L.inv_mc[o];
+}
+
+// one red (color 0) or black (color 1) half sweep; zero_init: x starts at 0
+__global__ void k_rb(const LevelDev L, int color, int zero_init) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > L.nx || J > L.ny) return;
+    size_t o = (size_t)J * L.P + I;
+    if (((I + J) & 1) == color) L.x[o] = zero_init ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
+    else if (zero_init) L.x[o] = 0.0;
+}
+
+// coarse rhs = sum over the aggregate of the fine residual rhs - M x
+__device__ __forceinline__ double resid(const LevelDev &L, size_t o) {
+    return L.rhs[o] - (L.mc[o] * L.x[o] - L.ce[o] * L.x[o + 1] - L.ce[o - 1] * L.x[o - 1]
+                       - L.cn[o] * L.x[o + L.P] - L.cn[o - L.P] * L.x[o - L.P]);
+}
+__global__ void k_restrict(const LevelDev f, const LevelDev c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > c.nx || J > c.ny) return;
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    double s = 0.0;
+    for (int fy = fy0; fy <= fy1; fy++)
+        for (int fx = fx0; fx <= fx1; fx++) s += resid(f, (size_t)fy * f.P + fx);
+    c.rhs[(size_t)J * c.P + I] = s;
+}
+__global__ void k_prolong(const LevelDev f, const LevelDev c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > f.nx || J > f.ny) return;
+    f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+}
+
+// V-cycle over levels [lb, nl) inside one CTA (levels of at most 32x32 nodes).
+struct BottomArgs {
+    LevelDev L[FS_MG_MAX_LEVELS];
+    int lb, nl, nu;
+};
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs a) {
+    const int t = threadIdx.x;
+    auto sweep = [&](const LevelDev &L, int color, int zero) {
+        for (int q = t; q < L.nx * L.ny; q += BOTTOM_THREADS) {
+            int I = q % L.nx + 1, J = q / L.nx + 1;
+            size_t o = (size_t)J * L.P + I;
+            if (((I + J) & 1) == color) L.x[o] = zero ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
+            else if (zero) L.x[o] = 0.0;
+        }
+        __syncthreads();
+    };
+    for (int l = a.lb; l < a.nl - 1; l++) {
+        const LevelDev &f = a.L[l], &c = a.L[l + 1];
+        sweep(f, 0, 1);
+        sweep(f, 1, 0);
+        for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
+        for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
+            int I = q % c.nx + 1, J = q / c.nx + 1;
+            const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+            double s = 0.0;
+            for (int fy = fy0; fy <= fy1; fy++)
+                for (int fx = fx0; fx <= fx1; fx++) s += resid(f, (size_t)fy * f.P + fx);
+            c.rhs[(size_t)J * c.P + I] = s;
+        }
+        __syncthreads();
+    }
+    {   // coarsest level: symmetric sweeps to convergence (it has very few nodes)
+        const LevelDev &c = a.L[a.nl - 1];
+        // palindromic sweep sequence (RB)^10 (BR)^10 keeps the cycle symmetric
+        sweep(c, 0, 1);
+        sweep(c, 1, 0);
+        for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
+        for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+    }
+    for (int l = a.nl - 2; l >= a.lb; l--) {
+        const LevelDev &f = a.L[l], &c = a.L[l + 1];
+        for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
+            int I = q % f.nx + 1, J = q / f.nx + 1;
+            f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+        }
+        __syncthreads();
+        for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
+    }
+}
+
+// ------------------------------------------------------------------------ CG
+struct CgArgs {
+    int nx, ny, P, nblk;
+    double *x, *r, *z, *p, *q, *rhs, *dinv, *part;
+    const double *mc, *ce, *cn;
+    Ctrl *ctrl;
+    double rtol;
+};
+
+__global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    double v = 0.0;
+    if (I <= a.nx && J <= a.ny) {
+        size_t o = (size_t)J * a.P + I;
+        a.x[o] = 0.0;
+        a.r[o] = a.rhs[o];
+        a.p[o] = 0.0;
+        double u = a.rhs[o] * a.dinv[o];
+        v = u * u;
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[0], a.nblk, &out) && threadIdx.x == 0) {
+        a.ctrl->bnorm2 = out;
+        a.ctrl->rnorm2 = out;
+        a.ctrl->relres = out > 0.0 ? 1.0 : 0.0;
+        a.ctrl->cg_done = out == 0.0 ? 1 : 0;
+        a.ctrl->cg_iters = 0;
+        a.ctrl->cg_fail = 0;
+        a.ctrl->rz = 0.0;
+    }
+}
+
+// rz = r.z; beta = rz/rz_old (0 on the first iteration)
+__global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    double v = 0.0;
+    if (I <= a.nx && J <= a.ny) {
+        size_t o = (size_t)J * a.P + I;
+        v = a.r[o] * a.z[o];
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->rz_old = c->rz;
+        c->rz = out;
+        c->beta = c->cg_iters == 0 ? 0.0 : out / c->rz_old;
+    }
+}
+
+// p = z + beta p ; q = M p needs p at the neighbours: two kernels
+__global__ void k_cg_p(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    if (I > a.nx || J > a.ny) return;
+    size_t o = (size_t)J * a.P + I;
+    a.p[o] = a.z[o] + a.ctrl->beta * a.p[o];
+}
+
+__global__ void __launch_bounds__(256) k_cg_q(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    double v = 0.0;
+    if (I <= a.nx && J <= a.ny) {
+        size_t o = (size_t)J * a.P + I;
+        double pq = a.mc[o] * a.p[o] - a.ce[o] * a.p[o + 1] - a.ce[o - 1] * a.p[o - 1]
+                  - a.cn[o] * a.p[o + a.P] - a.cn[o - a.P] * a.p[o - a.P];
+        a.q[o] = pq;
+        v = a.p[o] * pq;
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->pq = out;
+        if (!(out > 0.0)) { c->cg_fail = 1; c->alpha = 0.0; }
+        else c->alpha = c->rz / out;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cg_xr(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    double v = 0.0;
+    const double al = a.ctrl->alpha;
+    if (I <= a.nx && J <= a.ny) {
+        size_t o = (size_t)J * a.P + I;
+        a.x[o] += al * a.p[o];
+        double rr = a.r[o] - al * a.q[o];
+        a.r[o] = rr;
+        double u = rr * a.dinv[o];
+        v = u * u;
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->rnorm2 = out;
+        c->cg_iters += 1;
+        c->relres = c->bnorm2 > 0.0 ? sqrt(out / c->bnorm2) : 0.0;
+        if (c->relres <= a.rtol) c->cg_done = 1;
+        if (isnan(out)) c->cg_fail = 1;
+    }
+}
+
+// phi(interior) += d ; ph_mi = phi (lapl_lib.F90:112-119)
+__global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, int ny, int P) {
+    size_t n = (size_t)(ny + 2) * P;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
+        int gi = (int)(o % P), gj = (int)(o / P);
+        double v = ph[o];
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) v = v + x[o];
+        ph[o] = v;
+        phm[o] = v;
+    }
+}
+
+LevelDev level_dev(const MGLevel &m) {
+    LevelDev L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.extra = m.extra; L.inv_mc = m.inv_mc;
+    L.rhs = m.rhs; L.x = m.x; L.res = m.res;
+    return L;
+}
+
+dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+static int alloc_zero(fs_ctx *c, double **p, size_t n) {
+    cudaError_t e = cudaMalloc(p, n * sizeof(double));
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (Poisson)");
+    e = cudaMemset(*p, 0, n * sizeof(double));
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "cudaMemset");
+}
+
+int fs_lapl_alloc(fs_ctx *c) {
+    int nx = c->nx, ny = c->ny, nl = 0;
+    for (;;) {
+        MGLevel &m = c->mg[nl];
+        m.nx = nx; m.ny = ny;
+        m.pitch = ((nx + 2 + 31) / 32) * 32;
+        size_t n = (size_t)(ny + 2) * m.pitch;
+        int rc;
+        double **fields[] = {&m.mc, &m.ce, &m.cn, &m.extra, &m.inv_mc, &m.res};
+        for (double **f : fields)
+            if ((rc = alloc_zero(c, f, n))) return rc;
+        if (nl == 0) {
+            m.rhs = nullptr;   // bound to the CG vectors below
+            m.x = nullptr;
+        } else {
+            if ((rc = alloc_zero(c, &m.rhs, n))) return rc;
+            if ((rc = alloc_zero(c, &m.x, n))) return rc;
+        }
+        nl++;
+        if ((nx == 1 && ny == 1) || nl == FS_MG_MAX_LEVELS) break;
+        nx = (nx + 1) / 2;
+        ny = (ny + 1) / 2;
+    }
+    c->mg_nlev = nl;
+    size_t n0 = (size_t)(c->ny + 2) * c->pitch;
+    double **vecs[] = {&c->p, &c->q, &c->z, &c->r, &c->xs, &c->bs, &c->dinv};
+    for (double **v : vecs) {
+        int rc = alloc_zero(c, v, n0);
+        if (rc) return rc;
+    }
+    c->mg[0].rhs = c->r;
+    c->mg[0].x = c->z;
+    dim3 g = grid2(c->nx, c->ny, dim3(32, 8));
+    c->cg_nblk = g.x * g.y;
+    return alloc_zero(c, &c->d_cg_part, (size_t)c->cg_nblk);
+}
+
+void fs_lapl_free(fs_ctx *c) {
+    for (int l = 0; l < c->mg_nlev; l++) {
+        MGLevel &m = c->mg[l];
+        double *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.res};
+        for (double *f : fs) cudaFree(f);
+        if (l > 0) { cudaFree(m.rhs); cudaFree(m.x); }
+    }
+    double *vs[] = {c->p, c->q, c->z, c->r, c->xs, c->bs, c->dinv, c->d_cg_part};
+    for (double *v : vs) cudaFree(v);
+    c->mg_nlev = 0;
+}
+
+static void vcycle(fs_ctx *c) {
+    const int nl = c->mg_nlev, nu = c->cfg.mg_smooth;
+    int lb = 0;
+    while (lb < nl && (c->mg[lb].nx > BOTTOM_N || c->mg[lb].ny > BOTTOM_N)) lb++;
+    dim3 b(32, 8);
+    for (int l = 0; l < lb; l++) {
+        LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        dim3 g = grid2(f.nx, f.ny, b);
+        k_rb<<<g, b, 0, c->stream>>>(f, 0, 1);
+        k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+        for (int it = 1; it < nu; it++) {
+            k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+            k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+        }
+        k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+    }
+    BottomArgs ba;
+    for (int l = 0; l < nl; l++) ba.L[l] = level_dev(c->mg[l]);
+    ba.lb = lb;
+    ba.nl = nl;
+    ba.nu = nu;
+    k_bottom<<<1, BOTTOM_THREADS, 0, c->stream>>>(ba);
+    for (int l = lb - 1; l >= 0; l--) {
+        LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        dim3 g = grid2(f.nx, f.ny, b);
+        k_prolong<<<g, b, 0, c->stream>>>(f, cc);
+        for (int it = 0; it < nu; it++) {
+            k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+            k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+        }
+    }
+}
+
+int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
+    const int ns = c->cfg.nspecies;
+    (void)ns;
+    AsmArgs a;
+    a.pp = c->pp;
+    a.m = c->mesh;
+    a.tab = c->d_tab;
+    a.ni = c->sp[0].buf[c->lev[0]];
+    a.ne = c->sp[1].buf[c->lev[0]];
+    a.nt = c->sp[2].buf[c->lev[0]];
+    a.ph = c->ph;
+    a.phm = c->ph_mi;
+    a.ctrl = c->d_ctrl;
+    a.ctrl_w = c->d_ctrl;
+    MGLevel &m0 = c->mg[0];
+    a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
+    a.rhs = c->bs;   // scaled right-hand side D b
+    a.dinv = c->dinv;
+    // status bits of the assembly
+    cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);
+    dim3 g = grid2(c->nx, c->ny, dim3(LBX, LBY));
+    k_assemble<<<g, LNT, 0, c->stream>>>(a);
+    // coarse operators
+    dim3 b2(16, 16);
+    for (int l = 0; l + 1 < c->mg_nlev; l++) {
+        LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        k_coarsen<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(f, cc);
+        k_coarsen_diag<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
+    }
+    // CG on M d = D b
+    CgArgs ca;
+    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch; ca.nblk = c->cg_nblk;
+    ca.x = c->xs; ca.r = c->r; ca.z = c->z; ca.p = c->p; ca.q = c->q;
+    ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
+    ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
+    ca.ctrl = c->d_ctrl;
+    ca.rtol = c->cfg.lapl_rtol;
+    dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
+    k_cg_init<<<gb, 256, 0, c->stream>>>(ca);
+    int rc = fs_sync_ctrl(c);
+    if (rc) return rc;
+    if (c->h_ctrl->status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
+    if (c->h_ctrl->status & FS_ST_DFDPH_NAN) return fs_set_error(c, FS_ERR_NAN, "NaN in dFdPh");
+    int it = 0;
+    bool ok = c->h_ctrl->cg_done != 0;
+    if (c->h_ctrl->status & FS_ST_BNAN) {
+        *lerr = 1; *iters = 0; *relres = NAN;
+        return FS_OK;
+    }
+    while (!ok && it < c->cfg.lapl_maxit) {
+        vcycle(c);
+        k_cg_rz<<<gb, 256, 0, c->stream>>>(ca);
+        k_cg_p<<<gb, 256, 0, c->stream>>>(ca);
+        k_cg_q<<<gb, 256, 0, c->stream>>>(ca);
+        k_cg_xr<<<gb, 256, 0, c->stream>>>(ca);
+        rc = fs_sync_ctrl(c);
+        if (rc) return rc;
+        it = c->h_ctrl->cg_iters;
+        if (c->h_ctrl->cg_fail) break;
+        ok = c->h_ctrl->cg_done != 0;
+    }
+    *iters = c->h_ctrl->cg_iters;
+    *relres = c->h_ctrl->relres;
+    if (!ok) {
+        *lerr = 1;
+        return FS_OK;
+    }
+    *lerr = 0;
+    k_phi_update<<<4 * 152, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels");
+    return FS_OK;
+}

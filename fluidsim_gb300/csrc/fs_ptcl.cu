@@ -1,0 +1,511 @@
+// fs_ptcl.cu -- the particle step on the GPU (plain FP64 path).
+//
+// One launch per RK-Merson stage does what the reference does in the cell
+// loop of ptcl_step plus rk_step for every species (ptcl_lib.F90:44-57,
+// ptclEqn ptcl_lib.F90:99-550, rk_step ptcl_props.F90:71-139):
+//   * a CTA owns a 32x8 tile of interior nodes and stages the tile plus a
+//     one-node halo of n_i, n_e, n_t (, n_m) and phi in shared memory;
+//   * per node it evaluates the mean energy Te = nt/ne and the table
+//     coefficients once (the reference re-evaluates them for every face);
+//   * per face it evaluates the Scharfetter-Gummel flux once (get_Flux,
+//     ptcl_props.F90:142-165) -- both nodes of a face see the same value,
+//     as in the reference, where the two nodes compute identical expressions;
+//     the electron and energy fluxes share one exponential because
+//     mut/Dt = mue/De (ptcl_lib.F90:142-143);
+//   * per node it forms the divergence, the sources and k_s, and applies the
+//     Merson stage combination with the density floor; stage 5 also produces
+//     per-CTA partial sums of the error norm, the dielectric relaxation time
+//     t_m and the electrode-current rows of circ_step (circ_lib.F90:87-151).
+// A one-CTA controller kernel then applies the PI step-size control of
+// ptcl_lib.F90:59-95 on the device.
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "fs_internal.h"
+
+#define BX 32
+#define BY 8
+#define NT (BX * BY)
+#define HX (BX + 2)
+#define HY (BY + 2)
+
+namespace {
+
+struct StageArgs {
+    PhysParams pp;
+    MeshDev m;
+    const double *tab;
+    const double *nin[FS_MAX_SPECIES];
+    const double *nbase[FS_MAX_SPECIES];
+    double *nout[FS_MAX_SPECIES];
+    const double *k1[FS_MAX_SPECIES];
+    const double *k3[FS_MAX_SPECIES];
+    const double *k4[FS_MAX_SPECIES];
+    double *kout[FS_MAX_SPECIES];
+    const double *ph;
+    Ctrl *ctrl;
+    double *part;     // [species][nblk] partial error sums
+    double *rows;     // [2][ny+2] current rows
+    int stage;
+    int nblk;
+};
+
+__device__ __forceinline__ void tab_index(const PhysParams &pp, double T, int &k, double &w) {
+    double x = log(T * pp.ph0);
+    double u = (x - pp.lemin) * pp.inv_h;
+    if (!(u >= 0.0)) u = 0.0;
+    if (u > (double)(pp.ntab - 1)) u = (double)(pp.ntab - 1);
+    int i = (int)u;
+    if (i > pp.ntab - 2) i = pp.ntab - 2;
+    k = i;
+    w = u - (double)i;
+}
+
+__device__ __forceinline__ double tab_val(const double *tab, int k, double w, int row) {
+    const double *t = tab + (size_t)k * FS_TAB_STRIDE;
+    return __ldg(t + row) + w * __ldg(t + 8 + row);
+}
+
+// get_Flux for q = +1 (ions, constant mui/Di)
+__device__ __forceinline__ double sg_ion(const PhysParams &pp, double E, double dh, double inv_dh,
+                                         double nl, double nr) {
+    const double tol = 9.9999999600419720025e-13;   // REAL(4) 1e-12
+    double v = pp.mui * E;
+    double arg = v * dh / pp.Di;
+    if (fabs(E) < tol) return pp.Di * (nl - nr) * inv_dh;
+    if (arg > 0) {
+        double ex = exp(fmax(-arg, -100.0));
+        return v * (nl - nr * ex) / (1.0 - ex);
+    }
+    double ex = exp(fmax(arg, -100.0));
+    return v * (nr - nl * ex) / (1.0 - ex);
+}
+
+// get_Flux for q = -1 with (mue, De) and (5/3 mue, 5/3 De): one exponential
+__device__ __forceinline__ void sg_elec(double E, double dh, double inv_dh, double mue, double De,
+                                        double nel, double ner, double ntl, double ntr,
+                                        double &fe, double &ft) {
+    const double tol = 9.9999999600419720025e-13;
+    const double f53 = 5.0 / 3.0;
+    double mut = f53 * mue, Dt = f53 * De;
+    double ve = -mue * E, vt = -mut * E;
+    double arg = ve * dh / De;
+    if (fabs(E) < tol) {
+        fe = De * (nel - ner) * inv_dh;
+        ft = Dt * (ntl - ntr) * inv_dh;
+        return;
+    }
+    double ex;
+    if (arg > 0) {
+        ex = exp(fmax(-arg, -100.0));
+        double inv = 1.0 / (1.0 - ex);
+        fe = ve * (nel - ner * ex) * inv;
+        ft = vt * (ntl - ntr * ex) * inv;
+    } else {
+        ex = exp(fmax(arg, -100.0));
+        double inv = 1.0 / (1.0 - ex);
+        fe = ve * (ner - nel * ex) * inv;
+        ft = vt * (ntr - ntl * ex) * inv;
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
+    __shared__ double s_n[NS][HY][HX];
+    __shared__ double s_ph[HY][HX];
+    __shared__ double s_te[HY][HX];
+    __shared__ double s_mue[HY][HX];
+    __shared__ double s_de[HY][HX];
+    __shared__ double s_w[BY][BX];
+    __shared__ int s_k[BY][BX];
+    __shared__ double s_fx[NS][BY][BX + 1];   // x-face left of tile column c
+    __shared__ double s_fy[NS][BY + 1][BX];   // y-face below tile row r
+    __shared__ double s_ex[BY][BX + 1];       // face field as used by the Joule term
+    __shared__ double s_ey[BY + 1][BX];
+    __shared__ double s_red[NS][NT / 32];
+    __shared__ double s_tm[NT / 32];
+
+    const PhysParams &pp = a.pp;
+    const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
+    const int tid = threadIdx.x;
+    const int gx0 = blockIdx.x * BX + 1, gy0 = blockIdx.y * BY + 1;
+    unsigned int st = 0;
+
+    // phase 1: tile + halo of the stage state and phi
+    for (int q = tid; q < HX * HY; q += NT) {
+        int lx = q % HX, ly = q / HX;
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        bool in = gi <= nx + 1 && gj <= ny + 1;
+        size_t o = (size_t)gj * P + gi;
+#pragma unroll
+        for (int s = 0; s < NS; s++) s_n[s][ly][lx] = in ? a.nin[s][o] : 0.0;
+        s_ph[ly][lx] = in ? a.ph[o] : 0.0;
+    }
+    __syncthreads();
+    // phase 2: mean energy and table coefficients of every interior node of the tile+halo
+    for (int q = tid; q < HX * HY; q += NT) {
+        int lx = q % HX, ly = q / HX;
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        double te = 0, mu = 0, de = 0;
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
+            double nte = s_n[2][ly][lx], nee = s_n[1][ly][lx];
+            if ((nte >= 0.0) && (nee >= 0.0)) te = nte / nee;
+            else { st |= FS_ST_NEG_DENSITY; te = 1e-8; }
+            int k; double w;
+            tab_index(pp, te, k, w);
+            mu = tab_val(a.tab, k, w, 0);
+            de = tab_val(a.tab, k, w, 1);
+            if (lx >= 1 && lx <= BX && ly >= 1 && ly <= BY) { s_k[ly - 1][lx - 1] = k; s_w[ly - 1][lx - 1] = w; }
+        }
+        s_te[ly][lx] = te; s_mue[ly][lx] = mu; s_de[ly][lx] = de;
+    }
+    __syncthreads();
+
+    // phase 3a: x faces.  Face c of tile row r lies between nodes gi = gx0-1+c and gi+1.
+    for (int q = tid; q < BY * (BX + 1); q += NT) {
+        int c = q % (BX + 1), r = q / (BX + 1);
+        int gi = gx0 - 1 + c, gj = gy0 + r;
+        if (gj > ny || gi > nx) continue;
+        int lx = c, ly = r + 1;   // left node in halo coordinates
+        double E = -(s_ph[ly][lx + 1] - s_ph[ly][lx]) * a.m.inv_dx[gi];
+        double fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
+        int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;       // type of left node
+        int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;      // type of right node
+        if (gi == 0 && tr == -1) {           // vacuum face of the first node
+            eu = 0.0;
+        } else if (gi == nx && tl == 1) {    // vacuum face of the last node
+            eu = 0.0;
+        } else if ((gi == 0 && tr == -2) || (gi == nx && tl == 2)) {   // electrode face
+            const bool left = gi == 0;
+            const int lc = left ? lx + 1 : lx;     // the interior node
+            double te = s_te[ly][lc], ni = s_n[0][ly][lc], ne = s_n[1][ly][lc], nt = s_n[2][ly][lc];
+            double phg = left ? s_ph[ly][lx] : s_ph[ly][lx + 1];
+            double aa = (phg > s_ph[ly][lc]) ? 1.0 : 0.0;
+            double mue = s_mue[ly][lc], mut = (5.0 / 3.0) * mue;
+            double ve = sqrt(pp.ve_coef * te) * pp.t0 / pp.x0;
+            double sgn = left ? -1.0 : 1.0;
+            fi = (1.0 - aa) * pp.mui * E * ni + sgn * (2.5e-1 * pp.vi * ni);
+            fe = -(aa * mue * E * ne) + sgn * (2.5e-1 * ve * ne) - pp.gam * fi;
+            ft = -(aa * mut * E * nt) + sgn * (1.0 / 3.0 * ve * nt) - pp.gam * te * fi;
+            if (NS == 4) fm = sgn * (5e-1 * pp.vi * s_n[3][ly][lc]);
+        } else {                              // Scharfetter-Gummel face
+            double dh = a.m.dx[gi], idh = a.m.inv_dx[gi];
+            double mue = 5e-1 * (s_mue[ly][lx] + s_mue[ly][lx + 1]);
+            double De = 5e-1 * (s_de[ly][lx] + s_de[ly][lx + 1]);
+            fi = sg_ion(pp, E, dh, idh, s_n[0][ly][lx], s_n[0][ly][lx + 1]);
+            sg_elec(E, dh, idh, mue, De, s_n[1][ly][lx], s_n[1][ly][lx + 1],
+                    s_n[2][ly][lx], s_n[2][ly][lx + 1], fe, ft);
+            if (NS == 4) fm = -pp.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
+            if (a.stage == 5) {
+                if (gi == 1 && a.m.dr_a[gj] != 0.0) a.rows[gj] = a.m.dr_a[gj] * (fi - fe);
+                if (gi == nx - 1 && a.m.dr_c[gj] != 0.0) a.rows[(ny + 2) + gj] = a.m.dr_c[gj] * (fi - fe);
+            }
+        }
+        s_fx[0][r][c] = fi; s_fx[1][r][c] = fe; s_fx[2][r][c] = ft;
+        if (NS == 4) s_fx[3][r][c] = fm;
+        s_ex[r][c] = eu;
+    }
+    __syncthreads();
+    // phase 3b: y faces.  Face r of tile column c lies between gj = gy0-1+r and gj+1.
+    for (int q = tid; q < (BY + 1) * BX; q += NT) {
+        int c = q % BX, r = q / BX;
+        int gi = gx0 + c, gj = gy0 - 1 + r;
+        if (gi > nx || gj > ny) continue;
+        int lx = c + 1, ly = r;     // lower node in halo coordinates
+        double E = -(s_ph[ly + 1][lx] - s_ph[ly][lx]) * a.m.inv_dy[gj];
+        double fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
+        int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
+        int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
+        if (gj == 0 && tt == -1) {
+            eu = 0.0;
+        } else if (gj == ny && tb == 1) {
+            eu = 0.0;
+        } else if ((gj == 0 && tt == -2) || (gj == ny && tb == 2)) {
+            const bool low = gj == 0;
+            const int lc = low ? ly + 1 : ly;
+            double te = s_te[lc][lx], ni = s_n[0][lc][lx], ne = s_n[1][lc][lx], nt = s_n[2][lc][lx];
+            double phg = low ? s_ph[ly][lx] : s_ph[ly + 1][lx];
+            double aa = (phg > s_ph[lc][lx]) ? 1.0 : 0.0;
+            double mue = s_mue[lc][lx], mut = (5.0 / 3.0) * mue;
+            double ve = sqrt(pp.ve_coef * te) * pp.t0 / pp.x0;
+            double sgn = low ? -1.0 : 1.0;
+            fi = (1.0 - aa) * pp.mui * E * ni + sgn * (2.5e-1 * pp.vi * ni);
+            // the reference's upper y electrode takes gamma times the x-direction
+            // ion flux of the node's upper x face (ptcl_lib.F90:427-433)
+            double fix = low ? fi : s_fx[0][lc - 1][lx];
+            fe = -(aa * mue * E * ne) + sgn * (2.5e-1 * ve * ne) - pp.gam * fix;
+            ft = -(aa * mut * E * nt) + sgn * (1.0 / 3.0 * ve * nt) - pp.gam * te * fix;
+            if (NS == 4) fm = sgn * (5e-1 * pp.vi * s_n[3][lc][lx]);
+        } else {
+            double dh = a.m.dy[gj], idh = a.m.inv_dy[gj];
+            double mue = 5e-1 * (s_mue[ly][lx] + s_mue[ly + 1][lx]);
+            double De = 5e-1 * (s_de[ly][lx] + s_de[ly + 1][lx]);
+            fi = sg_ion(pp, E, dh, idh, s_n[0][ly][lx], s_n[0][ly + 1][lx]);
+            sg_elec(E, dh, idh, mue, De, s_n[1][ly][lx], s_n[1][ly + 1][lx],
+                    s_n[2][ly][lx], s_n[2][ly + 1][lx], fe, ft);
+            if (NS == 4) fm = -pp.Dm * (s_n[3][ly + 1][lx] - s_n[3][ly][lx]) * idh;
+        }
+        s_fy[0][r][c] = fi; s_fy[1][r][c] = fe; s_fy[2][r][c] = ft;
+        if (NS == 4) s_fy[3][r][c] = fm;
+        s_ey[r][c] = eu;
+    }
+    __syncthreads();
+
+    // phase 4: one node per thread
+    const int lx = tid % BX, ly = tid / BX;
+    const int gi = gx0 + lx, gj = gy0 + ly;
+    double qerr[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) qerr[s] = 0.0;
+    double tm = 1e300;
+    if (gi <= nx && gj <= ny) {
+        const size_t o = (size_t)gj * P + gi;
+        const int hx = lx + 1, hy = ly + 1;
+        const double te = s_te[hy][hx];
+        const double ni = s_n[0][hy][hx], ne = s_n[1][hy][hx];
+        const double nm = NS == 4 ? s_n[3][hy][hx] : 0.0;
+        const int kk = s_k[ly][lx];
+        const double w = s_w[ly][lx];
+        const double k_ir = tab_val(a.tab, kk, w, 2), k_ex = tab_val(a.tab, kk, w, 3);
+        const double nu = tab_val(a.tab, kk, w, 4), beta = tab_val(a.tab, kk, w, 5);
+        const double idlx = a.m.inv_dlx[gi - 1], idly = a.m.inv_dly[gj - 1];
+        double dfdx[NS], dfdy[NS];
+        if (pp.cyl) {
+            double r0 = a.m.r[gj], rp = (a.m.r[gj + 1] + r0), rm = (r0 + a.m.r[gj - 1]);
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                dfdx[s] = (s_fx[s][ly][lx + 1] - s_fx[s][ly][lx]) * idlx;
+                dfdy[s] = (s_fy[s][ly + 1][lx] * rp / 2.0 - s_fy[s][ly][lx] * rm / 2.0) * idly / r0;
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                dfdx[s] = (s_fx[s][ly][lx + 1] - s_fx[s][ly][lx]) * idlx;
+                dfdy[s] = (s_fy[s][ly + 1][lx] - s_fy[s][ly][lx]) * idly;
+            }
+        }
+        const double fex = (s_fx[1][ly][lx + 1] + s_fx[1][ly][lx]) * 0.5;
+        const double exa = (s_ex[ly][lx] + s_ex[ly][lx + 1]) * 0.5;
+        const double fey = (s_fy[1][ly + 1][lx] + s_fy[1][ly][lx]) * 0.5;
+        const double eya = (s_ey[ly][lx] + s_ey[ly + 1][lx]) * 0.5;
+        double term_sie = k_ir * pp.ninf * ne - beta * ni * ne;
+        double k_si = 0, k_sc = 0;
+        if (NS == 4) {
+            k_sc = tab_val(a.tab, kk, w, 6);
+            k_si = tab_val(a.tab, kk, w, 7);
+            term_sie = term_sie + k_si * nm * ne + pp.k_mp * (nm * nm);
+        }
+        const double term_st1 = -(fex * exa + fey * eya);
+        const double term_st2 = -(ne * nu * pp.me / pp.mi * (te / 1.5 - pp.tg * pp.kb / pp.e / pp.ph0));
+        double term_st3 = -(pp.h_ir * k_ir * pp.ninf * ne) - pp.h_si * k_si * nm * ne
+                        - pp.h_ex * k_ex * pp.ninf * ne;
+        double kv[NS];
+        kv[0] = -dfdx[0] - dfdy[0] + term_sie;
+        kv[1] = -dfdx[1] - dfdy[1] + term_sie;
+        kv[2] = -dfdx[2] - dfdy[2] + term_st1 + term_st2 + term_st3;
+        if (NS == 4) {
+            double term_sm = k_ex * pp.ninf * ne - k_si * nm * ne - k_sc * nm * ne - pp.k_r * nm * ne
+                           - 2.0 * pp.k_mp * (nm * nm) - pp.k_2q * pp.ninf * nm
+                           - pp.k_3q * (pp.ninf * pp.ninf) * nm;
+            kv[3] = -dfdx[3] - dfdy[3] + term_sm;
+        }
+        const double dt = a.ctrl->dt;
+        const int stg = a.stage;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            if (isnan(kv[s])) st |= FS_ST_NAN;
+            if (a.kout[s]) a.kout[s][o] = kv[s];
+            const double n3 = a.nbase[s][o];
+            double v;
+            if (stg == 1) v = n3 + kv[s] * dt * (1.0 / 3.0);
+            else if (stg == 2) v = n3 + dt * (a.k1[s][o] + kv[s]) * (1.0 / 6.0);
+            else if (stg == 3) v = n3 + dt * (a.k1[s][o] + kv[s] * 3.0) * 0.125;
+            else if (stg == 4) v = n3 + dt * (a.k1[s][o] - a.k3[s][o] * 3.0 + kv[s] * 4.0) * 0.5;
+            else {
+                const double k1 = a.k1[s][o], k3 = a.k3[s][o], k4 = a.k4[s][o];
+                v = n3 + dt * (k1 + k4 * 4.0 + kv[s]) * (1.0 / 6.0);
+                double err = fabs(dt * (k1 * (2.0 / 30.0) - k3 * (3.0 / 10.0) + k4 * (4.0 / 15.0)
+                                        - kv[s] * (1.0 / 30.0)));
+                double qq = err / (pp.abs_tol + pp.rel_tol * fabs(n3));
+                qerr[s] = qq * qq;
+            }
+            a.nout[s][o] = fmax(v, pp.nmin[s]);
+        }
+        if (stg == 5) {
+            // mue(2) as the reference leaves it when t_m is evaluated (ptcl_lib.F90:527)
+            const int ty = a.m.ty[(gj - 1) * nx + gi - 1], tx = a.m.tx[(gj - 1) * nx + gi - 1];
+            double mue2;
+            if (ty == 0 || ty < 0) mue2 = 5e-1 * (s_mue[hy][hx] + s_mue[hy + 1][hx]);
+            else if (ty == 1 && (tx == 0 || tx < 0)) mue2 = 5e-1 * (s_mue[hy][hx] + s_mue[hy][hx + 1]);
+            else mue2 = s_mue[hy][hx];
+            tm = 1.0 / (mue2 * ne + pp.mui * ni);
+        }
+    }
+    if (st) atomicOr(&a.ctrl->status, st);
+    if (a.stage == 5) {
+        const int wid = tid >> 5, lane = tid & 31;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            double v = warp_sum(qerr[s]);
+            if (lane == 0) s_red[s][wid] = v;
+        }
+        for (int o = 16; o > 0; o >>= 1) tm = fmin(tm, __shfl_down_sync(0xffffffffu, tm, o));
+        if (lane == 0) s_tm[wid] = tm;
+        __syncthreads();
+        if (tid < NS) {
+            double v = 0.0;
+            for (int wv = 0; wv < NT / 32; wv++) v += s_red[tid][wv];
+            a.part[(size_t)tid * a.nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+        }
+        if (tid == 0) {
+            double m = s_tm[0];
+            for (int wv = 1; wv < NT / 32; wv++) m = fmin(m, s_tm[wv]);
+            if (m > 0.0 && m < 1e300)
+                atomicMin((unsigned long long *)&a.ctrl->t_m, (unsigned long long)__double_as_longlong(m));
+        }
+    }
+}
+
+// circ_step ghost potentials (circ_lib.F90:178-198): DC, so Vd_mi = Vd_pl = Vsrc.
+__global__ void k_circ_ghost(double *ph, const int8_t *tx, const double *r, int nx, int ny, int P,
+                             double ew, double vd) {
+    int gj = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (gj > ny) return;
+    if (r[gj] <= ew) {
+        if (tx[(gj - 1) * nx + 0] == -2) ph[(size_t)gj * P + 0] = vd / 2.0;
+        if (tx[(gj - 1) * nx + nx - 1] == 2) ph[(size_t)gj * P + nx + 1] = vd / (-2.0);
+    }
+}
+
+// PI controller of ptcl_lib.F90:59-95 plus the current sums of circ_step.
+__global__ void k_controller(Ctrl *c, const double *part, int nblk, int ns, const double *rows,
+                             int ny, int adaptive, double dt_min) {
+    __shared__ double s[FS_MAX_SPECIES][256];
+    const int t = threadIdx.x;
+    for (int sp = 0; sp < ns; sp++) {
+        double v = 0.0;
+        for (int b = t; b < nblk; b += 256) v += part[(size_t)sp * nblk + b];
+        s[sp][t] = v;
+    }
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int sp = 0; sp < ns; sp++) s[sp][t] += s[sp][t + w];
+        __syncthreads();
+    }
+    if (t != 0) return;
+    // species order of the reference's sum: ni, ne, nm, nt
+    double e_ni = s[0][0], e_ne = s[1][0], e_nt = s[2][0], e_nm = ns == 4 ? s[3][0] : 0.0;
+    double err_cur = sqrt(e_ni + e_ne + e_nm + e_nt);
+    c->err_cur = err_cur;
+    double ida = 0.0, idc = 0.0;
+    for (int j = 1; j <= ny; j++) { ida = ida + rows[j]; idc = idc + rows[(ny + 2) + j]; }
+    c->ida = ida;
+    c->idc = idc;
+    c->rejected = 0;
+    if (!adaptive) return;
+    double scfac = 8e-1 * pow(err_cur, -7e-1 / 4.0) * pow(c->err_prev, 4e-1 / 4.0);
+    scfac = fmin(2.5, fmax(3e-1, scfac));
+    c->scfac = scfac;
+    c->dt = scfac * c->dt;
+    if (c->dt <= dt_min) { c->min_dt = 1; return; }
+    if (err_cur <= 1.0) c->err_prev = err_cur;
+    else c->rejected = 1;
+}
+
+__global__ void k_reset_step(Ctrl *c, double *rows, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) { c->t_m = 1e9; c->status = 0; c->rejected = 0; c->min_dt = 0; }
+    if (i < n) rows[i] = 0.0;
+}
+
+}  // namespace
+
+int fs_ptcl_alloc(fs_ctx *c) {
+    dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
+    c->nblk_stage = grid.x * grid.y;
+    cudaError_t e = cudaMalloc(&c->d_part, sizeof(double) * FS_MAX_SPECIES * c->nblk_stage);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc partials");
+    e = cudaMalloc(&c->d_rows, sizeof(double) * 2 * (c->ny + 2));
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc rows");
+    return cudaMemset(c->d_rows, 0, sizeof(double) * 2 * (c->ny + 2)) == cudaSuccess ? FS_OK
+                                                                                   : FS_ERR_CUDA;
+}
+
+static void launch_stage(fs_ctx *c, StageArgs &a) {
+    dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
+    if (c->cfg.nspecies == 4) k_stage<4><<<grid, NT, 0, c->stream>>>(a);
+    else k_stage<3><<<grid, NT, 0, c->stream>>>(a);
+}
+
+// ptcl_step: five stages, restart on rejection (ptcl_lib.F90:32-97).
+int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
+    const int ns = c->cfg.nspecies;
+    const int L2 = c->lev[1], L3 = c->lev[2];
+    int freeb[FS_NBUF], nf = 0;
+    for (int b = 0; b < FS_NBUF; b++)
+        if (b != L2 && b != L3) freeb[nf++] = b;
+    const int SA = freeb[0], SB = freeb[1], OUT = freeb[2];
+    int in1 = L2;
+    int attempts = 0;
+
+    k_reset_step<<<(2 * (c->ny + 2) + 255) / 256, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, 2 * (c->ny + 2));
+    for (;;) {
+        attempts++;
+        StageArgs a;
+        memset(&a, 0, sizeof(a));
+        a.pp = c->pp;
+        a.m = c->mesh;
+        a.tab = c->d_tab;
+        a.ph = c->ph;
+        a.ctrl = c->d_ctrl;
+        a.part = c->d_part;
+        a.rows = c->d_rows;
+        a.nblk = c->nblk_stage;
+        const int ins[5] = {in1, SA, SB, SA, SB};
+        const int outs[5] = {SA, SB, SA, SB, OUT};
+        for (int stg = 1; stg <= 5; stg++) {
+            a.stage = stg;
+            for (int s = 0; s < ns; s++) {
+                SpeciesBufs &b = c->sp[s];
+                a.nin[s] = b.buf[ins[stg - 1]];
+                a.nbase[s] = b.buf[L3];
+                a.nout[s] = b.buf[outs[stg - 1]];
+                a.k1[s] = b.k[0];
+                a.k3[s] = b.k[1];
+                a.k4[s] = b.k[2];
+                a.kout[s] = stg == 1 ? b.k[0] : stg == 3 ? b.k[1] : stg == 4 ? b.k[2] : nullptr;
+            }
+            launch_stage(c, a);
+            if (stg == 1)
+                k_circ_ghost<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
+                    c->ph, c->mesh.tx, c->mesh.r, c->nx, c->ny, c->pitch, c->cfg.ew, c->Vsrc);
+        }
+        k_controller<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_part, c->nblk_stage, ns, c->d_rows,
+                                               c->ny, c->cfg.adaptive, c->cfg.dt_min);
+        int rc = fs_sync_ctrl(c);
+        if (rc) return rc;
+        const Ctrl &h = *c->h_ctrl;
+        if (h.status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
+        if (h.status & FS_ST_NAN) return fs_set_error(c, FS_ERR_NAN, "NaN in particle right-hand side");
+        if (h.min_dt) return fs_set_error(c, FS_ERR_MIN_DT, "minimum timestep reached");
+        c->Vd_pl = c->Vd_mi = c->Vsrc;
+        if (!h.rejected) break;
+        c->st.rk_rejects++;
+        c->Vd_pl = c->Vd_or;
+        c->Vd_mi = c->Vd_or;
+        in1 = L3;   // n(:,:,1) = n(:,:,2) = n(:,:,3): restart from the base state
+        if (attempts > 100000) return fs_set_error(c, FS_ERR_MIN_DT, "RK restart limit");
+    }
+    c->lev[0] = OUT;
+    c->lev[1] = SB;
+    c->dt = c->h_ctrl->dt;
+    c->st.attempts += attempts;
+    if (attempts_out) *attempts_out = attempts;
+    return FS_OK;
+}

@@ -1,0 +1,209 @@
+/*
+ * fluidsim_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * fluidsim per-step hot path: Scharfetter-Gummel particle fluxes and RHS,
+ * local-mean-energy coefficients, RK-Merson stages with the embedded error
+ * estimate and adaptive dt, and the semi-implicit electrostatic Poisson solve.
+ *
+ * Every entry point replaces one Fortran subroutine (or one block of the main
+ * loop) of the reference.  The Fortran caller binds them through
+ * ISO_C_BINDING; plain pointers, sizes and POD structs only.
+ *
+ *   reference (file:line)                          entry point here
+ *   ---------------------------------------------  -----------------------
+ *   lapl_init  lapl_lib.F90:22-55                 \
+ *   ptcl_init  ptcl_lib.F90:15-30                  > fs_create
+ *   circ_init  circ_lib.F90:213-223               /
+ *   ptcl_step  ptcl_lib.F90:32-97                  fs_ptcl_step
+ *     (ptclEqn ptcl_lib.F90:99-550, rk_step ptcl_props.F90:30-140,
+ *      circ_step circ_lib.F90:19-210, get_Flux ptcl_props.F90:142-165)
+ *   lapl_solve lapl_lib.F90:57-121                 fs_lapl_solve
+ *     (laplEqn :123-379, laplJ :381-609, dFdPh :611-636, KSPSolve :103)
+ *   accept branch  main.F90:83-101                 fs_accept
+ *   reject branch  main.F90:103-121                fs_reject
+ *   main loop body main.F90:68-121                 fs_run (device-resident loop)
+ *   module arrays ni/ne/nt/nm (ptcl_lib.F90:7-10),
+ *     ph (lapl_lib.F90:14)                         fs_upload_state / fs_download_state
+ *   maxval(ne)  main.F90:131                       fs_max_ne
+ *   KSPDestroy/VecDestroy/MatDestroy main.F90:159  fs_destroy
+ *
+ * Array layout at the boundary is the reference's: Fortran column-major
+ * (bx+2, by+2[, level]) with a one-cell ghost ring, x fastest, leading
+ * dimension ld >= nx+2.  All field state lives in device memory owned by the
+ * context between calls; host arrays are only borrowed during upload/download.
+ *
+ * Return values: FS_OK (0) or a negative FS_ERR_* code; fs_last_error() gives
+ * the message.  No entry point calls exit/abort.  One host thread per context.
+ */
+#ifndef FLUIDSIM_GPU_H
+#define FLUIDSIM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_ABI_VERSION 1
+
+/* error codes */
+#define FS_OK                  0
+#define FS_ERR_INVALID        -1   /* bad argument or configuration            */
+#define FS_ERR_CUDA           -2   /* CUDA runtime error                        */
+#define FS_ERR_NAN            -3   /* NaN in a RHS (ptcl_lib.F90:530-549) or in
+                                      the Poisson RHS (lapl_lib.F90:376-378)    */
+#define FS_ERR_NEG_DENSITY    -4   /* get_Te negative density stop
+                                      (ptcl_props.F90:171-177)                  */
+#define FS_ERR_MIN_DT         -5   /* minimum timestep stop (ptcl_lib.F90:68-72) */
+#define FS_ERR_NOT_CONVERGED  -6   /* Krylov solve did not converge              */
+#define FS_ERR_UNSUPPORTED    -7   /* option outside the implemented scope       */
+#define FS_ERR_NOMEM          -8   /* device allocation failed                   */
+#define FS_ERR_NO_DEVICE      -9   /* no CUDA device / extension not usable      */
+
+/* fs_config.coef_mode */
+#define FS_COEF_FITS   0   /* reference polynomial fits (ptcl_props.F90:182-429)   */
+#define FS_COEF_TABLE  1   /* log-spaced table over mean energy, Arrhenius k_ir     */
+
+/* fs_config.precision */
+#define FS_PREC_FP64   0   /* plain FP64 path (the drop-in)                          */
+#define FS_PREC_MIXED  1   /* FP32 flux/RHS and multigrid, FP64 accumulation         */
+
+/* Run configuration.  Lengths in units of x0, voltage in units of ph0, time in
+ * units of t0 (props.F90:33-37), i.e. the reference's nondimensional units. */
+typedef struct fs_config {
+    int32_t abi_version;    /* must be FS_ABI_VERSION                               */
+    int32_t nx, ny;         /* interior nodes (g%nx, g%ny); one block: bx=nx, by=ny  */
+    int32_t nspecies;       /* 3: ni, ne, nt ; 4: + metastables nm                   */
+    int32_t coef_mode;      /* FS_COEF_*                                              */
+    int32_t cyl;            /* 1: cylindrical r-weighting in y (props.F90:47)          */
+    int32_t rf;             /* source waveform; 0 = DC is the implemented one          */
+    int32_t adaptive;       /* 1: PI dt controller + reject (reference)               */
+                            /* 0: dt held fixed, attempts never rejected              */
+    int32_t precision;      /* FS_PREC_*                                              */
+    int32_t lapl_maxit;     /* Krylov iteration cap                                   */
+    int32_t table_n;        /* table points (FS_COEF_TABLE)                           */
+    int32_t mg_smooth;      /* red-black GS iterations per V-cycle leg (default 2)    */
+    double  table_emin_ev;  /* table range in mean energy [eV]                        */
+    double  table_emax_ev;
+    double  kir_arrh_a;     /* Arrhenius ionisation prefactor [m^3/s] (table mode)    */
+    double  kir_arrh_e;     /* Arrhenius activation energy [eV]                       */
+    double  p_torr;         /* gas pressure (props.F90:41)                            */
+    double  tg_k;           /* gas temperature (props.F90:40)                         */
+    double  gam;            /* secondary emission coefficient (ptcl_props.F90:25)     */
+    double  n_init;         /* uniform initial density of ptcl_init (props.F90:44)    */
+    double  l, w, ew, gap;  /* g%l, g%w, g%ew, g%gap                                  */
+    double  vl;             /* applied voltage Vmax (circ_init)                       */
+    double  res;            /* circuit resistance (main.F90:43,286), nondim           */
+    double  abs_tol;        /* RK-Merson error tolerances (ptcl_props.F90:35)         */
+    double  rel_tol;
+    double  dt_min;         /* minimum-dt stop (ptcl_lib.F90:68), reference 1.1e-12   */
+    double  lapl_rtol;      /* Poisson relative residual ||A d + b|| / ||b||          */
+} fs_config;
+
+/* Mesh produced by the caller's g_init (props.F90:52-235). */
+typedef struct fs_mesh {
+    const double  *dx;      /* nx+1 : dx(i) = x(i+1) - x(i)                           */
+    const double  *dlx;     /* nx   : dlx(i) = (dx(i+1) + dx(i)) / 2                  */
+    const double  *dy;      /* ny+1                                                   */
+    const double  *dly;     /* ny                                                     */
+    const double  *r;       /* ny+2 : y node coordinates, g%r                          */
+    const int32_t *type_x;  /* nx*ny column-major g%type_x(i,j) at (i-1)+(j-1)*nx     */
+    const int32_t *type_y;  /* nx*ny column-major g%type_y                            */
+} fs_mesh;
+
+/* Derived physical constants (props.F90:24-47, ptcl_props.F90:5-25). */
+typedef struct fs_constants {
+    double pi, eps0, e, kb, me, x0, ph0, t0, wp02, w2;
+    double tg, p, ninf, n_zero;
+    double mi, mui, vi, Di, Dm, k_r, k_mp, k_2q, k_3q;
+    double h_ir, h_ex, h_si, h_sc, gam;
+    double nmin_nt;         /* energy-density floor n_zero/ph0/1e2 (ptcl_lib.F90:56)   */
+    double cap;             /* circuit capacitance (circ_lib.F90:221)                 */
+} fs_constants;
+
+/* Per-step statistics filled by fs_run / fs_get_stats. */
+typedef struct fs_stats {
+    double  t;              /* g%t                                                    */
+    double  dt;             /* g%dt                                                   */
+    double  t_m;            /* min dielectric relaxation time of the last step        */
+    double  ida, idc;       /* electrode currents of the last circ_step               */
+    double  err_cur;        /* last RK-Merson error norm                              */
+    double  lapl_relres;    /* last Poisson relative residual                         */
+    int64_t steps;          /* accepted main-loop iterations (ts)                     */
+    int64_t attempts;       /* RK attempts run (including rejected ones)              */
+    int64_t rk_rejects;     /* attempts rejected by the error norm                    */
+    int64_t lapl_rejects;   /* steps rejected because the Poisson solve failed        */
+    int64_t lapl_iters;     /* total Krylov iterations                                */
+    int32_t last_lapl_iters;
+    int32_t lerr;           /* lerr of the last Poisson solve                         */
+} fs_stats;
+
+typedef struct fs_ctx fs_ctx;
+
+/* Library identification: ABI version, and the device it runs on. */
+int32_t fs_abi_version(void);
+
+/* Derived constants for a configuration (host only, no device needed). */
+int fs_get_constants(const fs_config *cfg, fs_constants *out);
+
+/* Coefficient table (FS_COEF_TABLE) as the device uses it: ncoef rows of
+ * table_n values, rows in the order mue, De, k_ir, k_ex, nu, beta, k_sc, k_si.
+ * Host only.  out must hold 8*table_n doubles. */
+int fs_build_table(const fs_config *cfg, double *out);
+
+/* lapl_init + ptcl_init + circ_init: allocate all device state, set the
+ * reference's uniform initial state (ni=ne=nm=n_init, nt=ne*Tg*kb/e/ph0,
+ * ph=ph_mi=0, t=0), Vmax=Vd=vl.  dt is set with fs_set_time. */
+int fs_create(const fs_config *cfg, const fs_mesh *mesh, fs_ctx **out);
+void fs_destroy(fs_ctx *ctx);
+
+/* Message of the last error on ctx (or of the last failed fs_create when
+ * ctx is NULL). */
+const char *fs_last_error(const fs_ctx *ctx);
+
+/* g%t and g%dt. */
+int fs_set_time(fs_ctx *ctx, double t, double dt);
+
+/* Module arrays <-> device.  Species arrays are (ld, ny+2, nlev) column-major
+ * like ni(bx+2,by+2,3); nlev = 3 (all RK levels) or 1 (the one array is used
+ * for every level).  nm may be NULL when nspecies == 3.  ph is (ld, ny+2).
+ * ph_mi (lapl_lib.F90:14) is set equal to ph on upload. */
+int fs_upload_state(fs_ctx *ctx, const double *ni, const double *ne,
+                    const double *nt, const double *nm, const double *ph,
+                    int32_t ld, int32_t nlev);
+int fs_download_state(fs_ctx *ctx, double *ni, double *ne, double *nt,
+                      double *nm, double *ph, int32_t ld, int32_t nlev);
+
+/* ptcl_step(g, ph, Em) with Em = 0: five RK-Merson stages, restarting on
+ * rejection, then the PI controller.  dt_inout is g%dt (in: the dt to use; out:
+ * the controller's next dt).  t_m_out: min over stage-5 cells of
+ * 1/(mue*ne + mui*ni), starting from 1e9 (main.F90:74).  attempts_out: RK
+ * attempts including rejected ones.  Any output pointer may be NULL. */
+int fs_ptcl_step(fs_ctx *ctx, double *dt_inout, double *t_m_out,
+                 double *ida_out, double *idc_out, int32_t *attempts_out);
+
+/* lapl_solve(g, ne(:,:,1), ni(:,:,1), nt(:,:,1), sig, lerr): assemble the
+ * semi-implicit correction system with g%dt = dt, solve it to cfg->lapl_rtol,
+ * and on success ph += delta, ph_mi = ph.  lerr_out = 0 converged, 1 not
+ * (the caller then rejects the step, main.F90:102-121). */
+int fs_lapl_solve(fs_ctx *ctx, double dt, int32_t *lerr_out,
+                  int32_t *iters_out, double *relres_out);
+
+/* Level rotation of main.F90:83-101 (accept: t += dt, n3 <- n2, n2 <- n1)
+ * and main.F90:103-121 (reject: dt /= 2, n1 <- n3, n2 <- n3). */
+int fs_accept(fs_ctx *ctx);
+int fs_reject(fs_ctx *ctx);
+
+/* nsteps iterations of the main.F90:68-121 loop body on the device:
+ * ptcl_step (when ts > 1), lapl_solve, accept or reject.  Host work per
+ * iteration is limited to reading back the control scalars. */
+int fs_run(fs_ctx *ctx, int32_t nsteps, fs_stats *stats_out);
+
+int fs_get_stats(fs_ctx *ctx, fs_stats *out);
+
+/* maxval(ne(:,:,1)) over the interior (main.F90:131). */
+int fs_max_ne(fs_ctx *ctx, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDSIM_GPU_H */
