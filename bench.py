@@ -1,0 +1,356 @@
+"""Benchmark of the fluidsim hot path on one GB300 (or N independent replicas).
+
+Metric: steps/s of the 2D argon DC glow at 1024x1024 nodes -- one step is one
+iteration of the reference's main loop (main.F90:68-121): ptcl_step with all
+of its RK-Merson attempts, then lapl_solve (Poisson to 1e-8 relative residual),
+then the accept/reject rotation.  Synthetic seeded inputs (Gaussian blob plus
+1% noise, the workload's own definition; no dataset is involved).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--n 1024]
+                  [--impl gb300|reference] [--dt adaptive|fixed]
+
+The gb300 arm prints one JSON line with the device-resident throughput
+(`value`), the end-to-end throughput through the C ABI with host buffers
+(`e2e`), a roofline object for the dominant kernel (the RK stage kernel),
+the CPU oracle timed on the host cores (`cpu_baseline`), SM clocks sampled
+during the timed region and the number of kernels launched.
+
+The reference arm (--impl reference) times the reference algorithm's CPU
+implementation -- the C++ oracle, a restatement of the Fortran, because the
+Fortran/MPI/PETSc reference cannot be built on this machine -- on all host
+cores, on the same workload, a bounded number of steps.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s, 1024² glow: plain FP64 vs mixed+learned-PC at 1e-8 Poisson resid"
+UNIT = "steps/s"
+# FP64 algorithmic bytes of one RK stage launch per interior node:
+# one RK-Merson attempt moves (25 S + 5) * 8 bytes per node with S = 3 species
+# (stage 1 reads n2, n3, phi and writes k1, n2'; ...; stage 5 reads n2, n3,
+# k1, k3, k4, phi and writes n1), i.e. 640 B per node per attempt, 128 B per stage.
+STAGE_BYTES_PER_NODE = (25 * 3 + 5) * 8 / 5.0
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(n, dt_mode, rtol=1e-8):
+    from fluidsim_gb300 import config
+    cfg = config.glow(n, adaptive=1 if dt_mode == "adaptive" else 0, lapl_rtol=rtol,
+                      lapl_maxit=500)
+    if dt_mode == "fixed":
+        # fixed dt below the electron drift CFL of the finest cell (1e-12 s at 64^2)
+        cfg = cfg.replace(dt0=cfg.dt0 * min(1.0, 64.0 / n))
+    return cfg
+
+
+def initial_state(cfg, mesh, k):
+    from fluidsim_gb300 import grid
+    return grid.blob_state(mesh, k, noise=0.01, seed=1)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def time_oracle(cfg, mesh, state, t, dt, ts, max_seconds, max_steps, threads):
+    """Run the oracle from a given state; returns (steps, seconds)."""
+    from oracle import oracle
+    oracle.set_threads(threads)
+    o = oracle.OracleDischarge(cfg, mesh, state, solver=oracle.SOLVER_BICGSTAB)
+    o.set_time(t, dt)
+    o.ts = ts
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps:
+        o.step()
+        steps += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    el = time.perf_counter() - t0
+    o.close()
+    return steps, el
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU implementation."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from fluidsim_gb300 import api
+    from oracle import oracle
+    oracle.build()
+    cfg = workload(args.n, args.dt)
+    mesh = cfg.mesh()
+    k = api.constants(cfg, oracle.load(), "or_")
+    st = initial_state(cfg, mesh, k)
+    threads = cpu_threads()
+    oracle.set_threads(threads)
+    o = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_BICGSTAB)
+    # start-up iterations (Poisson only) and warm-up steps, untimed
+    for _ in range(2 + min(args.warmup, 1)):
+        o.step()
+    budget = float(os.environ.get("FS_REF_BUDGET_S", "60"))
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < args.steps:
+        o.step()
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    v = steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded Gaussian blob + 1% noise",
+        "config": {"workload": "2D Ar DC glow %dx%d, %s dt, Poisson rtol 1e-8" % (args.n, args.n, args.dt),
+                   "solver": "BiCGStab + block-Jacobi ILU(0), one block per thread"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d main-loop steps of the same workload after start-up" % steps},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from fluidsim_gb300 import api
+    torch.cuda.init()
+
+    cfg = workload(args.n, args.dt)
+    mesh = cfg.mesh()
+    k = api.constants(cfg)
+    st0 = initial_state(cfg, mesh, k)
+    d = api.Discharge(cfg, mesh, st0)
+    stream = torch.cuda.ExternalStream(d.stream_handle())
+
+    # start-up (two Poisson-only iterations) and warm-up steps
+    d.run(2 + args.warmup)
+    warm_state = d.download(nlev=3)
+    warm_t, warm_dt, warm_ts = d.t, d.dt, d.ts
+    warm_stats = d.stats()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- timed region: device-resident steps --------------------------------
+    sampler = ClockSampler(local)
+    sampler.start()
+    d.profile(True)
+    n_launch0 = d.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s = d.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    launches = d.launch_count() - n_launch0
+    prof = d.profile_read()
+    d.profile(False)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    attempts = s["attempts"] - warm_stats["attempts"]
+    iters = s["lapl_iters"] - warm_stats["lapl_iters"]
+
+    # ---- end to end through the C ABI with host buffers ---------------------
+    pinned = {}
+    for key in ("ni", "ne", "nt", "ph"):
+        a = warm_state[key]
+        t = torch.empty(a.shape[::-1], dtype=torch.float64, pin_memory=True)
+        v = t.numpy().T          # Fortran-ordered view of pinned memory
+        v[...] = a
+        pinned[key] = v
+    d.set_time(warm_t, warm_dt)
+    d.ts = warm_ts
+    out = {key: torch.empty(pinned[key].shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
+           for key in ("ni", "ne", "nt", "ph")}
+    state_bytes = sum(a.nbytes for a in pinned.values())
+    barrier()
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    d.upload(pinned)
+    for _ in range(args.steps):
+        d.step()                  # fs_ptcl_step + fs_lapl_solve + fs_accept/fs_reject
+    fin = d.download(nlev=3)
+    for key in ("ni", "ne", "nt"):
+        out[key][...] = fin[key][:, :, 0]
+    e3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = e2.elapsed_time(e3)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+
+    # ---- roofline of the dominant kernel (RK stage) -------------------------
+    peak, peak_kind = measured_peaks()
+    st_ms, st_n = prof["stage"]
+    nodes = cfg.nx * cfg.ny
+    stage_ms = st_ms / max(st_n, 1)
+    achieved = STAGE_BYTES_PER_NODE * nodes / (stage_ms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("bytes_per_launch_%d" % args.n)
+
+    # ---- CPU baseline: the oracle on the host cores, bounded sample ---------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = cpu_threads()
+        steps_c, el_c = time_oracle(cfg, mesh, warm_state, warm_t, warm_dt, warm_ts,
+                                    max_seconds=args.cpu_seconds, max_steps=args.steps, threads=threads)
+        cpu = {"value": steps_c / el_c, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d main-loop steps of the %dx%d workload from the warmed-up state "
+                         "(C++ oracle, OpenMP, BiCGStab+ILU(0))" % (steps_c, args.n, args.n)}
+
+    if rank == 0:
+        total_ms = {kk: v[0] for kk, v in prof.items()}
+        line = {
+            "metric": METRIC, "value": ws * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded Gaussian blob (1e14 m^-3, sigma 1 mm) + 1% noise",
+            "config": {"workload": "2D Ar DC glow %dx%d, plain FP64 path" % (args.n, args.n),
+                       "dt": args.dt, "poisson_rtol": 1e-8, "species": 3,
+                       "rk_attempts": attempts, "cg_iters_per_step": iters / args.steps,
+                       "l2": "working set per step > 129 MB L2 (no flush needed)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": ws * args.steps / (ms_e2e * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": (state_bytes + 8 * args.steps) / args.steps,
+                    "d2h_bytes_per_step": (3 * state_bytes + 56 * args.steps) / args.steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_stage (RK-Merson stage, FP64)", "peak_kind": peak_kind,
+                         "stage_ms": stage_ms},
+            "kernel_ms_per_step": {kk: v / args.steps for kk, v in total_ms.items()},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    d.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--dt", default="adaptive", choices=("adaptive", "fixed"))
+    ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -45,6 +45,14 @@ def load_library():
     lib.fs_abi_version.restype = C.c_int32
     lib.fs_max_ne.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.fs_max_ne.restype = C.c_int
+    lib.fs_stream.argtypes = [C.c_void_p]
+    lib.fs_stream.restype = C.c_void_p
+    lib.fs_profile.argtypes = [C.c_void_p, C.c_int32]
+    lib.fs_profile.restype = C.c_int
+    lib.fs_profile_read.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]
+    lib.fs_profile_read.restype = C.c_int
+    lib.fs_launch_count.argtypes = [C.c_void_p]
+    lib.fs_launch_count.restype = C.c_int64
     _lib = lib
     return lib
 
@@ -203,6 +211,25 @@ class Discharge(Handle):
         self.set_time(0.0, cfg.dt0)
         if state is not None:
             self.upload(state)
+
+    PROF_CLASSES = ("stage", "assemble", "smooth", "transfer", "bottom", "cg", "coarsen", "control")
+
+    def stream_handle(self):
+        """cudaStream_t (as an int) that all of this context's work runs on."""
+        return self._lib.fs_stream(self.ctx)
+
+    def profile(self, enable=True):
+        self.check(self._lib.fs_profile(self.ctx, 1 if enable else 0))
+
+    def profile_read(self):
+        n = len(self.PROF_CLASSES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int64 * n)()
+        self.check(self._lib.fs_profile_read(self.ctx, ms, cnt, n))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_CLASSES)}
+
+    def launch_count(self):
+        return self._lib.fs_launch_count(self.ctx)
 
     def max_ne(self):
         v = C.c_double()

@@ -33,7 +33,48 @@ int fs_sync_ctrl(fs_ctx *c) {
     cudaError_t e = cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess && c->prof_on) fs_prof_drain(c);
     return fs_cuda_check(c, e, "stream");
+}
+
+void fs_prof_begin(fs_ctx *c, int cls) {
+    c->launches++;
+    if (!c->prof_on) return;
+    ProfPair p;
+    if (!c->prof_free.empty()) {
+        p = c->prof_free.back();
+        c->prof_free.pop_back();
+    } else {
+        cudaEventCreate(&p.a);
+        cudaEventCreate(&p.b);
+    }
+    p.cls = cls;
+    cudaEventRecord(p.a, c->stream);
+    c->prof_pending.push_back(p);
+}
+
+void fs_prof_end(fs_ctx *c) {
+    if (!c->prof_on || c->prof_pending.empty()) return;
+    cudaEventRecord(c->prof_pending.back().b, c->stream);
+}
+
+void fs_prof_drain(fs_ctx *c) {
+    for (ProfPair &p : c->prof_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            c->prof_ms[p.cls] += ms;
+            c->prof_n[p.cls] += 1;
+        }
+        c->prof_free.push_back(p);
+    }
+    c->prof_pending.clear();
+}
+
+void fs_prof_free(fs_ctx *c) {
+    for (ProfPair &p : c->prof_pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (ProfPair &p : c->prof_free) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    c->prof_pending.clear();
+    c->prof_free.clear();
 }
 
 namespace {
@@ -105,13 +146,16 @@ void free_ctx(fs_ctx *c) {
     cudaFree(c->d_types);
     cudaFree(c->d_tab);
     if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
+    fs_prof_free(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
 int set_dt_dev(fs_ctx *c, double dt) {
     c->dt = dt;
+    fs_prof_begin(c, PROF_OTHER);
     k_set_dt<<<1, 1, 0, c->stream>>>(c->d_ctrl, dt);
+    fs_prof_end(c);
     return fs_cuda_check(c, cudaGetLastError(), "set dt");
 }
 
@@ -440,6 +484,30 @@ int fs_get_stats(fs_ctx *c, fs_stats *out) {
     return FS_OK;
 }
 
+void *fs_stream(fs_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int64_t fs_launch_count(fs_ctx *c) { return c ? c->launches : -1; }
+
+int fs_profile(fs_ctx *c, int32_t enable) {
+    if (!c) return FS_ERR_INVALID;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) fs_prof_drain(c);
+    c->prof_on = enable != 0;
+    for (int i = 0; i < PROF_NCLASS; i++) { c->prof_ms[i] = 0.0; c->prof_n[i] = 0; }
+    return fs_cuda_check(c, e, "profile");
+}
+
+int fs_profile_read(fs_ctx *c, double *ms_out, int64_t *launches_out, int32_t n) {
+    if (!c || n < 0) return FS_ERR_INVALID;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) fs_prof_drain(c);
+    for (int i = 0; i < n && i < PROF_NCLASS; i++) {
+        if (ms_out) ms_out[i] = c->prof_ms[i];
+        if (launches_out) launches_out[i] = c->prof_n[i];
+    }
+    return fs_cuda_check(c, e, "profile_read");
+}
+
 // maxval(ne) over the whole module array, every level and the ghost ring
 // included (main.F90:131).
 int fs_max_ne(fs_ctx *c, double *out) {
@@ -448,6 +516,7 @@ int fs_max_ne(fs_ctx *c, double *out) {
     cudaError_t e = cudaMallocAsync((void **)&d, sizeof(double), c->stream);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "max_ne");
     const SpeciesBufs &b = c->sp[1];
+    c->launches++;
     k_max3<<<1, 1024, 0, c->stream>>>(b.buf[c->lev[0]], b.buf[c->lev[1]], b.buf[c->lev[2]], c->nx, c->ny,
                                        c->pitch, d);
     e = cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, c->stream);

@@ -81,6 +81,15 @@ struct MGLevel {
     double *rhs, *x, *res;
 };
 
+// Kernel classes timed by the optional per-launch event profiler.
+enum ProfClass { PROF_STAGE = 0, PROF_ASSEMBLE, PROF_SMOOTH, PROF_TRANSFER, PROF_BOTTOM, PROF_CG,
+                 PROF_COARSEN, PROF_OTHER, PROF_NCLASS };
+
+struct ProfPair {
+    cudaEvent_t a, b;
+    int cls;
+};
+
 struct fs_ctx {
     fs_config cfg;
     fs_constants k;
@@ -119,6 +128,13 @@ struct fs_ctx {
     double *d_cg_part;
     int cg_nblk;
 
+    // per-launch event profiler (off unless fs_profile enables it)
+    int prof_on;
+    int64_t launches;            // kernels launched by this context
+    std::vector<ProfPair> prof_pending, prof_free;
+    double prof_ms[PROF_NCLASS];
+    int64_t prof_n[PROF_NCLASS];
+
     // host mirrors of scalar state
     double t, dt;
     double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or;
@@ -141,3 +157,8 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
 // misc device helpers (fs_api.cu)
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
 int fs_sync_ctrl(fs_ctx *c);
+// profiler: bracket one launch; drained at every fs_sync_ctrl
+void fs_prof_begin(fs_ctx *c, int cls);
+void fs_prof_end(fs_ctx *c);
+void fs_prof_drain(fs_ctx *c);
+void fs_prof_free(fs_ctx *c);

@@ -22,6 +22,7 @@
 // All reductions are two-level and fixed-order: per-CTA partials, then the
 // last CTA to finish sums them in index order.
 #include <cstdio>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
@@ -126,6 +127,11 @@ __device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double
     double am = vm * dh / D;
     if (fabs(vm) < 1e-12) {
         df = 0.0;
+    } else if (fabs(am) < 0.05) {
+        // series of the same function near a = 0, where the closed form
+        // cancels catastrophically: (n1+n2)/2 + (n1-n2)(a/6 - a^3/180 + a^5/5040)
+        double dn = nl - nr, a2 = am * am;
+        df = 0.5 * (nl + nr) + dn * am * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
     } else {
         double ex = (Emi == E) ? exa : exp(-fabs(am));
         double one = 1.0 - ex;
@@ -666,34 +672,51 @@ static void vcycle(fs_ctx *c) {
     for (int l = 0; l < lb; l++) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
         dim3 g = grid2(f.nx, f.ny, b);
+        fs_prof_begin(c, PROF_SMOOTH);
         k_rb<<<g, b, 0, c->stream>>>(f, 0, 1);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_SMOOTH);
         k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+        fs_prof_end(c);
         for (int it = 1; it < nu; it++) {
+            fs_prof_begin(c, PROF_SMOOTH);
             k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+            fs_prof_end(c);
+            fs_prof_begin(c, PROF_SMOOTH);
             k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+            fs_prof_end(c);
         }
+        fs_prof_begin(c, PROF_TRANSFER);
         k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
     }
     BottomArgs ba;
     for (int l = 0; l < nl; l++) ba.L[l] = level_dev(c->mg[l]);
     ba.lb = lb;
     ba.nl = nl;
     ba.nu = nu;
+    fs_prof_begin(c, PROF_BOTTOM);
     k_bottom<<<1, BOTTOM_THREADS, 0, c->stream>>>(ba);
+    fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
         dim3 g = grid2(f.nx, f.ny, b);
+        fs_prof_begin(c, PROF_TRANSFER);
         k_prolong<<<g, b, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
+            fs_prof_begin(c, PROF_SMOOTH);
             k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+            fs_prof_end(c);
+            fs_prof_begin(c, PROF_SMOOTH);
             k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+            fs_prof_end(c);
         }
     }
 }
 
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
-    const int ns = c->cfg.nspecies;
-    (void)ns;
+    static const bool trace = getenv("FS_TRACE_CG") != nullptr;
     AsmArgs a;
     a.pp = c->pp;
     a.m = c->mesh;
@@ -710,15 +733,21 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.rhs = c->bs;   // scaled right-hand side D b
     a.dinv = c->dinv;
     // status bits of the assembly
-    cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);
+    cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);   // not a kernel
     dim3 g = grid2(c->nx, c->ny, dim3(LBX, LBY));
+    fs_prof_begin(c, PROF_ASSEMBLE);
     k_assemble<<<g, LNT, 0, c->stream>>>(a);
+    fs_prof_end(c);
     // coarse operators
     dim3 b2(16, 16);
     for (int l = 0; l + 1 < c->mg_nlev; l++) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        fs_prof_begin(c, PROF_COARSEN);
         k_coarsen<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_COARSEN);
         k_coarsen_diag<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
+        fs_prof_end(c);
     }
     // CG on M d = D b
     CgArgs ca;
@@ -729,7 +758,9 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
     dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
+    fs_prof_begin(c, PROF_CG);
     k_cg_init<<<gb, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
     int rc = fs_sync_ctrl(c);
     if (rc) return rc;
     if (c->h_ctrl->status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
@@ -742,13 +773,25 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     }
     while (!ok && it < c->cfg.lapl_maxit) {
         vcycle(c);
+        fs_prof_begin(c, PROF_CG);
         k_cg_rz<<<gb, 256, 0, c->stream>>>(ca);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_CG);
         k_cg_p<<<gb, 256, 0, c->stream>>>(ca);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_CG);
         k_cg_q<<<gb, 256, 0, c->stream>>>(ca);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_CG);
         k_cg_xr<<<gb, 256, 0, c->stream>>>(ca);
+        fs_prof_end(c);
         rc = fs_sync_ctrl(c);
         if (rc) return rc;
         it = c->h_ctrl->cg_iters;
+        if (trace)
+            fprintf(stderr, "cg %d relres %.3e rz %.3e pq %.3e alpha %.3e beta %.3e fail %d\n", it,
+                    c->h_ctrl->relres, c->h_ctrl->rz, c->h_ctrl->pq, c->h_ctrl->alpha, c->h_ctrl->beta,
+                    c->h_ctrl->cg_fail);
         if (c->h_ctrl->cg_fail) break;
         ok = c->h_ctrl->cg_done != 0;
     }
@@ -759,6 +802,7 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
         return FS_OK;
     }
     *lerr = 0;
+    c->launches++;
     k_phi_update<<<4 * 152, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels");

@@ -223,10 +223,12 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
         if (gj == 0 && tt == -1) {
             eu = 0.0;
+        } else if (gj == 0 && tt == -2) {
+            // ptclEqn has no lower y electrode: zero flux, face field kept (ptcl_lib.F90:287-367)
         } else if (gj == ny && tb == 1) {
             eu = 0.0;
-        } else if ((gj == 0 && tt == -2) || (gj == ny && tb == 2)) {
-            const bool low = gj == 0;
+        } else if (gj == ny && tb == 2) {
+            const bool low = false;
             const int lc = low ? ly + 1 : ly;
             double te = s_te[lc][lx], ni = s_n[0][lc][lx], ne = s_n[1][lc][lx], nt = s_n[2][lc][lx];
             double phg = low ? s_ph[ly][lx] : s_ph[ly + 1][lx];
@@ -454,6 +456,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     int in1 = L2;
     int attempts = 0;
 
+    c->launches++;
     k_reset_step<<<(2 * (c->ny + 2) + 255) / 256, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, 2 * (c->ny + 2));
     for (;;) {
         attempts++;
@@ -481,11 +484,14 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
                 a.k4[s] = b.k[2];
                 a.kout[s] = stg == 1 ? b.k[0] : stg == 3 ? b.k[1] : stg == 4 ? b.k[2] : nullptr;
             }
+            fs_prof_begin(c, PROF_STAGE);
             launch_stage(c, a);
-            if (stg == 1)
+            fs_prof_end(c);
+            if (stg == 1 && ++c->launches)
                 k_circ_ghost<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
                     c->ph, c->mesh.tx, c->mesh.r, c->nx, c->ny, c->pitch, c->cfg.ew, c->Vsrc);
         }
+        c->launches++;
         k_controller<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_part, c->nblk_stage, ns, c->d_rows,
                                                c->ny, c->cfg.adaptive, c->cfg.dt_min);
         int rc = fs_sync_ctrl(c);

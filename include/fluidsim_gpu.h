@@ -200,8 +200,26 @@ int fs_run(fs_ctx *ctx, int32_t nsteps, fs_stats *stats_out);
 
 int fs_get_stats(fs_ctx *ctx, fs_stats *out);
 
-/* maxval(ne(:,:,1)) over the interior (main.F90:131). */
+/* maxval(ne) over the whole module array -- every level, ghosts included
+ * (main.F90:131). */
 int fs_max_ne(fs_ctx *ctx, double *out);
+
+/* ---- diagnostics with no counterpart in the reference ------------------- */
+
+/* The cudaStream_t all of ctx's work is issued on (for CUDA-event timing). */
+void *fs_stream(fs_ctx *ctx);
+
+/* Per-launch CUDA-event timing of kernel classes: 0 RK stage, 1 Poisson
+ * assembly, 2 multigrid smoothing, 3 multigrid transfer, 4 bottom solve,
+ * 5 CG vector kernels, 6 coarse operators, 7 control kernels.  fs_profile(ctx, 1) resets and
+ * enables it; fs_profile_read returns total milliseconds and launch counts
+ * of the first n classes. */
+#define FS_PROF_NCLASS 8   /* class 7: small control kernels */
+int fs_profile(fs_ctx *ctx, int32_t enable);
+int fs_profile_read(fs_ctx *ctx, double *ms_out, int64_t *launches_out, int32_t n);
+
+/* Number of kernels ctx has launched since fs_create. */
+int64_t fs_launch_count(fs_ctx *ctx);
 
 #ifdef __cplusplus
 }

@@ -361,6 +361,15 @@ inline double dfdph(double E_pl, double E_mi, int q, double mu, double D, double
     double df;
     if (std::fabs(v_mi) < tol) {
         df = 0.0;
+    } else if (std::fabs(a_mi) < 0.05) {
+        // Same function as below, evaluated by its series: with the SG flux
+        // F = (D/dx)(B(-a) n1 - B(a) n2), B(x) = x/(e^x - 1), dF/dv =
+        // (n1+n2)/2 + (n1-n2)(a/6 - a^3/180 + a^5/5040) + O(a^7).  The closed
+        // form cancels here (two terms ~ (n1-n2)/a leave ~(n1+n2)/2 with an
+        // error ~2e-16 |n1-n2| / a^2, all digits lost for |a| < 1e-8), so the
+        // reference's own value is rounding noise near a = 0.
+        double dn = n1 - n2, a2 = a_mi * a_mi;
+        df = 0.5 * (n1 + n2) + dn * a_mi * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
     } else if (a_mi > 0) {
         double ex = std::exp(-a_mi);
         df = (n1 - n2 * ex) / (1.0 - ex) + v_mi * ex * (n2 - n1) / ((1.0 - ex) * (1.0 - ex)) * dx / D;

@@ -25,7 +25,7 @@ def _pair(built, n, ny=None, **kw):
 
 @pytest.mark.parametrize("n,ny", [(24, 20), (64, 64), (37, 29)])
 def test_one_step_fixed_dt(built, n, ny):
-    cfg, k, gpu, ref = _pair(built, n, ny, adaptive=0, lapl_rtol=1e-13)
+    cfg, k, gpu, ref = _pair(built, n, ny, adaptive=0, lapl_rtol=1e-14)
     for s in range(3):
         gi, ri = gpu.step(), ref.step()
         assert gi["lerr"] == 0 and ri["lerr"] == 0
@@ -34,7 +34,7 @@ def test_one_step_fixed_dt(built, n, ny):
 
 
 def test_adaptive_steps(built):
-    cfg, k, gpu, ref = _pair(built, 32, 32, lapl_rtol=1e-13)
+    cfg, k, gpu, ref = _pair(built, 32, 32, lapl_rtol=1e-14)
     for s in range(8):
         gi, ri = gpu.step(), ref.step()
         if s >= 2:

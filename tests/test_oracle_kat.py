@@ -53,7 +53,7 @@ def test_flux_clamp():
     assert flux(E, dh, 1, mu, D, nl, nr) == pytest.approx(want, rel=1e-14)
 
 
-@pytest.mark.parametrize("E", [0.3, -2.0, 17.0, -60.0])
+@pytest.mark.parametrize("E", [0.3, -2.0, 17.0, -60.0, 1e-4, -3e-3, 4.7e-3])
 @pytest.mark.parametrize("q", [1, -1])
 def test_dfdph_is_flux_derivative(E, q):
     mu, D, dx, n1, n2 = 1.7, 0.8, 0.6, 3.0, 1.2
@@ -62,6 +62,18 @@ def test_dfdph_is_flux_derivative(E, q):
     # d flux / dE = q mu d flux / dv
     got = q * mu * oracle.dfdph(E, E, q, mu, D, dx, n1, n2)
     assert got == pytest.approx(num, rel=1e-6)
+
+
+def test_dfdph_continuous_across_series_branch():
+    # |a| = 0.05 separates the series from the closed form; both sides agree
+    mu, D, dx, n1, n2 = 2.0, 1.0, 0.5, 3.0, 1.0
+    E0 = 0.05 * D / (mu * dx)
+    lo = oracle.dfdph(E0 * (1 - 1e-13), E0 * (1 - 1e-13), 1, mu, D, dx, n1, n2)
+    hi = oracle.dfdph(E0 * (1 + 1e-13), E0 * (1 + 1e-13), 1, mu, D, dx, n1, n2)
+    assert lo == pytest.approx(hi, rel=1e-12)
+    # and the a -> 0 limit is the mean density
+    tiny = oracle.dfdph(1e-11, 1e-11, 1, mu, D, dx, n1, n2)
+    assert tiny == pytest.approx(0.5 * (n1 + n2), rel=1e-10)
 
 
 def _vacuum_cfg(n=6, **kw):
