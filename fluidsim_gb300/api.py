@@ -218,8 +218,16 @@ class Discharge(Handle):
         """cudaStream_t (as an int) that all of this context's work runs on."""
         return self._lib.fs_stream(self.ctx)
 
-    def profile(self, enable=True):
-        self.check(self._lib.fs_profile(self.ctx, 1 if enable else 0))
+    def profile(self, classes=None):
+        """Time the given kernel classes (names from PROF_CLASSES; None = all,
+        [] = off) with CUDA events around each launch."""
+        if classes is None:
+            mask = (1 << len(self.PROF_CLASSES)) - 1
+        else:
+            mask = 0
+            for c in classes:
+                mask |= 1 << self.PROF_CLASSES.index(c)
+        self.check(self._lib.fs_profile(self.ctx, mask))
 
     def profile_read(self):
         n = len(self.PROF_CLASSES)

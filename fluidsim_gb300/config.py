@@ -79,8 +79,14 @@ def glow(n=64, **kw):
     cathode at x = 0 at -250 V against a grounded anode, Neumann side walls,
     gamma = 0.07, three species, 200-point rate table 0.1-50 eV with Arrhenius
     ionisation 2.3e-14 exp(-15.8/eps) m^3/s, geometric 1.05 mesh toward both
-    electrodes, RK-Merson rel tol 1e-4, Poisson to 1e-10."""
-    cfg = RunConfig(nx=n, ny=n)
+    electrodes, RK-Merson rel tol 1e-4, Poisson to 1e-10.
+
+    The first dt is 1e-12 s on grids up to 64x64 and shrinks as 64/n above:
+    electrons drift ~13 um per ps in the initial field (mue ~ 530 m^2/Vs at
+    1 eV, 1 Torr), so 1e-12 s exceeds the drift CFL limit of the smallest
+    cell above ~128x128 and the first RK attempt overflows before the
+    controller can react (the reference does the same)."""
+    cfg = RunConfig(nx=n, ny=n, dt0=1e-12 / T0 * min(1.0, 64.0 / n))
     return cfg.replace(**kw)
 
 

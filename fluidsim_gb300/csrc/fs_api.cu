@@ -39,7 +39,7 @@ int fs_sync_ctrl(fs_ctx *c) {
 
 void fs_prof_begin(fs_ctx *c, int cls) {
     c->launches++;
-    if (!c->prof_on) return;
+    if (!(c->prof_on & (1 << cls))) return;
     ProfPair p;
     if (!c->prof_free.empty()) {
         p = c->prof_free.back();
@@ -49,13 +49,15 @@ void fs_prof_begin(fs_ctx *c, int cls) {
         cudaEventCreate(&p.b);
     }
     p.cls = cls;
+    p.closed = 0;
     cudaEventRecord(p.a, c->stream);
     c->prof_pending.push_back(p);
 }
 
 void fs_prof_end(fs_ctx *c) {
-    if (!c->prof_on || c->prof_pending.empty()) return;
+    if (!c->prof_on || c->prof_pending.empty() || c->prof_pending.back().closed) return;
     cudaEventRecord(c->prof_pending.back().b, c->stream);
+    c->prof_pending.back().closed = 1;
 }
 
 void fs_prof_drain(fs_ctx *c) {
@@ -141,6 +143,9 @@ void free_ctx(fs_ctx *c) {
     cudaFree(c->ph_mi);
     cudaFree(c->d_part);
     cudaFree(c->d_rows);
+    double *faces[] = {c->fx_e, c->fx_cl, c->fx_cr, c->fy_e, c->fy_cl, c->fy_cr,
+                       c->fx_dl, c->fx_dr, c->fy_dl, c->fy_dr};
+    for (double *f : faces) cudaFree(f);
     cudaFree(c->d_ctrl);
     cudaFree(c->d_mesh_blob);
     cudaFree(c->d_types);
@@ -364,6 +369,7 @@ int fs_upload_state(fs_ctx *c, const double *ni, const double *ne, const double 
         else { c->lev[0] = 0; c->lev[1] = 1; c->lev[2] = 2; }
     }
     if (ph && e == cudaSuccess) {
+        c->faces_valid = 0;
         e = cudaMemcpy2DAsync(c->ph, dp, ph, hp, w, rows, cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(c->ph_mi, c->ph, c->field_elems * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
@@ -492,7 +498,7 @@ int fs_profile(fs_ctx *c, int32_t enable) {
     if (!c) return FS_ERR_INVALID;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) fs_prof_drain(c);
-    c->prof_on = enable != 0;
+    c->prof_on = enable & ((1 << PROF_NCLASS) - 1);
     for (int i = 0; i < PROF_NCLASS; i++) { c->prof_ms[i] = 0.0; c->prof_n[i] = 0; }
     return fs_cuda_check(c, e, "profile");
 }

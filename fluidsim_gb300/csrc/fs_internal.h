@@ -88,6 +88,7 @@ enum ProfClass { PROF_STAGE = 0, PROF_ASSEMBLE, PROF_SMOOTH, PROF_TRANSFER, PROF
 struct ProfPair {
     cudaEvent_t a, b;
     int cls;
+    int closed;
 };
 
 struct fs_ctx {
@@ -118,17 +119,30 @@ struct fs_ctx {
     double *d_part;              // per-block partial sums (4 species)
     int nblk_stage;              // blocks of one stage launch
     double *d_rows;              // per-row current contributions (2*(ny+2))
+    // per-step face data (phi is frozen during ptcl_step): field E and the
+    // ion SG flux coefficients, flux = cl*n_left - cr*n_right, for the x face
+    // east of node (gi,gj) and the y face north of it
+    // and of dFdPh, dF/dv = dl*n_left + dr*n_right (lapl_lib.F90:611-636)
+    double *fx_e, *fx_cl, *fx_cr, *fy_e, *fy_cl, *fy_cr;
+    double *fx_dl, *fx_dr, *fy_dl, *fy_dr;
+    int faces_valid;             // face data matches the current phi
     Ctrl *d_ctrl;
     Ctrl *h_ctrl;                // pinned mirror
 
     // Poisson
     MGLevel mg[FS_MG_MAX_LEVELS];
     int mg_nlev;
+    int mg_fused;                // coarse launched levels use the fused kernels
     double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D
     double *d_cg_part;
     int cg_nblk;
+    // CG loop as a CUDA graph with a conditional WHILE node (built on first use)
+    cudaGraph_t cg_graph;
+    cudaGraphExec_t cg_exec;
+    int cg_graph_built;
+    int cg_body_kernels;         // kernels per loop iteration (launch accounting)
 
-    // per-launch event profiler (off unless fs_profile enables it)
+    // per-launch event profiler: bitmask of the timed kernel classes (0 = off)
     int prof_on;
     int64_t launches;            // kernels launched by this context
     std::vector<ProfPair> prof_pending, prof_free;
@@ -150,6 +164,7 @@ void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<doub
 // particle kernels (fs_ptcl.cu)
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts);
 int fs_ptcl_alloc(fs_ctx *c);
+void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
 void fs_lapl_free(fs_ctx *c);

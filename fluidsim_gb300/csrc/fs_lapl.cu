@@ -23,6 +23,7 @@
 // last CTA to finish sums them in index order.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
@@ -85,6 +86,7 @@ struct AsmArgs {
     MeshDev m;
     const double *tab;
     const double *ni, *ne, *nt, *ph, *phm;
+    const double *fx_e, *fx_cl, *fx_cr, *fx_dl, *fx_dr, *fy_e, *fy_cl, *fy_cr, *fy_dl, *fy_dr;
     const Ctrl *ctrl;
     Ctrl *ctrl_w;
     double *mc, *ce, *cn, *extra, *inv_mc, *rhs, *dinv;
@@ -118,6 +120,9 @@ __device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double
     double exa = exp(-fabs(arg));
     if (fabs((double)q * E) < tolf) {
         flux = D * (nl - nr) / dh;
+    } else if (fabs(arg) < 1e-2) {   // Bernoulli form near a = 0
+        double a2 = arg * arg;
+        flux = D * ((nl - nr) + 0.5 * arg * (nl + nr) + a2 * (1.0 / 12.0 - a2 / 720.0) * (nl - nr)) / dh;
     } else {
         double ex = fabs(arg) > 100.0 ? exp(-100.0) : exa;
         if (arg > 0) flux = v * (nl - nr * ex) / (1.0 - ex);
@@ -139,6 +144,37 @@ __device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double
         else df = (nr - nl * ex) / one + vm * ex * (nr - nl) / (one * one) * dh / D;
     }
     if (isnan(df)) st |= FS_ST_DFDPH_NAN;
+}
+
+// Electron flux of laplEqn and dFdPh of laplJ on one face when E_mi == E (the
+// interior faces: ph_mi equals ph there), sharing one exponential.
+__device__ __forceinline__ void elec_face(double E, double dh, double idh, double mue, double De,
+                                          double nl, double nr, double e100, double &flux,
+                                          double &df) {
+    const double tolf = 9.9999999600419720025e-13;
+    double v = -mue * E;
+    double arg = v * dh / De;
+    double aa = fabs(arg);
+    double ex = aa >= 1e-2 ? exp(-aa) : 0.0;
+    if (fabs(E) < tolf) {
+        flux = De * (nl - nr) * idh;
+    } else if (aa < 1e-2) {
+        double a2 = arg * arg;
+        flux = De * ((nl - nr) + 0.5 * arg * (nl + nr) + a2 * (1.0 / 12.0 - a2 / 720.0) * (nl - nr)) * idh;
+    } else {
+        double exf = aa > 100.0 ? e100 : ex;
+        double i1 = 1.0 / (1.0 - exf);
+        flux = arg > 0 ? v * (nl - nr * exf) * i1 : v * (nr - nl * exf) * i1;
+    }
+    if (fabs(v) < 1e-12) {
+        df = 0.0;
+    } else if (aa < 0.05) {
+        double a2 = arg * arg;
+        df = 0.5 * (nl + nr) + (nl - nr) * arg * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
+    } else {
+        double i1 = 1.0 / (1.0 - ex), t = arg * ex * (nr - nl) * i1 * i1;
+        df = (arg > 0 ? (nl - nr * ex) : (nr - nl * ex)) * i1 + t;
+    }
 }
 
 __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
@@ -188,9 +224,9 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         int gi = gx0 - 1 + c, gj = gy0 + r;
         if (gj > ny || gi > nx) continue;
         int lx = c, ly = r + 1;
-        double dh = a.m.dx[gi];
-        double E = -(s_ph[ly][lx + 1] - s_ph[ly][lx]) / dh;
-        double Emi = -(s_pm[ly][lx + 1] - s_pm[ly][lx]) / dh;
+        const size_t of = (size_t)gj * P + gi;
+        double dh = a.m.dx[gi], idh = a.m.inv_dx[gi];
+        double E = a.fx_e[of];
         int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;
         int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;
         double fi = 0, fe = 0, eu = E, cf = 0;
@@ -206,9 +242,9 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
             fi = (1.0 - aa) * pp.mui * E * ni - 2.5e-1 * pp.vi * ni;
             fe = -(aa * mue * E * ne) - 2.5e-1 * ve * ne - pp.gam * fi;
             int ac = (s_ph[ly][lx] > s_ph[ly][lc]) ? 1 : 0;
-            double dfi = (double)(1 - ac) * pp.mui * ni / dh;
-            double dfe = -((double)ac * mue * ne / dh) - pp.gam * dfi;
-            cf = 1.0 / dh + dt * (dfi - dfe);         // Dirichlet conductance of the row
+            double dfi = (double)(1 - ac) * pp.mui * ni * idh;
+            double dfe = -((double)ac * mue * ne * idh) - pp.gam * dfi;
+            cf = idh + dt * (dfi - dfe);              // Dirichlet conductance of the row
         } else if (gi == nx && tl == 2) {          // anode-side electrode row
             int lc = lx;
             double te = s_te[ly][lc], ni = s_ni[ly][lc], ne = s_ne[ly][lc], mue = s_mu[ly][lc];
@@ -217,18 +253,27 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
             fi = (1.0 - aa) * pp.mui * E * ni + 2.5e-1 * pp.vi * ni;
             fe = -(aa * mue * E * ne) + 2.5e-1 * ve * ne - pp.gam * fi;
             int ac = (s_ph[ly][lx + 1] > s_ph[ly][lc]) ? 1 : 0;
-            double dfi = (double)(ac - 1) * pp.mui * ni / dh;
-            double dfe = (double)ac * mue * ne / dh - pp.gam * dfi;
-            cf = 1.0 / dh - dt * (dfi - dfe);
+            double dfi = (double)(ac - 1) * pp.mui * ni * idh;
+            double dfe = (double)ac * mue * ne * idh - pp.gam * dfi;
+            cf = idh - dt * (dfi - dfe);
         } else {
             double mue = 5e-1 * (s_mu[ly][lx] + s_mu[ly][lx + 1]);
             double De = 5e-1 * (s_de[ly][lx] + s_de[ly][lx + 1]);
+            const double nil = s_ni[ly][lx], nir = s_ni[ly][lx + 1], nel = s_ne[ly][lx], ner = s_ne[ly][lx + 1];
             double dFi, dFe;
-            sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, s_ni[ly][lx], s_ni[ly][lx + 1], fi, dFi, st);
-            sg_and_dfdph(-1, E, Emi, dh, mue, De, s_ne[ly][lx], s_ne[ly][lx + 1], fe, dFe, st);
-            double dfi_mi = pp.mui / dh * dFi;
-            double dfe_mi = -(mue / dh * dFe);
-            cf = 1.0 / dh + dt * (dfi_mi - dfe_mi);
+            if (s_pm[ly][lx] == s_ph[ly][lx] && s_pm[ly][lx + 1] == s_ph[ly][lx + 1]) {
+                fi = a.fx_cl[of] * nil - a.fx_cr[of] * nir;
+                dFi = a.fx_dl[of] * nil + a.fx_dr[of] * nir;
+                elec_face(E, dh, idh, mue, De, nel, ner, pp.e100, fe, dFe);
+            } else {
+                double Emi = -(s_pm[ly][lx + 1] - s_pm[ly][lx]) / dh;
+                sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, nil, nir, fi, dFi, st);
+                sg_and_dfdph(-1, E, Emi, dh, mue, De, nel, ner, fe, dFe, st);
+            }
+            if (isnan(dFi) || isnan(dFe)) st |= FS_ST_DFDPH_NAN;
+            double dfi_mi = pp.mui * idh * dFi;
+            double dfe_mi = -(mue * idh * dFe);
+            cf = idh + dt * (dfi_mi - dfe_mi);
         }
         s_xfi[r][c] = fi; s_xfe[r][c] = fe; s_xe[r][c] = eu; s_xc[r][c] = cf;
     }
@@ -238,9 +283,9 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         int gi = gx0 + c, gj = gy0 - 1 + r;
         if (gi > nx || gj > ny) continue;
         int lx = c + 1, ly = r;
-        double dh = a.m.dy[gj];
-        double E = -(s_ph[ly + 1][lx] - s_ph[ly][lx]) / dh;
-        double Emi = -(s_pm[ly + 1][lx] - s_pm[ly][lx]) / dh;
+        const size_t of = (size_t)gj * P + gi;
+        double dh = a.m.dy[gj], idh = a.m.inv_dy[gj];
+        double E = a.fy_e[of];
         int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
         int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
         double fi = 0, fe = 0, eu = E, cf = 0;
@@ -270,12 +315,21 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         } else {
             double mue = 5e-1 * (s_mu[ly][lx] + s_mu[ly + 1][lx]);
             double De = 5e-1 * (s_de[ly][lx] + s_de[ly + 1][lx]);
+            const double nil = s_ni[ly][lx], nir = s_ni[ly + 1][lx], nel = s_ne[ly][lx], ner = s_ne[ly + 1][lx];
             double dFi, dFe;
-            sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, s_ni[ly][lx], s_ni[ly + 1][lx], fi, dFi, st);
-            sg_and_dfdph(-1, E, Emi, dh, mue, De, s_ne[ly][lx], s_ne[ly + 1][lx], fe, dFe, st);
-            double dfi_mi = pp.mui / dh * dFi;
-            double dfe_mi = -(mue / dh * dFe);
-            cf = 1.0 / dh + dt * (dfi_mi - dfe_mi);
+            if (s_pm[ly][lx] == s_ph[ly][lx] && s_pm[ly + 1][lx] == s_ph[ly + 1][lx]) {
+                fi = a.fy_cl[of] * nil - a.fy_cr[of] * nir;
+                dFi = a.fy_dl[of] * nil + a.fy_dr[of] * nir;
+                elec_face(E, dh, idh, mue, De, nel, ner, pp.e100, fe, dFe);
+            } else {
+                double Emi = -(s_pm[ly + 1][lx] - s_pm[ly][lx]) / dh;
+                sg_and_dfdph(1, E, Emi, dh, pp.mui, pp.Di, nil, nir, fi, dFi, st);
+                sg_and_dfdph(-1, E, Emi, dh, mue, De, nel, ner, fe, dFe, st);
+            }
+            if (isnan(dFi) || isnan(dFe)) st |= FS_ST_DFDPH_NAN;
+            double dfi_mi = pp.mui * idh * dFi;
+            double dfe_mi = -(mue * idh * dFe);
+            cf = idh + dt * (dfi_mi - dfe_mi);
         }
         s_yfi[r][c] = fi; s_yfe[r][c] = fe; s_ye[r][c] = eu; s_yc[r][c] = cf;
     }
@@ -285,24 +339,25 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
     if (gi <= nx && gj <= ny) {
         const size_t o = (size_t)gj * P + gi;
         const double dlx = a.m.dlx[gi - 1], dly = a.m.dly[gj - 1];
+        const double idlx = a.m.inv_dlx[gi - 1], idly = a.m.inv_dly[gj - 1];
         const int tx = a.m.tx[(gj - 1) * nx + gi - 1], ty = a.m.ty[(gj - 1) * nx + gi - 1];
         // cylindrical weights: r(j) of the row, face radii of the y faces
         const double wr = pp.cyl ? a.m.r[gj] : 1.0;
         const double wn = pp.cyl ? (a.m.r[gj + 1] + a.m.r[gj]) / 2.0 : 1.0;
         const double ws = pp.cyl ? (a.m.r[gj] + a.m.r[gj - 1]) / 2.0 : 1.0;
         // b of laplEqn (lapl_lib.F90:250-375)
-        double dfdx = -(s_xe[ly][lx + 1] - s_xe[ly][lx]) / dlx;
-        double dflxe_x = (s_xfe[ly][lx + 1] - s_xfe[ly][lx]) / dlx;
-        double dflxi_x = (s_xfi[ly][lx + 1] - s_xfi[ly][lx]) / dlx;
+        double dfdx = -(s_xe[ly][lx + 1] - s_xe[ly][lx]) * idlx;
+        double dflxe_x = (s_xfe[ly][lx + 1] - s_xfe[ly][lx]) * idlx;
+        double dflxi_x = (s_xfi[ly][lx + 1] - s_xfi[ly][lx]) * idlx;
         double dfdy, dflxi_y, dflxe_y;
         if (pp.cyl) {
             dfdy = -(s_ye[ly + 1][lx] * wn - s_ye[ly][lx] * ws) / dly / wr;
             dflxi_y = (s_yfi[ly + 1][lx] * wn - s_yfi[ly][lx] * ws) / dly / wr;
             dflxe_y = (s_yfe[ly + 1][lx] * wn - s_yfe[ly][lx] * ws) / dly / wr;
         } else {
-            dfdy = -(s_ye[ly + 1][lx] - s_ye[ly][lx]) / dly;
-            dflxi_y = (s_yfi[ly + 1][lx] - s_yfi[ly][lx]) / dly;
-            dflxe_y = (s_yfe[ly + 1][lx] - s_yfe[ly][lx]) / dly;
+            dfdy = -(s_ye[ly + 1][lx] - s_ye[ly][lx]) * idly;
+            dflxi_y = (s_yfi[ly + 1][lx] - s_yfi[ly][lx]) * idly;
+            dflxe_y = (s_yfe[ly + 1][lx] - s_yfe[ly][lx]) * idly;
         }
         double b = dfdx + dfdy + s_ni[ly + 1][lx + 1] - s_ne[ly + 1][lx + 1]
                  - dt * (dflxi_x + dflxi_y - dflxe_x - dflxe_y);
@@ -434,6 +489,117 @@ __global__ void k_prolong(const LevelDev f, const LevelDev c) {
     f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
 }
 
+// ---------------------------------------------- fused (temporally blocked) levels
+// One CTA owns an MTX x MTY tile of a level plus a halo of 2*nu nodes held in
+// shared memory.  Down: nu red-black sweeps from x = 0, the residual and its
+// 2x2 aggregate sums (the coarse right-hand side) in one launch.  Up: the
+// coarse correction and nu black-red sweeps in one launch.  With x = 0 the
+// first sweep needs no neighbours, and each later sweep updates a region one
+// ring smaller, so after 2*nu sweeps the tile (and, going down, its first
+// ring) holds exactly the values the unfused sweeps produce.
+#define MTX 32
+#define MTY 16
+
+template <typename T>
+struct LvT {
+    int nx, ny, P;
+    const T *mc, *ce, *cn, *inv_mc;
+    T *rhs, *x;
+};
+
+template <typename T, int NU>
+__global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c) {
+    constexpr int H = 2 * NU, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *smc = simc + W, *sce = smc + W,
+      *scn = sce + W, *sr = scn + W;
+    const int gx0 = blockIdx.x * MTX + 1, gy0 = blockIdx.y * MTY + 1;
+    for (int q = threadIdx.x; q < W; q += blockDim.x) {
+        const int lx = q % WX, ly = q / WX, gi = gx0 - H + lx, gj = gy0 - H + ly;
+        const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
+        const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
+        const size_t o = (size_t)gj * f.P + gi;
+        sx[q] = T(0);
+        srhs[q] = in ? f.rhs[o] : T(0);
+        simc[q] = in ? f.inv_mc[o] : T(0);
+        smc[q] = in ? f.mc[o] : T(0);
+        sce[q] = arr ? f.ce[o] : T(0);
+        scn[q] = arr ? f.cn[o] : T(0);
+    }
+    __syncthreads();
+    for (int s = 0; s < 2 * NU; s++) {
+        const int color = s & 1, lo = s, hx = WX - 1 - s, hy = WY - 1 - s;
+        const int nxr = hx - lo + 1, n = nxr * (hy - lo + 1);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int lx = lo + q % nxr, ly = lo + q / nxr;
+            const int gi = gx0 - H + lx, gj = gy0 - H + ly;
+            if (((gi + gj) & 1) != color) continue;
+            const int k = ly * WX + lx;
+            if (s == 0) sx[k] = srhs[k] * simc[k];
+            else sx[k] = (srhs[k] + sce[k] * sx[k + 1] + sce[k - 1] * sx[k - 1] + scn[k] * sx[k + WX]
+                          + scn[k - WX] * sx[k - WX]) * simc[k];
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
+        const int tx = q % MTX, ty = q / MTX, lx = H + tx, ly = H + ty;
+        const int gi = gx0 + tx, gj = gy0 + ty;
+        const int k = ly * WX + lx;
+        T r = T(0);
+        if (gi <= f.nx && gj <= f.ny) {
+            r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
+                           - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
+            f.x[(size_t)gj * f.P + gi] = sx[k];
+        }
+        sr[q] = r;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < (MTX / 2) * (MTY / 2); q += blockDim.x) {
+        const int ci = q % (MTX / 2), cj = q / (MTX / 2);
+        const int I = (gx0 - 1) / 2 + 1 + ci, J = (gy0 - 1) / 2 + 1 + cj;
+        if (I > c.nx || J > c.ny) continue;
+        const int t0 = (2 * cj) * MTX + 2 * ci;
+        c.rhs[(size_t)J * c.P + I] = sr[t0] + sr[t0 + 1] + sr[t0 + MTX] + sr[t0 + MTX + 1];
+    }
+}
+
+template <typename T, int NU>
+__global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
+    constexpr int H = 2 * NU, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *sce = simc + W, *scn = sce + W;
+    const int gx0 = blockIdx.x * MTX + 1, gy0 = blockIdx.y * MTY + 1;
+    for (int q = threadIdx.x; q < W; q += blockDim.x) {
+        const int lx = q % WX, ly = q / WX, gi = gx0 - H + lx, gj = gy0 - H + ly;
+        const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
+        const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
+        const size_t o = (size_t)gj * f.P + gi;
+        sx[q] = in ? f.x[o] + c.x[(size_t)((gj + 1) / 2) * c.P + (gi + 1) / 2] : T(0);
+        srhs[q] = in ? f.rhs[o] : T(0);
+        simc[q] = in ? f.inv_mc[o] : T(0);
+        sce[q] = arr ? f.ce[o] : T(0);
+        scn[q] = arr ? f.cn[o] : T(0);
+    }
+    __syncthreads();
+    for (int s = 0; s < 2 * NU; s++) {
+        const int color = (s & 1) ? 0 : 1, lo = s + 1, hx = WX - 2 - s, hy = WY - 2 - s;
+        const int nxr = hx - lo + 1, n = nxr * (hy - lo + 1);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int lx = lo + q % nxr, ly = lo + q / nxr;
+            const int gi = gx0 - H + lx, gj = gy0 - H + ly;
+            if (((gi + gj) & 1) != color) continue;
+            const int k = ly * WX + lx;
+            sx[k] = (srhs[k] + sce[k] * sx[k + 1] + sce[k - 1] * sx[k - 1] + scn[k] * sx[k + WX]
+                     + scn[k - WX] * sx[k - WX]) * simc[k];
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
+        const int tx = q % MTX, ty = q / MTX, gi = gx0 + tx, gj = gy0 + ty;
+        if (gi <= f.nx && gj <= f.ny) f.x[(size_t)gj * f.P + gi] = sx[(H + ty) * WX + H + tx];
+    }
+}
+
 // V-cycle over levels [lb, nl) inside one CTA (levels of at most 32x32 nodes).
 struct BottomArgs {
     LevelDev L[FS_MG_MAX_LEVELS];
@@ -465,13 +631,15 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs a) {
         }
         __syncthreads();
     }
-    {   // coarsest level: symmetric sweeps to convergence (it has very few nodes)
+    {   // coarsest level: a single node is solved exactly by one red sweep;
+        // otherwise symmetric sweeps, the palindrome (RB)^10 (BR)^10
         const LevelDev &c = a.L[a.nl - 1];
-        // palindromic sweep sequence (RB)^10 (BR)^10 keeps the cycle symmetric
         sweep(c, 0, 1);
-        sweep(c, 1, 0);
-        for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
-        for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+        if (c.nx * c.ny > 1) {
+            sweep(c, 1, 0);
+            for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
+            for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+        }
     }
     for (int l = a.nl - 2; l >= a.lb; l--) {
         const LevelDev &f = a.L[l], &c = a.L[l + 1];
@@ -491,6 +659,9 @@ struct CgArgs {
     const double *mc, *ce, *cn;
     Ctrl *ctrl;
     double rtol;
+    int maxit;
+    int use_cond;                          // loop runs under a conditional WHILE node
+    cudaGraphConditionalHandle cond;
 };
 
 __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
@@ -501,6 +672,7 @@ __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
         a.x[o] = 0.0;
         a.r[o] = a.rhs[o];
         a.p[o] = 0.0;
+        a.q[o] = 0.0;
         double u = a.rhs[o] * a.dinv[o];
         v = u * u;
     }
@@ -533,29 +705,51 @@ __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
     }
 }
 
-// p = z + beta p ; q = M p needs p at the neighbours: two kernels
-__global__ void k_cg_p(const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
-    if (I > a.nx || J > a.ny) return;
-    size_t o = (size_t)J * a.P + I;
-    a.p[o] = a.z[o] + a.ctrl->beta * a.p[o];
-}
-
-__global__ void __launch_bounds__(256) k_cg_q(const CgArgs a) {
+// Last half sweep of the fine level (red, after the black one) fused with
+// rz = r.z over all nodes and beta = rz/rz_old (0 on the first iteration).
+__global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a) {
     int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
+    if (I <= L.nx && J <= L.ny) {
+        size_t o = (size_t)J * L.P + I;
+        double z = L.x[o];
+        if (((I + J) & 1) == 0) {
+            z = gs_node(L, o);
+            L.x[o] = z;
+        }
+        v = L.rhs[o] * z;   // black nodes are final after the previous half sweep
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->rz_old = c->rz;
+        c->rz = out;
+        c->beta = c->cg_iters == 0 ? 0.0 : out / c->rz_old;
+    }
+}
+
+// p = z + beta p ; q = M z + beta q (= M p, since q held M p_old) ; pq = p.q ;
+// alpha = rz / pq.  Pointwise in p and q, so no halo of p is needed.
+__global__ void __launch_bounds__(256) k_cg_pq(const CgArgs a) {
+    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
+    double v = 0.0;
+    const double be = a.ctrl->beta;
     if (I <= a.nx && J <= a.ny) {
         size_t o = (size_t)J * a.P + I;
-        double pq = a.mc[o] * a.p[o] - a.ce[o] * a.p[o + 1] - a.ce[o - 1] * a.p[o - 1]
-                  - a.cn[o] * a.p[o + a.P] - a.cn[o - a.P] * a.p[o - a.P];
-        a.q[o] = pq;
-        v = a.p[o] * pq;
+        double mz = a.mc[o] * a.z[o] - a.ce[o] * a.z[o + 1] - a.ce[o - 1] * a.z[o - 1]
+                  - a.cn[o] * a.z[o + a.P] - a.cn[o - a.P] * a.z[o - a.P];
+        double pn = a.z[o] + be * a.p[o];
+        double qn = mz + be * a.q[o];
+        a.p[o] = pn;
+        a.q[o] = qn;
+        v = pn * qn;
     }
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
         c->pq = out;
-        if (!(out > 0.0)) { c->cg_fail = 1; c->alpha = 0.0; }
+        if (c->cg_done) c->alpha = 0.0;   // right-hand side was zero: nothing to do
+        else if (!(out > 0.0)) { c->cg_fail = 1; c->alpha = 0.0; }
         else c->alpha = c->rz / out;
     }
 }
@@ -580,11 +774,15 @@ __global__ void __launch_bounds__(256) k_cg_xr(const CgArgs a) {
         c->relres = c->bnorm2 > 0.0 ? sqrt(out / c->bnorm2) : 0.0;
         if (c->relres <= a.rtol) c->cg_done = 1;
         if (isnan(out)) c->cg_fail = 1;
+        if (a.use_cond && (c->cg_done || c->cg_fail || c->cg_iters >= a.maxit))
+            cudaGraphSetConditional(a.cond, 0u);
     }
 }
 
-// phi(interior) += d ; ph_mi = phi (lapl_lib.F90:112-119)
-__global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, int ny, int P) {
+// phi(interior) += d ; ph_mi = phi (lapl_lib.F90:112-119), only after convergence
+__global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, int ny, int P,
+                             const Ctrl *ctrl) {
+    if (!ctrl->cg_done || ctrl->cg_fail) return;
     size_t n = (size_t)(ny + 2) * P;
     for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
         int gi = (int)(o % P), gj = (int)(o / P);
@@ -604,6 +802,24 @@ LevelDev level_dev(const MGLevel &m) {
 }
 
 dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+LvT<double> lvt(const MGLevel &m) {
+    LvT<double> L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x;
+    return L;
+}
+
+template <typename T>
+size_t mg_down_smem(int nu) {
+    size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
+    return (6 * W + MTX * MTY) * sizeof(T);
+}
+template <typename T>
+size_t mg_up_smem(int nu) {
+    size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
+    return 5 * W * sizeof(T);
+}
 
 }  // namespace
 
@@ -639,6 +855,9 @@ int fs_lapl_alloc(fs_ctx *c) {
         ny = (ny + 1) / 2;
     }
     c->mg_nlev = nl;
+    c->mg_fused = c->cfg.mg_smooth == 2;
+    cudaFuncSetAttribute(k_mg_down<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<double>(2));
+    cudaFuncSetAttribute(k_mg_up<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<double>(2));
     size_t n0 = (size_t)(c->ny + 2) * c->pitch;
     double **vecs[] = {&c->p, &c->q, &c->z, &c->r, &c->xs, &c->bs, &c->dinv};
     for (double **v : vecs) {
@@ -653,6 +872,11 @@ int fs_lapl_alloc(fs_ctx *c) {
 }
 
 void fs_lapl_free(fs_ctx *c) {
+    if (c->cg_graph_built) {
+        cudaGraphExecDestroy(c->cg_exec);
+        cudaGraphDestroy(c->cg_graph);
+        c->cg_graph_built = 0;
+    }
     for (int l = 0; l < c->mg_nlev; l++) {
         MGLevel &m = c->mg[l];
         double *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.res};
@@ -664,13 +888,20 @@ void fs_lapl_free(fs_ctx *c) {
     c->mg_nlev = 0;
 }
 
-static void vcycle(fs_ctx *c) {
+static void vcycle(fs_ctx *c, const CgArgs *ca) {
     const int nl = c->mg_nlev, nu = c->cfg.mg_smooth;
     int lb = 0;
     while (lb < nl && (c->mg[lb].nx > BOTTOM_N || c->mg[lb].ny > BOTTOM_N)) lb++;
     dim3 b(32, 8);
     for (int l = 0; l < lb; l++) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        if (c->mg_fused && l > 0) {
+            LvT<double> F = lvt(c->mg[l]), C = lvt(c->mg[l + 1]);
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_down<double, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_down_smem<double>(2), c->stream>>>(F, C);
+            fs_prof_end(c);
+            continue;
+        }
         dim3 g = grid2(f.nx, f.ny, b);
         fs_prof_begin(c, PROF_SMOOTH);
         k_rb<<<g, b, 0, c->stream>>>(f, 0, 1);
@@ -700,6 +931,13 @@ static void vcycle(fs_ctx *c) {
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        if (c->mg_fused && l > 0) {
+            LvT<double> F = lvt(c->mg[l]), C = lvt(c->mg[l + 1]);
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_up<double, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_up_smem<double>(2), c->stream>>>(F, C);
+            fs_prof_end(c);
+            continue;
+        }
         dim3 g = grid2(f.nx, f.ny, b);
         fs_prof_begin(c, PROF_TRANSFER);
         k_prolong<<<g, b, 0, c->stream>>>(f, cc);
@@ -709,10 +947,75 @@ static void vcycle(fs_ctx *c) {
             k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
             fs_prof_end(c);
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+            if (l == 0 && it == nu - 1)
+                k_rb_rz<<<grid2(f.nx, f.ny, dim3(32, 8)), 256, 0, c->stream>>>(f, *ca);
+            else
+                k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
             fs_prof_end(c);
         }
     }
+    if (lb == 0) {   // the whole V-cycle ran in the bottom kernel: r.z separately
+        fs_prof_begin(c, PROF_CG);
+        k_cg_rz<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(*ca);
+        fs_prof_end(c);
+    }
+}
+
+// One PCG iteration: z = B r, rz, p = z + beta p, q = M p, x/r update.
+static void cg_iteration(fs_ctx *c, const CgArgs &ca, dim3 gb) {
+    vcycle(c, &ca);
+    fs_prof_begin(c, PROF_CG);
+    k_cg_pq<<<gb, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cg_xr<<<gb, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+}
+
+// Graph: WHILE(cond) { one PCG iteration } -> phi update.  The last CTA of the
+// residual reduction clears cond on convergence, breakdown or the iteration cap.
+static int build_cg_graph(fs_ctx *c, CgArgs ca) {
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "CG graph create");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return fs_cuda_check(c, e, "CG while node"); }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ca.use_cond = 1;
+    ca.cond = h;
+    const int prof = c->prof_on;
+    c->prof_on = 0;
+    const int64_t l0 = c->launches;
+    dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
+    e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cg_iteration(c, ca, gb);
+        e = cudaStreamEndCapture(c->stream, &body);
+    }
+    c->cg_body_kernels = (int)(c->launches - l0);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        k_phi_update<<<4 * 152, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
+        e = cudaStreamEndCapture(c->stream, &g);
+    }
+    c->launches = l0;
+    c->prof_on = prof;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cg_exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fs_cuda_check(c, e, "CG graph capture");
+    }
+    c->cg_graph = g;
+    c->cg_graph_built = 1;
+    return FS_OK;
 }
 
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
@@ -726,6 +1029,9 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.nt = c->sp[2].buf[c->lev[0]];
     a.ph = c->ph;
     a.phm = c->ph_mi;
+    fs_faces_update(c);   // E and the ion coefficients of the current phi
+    a.fx_e = c->fx_e; a.fx_cl = c->fx_cl; a.fx_cr = c->fx_cr; a.fx_dl = c->fx_dl; a.fx_dr = c->fx_dr;
+    a.fy_e = c->fy_e; a.fy_cl = c->fy_cl; a.fy_cr = c->fy_cr; a.fy_dl = c->fy_dl; a.fy_dr = c->fy_dr;
     a.ctrl = c->d_ctrl;
     a.ctrl_w = c->d_ctrl;
     MGLevel &m0 = c->mg[0];
@@ -757,6 +1063,9 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
+    ca.maxit = c->cfg.lapl_maxit;
+    ca.use_cond = 0;
+    ca.cond = 0;
     dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
     fs_prof_begin(c, PROF_CG);
     k_cg_init<<<gb, 256, 0, c->stream>>>(ca);
@@ -771,20 +1080,26 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
         *lerr = 1; *iters = 0; *relres = NAN;
         return FS_OK;
     }
+    const int poisson_classes = (1 << PROF_SMOOTH) | (1 << PROF_TRANSFER) | (1 << PROF_BOTTOM) | (1 << PROF_CG);
+    if (!ok && !(c->prof_on & poisson_classes)) {
+        // whole CG loop and the phi update as one graph launch
+        if (!c->cg_graph_built && (rc = build_cg_graph(c, ca))) return rc;
+        int before = 0;
+        cudaError_t e = cudaGraphLaunch(c->cg_exec, c->stream);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "CG graph launch");
+        (void)before;
+        rc = fs_sync_ctrl(c);
+        if (rc) return rc;
+        c->launches += (int64_t)c->h_ctrl->cg_iters * c->cg_body_kernels + 1;
+        *iters = c->h_ctrl->cg_iters;
+        *relres = c->h_ctrl->relres;
+        bool conv = c->h_ctrl->cg_done && !c->h_ctrl->cg_fail;
+        *lerr = conv ? 0 : 1;
+        if (conv) c->faces_valid = 0;   // phi += d happened in the graph
+        return FS_OK;
+    }
     while (!ok && it < c->cfg.lapl_maxit) {
-        vcycle(c);
-        fs_prof_begin(c, PROF_CG);
-        k_cg_rz<<<gb, 256, 0, c->stream>>>(ca);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_CG);
-        k_cg_p<<<gb, 256, 0, c->stream>>>(ca);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_CG);
-        k_cg_q<<<gb, 256, 0, c->stream>>>(ca);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_CG);
-        k_cg_xr<<<gb, 256, 0, c->stream>>>(ca);
-        fs_prof_end(c);
+        cg_iteration(c, ca, gb);
         rc = fs_sync_ctrl(c);
         if (rc) return rc;
         it = c->h_ctrl->cg_iters;
@@ -802,8 +1117,9 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
         return FS_OK;
     }
     *lerr = 0;
+    c->faces_valid = 0;
     c->launches++;
-    k_phi_update<<<4 * 152, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch);
+    k_phi_update<<<4 * 152, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels");
     return FS_OK;

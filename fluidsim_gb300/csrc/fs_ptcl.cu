@@ -43,6 +43,7 @@ struct StageArgs {
     const double *k4[FS_MAX_SPECIES];
     double *kout[FS_MAX_SPECIES];
     const double *ph;
+    const double *fx_e, *fx_cl, *fx_cr, *fy_e, *fy_cl, *fy_cr;
     Ctrl *ctrl;
     double *part;     // [species][nblk] partial error sums
     double *rows;     // [2][ny+2] current rows
@@ -66,19 +67,31 @@ __device__ __forceinline__ double tab_val(const double *tab, int k, double w, in
     return __ldg(t + row) + w * __ldg(t + 8 + row);
 }
 
-// get_Flux for q = +1 (ions, constant mui/Di)
-__device__ __forceinline__ double sg_ion(const PhysParams &pp, double E, double dh, double inv_dh,
-                                         double nl, double nr) {
+// get_Flux for q = +1 (ions: mui and Di are constants, so on a face the flux
+// is linear in the two densities, flux = cl*n_left - cr*n_right, with
+// coefficients fixed for the whole step while phi is frozen)
+__device__ __forceinline__ void ion_coef(const PhysParams &pp, double E, double dh, double inv_dh,
+                                         double &cl, double &cr) {
     const double tol = 9.9999999600419720025e-13;   // REAL(4) 1e-12
     double v = pp.mui * E;
     double arg = v * dh / pp.Di;
-    if (fabs(E) < tol) return pp.Di * (nl - nr) * inv_dh;
-    if (arg > 0) {
+    if (fabs(E) < tol) {
+        cl = cr = pp.Di * inv_dh;
+    } else if (fabs(arg) < 1e-2) {   // Bernoulli form near a = 0, where 1 - exp(-a) cancels
+        double a2 = arg * arg, c2 = a2 * (1.0 / 12.0 - a2 / 720.0), d = pp.Di * inv_dh;
+        cl = d * (1.0 + 0.5 * arg + c2);
+        cr = d * (1.0 - 0.5 * arg + c2);
+    } else if (arg > 0) {
         double ex = exp(fmax(-arg, -100.0));
-        return v * (nl - nr * ex) / (1.0 - ex);
+        double inv = 1.0 / (1.0 - ex);
+        cl = v * inv;
+        cr = v * ex * inv;
+    } else {
+        double ex = exp(fmax(arg, -100.0));
+        double inv = 1.0 / (1.0 - ex);
+        cl = -(v * ex * inv);
+        cr = -(v * inv);
     }
-    double ex = exp(fmax(arg, -100.0));
-    return v * (nr - nl * ex) / (1.0 - ex);
 }
 
 // get_Flux for q = -1 with (mue, De) and (5/3 mue, 5/3 De): one exponential
@@ -93,6 +106,12 @@ __device__ __forceinline__ void sg_elec(double E, double dh, double inv_dh, doub
     if (fabs(E) < tol) {
         fe = De * (nel - ner) * inv_dh;
         ft = Dt * (ntl - ntr) * inv_dh;
+        return;
+    }
+    if (fabs(arg) < 1e-2) {   // Bernoulli form near a = 0
+        double a2 = arg * arg, c2 = a2 * (1.0 / 12.0 - a2 / 720.0);
+        fe = De * ((nel - ner) + 0.5 * arg * (nel + ner) + c2 * (nel - ner)) * inv_dh;
+        ft = Dt * ((ntl - ntr) + 0.5 * arg * (ntl + ntr) + c2 * (ntl - ntr)) * inv_dh;
         return;
     }
     double ex;
@@ -172,7 +191,8 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         int gi = gx0 - 1 + c, gj = gy0 + r;
         if (gj > ny || gi > nx) continue;
         int lx = c, ly = r + 1;   // left node in halo coordinates
-        double E = -(s_ph[ly][lx + 1] - s_ph[ly][lx]) * a.m.inv_dx[gi];
+        const size_t of = (size_t)gj * P + gi;
+        double E = a.fx_e[of];
         double fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
         int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;       // type of left node
         int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;      // type of right node
@@ -197,7 +217,7 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             double dh = a.m.dx[gi], idh = a.m.inv_dx[gi];
             double mue = 5e-1 * (s_mue[ly][lx] + s_mue[ly][lx + 1]);
             double De = 5e-1 * (s_de[ly][lx] + s_de[ly][lx + 1]);
-            fi = sg_ion(pp, E, dh, idh, s_n[0][ly][lx], s_n[0][ly][lx + 1]);
+            fi = a.fx_cl[of] * s_n[0][ly][lx] - a.fx_cr[of] * s_n[0][ly][lx + 1];
             sg_elec(E, dh, idh, mue, De, s_n[1][ly][lx], s_n[1][ly][lx + 1],
                     s_n[2][ly][lx], s_n[2][ly][lx + 1], fe, ft);
             if (NS == 4) fm = -pp.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
@@ -217,7 +237,8 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         int gi = gx0 + c, gj = gy0 - 1 + r;
         if (gi > nx || gj > ny) continue;
         int lx = c + 1, ly = r;     // lower node in halo coordinates
-        double E = -(s_ph[ly + 1][lx] - s_ph[ly][lx]) * a.m.inv_dy[gj];
+        const size_t of = (size_t)gj * P + gi;
+        double E = a.fy_e[of];
         double fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
         int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
         int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
@@ -247,7 +268,7 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             double dh = a.m.dy[gj], idh = a.m.inv_dy[gj];
             double mue = 5e-1 * (s_mue[ly][lx] + s_mue[ly + 1][lx]);
             double De = 5e-1 * (s_de[ly][lx] + s_de[ly + 1][lx]);
-            fi = sg_ion(pp, E, dh, idh, s_n[0][ly][lx], s_n[0][ly + 1][lx]);
+            fi = a.fy_cl[of] * s_n[0][ly][lx] - a.fy_cr[of] * s_n[0][ly + 1][lx];
             sg_elec(E, dh, idh, mue, De, s_n[1][ly][lx], s_n[1][ly + 1][lx],
                     s_n[2][ly][lx], s_n[2][ly + 1][lx], fe, ft);
             if (NS == 4) fm = -pp.Dm * (s_n[3][ly + 1][lx] - s_n[3][ly][lx]) * idh;
@@ -373,31 +394,99 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
     }
 }
 
+// dFdPh for ions (lapl_lib.F90:611-636) at field E is linear in the two
+// densities, dF/dv = dl*n1 + dr*n2, with the same small-|a| series as the oracle.
+__device__ __forceinline__ void ion_dcoef(const PhysParams &pp, double E, double dh, double &dl,
+                                          double &dr) {
+    double v = pp.mui * E;
+    double a = v * dh / pp.Di;
+    if (fabs(v) < 1e-12) {
+        dl = dr = 0.0;
+    } else if (fabs(a) < 0.05) {
+        double a2 = a * a, sres = a * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
+        dl = 0.5 + sres;
+        dr = 0.5 - sres;
+    } else if (a > 0) {
+        double ex = exp(-a), i1 = 1.0 / (1.0 - ex), t = a * ex * i1 * i1;
+        dl = i1 - t;
+        dr = -(ex * i1) + t;
+    } else {
+        double ex = exp(a), i1 = 1.0 / (1.0 - ex), t = a * ex * i1 * i1;
+        dl = -(ex * i1) - t;
+        dr = i1 + t;
+    }
+}
+
+struct FaceArgs {
+    double *fx_e, *fx_cl, *fx_cr, *fx_dl, *fx_dr, *fy_e, *fy_cl, *fy_cr, *fy_dl, *fy_dr;
+};
+
+// Face data while phi is frozen: E = -(phi_R - phi_L)/h as ptclEqn forms it
+// (ptcl_lib.F90:112-121,286-298), the ion flux coefficients and the ion dFdPh
+// coefficients.  x face east of (gi,gj) for gi = 0..nx, y face north of it for gj = 0..ny.
+__global__ void k_faces(const PhysParams pp, const MeshDev m, const double *ph, const FaceArgs f) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x, gj = blockIdx.y * blockDim.y + threadIdx.y;
+    const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
+    if (gi > nx || gj > ny) return;
+    const size_t o = (size_t)gj * P + gi;
+    if (gj >= 1) {
+        double E = -(ph[o + 1] - ph[o]) / m.dx[gi];
+        double cl, cr, dl, dr;
+        ion_coef(pp, E, m.dx[gi], m.inv_dx[gi], cl, cr);
+        ion_dcoef(pp, E, m.dx[gi], dl, dr);
+        f.fx_e[o] = E; f.fx_cl[o] = cl; f.fx_cr[o] = cr; f.fx_dl[o] = dl; f.fx_dr[o] = dr;
+    }
+    if (gi >= 1) {
+        double E = -(ph[o + P] - ph[o]) / m.dy[gj];
+        double cl, cr, dl, dr;
+        ion_coef(pp, E, m.dy[gj], m.inv_dy[gj], cl, cr);
+        ion_dcoef(pp, E, m.dy[gj], dl, dr);
+        f.fy_e[o] = E; f.fy_cl[o] = cl; f.fy_cr[o] = cr; f.fy_dl[o] = dl; f.fy_dr[o] = dr;
+    }
+}
+
 // circ_step ghost potentials (circ_lib.F90:178-198): DC, so Vd_mi = Vd_pl = Vsrc.
-__global__ void k_circ_ghost(double *ph, const int8_t *tx, const double *r, int nx, int ny, int P,
-                             double ew, double vd) {
+// The fields of the two electrode faces of the row follow the new ghosts.
+__global__ void k_circ_ghost(double *ph, const int8_t *tx, const double *r, const double *dx,
+                             double *fx_e, int nx, int ny, int P, double ew, double vd) {
     int gj = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (gj > ny) return;
+    const size_t o = (size_t)gj * P;
     if (r[gj] <= ew) {
-        if (tx[(gj - 1) * nx + 0] == -2) ph[(size_t)gj * P + 0] = vd / 2.0;
-        if (tx[(gj - 1) * nx + nx - 1] == 2) ph[(size_t)gj * P + nx + 1] = vd / (-2.0);
+        if (tx[(gj - 1) * nx + 0] == -2) {
+            ph[o + 0] = vd / 2.0;
+            fx_e[o + 0] = -(ph[o + 1] - ph[o + 0]) / dx[0];
+        }
+        if (tx[(gj - 1) * nx + nx - 1] == 2) {
+            ph[o + nx + 1] = vd / (-2.0);
+            fx_e[o + nx] = -(ph[o + nx + 1] - ph[o + nx]) / dx[nx];
+        }
     }
 }
 
 // PI controller of ptcl_lib.F90:59-95 plus the current sums of circ_step.
-__global__ void k_controller(Ctrl *c, const double *part, int nblk, int ns, const double *rows,
-                             int ny, int adaptive, double dt_min) {
-    __shared__ double s[FS_MAX_SPECIES][256];
+// All sums are fixed-order: strided per-thread partials, then a fixed tree.
+__global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part, int nblk, int ns,
+                                                    const double *rows, int ny, int adaptive,
+                                                    double dt_min) {
+    __shared__ double s[FS_MAX_SPECIES + 2][256];
     const int t = threadIdx.x;
     for (int sp = 0; sp < ns; sp++) {
         double v = 0.0;
         for (int b = t; b < nblk; b += 256) v += part[(size_t)sp * nblk + b];
         s[sp][t] = v;
     }
+    double ra = 0.0, rc = 0.0;
+    for (int j = 1 + t; j <= ny; j += 256) { ra += rows[j]; rc += rows[(ny + 2) + j]; }
+    s[FS_MAX_SPECIES][t] = ra;
+    s[FS_MAX_SPECIES + 1][t] = rc;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
-        if (t < w)
+        if (t < w) {
             for (int sp = 0; sp < ns; sp++) s[sp][t] += s[sp][t + w];
+            s[FS_MAX_SPECIES][t] += s[FS_MAX_SPECIES][t + w];
+            s[FS_MAX_SPECIES + 1][t] += s[FS_MAX_SPECIES + 1][t + w];
+        }
         __syncthreads();
     }
     if (t != 0) return;
@@ -405,10 +494,8 @@ __global__ void k_controller(Ctrl *c, const double *part, int nblk, int ns, cons
     double e_ni = s[0][0], e_ne = s[1][0], e_nt = s[2][0], e_nm = ns == 4 ? s[3][0] : 0.0;
     double err_cur = sqrt(e_ni + e_ne + e_nm + e_nt);
     c->err_cur = err_cur;
-    double ida = 0.0, idc = 0.0;
-    for (int j = 1; j <= ny; j++) { ida = ida + rows[j]; idc = idc + rows[(ny + 2) + j]; }
-    c->ida = ida;
-    c->idc = idc;
+    c->ida = s[FS_MAX_SPECIES][0];
+    c->idc = s[FS_MAX_SPECIES + 1][0];
     c->rejected = 0;
     if (!adaptive) return;
     double scfac = 8e-1 * pow(err_cur, -7e-1 / 4.0) * pow(c->err_prev, 4e-1 / 4.0);
@@ -428,6 +515,16 @@ __global__ void k_reset_step(Ctrl *c, double *rows, int n) {
 
 }  // namespace
 
+void fs_faces_update(fs_ctx *c) {
+    if (c->faces_valid) return;
+    dim3 b(32, 8), g((c->nx + 1 + 31) / 32, (c->ny + 1 + 7) / 8);
+    FaceArgs f = {c->fx_e, c->fx_cl, c->fx_cr, c->fx_dl, c->fx_dr, c->fy_e, c->fy_cl, c->fy_cr, c->fy_dl, c->fy_dr};
+    fs_prof_begin(c, PROF_OTHER);
+    k_faces<<<g, b, 0, c->stream>>>(c->pp, c->mesh, c->ph, f);
+    fs_prof_end(c);
+    c->faces_valid = 1;
+}
+
 int fs_ptcl_alloc(fs_ctx *c) {
     dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
     c->nblk_stage = grid.x * grid.y;
@@ -435,6 +532,13 @@ int fs_ptcl_alloc(fs_ctx *c) {
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc partials");
     e = cudaMalloc(&c->d_rows, sizeof(double) * 2 * (c->ny + 2));
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc rows");
+    double **faces[] = {&c->fx_e, &c->fx_cl, &c->fx_cr, &c->fy_e, &c->fy_cl, &c->fy_cr,
+                        &c->fx_dl, &c->fx_dr, &c->fy_dl, &c->fy_dr};
+    for (double **f : faces) {
+        e = cudaMalloc(f, sizeof(double) * c->field_elems);
+        if (e == cudaSuccess) e = cudaMemset(*f, 0, sizeof(double) * c->field_elems);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc faces");
+    }
     return cudaMemset(c->d_rows, 0, sizeof(double) * 2 * (c->ny + 2)) == cudaSuccess ? FS_OK
                                                                                    : FS_ERR_CUDA;
 }
@@ -458,6 +562,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
 
     c->launches++;
     k_reset_step<<<(2 * (c->ny + 2) + 255) / 256, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, 2 * (c->ny + 2));
+    fs_faces_update(c);
     for (;;) {
         attempts++;
         StageArgs a;
@@ -466,6 +571,8 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
         a.m = c->mesh;
         a.tab = c->d_tab;
         a.ph = c->ph;
+        a.fx_e = c->fx_e; a.fx_cl = c->fx_cl; a.fx_cr = c->fx_cr;
+        a.fy_e = c->fy_e; a.fy_cl = c->fy_cl; a.fy_cr = c->fy_cr;
         a.ctrl = c->d_ctrl;
         a.part = c->d_part;
         a.rows = c->d_rows;
@@ -489,7 +596,8 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
             fs_prof_end(c);
             if (stg == 1 && ++c->launches)
                 k_circ_ghost<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
-                    c->ph, c->mesh.tx, c->mesh.r, c->nx, c->ny, c->pitch, c->cfg.ew, c->Vsrc);
+                    c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->nx, c->ny, c->pitch, c->cfg.ew,
+                    c->Vsrc);
         }
         c->launches++;
         k_controller<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_part, c->nblk_stage, ns, c->d_rows,

@@ -1,0 +1,128 @@
+! fs_gpu_mod.F90 -- ISO_C_BINDING interfaces to libfluidsim_gb300.so
+! (include/fluidsim_gpu.h) and thin wrappers with the argument lists of the
+! reference's module subroutines.  A maintainer replaces the bodies of
+! ptcl_step (ptcl_lib.F90:32-97) and lapl_solve (lapl_lib.F90:57-121) and the
+! array rotation of main.F90:83-121 with calls to the wrappers below; the
+! module arrays ni/ne/nt/nm and ph stay as host mirrors refreshed by
+! fs_sync_from_device before writeOut (main.F90:297-303).
+module fs_gpu_mod
+  use iso_c_binding
+  implicit none
+
+  type, bind(C) :: fs_config
+    integer(c_int32_t) :: abi_version, nx, ny, nspecies, coef_mode, cyl, rf, &
+                          adaptive, precision, lapl_maxit, table_n, mg_smooth
+    real(c_double) :: table_emin_ev, table_emax_ev, kir_arrh_a, kir_arrh_e, &
+                      p_torr, tg_k, gam, n_init, l, w, ew, gap, vl, res, &
+                      abs_tol, rel_tol, dt_min, lapl_rtol
+  end type
+
+  type, bind(C) :: fs_mesh
+    type(c_ptr) :: dx, dlx, dy, dly, r, type_x, type_y
+  end type
+
+  interface
+    integer(c_int) function fs_create(cfg, mesh, ctx) bind(C, name="fs_create")
+      import :: c_int, c_ptr, fs_config, fs_mesh
+      type(fs_config), intent(in) :: cfg
+      type(fs_mesh), intent(in) :: mesh
+      type(c_ptr), intent(out) :: ctx
+    end function
+    subroutine fs_destroy(ctx) bind(C, name="fs_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end subroutine
+    integer(c_int) function fs_set_time(ctx, t, dt) bind(C, name="fs_set_time")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: t, dt
+    end function
+    integer(c_int) function fs_upload_state(ctx, ni, ne, nt, nm, ph, ld, nlev) &
+        bind(C, name="fs_upload_state")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: ni(*), ne(*), nt(*), nm(*), ph(*)
+      integer(c_int32_t), value :: ld, nlev
+    end function
+    integer(c_int) function fs_download_state(ctx, ni, ne, nt, nm, ph, ld, nlev) &
+        bind(C, name="fs_download_state")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: ni(*), ne(*), nt(*), nm(*), ph(*)
+      integer(c_int32_t), value :: ld, nlev
+    end function
+    integer(c_int) function fs_ptcl_step(ctx, dt, t_m, ida, idc, attempts) &
+        bind(C, name="fs_ptcl_step")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_double), intent(inout) :: dt
+      real(c_double), intent(out) :: t_m, ida, idc
+      integer(c_int32_t), intent(out) :: attempts
+    end function
+    integer(c_int) function fs_lapl_solve(ctx, dt, lerr, iters, relres) &
+        bind(C, name="fs_lapl_solve")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_double), value :: dt
+      integer(c_int32_t), intent(out) :: lerr, iters
+      real(c_double), intent(out) :: relres
+    end function
+    integer(c_int) function fs_accept(ctx) bind(C, name="fs_accept")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function fs_reject(ctx) bind(C, name="fs_reject")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function fs_max_ne(ctx, v) bind(C, name="fs_max_ne")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: v
+    end function
+    type(c_ptr) function fs_last_error(ctx) bind(C, name="fs_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end function
+  end interface
+
+  type(c_ptr), save :: fs_ctx = c_null_ptr
+
+contains
+
+  ! stop with the library's message on a negative return code (the reference
+  ! stops on the same conditions: ptcl_props.F90:174, ptcl_lib.F90:71)
+  subroutine fs_check(rc)
+    integer(c_int), intent(in) :: rc
+    character(kind=c_char), pointer :: msg(:)
+    integer :: n
+    if (rc == 0) return
+    call c_f_pointer(fs_last_error(fs_ctx), msg, [512])
+    n = 0
+    do while (n < 512)
+      if (msg(n+1) == c_null_char) exit
+      n = n + 1
+    end do
+    write(*,*) 'fluidsim_gb300 error', rc, ': ', msg(1:n)
+    stop
+  end subroutine
+
+  ! ptcl_step(g, ph, Em) with Em = 0: g%dt in, controller's dt out
+  subroutine ptcl_step_gpu(dt, t_m)
+    real(8), intent(inout) :: dt, t_m
+    real(c_double) :: tm, ida, idc
+    integer(c_int32_t) :: att
+    call fs_check(fs_ptcl_step(fs_ctx, dt, tm, ida, idc, att))
+    t_m = min(t_m, tm)
+  end subroutine
+
+  ! lapl_solve(g, ne(:,:,1), ni(:,:,1), nt(:,:,1), sig, lerr)
+  subroutine lapl_solve_gpu(dt, lerr)
+    real(8), intent(in) :: dt
+    integer, intent(out) :: lerr
+    integer(c_int32_t) :: l, it
+    real(c_double) :: rr
+    call fs_check(fs_lapl_solve(fs_ctx, dt, l, it, rr))
+    lerr = l
+  end subroutine
+end module

@@ -130,13 +130,19 @@ def uniform_pm1(seed, stream, n):
 
 
 def blob_state(mesh, consts, peak_m3=1e14, floor_m3=1e8, sigma_m=1e-3,
-               energy_ev=1.0, noise=0.0, seed=0):
+               energy_ev=1.0, noise=0.0, seed=0, vl=None):
     """Quasi-neutral Gaussian blob at the gap centre on a density floor.
 
     Returns Fortran-ordered (nx+2, ny+2) arrays ni, ne, nt (nt = ne * energy / ph0,
-    i.e. mean energy ``energy_ev``) and ph = 0.  With ``noise`` > 0 each
+    i.e. mean energy ``energy_ev``) and ph.  With ``noise`` > 0 each
     species density is multiplied by (1 + noise*U(-1,1)), U from a
     counter-based generator seeded by (seed, species, cell index).
+
+    ph is zero inside.  With ``vl`` (nondimensional applied voltage) its
+    electrode ghost columns hold +vl/2 at x = 0 and -vl/2 at x = l, the values
+    circ_step writes there (circ_lib.F90:185-194), so the applied voltage is on
+    from t = 0.  Without it they are 0 as after ptcl_init/lapl_init, and the
+    first RK stage then sees different boundary potentials than the next four.
     """
     x0 = consts["x0"]
     ph0 = consts["ph0"]
@@ -153,5 +159,8 @@ def blob_state(mesh, consts, peak_m3=1e14, floor_m3=1e8, sigma_m=1e-3,
         ne = ne * (1.0 + noise * uniform_pm1(seed, 1, n.size).reshape(shape, order="F"))
     nt = ne * (energy_ev / ph0)
     ph = np.zeros(shape)
+    if vl is not None:
+        ph[0, :] = vl / 2.0
+        ph[-1, :] = vl / (-2.0)
     f = np.asfortranarray
     return dict(ni=f(ni), ne=f(ne), nt=f(nt), ph=f(ph))

@@ -211,9 +211,12 @@ void *fs_stream(fs_ctx *ctx);
 
 /* Per-launch CUDA-event timing of kernel classes: 0 RK stage, 1 Poisson
  * assembly, 2 multigrid smoothing, 3 multigrid transfer, 4 bottom solve,
- * 5 CG vector kernels, 6 coarse operators, 7 control kernels.  fs_profile(ctx, 1) resets and
- * enables it; fs_profile_read returns total milliseconds and launch counts
- * of the first n classes. */
+ * 5 CG vector kernels, 6 coarse operators, 7 control kernels.
+ * fs_profile(ctx, mask) resets the totals and times the classes whose bit
+ * (1 << class) is set in mask (0 turns it off).  Timing any of classes 2-5
+ * runs the Krylov loop from the host instead of as one CUDA graph.
+ * fs_profile_read returns total milliseconds and launch counts of the first
+ * n classes. */
 #define FS_PROF_NCLASS 8   /* class 7: small control kernels */
 int fs_profile(fs_ctx *ctx, int32_t enable);
 int fs_profile_read(fs_ctx *ctx, double *ms_out, int64_t *launches_out, int32_t n);

@@ -335,6 +335,14 @@ inline double get_flux(double E, double dh, int q, double mu, double D, double n
     double flux;
     if (std::fabs((double)q * E) < tol) {
         flux = D * (nl - nr) / dh;
+    } else if (std::fabs(arg) < 1e-2) {
+        // Same function in its Bernoulli form, (D/dh)(B(-a) nl - B(a) nr) with
+        // B(x) = x/(e^x - 1) = 1 - x/2 + x^2/12 - x^4/720 + O(x^6).  The closed
+        // form below divides by 1 - exp(-a), which carries a relative error
+        // ~1e-16/|a| and is exactly 0 for |a| < 1.1e-16 (a division by zero the
+        // reference hits where E is rounding noise just above the 1e-12 cut).
+        double a2 = arg * arg;
+        flux = D * ((nl - nr) + 0.5 * arg * (nl + nr) + a2 * (1.0 / 12.0 - a2 / 720.0) * (nl - nr)) / dh;
     } else if (arg > 0) {
         flux = v * (nl - nr * std::exp(std::max(-arg, -100.0))) / (1.0 - std::exp(std::max(-arg, -100.0)));
     } else {

@@ -1,7 +1,14 @@
 """GPU path against the CPU oracle on identical seeded inputs (needs a GB300).
 
-Tolerances: relative L-infinity per field, with the density floor n_zero as
-absolute guard, <= 1e-10 after one step; phi relative to max|phi|.
+Per-field error: relative L-infinity over interior nodes, with the density
+floor n_zero as absolute guard; phi relative to max|phi|.  Poisson solves are
+converged far below the bar (GPU CG to 1e-14, oracle banded LU).
+
+Bars: 1e-10 after one step.  On the fixed-dt start (dt = 1e-12 s on the
+seeded blob, where the first steps' error norm is ~1e6) the step itself
+amplifies rounding: a 1e-15 relative perturbation of the inputs moves the
+oracle's own result by up to ~3e-10.  There the bar is the larger of 1e-10 and
+10x that measured conditioning floor.
 """
 import numpy as np
 import pytest
@@ -11,34 +18,128 @@ from tests._util import field_errors
 pytestmark = pytest.mark.gpu
 
 
-def _pair(built, n, ny=None, **kw):
+def _setup(n, ny=None, seed=7, **kw):
     from fluidsim_gb300 import api, config, grid
-    from oracle import oracle
     cfg = config.glow(n, ny=ny or n, **kw)
     mesh = cfg.mesh()
     k = api.constants(cfg)
-    st = grid.blob_state(mesh, k, noise=0.01, seed=7)
-    gpu = api.Discharge(cfg, mesh, st)
-    ref = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_DIRECT)
-    return cfg, k, gpu, ref
+    st = grid.blob_state(mesh, k, noise=0.01, seed=seed)
+    return cfg, mesh, k, st
+
+
+def _oracle(cfg, mesh, st):
+    from oracle import oracle
+    return oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_DIRECT)
+
+
+def _floor(cfg, mesh, k, st, nsteps):
+    """Oracle vs oracle on inputs perturbed by 1e-15 (relative), same steps."""
+    rng = np.random.default_rng(0)
+    st2 = {f: (np.asfortranarray(v * (1 + 1e-15 * rng.standard_normal(v.shape))) if f != "ph" else v)
+           for f, v in st.items()}
+    a, b = _oracle(cfg, mesh, st), _oracle(cfg, mesh, st2)
+    for _ in range(nsteps):
+        a.step(), b.step()
+    return field_errors(a.download(), b.download(), k["n_zero"])
 
 
 @pytest.mark.parametrize("n,ny", [(24, 20), (64, 64), (37, 29)])
-def test_one_step_fixed_dt(built, n, ny):
-    cfg, k, gpu, ref = _pair(built, n, ny, adaptive=0, lapl_rtol=1e-14)
-    for s in range(3):
+def test_fixed_dt_start(built, n, ny):
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(n, ny, adaptive=0, lapl_rtol=1e-14)
+    gpu, ref = api.Discharge(cfg, mesh, st), _oracle(cfg, mesh, st)
+    for _ in range(3):            # two Poisson-only start-up iterations, one full step
         gi, ri = gpu.step(), ref.step()
         assert gi["lerr"] == 0 and ri["lerr"] == 0
     e = field_errors(gpu.download(), ref.download(), k["n_zero"])
-    assert max(e.values()) < 1e-10, e
+    fl = _floor(cfg, mesh, k, st, 3)
+    for f in e:
+        assert e[f] <= max(1e-10, 10 * fl[f]), (f, e, fl)
 
 
-def test_adaptive_steps(built):
-    cfg, k, gpu, ref = _pair(built, 32, 32, lapl_rtol=1e-14)
+@pytest.mark.parametrize("n", [32, 64])
+def test_adaptive_steps(built, n):
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(n, lapl_rtol=1e-14)
+    gpu, ref = api.Discharge(cfg, mesh, st), _oracle(cfg, mesh, st)
     for s in range(8):
         gi, ri = gpu.step(), ref.step()
         if s >= 2:
+            # the controller's decisions match exactly; dt itself comes from the
+            # Merson error estimate, a difference of stage derivatives that
+            # cancels to O(dt^4) and amplifies 1e-16 rounding ~1e7-fold
             assert gi["attempts"] == ri["attempts"], (s, gi, ri)
-            assert abs(gi["dt"] - ri["dt"]) <= 1e-9 * abs(ri["dt"]), (s, gi, ri)
+            assert abs(gi["dt"] - ri["dt"]) <= 1e-6 * abs(ri["dt"]), (s, gi, ri)
+            assert gi["t_m"] == pytest.approx(ri["t_m"], rel=1e-10)
+        e = field_errors(gpu.download(), ref.download(), k["n_zero"])
+        assert max(e.values()) < 1e-10, (s, e)
+
+
+def test_levels_and_download_layout(built):
+    """All three RK levels after a step match, including the stage-4 state the
+    reference keeps as n(:,:,2) (quirk: it becomes the next step's base)."""
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(20, 16, lapl_rtol=1e-14)
+    gpu, ref = api.Discharge(cfg, mesh, st), _oracle(cfg, mesh, st)
+    for _ in range(3):
+        gpu.step(), ref.step()
+    gpu.ptcl_step(), ref.ptcl_step()
+    g, r = gpu.download(nlev=3), ref.download(nlev=3)
+    for lev in range(3):
+        gl = {f: g[f][:, :, lev] for f in ("ni", "ne", "nt")}
+        rl = {f: r[f][:, :, lev] for f in ("ni", "ne", "nt")}
+        gl["ph"], rl["ph"] = g["ph"], r["ph"]
+        e = field_errors(gl, rl, k["n_zero"])
+        assert max(e.values()) < 1e-10, (lev, e)
+    # ghost potentials set by circ_step: +-V/2 at the electrodes
+    vd = cfg.vl
+    assert np.allclose(g["ph"][0, 1:-1], vd / 2) and np.allclose(g["ph"][-1, 1:-1], -vd / 2)
+
+
+def test_reject_restores_base(built):
+    """fs_reject: n1 = n2 = n3 and dt halved (main.F90:103-121)."""
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(20, 16)
+    gpu = api.Discharge(cfg, mesh, st)
+    for _ in range(3):
+        gpu.step()
+    gpu.ptcl_step()
+    before = gpu.download(nlev=3)
+    dt = gpu.dt
+    gpu.reject()
+    after = gpu.download(nlev=3)
+    assert gpu.dt == dt / 2
+    for f in ("ni", "ne", "nt"):
+        for lev in range(3):
+            assert np.array_equal(after[f][:, :, lev], before[f][:, :, 2])
+
+
+@pytest.mark.parametrize("n", [128, 256])
+def test_poisson_solve_multilevel(built, n):
+    """One semi-implicit Poisson solve on grids deep enough for several launched
+    multigrid levels, against the oracle's banded LU."""
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(n, lapl_rtol=1e-13, lapl_maxit=200)
+    st["ph"][0, :] = cfg.vl / 2
+    st["ph"][-1, :] = -cfg.vl / 2
+    gpu, ref = api.Discharge(cfg, mesh, st), _oracle(cfg, mesh, st)
+    gi, ri = gpu.lapl_solve(), ref.lapl_solve()
+    assert gi["lerr"] == 0 and ri["lerr"] == 0
+    assert gi["iters"] < 40, gi
+    e = field_errors(gpu.download(), ref.download(), k["n_zero"])
+    assert e["ph"] < 1e-10, e
+
+
+def test_adaptive_run_128(built):
+    from fluidsim_gb300 import api
+    cfg, mesh, k, st = _setup(128, lapl_rtol=1e-13)
+    st["ph"][0, :] = cfg.vl / 2
+    st["ph"][-1, :] = -cfg.vl / 2
+    gpu, ref = api.Discharge(cfg, mesh, st), _oracle(cfg, mesh, st)
+    for s in range(6):
+        gi, ri = gpu.step(), ref.step()
+        assert gi["lerr"] == 0 and ri["lerr"] == 0
+        if s >= 2:
+            assert gi["attempts"] == ri["attempts"], (s, gi, ri)
     e = field_errors(gpu.download(), ref.download(), k["n_zero"])
     assert max(e.values()) < 1e-9, e

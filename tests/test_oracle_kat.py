@@ -192,3 +192,35 @@ def test_poisson_rows_symmetric_after_volume_scaling(built):
                 assert A[q, 3] == pytest.approx(A[q + nx, 2], rel=1e-14)
     # diagonally dominant M-matrix rows: -A_c >= sum of off-diagonals
     assert np.all(-A[:, 4] >= A[:, :4].sum(axis=1) * (1 - 1e-12))
+
+
+@pytest.mark.parametrize("a", [3e-17, 1e-14, 1e-9, 1e-4, 0.0099, 0.0101, 0.3, 7.0])
+@pytest.mark.parametrize("q", [1, -1])
+def test_flux_matches_high_precision(a, q):
+    """get_Flux against a 50-digit evaluation of the same function: the small
+    Peclet branch (|a| < 1e-2) and the closed form both hold to ~1e-14."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    mu, D, dh, nl, nr = 1e-3, 1e3, 0.5, 3.0, 2.0   # |E| stays above the 1e-12 cut
+    E = q * a * D / (mu * dh)          # so that arg = q*mu*E*dh/D = a
+    assert abs(E) > 1e-12
+    v = mp.mpf(q) * mu * mp.mpf(E)
+    A = v * dh / D
+    exact = v * (nl - nr * mp.e ** (-A)) / (1 - mp.e ** (-A))
+    got = flux(E, dh, q, mu, D, nl, nr)
+    assert abs(got - float(exact)) <= 2e-14 * float(abs(exact)), (got, exact)
+
+
+@pytest.mark.parametrize("a", [1e-12, 1e-7, 0.049, 0.051, 2.0])
+def test_dfdph_matches_high_precision(a):
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    mu, D, dx, n1, n2 = 1.1, 0.9, 0.5, 4.0, 1.5
+    E = a * D / (mu * dx)
+
+    def F(vv):
+        A = vv * dx / D
+        return vv * (n1 - n2 * mp.e ** (-A)) / (1 - mp.e ** (-A))
+    exact = mp.diff(F, mp.mpf(mu) * mp.mpf(E))
+    got = oracle.dfdph(E, E, 1, mu, D, dx, n1, n2)
+    assert abs(got - float(exact)) <= 1e-12 * float(abs(exact)), (got, exact)
