@@ -204,6 +204,8 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     c->pitch = ((cfg->nx + 2 + 31) / 32) * 32;
     c->field_elems = (size_t)(cfg->ny + 2) * c->pitch;
     cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
+    if (c->nsm < 1) c->nsm = 1;
     fs_host_constants(*cfg, c->k);
     const fs_constants &k = c->k;
     const int nx = c->nx, ny = c->ny;

@@ -98,6 +98,7 @@ struct fs_ctx {
     int nx, ny, pitch;
     size_t field_elems;          // (ny+2)*pitch
     int device;
+    int nsm;                     // multiprocessors of the device
     cudaStream_t stream;
     std::string err;
 

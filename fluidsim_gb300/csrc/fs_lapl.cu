@@ -461,15 +461,22 @@ __device__ __forceinline__ double gs_node(const LevelDev &L, size_t o) {
 }
 
 // one red (color 0) or black (color 1) half sweep; zero_init: x starts at 0
+// Each thread owns the column pair (2t+1, 2t+2) of a row and updates the
+// node of the swept colour in it, so every lane does useful FP64 work.
 __global__ void k_rb(const LevelDev L, int color, int zero_init) {
-    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (I > L.nx || J > L.ny) return;
-    size_t o = (size_t)J * L.P + I;
-    if (((I + J) & 1) == color) L.x[o] = zero_init ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
-    else if (zero_init) L.x[o] = 0.0;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int c0 = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + 1;
+    if (J > L.ny || c0 > L.nx) return;
+    const int I = ((c0 + J) & 1) == color ? c0 : c0 + 1, Io = I == c0 ? c0 + 1 : c0;
+    if (zero_init && Io <= L.nx) L.x[(size_t)J * L.P + Io] = 0.0;
+    if (I > L.nx) return;
+    const size_t o = (size_t)J * L.P + I;
+    L.x[o] = zero_init ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
 }
 
-// coarse rhs = sum over the aggregate of the fine residual rhs - M x
+// coarse rhs = sum over the aggregate of the fine residual rhs - M x.  The
+// pre-smoothing ends with a black half sweep, after which every black node's
+// residual is zero (to rounding), so only the red nodes are summed.
 __device__ __forceinline__ double resid(const LevelDev &L, size_t o) {
     return L.rhs[o] - (L.mc[o] * L.x[o] - L.ce[o] * L.x[o + 1] - L.ce[o - 1] * L.x[o - 1]
                        - L.cn[o] * L.x[o + L.P] - L.cn[o - L.P] * L.x[o - L.P]);
@@ -480,7 +487,8 @@ __global__ void k_restrict(const LevelDev f, const LevelDev c) {
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
     double s = 0.0;
     for (int fy = fy0; fy <= fy1; fy++)
-        for (int fx = fx0; fx <= fx1; fx++) s += resid(f, (size_t)fy * f.P + fx);
+        for (int fx = fx0; fx <= fx1; fx++)
+            if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
     c.rhs[(size_t)J * c.P + I] = s;
 }
 __global__ void k_prolong(const LevelDev f, const LevelDev c) {
@@ -547,8 +555,9 @@ __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c)
         const int k = ly * WX + lx;
         T r = T(0);
         if (gi <= f.nx && gj <= f.ny) {
-            r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
-                           - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
+            if (((gi + gj) & 1) == 0)   // black residuals vanish after the last (black) sweep
+                r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
+                               - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
             f.x[(size_t)gj * f.P + gi] = sx[k];
         }
         sr[q] = r;
@@ -626,7 +635,8 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs a) {
             const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
             double s = 0.0;
             for (int fy = fy0; fy <= fy1; fy++)
-                for (int fx = fx0; fx <= fx1; fx++) s += resid(f, (size_t)fy * f.P + fx);
+                for (int fx = fx0; fx <= fx1; fx++)
+                    if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
             c.rhs[(size_t)J * c.P + I] = s;
         }
         __syncthreads();
@@ -655,6 +665,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs a) {
 // ------------------------------------------------------------------------ CG
 struct CgArgs {
     int nx, ny, P, nblk;
+    dim3 grid;                             // nblk CTAs of 256 threads, grid-stride over nodes
     double *x, *r, *z, *p, *q, *rhs, *dinv, *part;
     const double *mc, *ce, *cn;
     Ctrl *ctrl;
@@ -664,18 +675,24 @@ struct CgArgs {
     cudaGraphConditionalHandle cond;
 };
 
+// grid-stride loop over the interior nodes; o is the node's field offset
+#define CG_NODES(a, ...)                                                                   \
+    for (long q_ = blockIdx.x * 256L + threadIdx.x; q_ < (long)(a).nx * (a).ny;           \
+         q_ += (long)gridDim.x * 256L) {                                                   \
+        const size_t o = (size_t)(q_ / (a).nx + 1) * (a).P + (size_t)(q_ % (a).nx + 1);   \
+        __VA_ARGS__                                                                        \
+    }
+
 __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
-    if (I <= a.nx && J <= a.ny) {
-        size_t o = (size_t)J * a.P + I;
+    CG_NODES(a, {
         a.x[o] = 0.0;
         a.r[o] = a.rhs[o];
         a.p[o] = 0.0;
         a.q[o] = 0.0;
         double u = a.rhs[o] * a.dinv[o];
-        v = u * u;
-    }
+        v += u * u;
+    })
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[0], a.nblk, &out) && threadIdx.x == 0) {
         a.ctrl->bnorm2 = out;
@@ -690,12 +707,8 @@ __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
 
 // rz = r.z; beta = rz/rz_old (0 on the first iteration)
 __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
-    if (I <= a.nx && J <= a.ny) {
-        size_t o = (size_t)J * a.P + I;
-        v = a.r[o] * a.z[o];
-    }
+    CG_NODES(a, { v += a.r[o] * a.z[o]; })
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
@@ -708,17 +721,16 @@ __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
 // Last half sweep of the fine level (red, after the black one) fused with
 // rz = r.z over all nodes and beta = rz/rz_old (0 on the first iteration).
 __global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
-    if (I <= L.nx && J <= L.ny) {
-        size_t o = (size_t)J * L.P + I;
+    CG_NODES(a, {
+        const int I = (int)(q_ % a.nx) + 1, J = (int)(q_ / a.nx) + 1;
         double z = L.x[o];
         if (((I + J) & 1) == 0) {
             z = gs_node(L, o);
             L.x[o] = z;
         }
-        v = L.rhs[o] * z;   // black nodes are final after the previous half sweep
-    }
+        v += L.rhs[o] * z;   // black nodes are final after the previous half sweep
+    })
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
@@ -731,19 +743,17 @@ __global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a)
 // p = z + beta p ; q = M z + beta q (= M p, since q held M p_old) ; pq = p.q ;
 // alpha = rz / pq.  Pointwise in p and q, so no halo of p is needed.
 __global__ void __launch_bounds__(256) k_cg_pq(const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
     const double be = a.ctrl->beta;
-    if (I <= a.nx && J <= a.ny) {
-        size_t o = (size_t)J * a.P + I;
+    CG_NODES(a, {
         double mz = a.mc[o] * a.z[o] - a.ce[o] * a.z[o + 1] - a.ce[o - 1] * a.z[o - 1]
                   - a.cn[o] * a.z[o + a.P] - a.cn[o - a.P] * a.z[o - a.P];
         double pn = a.z[o] + be * a.p[o];
         double qn = mz + be * a.q[o];
         a.p[o] = pn;
         a.q[o] = qn;
-        v = pn * qn;
-    }
+        v += pn * qn;
+    })
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
@@ -755,17 +765,15 @@ __global__ void __launch_bounds__(256) k_cg_pq(const CgArgs a) {
 }
 
 __global__ void __launch_bounds__(256) k_cg_xr(const CgArgs a) {
-    int I = blockIdx.x * 32 + threadIdx.x % 32 + 1, J = blockIdx.y * 8 + threadIdx.x / 32 + 1;
     double v = 0.0;
     const double al = a.ctrl->alpha;
-    if (I <= a.nx && J <= a.ny) {
-        size_t o = (size_t)J * a.P + I;
+    CG_NODES(a, {
         a.x[o] += al * a.p[o];
         double rr = a.r[o] - al * a.q[o];
         a.r[o] = rr;
         double u = rr * a.dinv[o];
-        v = u * u;
-    }
+        v += u * u;
+    })
     double out;
     if (grid_sum<256>(v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
@@ -902,7 +910,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
             fs_prof_end(c);
             continue;
         }
-        dim3 g = grid2(f.nx, f.ny, b);
+        dim3 g = grid2((f.nx + 1) / 2, f.ny, b);
         fs_prof_begin(c, PROF_SMOOTH);
         k_rb<<<g, b, 0, c->stream>>>(f, 0, 1);
         fs_prof_end(c);
@@ -938,25 +946,25 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
             fs_prof_end(c);
             continue;
         }
-        dim3 g = grid2(f.nx, f.ny, b);
+        dim3 g = grid2(f.nx, f.ny, b), gh = grid2((f.nx + 1) / 2, f.ny, b);
         fs_prof_begin(c, PROF_TRANSFER);
         k_prolong<<<g, b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+            k_rb<<<gh, b, 0, c->stream>>>(f, 1, 0);
             fs_prof_end(c);
             fs_prof_begin(c, PROF_SMOOTH);
             if (l == 0 && it == nu - 1)
-                k_rb_rz<<<grid2(f.nx, f.ny, dim3(32, 8)), 256, 0, c->stream>>>(f, *ca);
+                k_rb_rz<<<ca->grid, 256, 0, c->stream>>>(f, *ca);
             else
-                k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
+                k_rb<<<gh, b, 0, c->stream>>>(f, 0, 0);
             fs_prof_end(c);
         }
     }
     if (lb == 0) {   // the whole V-cycle ran in the bottom kernel: r.z separately
         fs_prof_begin(c, PROF_CG);
-        k_cg_rz<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(*ca);
+        k_cg_rz<<<ca->grid, 256, 0, c->stream>>>(*ca);
         fs_prof_end(c);
     }
 }
@@ -965,10 +973,10 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
 static void cg_iteration(fs_ctx *c, const CgArgs &ca, dim3 gb) {
     vcycle(c, &ca);
     fs_prof_begin(c, PROF_CG);
-    k_cg_pq<<<gb, 256, 0, c->stream>>>(ca);
+    k_cg_pq<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     fs_prof_begin(c, PROF_CG);
-    k_cg_xr<<<gb, 256, 0, c->stream>>>(ca);
+    k_cg_xr<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
 }
 
@@ -1057,7 +1065,12 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     }
     // CG on M d = D b
     CgArgs ca;
-    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch; ca.nblk = c->cg_nblk;
+    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;
+    {
+        long nb = ((long)c->nx * c->ny + 255) / 256, cap = 4L * c->nsm;
+        ca.nblk = (int)(nb < cap ? nb : cap);
+        ca.grid = dim3(ca.nblk);
+    }
     ca.x = c->xs; ca.r = c->r; ca.z = c->z; ca.p = c->p; ca.q = c->q;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
     ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
@@ -1068,7 +1081,7 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.cond = 0;
     dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
     fs_prof_begin(c, PROF_CG);
-    k_cg_init<<<gb, 256, 0, c->stream>>>(ca);
+    k_cg_init<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     int rc = fs_sync_ctrl(c);
     if (rc) return rc;
@@ -1080,8 +1093,10 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
         *lerr = 1; *iters = 0; *relres = NAN;
         return FS_OK;
     }
+    // FS_NO_GRAPH=1 keeps the loop on the host so that a profiler sees each kernel
+    static const bool no_graph = getenv("FS_NO_GRAPH") != nullptr;
     const int poisson_classes = (1 << PROF_SMOOTH) | (1 << PROF_TRANSFER) | (1 << PROF_BOTTOM) | (1 << PROF_CG);
-    if (!ok && !(c->prof_on & poisson_classes)) {
+    if (!ok && !no_graph && !(c->prof_on & poisson_classes)) {
         // whole CG loop and the phi update as one graph launch
         if (!c->cg_graph_built && (rc = build_cg_graph(c, ca))) return rc;
         int before = 0;
