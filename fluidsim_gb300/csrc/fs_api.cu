@@ -88,22 +88,58 @@ __global__ void k_fill(double *p, size_t n, double v) {
 
 __global__ void k_set_dt(Ctrl *c, double dt) { c->dt = dt; }
 
-__global__ void k_max3(const double *a, const double *b, const double *d, int nx, int ny, int P, double *out) {
-    __shared__ double s[1024];
-    double m = -INFINITY;
+// maxval over the three RK levels of one species, ghost ring included:
+// pass 1, CTA b takes elements [b*FS_MAX_PER_CTA, (b+1)*FS_MAX_PER_CTA) of
+// the flattened (level, row, column) index space and writes its maximum to
+// part[b]; pass 2, one CTA reduces the partial maxima into *out.
+#define FS_MAX_PER_CTA 16384
+__global__ void __launch_bounds__(256) k_max_part(const double *a, const double *b, const double *d, int nx,
+                                                  int ny, int P, double *part) {
+    __shared__ double s[256];
+    const long n1 = (long)(nx + 2) * (ny + 2), n = 3 * n1;
+    const long lo = (long)blockIdx.x * FS_MAX_PER_CTA, hi = lo + FS_MAX_PER_CTA < n ? lo + FS_MAX_PER_CTA : n;
     const double *arr[3] = {a, b, d};
-    for (int l = 0; l < 3; l++)
-        for (int q = threadIdx.x; q < (nx + 2) * (ny + 2); q += blockDim.x) {
-            int gi = q % (nx + 2), gj = q / (nx + 2);
-            m = fmax(m, arr[l][(size_t)gj * P + gi]);
-        }
+    double m = -INFINITY;
+    for (long q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+        const int l = (int)(q / n1);
+        const long r = q - (long)l * n1;
+        const int gi = (int)(r % (nx + 2)), gj = (int)(r / (nx + 2));
+        m = fmax(m, arr[l][(size_t)gj * P + gi]);
+    }
     s[threadIdx.x] = m;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+__global__ void __launch_bounds__(256) k_max_final(const double *part, int nblk, double *out) {
+    __shared__ double s[256];
+    double m = -INFINITY;
+    for (int q = threadIdx.x; q < nblk; q += blockDim.x) m = fmax(m, part[q]);
+    s[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
         if ((int)threadIdx.x < w) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + w]);
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = s[0];
+}
+
+int max_parts(const fs_ctx *c) {
+    const long n = 3L * (c->nx + 2) * (c->ny + 2);
+    return (int)((n + FS_MAX_PER_CTA - 1) / FS_MAX_PER_CTA);
+}
+
+// Launch both passes of the ne maximum with scratch = nblk partials + 1 result.
+void launch_max_ne(fs_ctx *c, double *scratch, int nblk) {
+    const SpeciesBufs &b = c->sp[1];
+    c->launches += 2;
+    k_max_part<<<nblk, 256, 0, c->stream>>>(b.buf[c->lev[0]], b.buf[c->lev[1]], b.buf[c->lev[2]], c->nx, c->ny,
+                                            c->pitch, scratch);
+    k_max_final<<<1, 256, 0, c->stream>>>(scratch, nblk, scratch + nblk);
 }
 
 int validate(const fs_config *cfg, const fs_mesh *m) {
@@ -517,17 +553,16 @@ int fs_profile_read(fs_ctx *c, double *ms_out, int64_t *launches_out, int32_t n)
 }
 
 // maxval(ne) over the whole module array, every level and the ghost ring
-// included (main.F90:131).
+// included (main.F90:131).  The partial maxima live in scratch memory taken
+// from the stream-ordered allocator for the duration of the call.
 int fs_max_ne(fs_ctx *c, double *out) {
     if (!c || !out) return FS_ERR_INVALID;
+    const int nblk = max_parts(c);
     double *d;
-    cudaError_t e = cudaMallocAsync((void **)&d, sizeof(double), c->stream);
+    cudaError_t e = cudaMallocAsync((void **)&d, sizeof(double) * (nblk + 1), c->stream);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "max_ne");
-    const SpeciesBufs &b = c->sp[1];
-    c->launches++;
-    k_max3<<<1, 1024, 0, c->stream>>>(b.buf[c->lev[0]], b.buf[c->lev[1]], b.buf[c->lev[2]], c->nx, c->ny,
-                                       c->pitch, d);
-    e = cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    launch_max_ne(c, d, nblk);
+    e = cudaMemcpyAsync(out, d + nblk, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     cudaFreeAsync(d, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return fs_cuda_check(c, e, "max_ne");
