@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -566,6 +567,64 @@ int fs_max_ne(fs_ctx *c, double *out) {
     cudaFreeAsync(d, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return fs_cuda_check(c, e, "max_ne");
+}
+
+// ---------------------------------------------------------------------------
+// fs_max_ne_noalloc: fs_max_ne for callers that may not allocate device
+// memory once their run is set up -- for example a stepping loop that runs
+// with the stream-ordered allocator or cudaMalloc forbidden after
+// initialisation, where fs_max_ne's per-call scratch is not allowed.  The
+// partial maxima go to a file-scope device array instead: at most
+// FS_NOALLOC_MAX_PARTS partials of FS_MAX_PER_CTA values each, i.e. the three
+// RK levels of n_e with their ghost rings may hold up to 33,554,432 values
+// (a 3342 x 3342 grid); larger contexts are rejected with FS_ERR_INVALID.
+// Every GPU that loads this library holds the array (16 KB) until the
+// process exits.  The first call on a device looks up the array's device
+// address (cudaGetSymbolAddress) with that device current; make that first
+// call before any stream capture.  All calls share the one array and it keeps
+// the last call's contents: calls whose work overlaps on the GPU (two
+// contexts or streams at once) race on it.  Nothing in it has to start at
+// zero -- each call writes every partial it reads.
+#define FS_NOALLOC_MAX_PARTS 2048
+#define FS_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) double fs_noalloc_scratch[FS_NOALLOC_MAX_PARTS + 1];
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[FS_NOALLOC_MAX_DEVICES];
+
+extern "C" int fs_max_ne_noalloc(fs_ctx *c, double *out) {
+    if (!c || !out) return FS_ERR_INVALID;
+    const int nblk = max_parts(c);
+    if (nblk > FS_NOALLOC_MAX_PARTS)
+        return fs_set_error(c, FS_ERR_INVALID,
+                            "fs_max_ne_noalloc: %ld values exceed its scratch limit of %ld "
+                            "(%d partial maxima of %d values); use fs_max_ne",
+                            3L * (c->nx + 2) * (c->ny + 2), (long)FS_NOALLOC_MAX_PARTS * FS_MAX_PER_CTA,
+                            FS_NOALLOC_MAX_PARTS, FS_MAX_PER_CTA);
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "fs_max_ne_noalloc");
+    if (dev != c->device || dev < 0 || dev >= FS_NOALLOC_MAX_DEVICES)
+        return fs_set_error(c, FS_ERR_INVALID, "fs_max_ne_noalloc: the context's device %d must be current (is %d)",
+                            c->device, dev);
+    double *scratch;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            double *p = nullptr;
+            e = cudaGetSymbolAddress((void **)&p, fs_noalloc_scratch);
+            if (e != cudaSuccess) return fs_cuda_check(c, e, "fs_max_ne_noalloc: cudaGetSymbolAddress");
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    launch_max_ne(c, scratch, nblk);
+    // the result lands in the context's pinned control block, so no staging
+    e = cudaMemcpyAsync(&c->h_ctrl->host_result, scratch + nblk, sizeof(double), cudaMemcpyDeviceToHost,
+                        c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "fs_max_ne_noalloc");
+    *out = c->h_ctrl->host_result;
+    return FS_OK;
 }
 
 }  // extern "C"

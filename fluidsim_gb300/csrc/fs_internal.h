@@ -66,6 +66,7 @@ struct Ctrl {
     double rz, rz_old, pq, alpha, beta, rnorm2, bnorm2, relres;
     int cg_done, cg_iters, cg_fail, pad2;
     unsigned int counter[8];   // last-block-done counters of grid reductions
+    double host_result;        // host-side landing slot of single-value results
 };
 
 // One species' buffers.

@@ -224,6 +224,17 @@ int fs_profile_read(fs_ctx *ctx, double *ms_out, int64_t *launches_out, int32_t 
 /* Number of kernels ctx has launched since fs_create. */
 int64_t fs_launch_count(fs_ctx *ctx);
 
+/* fs_max_ne for callers that may not allocate device memory after set-up
+ * (this entry point has no counterpart in the reference): same result as
+ * fs_max_ne, with its scratch in a fixed device array of the library instead
+ * of per-call memory from the stream-ordered allocator.  The array holds the
+ * partial maxima of at most 33,554,432 values -- the three RK levels of n_e
+ * with ghost rings, i.e. grids up to 3342 x 3342; larger contexts get
+ * FS_ERR_INVALID.  The first call on a device looks the array up and must
+ * come before any stream capture.  Every call shares the array: calls whose
+ * GPU work overlaps race on it.  ctx's device must be current. */
+int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
+
 #ifdef __cplusplus
 }
 #endif
