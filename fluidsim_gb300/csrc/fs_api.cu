@@ -157,7 +157,8 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
     if (cfg->table_n < 2 || !(cfg->table_emax_ev > cfg->table_emin_ev) || !(cfg->table_emin_ev > 0))
         return fs_set_error(nullptr, FS_ERR_INVALID, "bad coefficient table range");
     if (cfg->rf != 0) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the DC source (rf = 0) is implemented");
-    if (cfg->precision != FS_PREC_FP64) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "precision mode not built");
+    if (cfg->precision != FS_PREC_FP64 && cfg->precision != FS_PREC_MIXED)
+        return fs_set_error(nullptr, FS_ERR_INVALID, "unknown precision mode %d", cfg->precision);
     if (cfg->mg_smooth < 1 || cfg->mg_smooth > 8) return fs_set_error(nullptr, FS_ERR_INVALID, "mg_smooth must be 1..8");
     if (cfg->lapl_maxit < 1) return fs_set_error(nullptr, FS_ERR_INVALID, "lapl_maxit must be positive");
     for (long q = 0; q < (long)cfg->nx * cfg->ny; q++) {
@@ -172,6 +173,10 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
 void free_ctx(fs_ctx *c) {
     if (!c) return;
     fs_lapl_free(c);
+    if (c->mixed) {
+        fs_lapl_free_mixed(c);
+        fs_mixed_free(c);
+    }
     for (int s = 0; s < FS_MAX_SPECIES; s++) {
         for (int b = 0; b < FS_NBUF; b++) cudaFree(c->sp[s].buf[b]);
         for (int k = 0; k < 3; k++) cudaFree(c->sp[s].k[k]);
@@ -316,8 +321,8 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     md.ty = c->d_types + (size_t)nx * ny;
 
     // coefficient table, node-major: 8 values then 8 slopes f(k+1)-f(k)
+    std::vector<double> rows;
     {
-        std::vector<double> rows;
         fs_host_table(*cfg, k, rows);
         const int n = cfg->table_n;
         std::vector<double> t((size_t)n * FS_TAB_STRIDE, 0.0);
@@ -355,7 +360,10 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     c->h_ctrl->err_prev = 1.0;
     c->h_ctrl->t_m = 1e9;
     CK(cudaMemcpyAsync(c->d_ctrl, c->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream), "ctrl init");
-    if ((rc = fs_ptcl_alloc(c)) || (rc = fs_lapl_alloc(c))) {
+    c->mixed = cfg->precision == FS_PREC_MIXED;
+    if ((rc = fs_ptcl_alloc(c)) || (rc = fs_lapl_alloc(c)) ||
+        (c->mixed && ((rc = fs_mixed_alloc(c, rows)) || (rc = fs_lapl_alloc_mixed(c)) ||
+                      (rc = fs_mixed_sync_logs(c))))) {
         g_err = c->err;
         free_ctx(c);
         return rc;
@@ -407,6 +415,7 @@ int fs_upload_state(fs_ctx *c, const double *ni, const double *ne, const double 
         if (nlev == 1) { c->lev[0] = c->lev[1] = c->lev[2] = 0; }
         else { c->lev[0] = 0; c->lev[1] = 1; c->lev[2] = 2; }
     }
+    if (e == cudaSuccess && c->mixed && fs_mixed_sync_logs(c)) return FS_ERR_CUDA;
     if (ph && e == cudaSuccess) {
         c->faces_valid = 0;
         e = cudaMemcpy2DAsync(c->ph, dp, ph, hp, w, rows, cudaMemcpyHostToDevice, c->stream);
@@ -445,7 +454,7 @@ int fs_ptcl_step(fs_ctx *c, double *dt_inout, double *t_m_out, double *ida_out, 
     int rc;
     if (dt_inout && (rc = set_dt_dev(c, *dt_inout))) return rc;
     int attempts = 0;
-    rc = fs_ptcl_step_impl(c, &attempts);
+    rc = c->mixed ? fs_ptcl_step_mixed(c, &attempts) : fs_ptcl_step_impl(c, &attempts);
     if (dt_inout) *dt_inout = c->h_ctrl->dt;
     if (t_m_out) *t_m_out = c->h_ctrl->t_m;
     if (ida_out) *ida_out = c->h_ctrl->ida;
@@ -460,7 +469,7 @@ int fs_lapl_solve(fs_ctx *c, double dt, int32_t *lerr_out, int32_t *iters_out, d
     if (rc) return rc;
     int lerr = 1, iters = 0;
     double relres = 0;
-    rc = fs_lapl_solve_impl(c, &lerr, &iters, &relres);
+    rc = c->mixed ? fs_lapl_solve_mixed(c, &lerr, &iters, &relres) : fs_lapl_solve_impl(c, &lerr, &iters, &relres);
     c->st.lapl_iters += iters;
     c->st.last_lapl_iters = iters;
     c->st.lapl_relres = relres;
@@ -497,11 +506,13 @@ int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out) {
         int rc;
         if (c->ts > 1) {
             int att = 0;
-            if ((rc = fs_ptcl_step_impl(c, &att))) return rc;
+            if ((rc = c->mixed ? fs_ptcl_step_mixed(c, &att) : fs_ptcl_step_impl(c, &att))) return rc;
         }
         int lerr = 1, iters = 0;
         double relres = 0;
-        if ((rc = fs_lapl_solve_impl(c, &lerr, &iters, &relres))) return rc;
+        if ((rc = c->mixed ? fs_lapl_solve_mixed(c, &lerr, &iters, &relres)
+                           : fs_lapl_solve_impl(c, &lerr, &iters, &relres)))
+            return rc;
         c->st.lapl_iters += iters;
         c->st.last_lapl_iters = iters;
         c->st.lapl_relres = relres;

@@ -75,6 +75,13 @@ struct SpeciesBufs {
     double *k[3];           // k1, k3, k4
 };
 
+// Multigrid level (FP32 mirror, mixed precision).
+struct MGLevelF {
+    int nx, ny, pitch;
+    float *mc, *ce, *cn, *extra, *inv_mc;
+    float *rhs, *x, *res;
+};
+
 // Multigrid level (FP64 plain path).
 struct MGLevel {
     int nx, ny, pitch;      // interior size; fields are (ny+2) x pitch with ghost ring
@@ -151,6 +158,20 @@ struct fs_ctx {
     double prof_ms[PROF_NCLASS];
     int64_t prof_n[PROF_NCLASS];
 
+    // mixed precision (FS_PREC_MIXED): FP32 log-density companions of the
+    // state buffers, FP32 stage derivatives, FP32 face data and table, FP32
+    // multigrid hierarchy
+    int mixed;
+    float *lbuf[FS_MAX_SPECIES][FS_NBUF];
+    float *k32[FS_MAX_SPECIES][3];
+    float *f32[10];              // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
+    float *d_tab32;
+    MGLevelF mgf[FS_MG_MAX_LEVELS];
+    cudaGraph_t cgm_graph;
+    cudaGraphExec_t cgm_exec;
+    int cgm_graph_built;
+    int cgm_body_kernels;
+
     // host mirrors of scalar state
     double t, dt;
     double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or;
@@ -163,14 +184,25 @@ int fs_set_error(fs_ctx *c, int code, const char *fmt, ...);
 void fs_host_constants(const fs_config &cfg, fs_constants &k);
 void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<double> &rows);
 
-// particle kernels (fs_ptcl.cu)
+// particle kernels (fs_ptcl.cu; the mixed-precision step in fs_mixed.cu)
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts);
+int fs_ptcl_step_mixed(fs_ctx *c, int *attempts);
+int fs_mixed_alloc(fs_ctx *c, const std::vector<double> &tab_rows);
+void fs_mixed_free(fs_ctx *c);
+int fs_mixed_sync_logs(fs_ctx *c);   // FP32 log companions of every state buffer
+void fs_faces_update_mixed(fs_ctx *c);
+int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres);
 int fs_ptcl_alloc(fs_ctx *c);
+void fs_ptcl_reset(fs_ctx *c);     // t_m, status and current rows of a new step
+int fs_ptcl_control(fs_ctx *c);   // controller + status check after five stages
 void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
 void fs_lapl_free(fs_ctx *c);
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
+// mixed-precision Poisson (fs_lapl_mixed.cu)
+int fs_lapl_alloc_mixed(fs_ctx *c);
+void fs_lapl_free_mixed(fs_ctx *c);
 // misc device helpers (fs_api.cu)
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
 int fs_sync_ctrl(fs_ctx *c);

@@ -1,0 +1,729 @@
+// fs_lapl_mixed.cu -- the semi-implicit Poisson solve in mixed precision
+// (FS_PREC_MIXED).
+//
+// Same system as fs_lapl.cu (laplEqn lapl_lib.F90:123-379, laplJ :381-609,
+// dFdPh :611-636), split by precision:
+//   * assembly: the flux and flux-derivative terms (every exponential) and
+//     the matrix coefficients in FP32; the Gauss-law part of the right-hand
+//     side, div E + n_i - n_e, and the assembled right-hand side in FP64;
+//   * the multigrid hierarchy and every V-cycle in FP32;
+//   * CG in FP64: the iterate, the residual, the search directions, the
+//     operator product (FP64 arithmetic on the FP32 coefficients) and every
+//     dot product.  Each V-cycle solves the correction equation for the FP64
+//     residual in FP32 -- the iterative-refinement step -- and the outer
+//     iteration is flexible CG (beta = z_new.(r_new - r_old) / z_old.r_old),
+//     which tolerates the rounding of the FP32 preconditioner, so the
+//     residual reaches lapl_rtol exactly as in the FP64 solver.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "fs_internal.h"
+#include "fs_mg.cuh"
+
+#define ABX 32
+#define ABY 8
+#define ANT (ABX * ABY)
+
+namespace {
+
+// B(x) = x/(e^x - 1) at +-a and -B'(+-a), from one expm1f.
+//   bm = B(-a), bp = B(a), dm = -B'(-a), dp = -B'(a);  dm + dp = 1.
+__device__ __forceinline__ void bern4(float a, float &bm, float &bp, float &dm, float &dp) {
+    const float x = fabsf(a);
+    float b_neg, b_pos, d_pos;   // B(-x), B(x), -B'(x) for x >= 0
+    if (x < 1e-3f) {
+        b_neg = 1.0f + 0.5f * x + x * x * (1.0f / 12.0f);
+        b_pos = 1.0f - 0.5f * x + x * x * (1.0f / 12.0f);
+    } else {
+        const float d = -expm1f(-x);      // 1 - e^-x
+        b_neg = x / d;
+        b_pos = b_neg * (1.0f - d);
+    }
+    if (x < 0.5f) {
+        const float x2 = x * x;
+        d_pos = 0.5f - x * (1.0f / 6.0f - x2 * (1.0f / 180.0f - x2 * (1.0f / 5040.0f - x2 * (1.0f / 151200.0f))));
+    } else {
+        const float d = -expm1f(-x), em = 1.0f - d;
+        d_pos = em * (x - d) / (d * d);
+    }
+    if (a >= 0.0f) { bm = b_neg; bp = b_pos; dp = d_pos; dm = 1.0f - d_pos; }
+    else { bm = b_pos; bp = b_neg; dm = d_pos; dp = 1.0f - d_pos; }
+}
+
+struct AsmMixArgs {
+    PhysParams pp;
+    MeshDev m;
+    const float *tab;
+    const double *ni, *ne, *nt, *ph, *phm;
+    const double *fx_e, *fy_e;
+    const float *f[10];
+    const Ctrl *ctrl;
+    Ctrl *ctrl_w;
+    float *mc, *ce, *cn, *extra, *inv_mc;
+    double *rhs, *dinv;
+};
+
+__device__ __forceinline__ void tab32(const PhysParams &pp, float lneps, int &k, float &w) {
+    float u = (lneps - (float)pp.lemin) * (float)pp.inv_h;
+    if (!(u >= 0.0f)) u = 0.0f;
+    if (u > (float)(pp.ntab - 1)) u = (float)(pp.ntab - 1);
+    int i = (int)u;
+    if (i > pp.ntab - 2) i = pp.ntab - 2;
+    k = i;
+    w = u - (float)i;
+}
+__device__ __forceinline__ float tv32(const float *tab, int k, float w, int row) {
+    const float *t = tab + (size_t)k * FS_TAB_STRIDE;
+    return __ldg(t + row) + w * __ldg(t + 8 + row);
+}
+
+// Interior face: ion and electron fluxes and the face conductance
+// 1/h + dt (mui/h dFi + mue/h dFe).
+__device__ __forceinline__ void sg_face_mix(const PhysParams &pp, const float *fc, size_t of, float E,
+                                            float Emi, bool same, float dh, float idh, float mue, float De,
+                                            float nil, float nir, float nel, float ner, float dt,
+                                            float &fi, float &fe, float &cf) {
+    const float mui = (float)pp.mui;
+    fi = fc[1] * nil - fc[2] * nir;
+    float dFi;
+    if (same) {
+        dFi = fc[3] * nil + fc[4] * nir;
+    } else {
+        float bm, bp, dm, dp;
+        bern4(mui * Emi * dh / (float)pp.Di, bm, bp, dm, dp);
+        dFi = fabs(pp.mui * (double)Emi) < 1e-12 ? 0.0f : dm * nil + dp * nir;
+    }
+    float bm, bp, dm, dp;
+    const float ae = -mue * E * dh / De;
+    bern4(ae, bm, bp, dm, dp);
+    fe = De * idh * (bm * nel - bp * ner);
+    float dFe;
+    if (same) {
+        dFe = fabsf(mue * E) < 1e-12f ? 0.0f : dm * nel + dp * ner;
+    } else {
+        bern4(-mue * Emi * dh / De, bm, bp, dm, dp);
+        dFe = fabsf(mue * Emi) < 1e-12f ? 0.0f : dm * nel + dp * ner;
+    }
+    cf = idh + dt * (mui * idh * dFi + mue * idh * dFe);
+}
+
+__global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
+    __shared__ float s_ni[ABY + 2][ABX + 2], s_ne[ABY + 2][ABX + 2];
+    __shared__ float s_te[ABY + 2][ABX + 2], s_mu[ABY + 2][ABX + 2], s_de[ABY + 2][ABX + 2];
+    __shared__ float s_xfi[ABY][ABX + 1], s_xfe[ABY][ABX + 1], s_xc[ABY][ABX + 1];
+    __shared__ float s_yfi[ABY + 1][ABX], s_yfe[ABY + 1][ABX], s_yc[ABY + 1][ABX];
+    __shared__ double s_xe[ABY][ABX + 1], s_ye[ABY + 1][ABX];
+    const PhysParams &pp = a.pp;
+    const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
+    const int tid = threadIdx.x;
+    const int gx0 = blockIdx.x * ABX + 1, gy0 = blockIdx.y * ABY + 1;
+    const double dt = a.ctrl->dt;
+    const float dtf = (float)dt;
+    const float ln_ph0 = (float)log(pp.ph0);
+    const float mui = (float)pp.mui, vi = (float)pp.vi, gam = (float)pp.gam;
+    const float ve_c = (float)pp.ve_coef, t0_x0 = (float)(pp.t0 / pp.x0);
+    unsigned int st = 0;
+    for (int q = tid; q < (ABX + 2) * (ABY + 2); q += ANT) {
+        int lx = q % (ABX + 2), ly = q / (ABX + 2);
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        bool in = gi <= nx + 1 && gj <= ny + 1;
+        size_t o = (size_t)gj * P + gi;
+        float ni = in ? (float)a.ni[o] : 0.0f, ne = in ? (float)a.ne[o] : 0.0f;
+        s_ni[ly][lx] = ni;
+        s_ne[ly][lx] = ne;
+        float te = 0, mu = 0, de = 0;
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
+            float nte = (float)a.nt[o];
+            if ((nte >= 0.0f) && (ne >= 0.0f)) te = nte / ne;
+            else { st |= FS_ST_NEG_DENSITY; te = 1e-8f; }
+            int k; float w;
+            tab32(pp, logf(te) + ln_ph0, k, w);
+            mu = tv32(a.tab, k, w, 0);
+            de = tv32(a.tab, k, w, 1);
+        }
+        s_te[ly][lx] = te; s_mu[ly][lx] = mu; s_de[ly][lx] = de;
+    }
+    __syncthreads();
+    // x faces between gi and gi+1
+    for (int q = tid; q < ABY * (ABX + 1); q += ANT) {
+        int c = q % (ABX + 1), r = q / (ABX + 1);
+        int gi = gx0 - 1 + c, gj = gy0 + r;
+        if (gj > ny || gi > nx) continue;
+        int lx = c, ly = r + 1;
+        const size_t of = (size_t)gj * P + gi;
+        const float dh = (float)a.m.dx[gi], idh = (float)a.m.inv_dx[gi];
+        const double E64 = a.fx_e[of];
+        const float E = a.f[0][of];
+        int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;
+        int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;
+        float fi = 0, fe = 0, cf = 0;
+        double eu = E64;
+        if (gi == 0 && tr == -1) {
+            eu = 0.0;
+        } else if (gi == nx && tl == 1) {
+            eu = 0.0;
+        } else if ((gi == 0 && tr == -2) || (gi == nx && tl == 2)) {   // electrode rows
+            const bool left = gi == 0;
+            const int lc = left ? lx + 1 : lx;
+            const size_t og = (size_t)gj * P + (left ? 0 : nx + 1), oc = (size_t)gj * P + (left ? 1 : nx);
+            const float te = s_te[ly][lc], ni = s_ni[ly][lc], ne = s_ne[ly][lc], mue = s_mu[ly][lc];
+            const int ac = (a.ph[og] > a.ph[oc]) ? 1 : 0;
+            const float aa = (float)ac;
+            const float ve = sqrtf(ve_c * te) * t0_x0;
+            const float sgn = left ? -1.0f : 1.0f;
+            fi = (1.0f - aa) * mui * E * ni + sgn * (0.25f * vi * ni);
+            fe = -(aa * mue * E * ne) + sgn * (0.25f * ve * ne) - gam * fi;
+            float dfi, dfe;
+            if (left) {
+                dfi = (float)(1 - ac) * mui * ni * idh;
+                dfe = -((float)ac * mue * ne * idh) - gam * dfi;
+                cf = idh + dtf * (dfi - dfe);
+            } else {
+                dfi = (float)(ac - 1) * mui * ni * idh;
+                dfe = (float)ac * mue * ne * idh - gam * dfi;
+                cf = idh - dtf * (dfi - dfe);
+            }
+        } else {
+            const float mue = 0.5f * (s_mu[ly][lx] + s_mu[ly][lx + 1]);
+            const float De = 0.5f * (s_de[ly][lx] + s_de[ly][lx + 1]);
+            const size_t ol = (size_t)gj * P + gi;
+            const bool same = a.phm[ol] == a.ph[ol] && a.phm[ol + 1] == a.ph[ol + 1];
+            const float Emi = same ? E : (float)(-(a.phm[ol + 1] - a.phm[ol]) / a.m.dx[gi]);
+            const float fc[5] = {E, a.f[1][of], a.f[2][of], a.f[3][of], a.f[4][of]};
+            sg_face_mix(pp, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly][lx + 1],
+                        s_ne[ly][lx], s_ne[ly][lx + 1], dtf, fi, fe, cf);
+            if (isnan(cf)) st |= FS_ST_DFDPH_NAN;
+        }
+        s_xfi[r][c] = fi; s_xfe[r][c] = fe; s_xe[r][c] = eu; s_xc[r][c] = cf;
+    }
+    // y faces between gj and gj+1
+    for (int q = tid; q < (ABY + 1) * ABX; q += ANT) {
+        int c = q % ABX, r = q / ABX;
+        int gi = gx0 + c, gj = gy0 - 1 + r;
+        if (gi > nx || gj > ny) continue;
+        int lx = c + 1, ly = r;
+        const size_t of = (size_t)gj * P + gi;
+        const float dh = (float)a.m.dy[gj], idh = (float)a.m.inv_dy[gj];
+        const double E64 = a.fy_e[of];
+        const float E = a.f[5][of];
+        int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
+        int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
+        float fi = 0, fe = 0, cf = 0;
+        double eu = E64;
+        if (gj == 0 && tt == -1) {
+            eu = 0.0;
+        } else if (gj == 0 && tt == -2) {
+            // laplEqn has no lower y electrode flux (zero); laplJ has its derivative
+            const int lc = ly + 1;
+            const float ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
+            const int ac = (a.ph[(size_t)0 * P + gi] > a.ph[(size_t)1 * P + gi]) ? 1 : 0;
+            const float dfi = (float)(1 - ac) * mui * ni / dh;
+            const float dfe = -((float)ac * mue * ne / dh) - gam * dfi;
+            cf = 1.0f / dh + dtf * (dfi - dfe);
+        } else if (gj == ny && tb == 1) {
+            eu = 0.0;
+        } else if (gj == ny && tb == 2) {
+            const int lc = ly;
+            const float te = s_te[lc][lx], ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
+            const int ac = (a.ph[(size_t)(ny + 1) * P + gi] > a.ph[(size_t)ny * P + gi]) ? 1 : 0;
+            const float aa = (float)ac;
+            const float ve = sqrtf(ve_c * te) * t0_x0;
+            fi = (1.0f - aa) * mui * E * ni + 0.25f * vi * ni;
+            fe = -(aa * mue * E * ne) + 0.25f * ve * ne - gam * fi;
+            const float dfi = (float)(ac - 1) * mui * ni / dh;
+            const float dfe = (float)ac * mue * ne / dh - gam * dfi;
+            cf = 1.0f / dh - dtf * (dfi - dfe);
+        } else {
+            const float mue = 0.5f * (s_mu[ly][lx] + s_mu[ly + 1][lx]);
+            const float De = 0.5f * (s_de[ly][lx] + s_de[ly + 1][lx]);
+            const size_t ol = (size_t)gj * P + gi;
+            const bool same = a.phm[ol] == a.ph[ol] && a.phm[ol + P] == a.ph[ol + P];
+            const float Emi = same ? E : (float)(-(a.phm[ol + P] - a.phm[ol]) / a.m.dy[gj]);
+            const float fc[5] = {E, a.f[6][of], a.f[7][of], a.f[8][of], a.f[9][of]};
+            sg_face_mix(pp, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly + 1][lx],
+                        s_ne[ly][lx], s_ne[ly + 1][lx], dtf, fi, fe, cf);
+            if (isnan(cf)) st |= FS_ST_DFDPH_NAN;
+        }
+        s_yfi[r][c] = fi; s_yfe[r][c] = fe; s_ye[r][c] = eu; s_yc[r][c] = cf;
+    }
+    __syncthreads();
+    const int lx = tid % ABX, ly = tid / ABX;
+    const int gi = gx0 + lx, gj = gy0 + ly;
+    if (gi <= nx && gj <= ny) {
+        const size_t o = (size_t)gj * P + gi;
+        const double dlx = a.m.dlx[gi - 1], dly = a.m.dly[gj - 1];
+        const double idlx = a.m.inv_dlx[gi - 1], idly = a.m.inv_dly[gj - 1];
+        const int tx = a.m.tx[(gj - 1) * nx + gi - 1], ty = a.m.ty[(gj - 1) * nx + gi - 1];
+        const double wr = pp.cyl ? a.m.r[gj] : 1.0;
+        const double wn = pp.cyl ? (a.m.r[gj + 1] + a.m.r[gj]) / 2.0 : 1.0;
+        const double ws = pp.cyl ? (a.m.r[gj] + a.m.r[gj - 1]) / 2.0 : 1.0;
+        // Gauss-law part in FP64
+        double dfdx = -(s_xe[ly][lx + 1] - s_xe[ly][lx]) * idlx;
+        double dfdy = pp.cyl ? -(s_ye[ly + 1][lx] * wn - s_ye[ly][lx] * ws) / dly / wr
+                             : -(s_ye[ly + 1][lx] - s_ye[ly][lx]) * idly;
+        // flux divergence in FP32
+        const float fidlx = (float)idlx, fidly = (float)idly;
+        float div = ((s_xfi[ly][lx + 1] - s_xfi[ly][lx]) - (s_xfe[ly][lx + 1] - s_xfe[ly][lx])) * fidlx;
+        if (pp.cyl) {
+            const float fwn = (float)wn, fws = (float)ws, fwr = (float)wr;
+            div += ((s_yfi[ly + 1][lx] * fwn - s_yfi[ly][lx] * fws) - (s_yfe[ly + 1][lx] * fwn - s_yfe[ly][lx] * fws))
+                   * fidly / fwr;
+        } else {
+            div += ((s_yfi[ly + 1][lx] - s_yfi[ly][lx]) - (s_yfe[ly + 1][lx] - s_yfe[ly][lx])) * fidly;
+        }
+        double b = dfdx + dfdy + (a.ni[o] - a.ne[o]) - dt * (double)div;
+        if (isnan(b)) st |= FS_ST_BNAN;
+        const float cw = s_xc[ly][lx], cee = s_xc[ly][lx + 1], cs = s_yc[ly][lx], cnn = s_yc[ly + 1][lx];
+        const float offw = gi > 1 ? cw : 0.0f, offe = gi < nx ? cee : 0.0f;
+        const float offs = gj > 1 ? cs : 0.0f, offn = gj < ny ? cnn : 0.0f;
+        float gx = 0.0f, gys = 0.0f, gyn = 0.0f;
+        if (gi == 1 && tx == -2) gx += cw;
+        if (gi == nx && tx == 2) gx += cee;
+        if (gj == 1 && ty == -2) gys += cs;
+        if (gj == ny && ty == 2) gyn += cnn;
+        if (gi == 1 && tx == -1) gx += (float)(1.0 / a.m.dx[0] - 1.0 / a.m.dx[1]);
+        if (gj == 1 && ty == -1) gyn += (float)(1.0 / a.m.dy[0] - 1.0 / a.m.dy[1]);
+        const float sx = (float)(dly * wr), fdlx = (float)dlx, fwn = (float)wn, fws = (float)ws;
+        const float extra = gx * sx + (gys * fws + gyn * fwn) * fdlx;
+        const float mc = (offw + offe) * sx + (offs * fws + offn * fwn) * fdlx + extra;
+        const double D = dlx * dly * wr;
+        a.mc[o] = mc;
+        a.inv_mc[o] = 1.0f / mc;
+        a.extra[o] = extra;
+        a.ce[o] = offe * sx;
+        a.cn[o] = offn * fwn * fdlx;
+        a.rhs[o] = b * D;
+        a.dinv[o] = 1.0 / D;
+    }
+    if (st) atomicOr(&a.ctrl_w->status, st);
+}
+
+// ---------------------------------------------------------------- FP64 CG
+struct CgmArgs {
+    int nx, ny, P, nblk;
+    dim3 grid;
+    double *x, *r, *p, *q, *rhs, *dinv, *part;
+    float *z, *r32;
+    const float *mc, *ce, *cn;
+    Ctrl *ctrl;
+    double rtol;
+    int maxit;
+    int use_cond;
+    cudaGraphConditionalHandle cond;
+};
+
+__global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
+    double v = 0.0;
+    CG_NODES(a, {
+        const double b = a.rhs[o];
+        a.x[o] = 0.0;
+        a.r[o] = b;
+        a.r32[o] = (float)b;
+        a.p[o] = 0.0;
+        a.q[o] = 0.0;
+        double u = b * a.dinv[o];
+        v += u * u;
+    })
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[0], a.nblk, &out) && threadIdx.x == 0) {
+        a.ctrl->bnorm2 = out;
+        a.ctrl->rnorm2 = out;
+        a.ctrl->relres = out > 0.0 ? 1.0 : 0.0;
+        a.ctrl->cg_done = out == 0.0 ? 1 : 0;
+        a.ctrl->cg_iters = 0;
+        a.ctrl->cg_fail = 0;
+        a.ctrl->rz = 0.0;
+    }
+}
+
+// rz = r.z and z.q (q = M p of the previous direction) in one pass, then the
+// flexible beta = -alpha z.q / rz_old (0 on the first iteration).
+__device__ __forceinline__ double block_sum2(double v, double w, double &wsum) {
+    __shared__ double s_a[8], s_b[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+        w += __shfl_down_sync(0xffffffffu, w, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { s_a[wid] = v; s_b[wid] = w; }
+    __syncthreads();
+    double ra = 0.0, rb = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 8; k++) { ra += s_a[k]; rb += s_b[k]; }
+    wsum = rb;
+    return ra;
+}
+
+__global__ void __launch_bounds__(256) k_cgm_rz(const CgmArgs a) {
+    double v = 0.0, w = 0.0;
+    CG_NODES(a, {
+        const double z = a.z[o];
+        v += a.r[o] * z;
+        w += z * a.q[o];
+    })
+    double ws;
+    double vs = block_sum2(v, w, ws);
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        a.part[blockIdx.x] = vs;
+        a.part[a.nblk + blockIdx.x] = ws;
+        __threadfence();
+        unsigned int prev = atomicAdd(&a.ctrl->counter[1], 1u);
+        s_last = prev == (unsigned int)a.nblk - 1u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    __shared__ double s_r[256], s_w[256];
+    double sv = 0.0, sw = 0.0;
+    for (int b = threadIdx.x; b < a.nblk; b += 256) {
+        sv += ((volatile double *)a.part)[b];
+        sw += ((volatile double *)a.part)[a.nblk + b];
+    }
+    s_r[threadIdx.x] = sv;
+    s_w[threadIdx.x] = sw;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) { s_r[threadIdx.x] += s_r[threadIdx.x + k]; s_w[threadIdx.x] += s_w[threadIdx.x + k]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->counter[1] = 0u;
+        c->rz_old = c->rz;
+        c->rz = s_r[0];
+        c->beta = c->cg_iters == 0 ? 0.0 : -c->alpha * s_w[0] / c->rz_old;
+    }
+}
+
+// p = z + beta p ; q = M z + beta q ; pq = p.q ; alpha = rz / pq (FP64
+// arithmetic on the FP32 preconditioned residual and coefficients)
+__global__ void __launch_bounds__(256) k_cgm_pq(const CgmArgs a) {
+    double v = 0.0;
+    const double be = a.ctrl->beta;
+    CG_NODES(a, {
+        const double zc = a.z[o];
+        double mz = (double)a.mc[o] * zc - (double)a.ce[o] * (double)a.z[o + 1]
+                  - (double)a.ce[o - 1] * (double)a.z[o - 1] - (double)a.cn[o] * (double)a.z[o + a.P]
+                  - (double)a.cn[o - a.P] * (double)a.z[o - a.P];
+        double pn = zc + be * a.p[o];
+        double qn = mz + be * a.q[o];
+        a.p[o] = pn;
+        a.q[o] = qn;
+        v += pn * qn;
+    })
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->pq = out;
+        if (c->cg_done) c->alpha = 0.0;
+        else if (!(out > 0.0)) { c->cg_fail = 1; c->alpha = 0.0; }
+        else c->alpha = c->rz / out;
+    }
+}
+
+// x += alpha p ; r -= alpha q (FP64) ; r32 = r for the next V-cycle
+__global__ void __launch_bounds__(256) k_cgm_xr(const CgmArgs a) {
+    double v = 0.0;
+    const double al = a.ctrl->alpha;
+    CG_NODES(a, {
+        a.x[o] += al * a.p[o];
+        double rr = a.r[o] - al * a.q[o];
+        a.r[o] = rr;
+        a.r32[o] = (float)rr;
+        double u = rr * a.dinv[o];
+        v += u * u;
+    })
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->rnorm2 = out;
+        c->cg_iters += 1;
+        c->relres = c->bnorm2 > 0.0 ? sqrt(out / c->bnorm2) : 0.0;
+        if (c->relres <= a.rtol) c->cg_done = 1;
+        if (isnan(out)) c->cg_fail = 1;
+        if (a.use_cond && (c->cg_done || c->cg_fail || c->cg_iters >= a.maxit))
+            cudaGraphSetConditional(a.cond, 0u);
+    }
+}
+
+LevelT<float> level_f(const MGLevelF &m) {
+    LevelT<float> L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.extra = m.extra; L.inv_mc = m.inv_mc;
+    L.rhs = m.rhs; L.x = m.x; L.res = nullptr;
+    return L;
+}
+LvT<float> lvt_f(const MGLevelF &m) {
+    LvT<float> L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x;
+    return L;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+int fs_lapl_alloc_mixed(fs_ctx *c) {
+    for (int l = 0; l < c->mg_nlev; l++) {
+        MGLevelF &m = c->mgf[l];
+        m.nx = c->mg[l].nx;
+        m.ny = c->mg[l].ny;
+        m.pitch = c->mg[l].pitch;
+        const size_t n = (size_t)(m.ny + 2) * m.pitch;
+        float **fields[] = {&m.mc, &m.ce, &m.cn, &m.extra, &m.inv_mc, &m.rhs, &m.x};
+        for (float **f : fields) {
+            cudaError_t e = cudaMalloc(f, n * sizeof(float));
+            if (e == cudaSuccess) e = cudaMemset(*f, 0, n * sizeof(float));
+            if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 multigrid)");
+        }
+        m.res = nullptr;
+    }
+    if (c->cg_nblk < 2 * 4 * c->nsm) {   // k_cgm_rz keeps two partials per CTA
+        cudaFree(c->d_cg_part);
+        cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * 2 * 4 * c->nsm);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (CG partials)");
+        c->cg_nblk = 2 * 4 * c->nsm;
+    }
+    cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<float>(2));
+    cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
+    return FS_OK;
+}
+
+void fs_lapl_free_mixed(fs_ctx *c) {
+    if (c->cgm_graph_built) {
+        cudaGraphExecDestroy(c->cgm_exec);
+        cudaGraphDestroy(c->cgm_graph);
+        c->cgm_graph_built = 0;
+    }
+    for (int l = 0; l < FS_MG_MAX_LEVELS; l++) {
+        MGLevelF &m = c->mgf[l];
+        float *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.rhs, m.x};
+        for (float *f : fs) cudaFree(f);
+        memset(&m, 0, sizeof(m));
+    }
+}
+
+// FP32 V-cycle on the correction equation: mgf[0].rhs holds the FP64
+// residual rounded to FP32, mgf[0].x receives z.
+static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
+    const int nl = c->mg_nlev, nu = c->cfg.mg_smooth;
+    const bool fused = nu == 2;
+    int lb = 0;
+    while (lb < nl && (c->mgf[lb].nx > BOTTOM_N || c->mgf[lb].ny > BOTTOM_N)) lb++;
+    dim3 b(32, 8);
+    for (int l = 0; l < lb; l++) {
+        LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+        if (fused) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_down<float, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_down_smem<float>(2), c->stream>>>(
+                lvt_f(c->mgf[l]), lvt_f(c->mgf[l + 1]));
+            fs_prof_end(c);
+            continue;
+        }
+        dim3 g = grid2((f.nx + 1) / 2, f.ny, b);
+        for (int it = 0; it < nu; it++) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_rb<float><<<g, b, 0, c->stream>>>(f, 0, it == 0);
+            fs_prof_end(c);
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_rb<float><<<g, b, 0, c->stream>>>(f, 1, 0);
+            fs_prof_end(c);
+        }
+        fs_prof_begin(c, PROF_TRANSFER);
+        k_restrict<float><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
+    }
+    BottomArgs<float> ba;
+    for (int l = 0; l < nl; l++) ba.L[l] = level_f(c->mgf[l]);
+    ba.lb = lb;
+    ba.nl = nl;
+    ba.nu = nu;
+    fs_prof_begin(c, PROF_BOTTOM);
+    k_bottom<float><<<1, BOTTOM_THREADS, 0, c->stream>>>(ba);
+    fs_prof_end(c);
+    for (int l = lb - 1; l >= 0; l--) {
+        LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+        if (fused) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_up<float, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_up_smem<float>(2), c->stream>>>(
+                lvt_f(c->mgf[l]), lvt_f(c->mgf[l + 1]));
+            fs_prof_end(c);
+            continue;
+        }
+        dim3 g = grid2(f.nx, f.ny, b), gh = grid2((f.nx + 1) / 2, f.ny, b);
+        fs_prof_begin(c, PROF_TRANSFER);
+        k_prolong<float><<<g, b, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
+        for (int it = 0; it < nu; it++) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_rb<float><<<gh, b, 0, c->stream>>>(f, 1, 0);
+            fs_prof_end(c);
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_rb<float><<<gh, b, 0, c->stream>>>(f, 0, 0);
+            fs_prof_end(c);
+        }
+    }
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_rz<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+}
+
+static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
+    vcycle_mixed(c, ca);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_pq<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_xr<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+}
+
+// WHILE(cond) { one iteration } -> phi update, as one graph (see fs_lapl.cu)
+static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "CG graph create");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return fs_cuda_check(c, e, "CG while node"); }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ca.use_cond = 1;
+    ca.cond = h;
+    const int prof = c->prof_on;
+    c->prof_on = 0;
+    const int64_t l0 = c->launches;
+    e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cg_iteration_mixed(c, ca);
+        e = cudaStreamEndCapture(c->stream, &body);
+    }
+    c->cgm_body_kernels = (int)(c->launches - l0);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        k_phi_update<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
+        e = cudaStreamEndCapture(c->stream, &g);
+    }
+    c->launches = l0;
+    c->prof_on = prof;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cgm_exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fs_cuda_check(c, e, "CG graph capture");
+    }
+    c->cgm_graph = g;
+    c->cgm_graph_built = 1;
+    return FS_OK;
+}
+
+int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
+    fs_faces_update_mixed(c);
+    AsmMixArgs a;
+    a.pp = c->pp;
+    a.m = c->mesh;
+    a.tab = c->d_tab32;
+    a.ni = c->sp[0].buf[c->lev[0]];
+    a.ne = c->sp[1].buf[c->lev[0]];
+    a.nt = c->sp[2].buf[c->lev[0]];
+    a.ph = c->ph;
+    a.phm = c->ph_mi;
+    a.fx_e = c->fx_e;
+    a.fy_e = c->fy_e;
+    for (int k = 0; k < 10; k++) a.f[k] = c->f32[k];
+    a.ctrl = c->d_ctrl;
+    a.ctrl_w = c->d_ctrl;
+    MGLevelF &m0 = c->mgf[0];
+    a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
+    a.rhs = c->bs;
+    a.dinv = c->dinv;
+    cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);
+    fs_prof_begin(c, PROF_ASSEMBLE);
+    k_assemble_mix<<<grid2(c->nx, c->ny, dim3(ABX, ABY)), ANT, 0, c->stream>>>(a);
+    fs_prof_end(c);
+    dim3 b2(16, 16);
+    for (int l = 0; l + 1 < c->mg_nlev; l++) {
+        LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+        fs_prof_begin(c, PROF_COARSEN);
+        k_coarsen<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(f, cc);
+        fs_prof_end(c);
+        fs_prof_begin(c, PROF_COARSEN);
+        k_coarsen_diag<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
+        fs_prof_end(c);
+    }
+    CgmArgs ca;
+    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;
+    {
+        long nb = ((long)c->nx * c->ny + 255) / 256, cap = 4L * c->nsm;
+        ca.nblk = (int)(nb < cap ? nb : cap);
+        ca.grid = dim3(ca.nblk);
+    }
+    ca.x = c->xs; ca.r = c->r; ca.p = c->p; ca.q = c->q;
+    ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
+    ca.z = m0.x; ca.r32 = m0.rhs;
+    ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
+    ca.ctrl = c->d_ctrl;
+    ca.rtol = c->cfg.lapl_rtol;
+    ca.maxit = c->cfg.lapl_maxit;
+    ca.use_cond = 0;
+    ca.cond = 0;
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_init<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    int rc = fs_sync_ctrl(c);
+    if (rc) return rc;
+    if (c->h_ctrl->status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
+    if (c->h_ctrl->status & FS_ST_DFDPH_NAN) return fs_set_error(c, FS_ERR_NAN, "NaN in dFdPh");
+    if (c->h_ctrl->status & FS_ST_BNAN) {
+        *lerr = 1; *iters = 0; *relres = NAN;
+        return FS_OK;
+    }
+    bool ok = c->h_ctrl->cg_done != 0;
+    static const bool no_graph = getenv("FS_NO_GRAPH") != nullptr;
+    const int poisson_classes = (1 << PROF_SMOOTH) | (1 << PROF_TRANSFER) | (1 << PROF_BOTTOM) | (1 << PROF_CG);
+    if (!ok && !no_graph && !(c->prof_on & poisson_classes)) {
+        if (!c->cgm_graph_built && (rc = build_cgm_graph(c, ca))) return rc;
+        cudaError_t e = cudaGraphLaunch(c->cgm_exec, c->stream);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "CG graph launch");
+        rc = fs_sync_ctrl(c);
+        if (rc) return rc;
+        c->launches += (int64_t)c->h_ctrl->cg_iters * c->cgm_body_kernels + 1;
+        *iters = c->h_ctrl->cg_iters;
+        *relres = c->h_ctrl->relres;
+        bool conv = c->h_ctrl->cg_done && !c->h_ctrl->cg_fail;
+        *lerr = conv ? 0 : 1;
+        if (conv) c->faces_valid = 0;
+        return FS_OK;
+    }
+    int it = 0;
+    while (!ok && it < c->cfg.lapl_maxit) {
+        cg_iteration_mixed(c, ca);
+        rc = fs_sync_ctrl(c);
+        if (rc) return rc;
+        it = c->h_ctrl->cg_iters;
+        if (c->h_ctrl->cg_fail) break;
+        ok = c->h_ctrl->cg_done != 0;
+    }
+    *iters = c->h_ctrl->cg_iters;
+    *relres = c->h_ctrl->relres;
+    if (!ok) {
+        *lerr = 1;
+        return FS_OK;
+    }
+    *lerr = 0;
+    c->faces_valid = 0;
+    c->launches++;
+    k_phi_update<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels (mixed)");
+    return FS_OK;
+}

@@ -1,0 +1,381 @@
+// fs_mg.cuh -- multigrid building blocks shared by the FP64 and the mixed
+// precision Poisson solvers: deterministic grid reductions, the 2x2
+// aggregation hierarchy (coarse operators, red-black Gauss-Seidel, restriction,
+// prolongation), the temporally blocked level kernels and the one-CTA bottom
+// solver, each templated on the arithmetic type of the level.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fs_internal.h"
+
+#define BOTTOM_N 32
+#define BOTTOM_THREADS 1024
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of v, then deterministic grid sum by the last CTA.  Returns true
+// in the last CTA (all threads), with *out written.
+template <int NTH>
+__device__ bool grid_sum(double v, double *part, unsigned int *counter, int nblk, double *out) {
+    __shared__ double s_w[NTH / 32];
+    __shared__ bool s_last;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int bid = blockIdx.x + blockIdx.y * gridDim.x;
+    v = warp_sum_d(v);
+    if ((tid & 31) == 0) s_w[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NTH / 32; w++) s += s_w[w];
+        part[bid] = s;
+        __threadfence();
+        unsigned int prev = atomicAdd(counter, 1u);
+        s_last = (prev == (unsigned int)nblk - 1u);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    __shared__ double s_r[NTH];
+    double s = 0.0;
+    for (int b = tid; b < nblk; b += NTH) s += ((volatile double *)part)[b];
+    s_r[tid] = s;
+    __syncthreads();
+    for (int w = NTH / 2; w > 0; w >>= 1) {
+        if (tid < w) s_r[tid] += s_r[tid + w];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *out = s_r[0];
+        *counter = 0u;
+    }
+    __syncthreads();
+    return true;
+}
+
+// ---------------------------------------------------------------- multigrid
+template <typename T>
+struct LevelT {
+    int nx, ny, P;
+    T *mc, *ce, *cn, *extra, *inv_mc, *rhs, *x, *res;
+};
+using LevelDev = LevelT<double>;
+
+template <typename T>
+__device__ __forceinline__ T inv_or_big(T c) {
+    const T tiny = sizeof(T) == 8 ? T(1e-300) : T(1e-37), big = sizeof(T) == 8 ? T(1e300) : T(1e37);
+    return c > tiny ? T(1) / c : big;
+}
+
+// coarse operator of one aggregate level (series along, parallel across faces)
+template <typename T>
+__device__ void coarsen_cell(const LevelT<T> &f, const LevelT<T> &c, int I, int J) {
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    const size_t oc = (size_t)J * c.P + I;
+    T ce = T(0), cn = T(0), ex = T(0);
+    if (I < c.nx) {
+        const int gx0 = fx1 + 1, gx1 = min(fx1 + 2, f.nx);
+        for (int fy = fy0; fy <= fy1; fy++) {
+            T R = inv_or_big(f.ce[(size_t)fy * f.P + fx1]);
+            if (fx1 > fx0) R += T(0.5) * inv_or_big(f.ce[(size_t)fy * f.P + fx0]);
+            if (gx1 > gx0) R += T(0.5) * inv_or_big(f.ce[(size_t)fy * f.P + gx0]);
+            ce += T(1) / R;
+        }
+    }
+    if (J < c.ny) {
+        const int gy0 = fy1 + 1, gy1 = min(fy1 + 2, f.ny);
+        for (int fx = fx0; fx <= fx1; fx++) {
+            T R = inv_or_big(f.cn[(size_t)fy1 * f.P + fx]);
+            if (fy1 > fy0) R += T(0.5) * inv_or_big(f.cn[(size_t)fy0 * f.P + fx]);
+            if (gy1 > gy0) R += T(0.5) * inv_or_big(f.cn[(size_t)gy0 * f.P + fx]);
+            cn += T(1) / R;
+        }
+    }
+    for (int fy = fy0; fy <= fy1; fy++)
+        for (int fx = fx0; fx <= fx1; fx++) {
+            T e = f.extra[(size_t)fy * f.P + fx];
+            if (e > T(0) && fx1 > fx0) {
+                T ci = f.ce[(size_t)fy * f.P + fx0];
+                e = T(1) / (T(1) / e + T(0.5) * inv_or_big(ci));
+            }
+            ex += e;
+        }
+    c.ce[oc] = ce;
+    c.cn[oc] = cn;
+    c.extra[oc] = ex;
+}
+
+template <typename T>
+__device__ void coarsen_diag(const LevelT<T> &c, int I, int J) {
+    const size_t oc = (size_t)J * c.P + I;
+    T mc = c.ce[oc] + c.ce[oc - 1] + c.cn[oc] + c.cn[oc - c.P] + c.extra[oc];
+    c.mc[oc] = mc;
+    c.inv_mc[oc] = mc > T(0) ? T(1) / mc : T(0);
+}
+
+template <typename T>
+__global__ void k_coarsen(const LevelT<T> f, const LevelT<T> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I <= c.nx && J <= c.ny) coarsen_cell(f, c, I, J);
+}
+template <typename T>
+__global__ void k_coarsen_diag(const LevelT<T> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I <= c.nx && J <= c.ny) coarsen_diag(c, I, J);
+}
+
+// Gauss-Seidel update of one node
+template <typename T>
+__device__ __forceinline__ T gs_node(const LevelT<T> &L, size_t o) {
+    return (L.rhs[o] + L.ce[o] * L.x[o + 1] + L.ce[o - 1] * L.x[o - 1] + L.cn[o] * L.x[o + L.P]
+            + L.cn[o - L.P] * L.x[o - L.P]) * L.inv_mc[o];
+}
+
+// one red (color 0) or black (color 1) half sweep; zero_init: x starts at 0
+// Each thread owns the column pair (2t+1, 2t+2) of a row and updates the
+// node of the swept colour in it, so every lane does useful FP64 work.
+template <typename T>
+__global__ void k_rb(const LevelT<T> L, int color, int zero_init) {
+    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int c0 = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + 1;
+    if (J > L.ny || c0 > L.nx) return;
+    const int I = ((c0 + J) & 1) == color ? c0 : c0 + 1, Io = I == c0 ? c0 + 1 : c0;
+    if (zero_init && Io <= L.nx) L.x[(size_t)J * L.P + Io] = T(0);
+    if (I > L.nx) return;
+    const size_t o = (size_t)J * L.P + I;
+    L.x[o] = zero_init ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
+}
+
+// coarse rhs = sum over the aggregate of the fine residual rhs - M x.  The
+// pre-smoothing ends with a black half sweep, after which every black node's
+// residual is zero (to rounding), so only the red nodes are summed.
+template <typename T>
+__device__ __forceinline__ T resid(const LevelT<T> &L, size_t o) {
+    return L.rhs[o] - (L.mc[o] * L.x[o] - L.ce[o] * L.x[o + 1] - L.ce[o - 1] * L.x[o - 1]
+                       - L.cn[o] * L.x[o + L.P] - L.cn[o - L.P] * L.x[o - L.P]);
+}
+template <typename T>
+__global__ void k_restrict(const LevelT<T> f, const LevelT<T> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > c.nx || J > c.ny) return;
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    T s = T(0);
+    for (int fy = fy0; fy <= fy1; fy++)
+        for (int fx = fx0; fx <= fx1; fx++)
+            if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
+    c.rhs[(size_t)J * c.P + I] = s;
+}
+template <typename T>
+__global__ void k_prolong(const LevelT<T> f, const LevelT<T> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > f.nx || J > f.ny) return;
+    f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+}
+
+// ---------------------------------------------- fused (temporally blocked) levels
+// One CTA owns an MTX x MTY tile of a level plus a halo of 2*nu nodes held in
+// shared memory.  Down: nu red-black sweeps from x = 0, the residual and its
+// 2x2 aggregate sums (the coarse right-hand side) in one launch.  Up: the
+// coarse correction and nu black-red sweeps in one launch.  With x = 0 the
+// first sweep needs no neighbours, and each later sweep updates a region one
+// ring smaller, so after 2*nu sweeps the tile (and, going down, its first
+// ring) holds exactly the values the unfused sweeps produce.
+#define MTX 32
+#define MTY 16
+
+template <typename T>
+struct LvT {
+    int nx, ny, P;
+    const T *mc, *ce, *cn, *inv_mc;
+    T *rhs, *x;
+};
+
+template <typename T, int NU>
+__global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c) {
+    constexpr int H = 2 * NU, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *smc = simc + W, *sce = smc + W,
+      *scn = sce + W, *sr = scn + W;
+    const int gx0 = blockIdx.x * MTX + 1, gy0 = blockIdx.y * MTY + 1;
+    for (int q = threadIdx.x; q < W; q += blockDim.x) {
+        const int lx = q % WX, ly = q / WX, gi = gx0 - H + lx, gj = gy0 - H + ly;
+        const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
+        const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
+        const size_t o = (size_t)gj * f.P + gi;
+        sx[q] = T(0);
+        srhs[q] = in ? f.rhs[o] : T(0);
+        simc[q] = in ? f.inv_mc[o] : T(0);
+        smc[q] = in ? f.mc[o] : T(0);
+        sce[q] = arr ? f.ce[o] : T(0);
+        scn[q] = arr ? f.cn[o] : T(0);
+    }
+    __syncthreads();
+    for (int s = 0; s < 2 * NU; s++) {
+        const int color = s & 1, lo = s, hx = WX - 1 - s, hy = WY - 1 - s;
+        const int nxr = hx - lo + 1, n = nxr * (hy - lo + 1);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int lx = lo + q % nxr, ly = lo + q / nxr;
+            const int gi = gx0 - H + lx, gj = gy0 - H + ly;
+            if (((gi + gj) & 1) != color) continue;
+            const int k = ly * WX + lx;
+            if (s == 0) sx[k] = srhs[k] * simc[k];
+            else sx[k] = (srhs[k] + sce[k] * sx[k + 1] + sce[k - 1] * sx[k - 1] + scn[k] * sx[k + WX]
+                          + scn[k - WX] * sx[k - WX]) * simc[k];
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
+        const int tx = q % MTX, ty = q / MTX, lx = H + tx, ly = H + ty;
+        const int gi = gx0 + tx, gj = gy0 + ty;
+        const int k = ly * WX + lx;
+        T r = T(0);
+        if (gi <= f.nx && gj <= f.ny) {
+            if (((gi + gj) & 1) == 0)   // black residuals vanish after the last (black) sweep
+                r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
+                               - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
+            f.x[(size_t)gj * f.P + gi] = sx[k];
+        }
+        sr[q] = r;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < (MTX / 2) * (MTY / 2); q += blockDim.x) {
+        const int ci = q % (MTX / 2), cj = q / (MTX / 2);
+        const int I = (gx0 - 1) / 2 + 1 + ci, J = (gy0 - 1) / 2 + 1 + cj;
+        if (I > c.nx || J > c.ny) continue;
+        const int t0 = (2 * cj) * MTX + 2 * ci;
+        c.rhs[(size_t)J * c.P + I] = sr[t0] + sr[t0 + 1] + sr[t0 + MTX] + sr[t0 + MTX + 1];
+    }
+}
+
+template <typename T, int NU>
+__global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
+    constexpr int H = 2 * NU, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *sce = simc + W, *scn = sce + W;
+    const int gx0 = blockIdx.x * MTX + 1, gy0 = blockIdx.y * MTY + 1;
+    for (int q = threadIdx.x; q < W; q += blockDim.x) {
+        const int lx = q % WX, ly = q / WX, gi = gx0 - H + lx, gj = gy0 - H + ly;
+        const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
+        const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
+        const size_t o = (size_t)gj * f.P + gi;
+        sx[q] = in ? f.x[o] + c.x[(size_t)((gj + 1) / 2) * c.P + (gi + 1) / 2] : T(0);
+        srhs[q] = in ? f.rhs[o] : T(0);
+        simc[q] = in ? f.inv_mc[o] : T(0);
+        sce[q] = arr ? f.ce[o] : T(0);
+        scn[q] = arr ? f.cn[o] : T(0);
+    }
+    __syncthreads();
+    for (int s = 0; s < 2 * NU; s++) {
+        const int color = (s & 1) ? 0 : 1, lo = s + 1, hx = WX - 2 - s, hy = WY - 2 - s;
+        const int nxr = hx - lo + 1, n = nxr * (hy - lo + 1);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int lx = lo + q % nxr, ly = lo + q / nxr;
+            const int gi = gx0 - H + lx, gj = gy0 - H + ly;
+            if (((gi + gj) & 1) != color) continue;
+            const int k = ly * WX + lx;
+            sx[k] = (srhs[k] + sce[k] * sx[k + 1] + sce[k - 1] * sx[k - 1] + scn[k] * sx[k + WX]
+                     + scn[k - WX] * sx[k - WX]) * simc[k];
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
+        const int tx = q % MTX, ty = q / MTX, gi = gx0 + tx, gj = gy0 + ty;
+        if (gi <= f.nx && gj <= f.ny) f.x[(size_t)gj * f.P + gi] = sx[(H + ty) * WX + H + tx];
+    }
+}
+
+// V-cycle over levels [lb, nl) inside one CTA (levels of at most 32x32 nodes).
+template <typename T>
+struct BottomArgs {
+    LevelT<T> L[FS_MG_MAX_LEVELS];
+    int lb, nl, nu;
+};
+template <typename T>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a) {
+    const int t = threadIdx.x;
+    auto sweep = [&](const LevelT<T> &L, int color, int zero) {
+        for (int q = t; q < L.nx * L.ny; q += BOTTOM_THREADS) {
+            int I = q % L.nx + 1, J = q / L.nx + 1;
+            size_t o = (size_t)J * L.P + I;
+            if (((I + J) & 1) == color) L.x[o] = zero ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
+            else if (zero) L.x[o] = T(0);
+        }
+        __syncthreads();
+    };
+    for (int l = a.lb; l < a.nl - 1; l++) {
+        const LevelT<T> &f = a.L[l], &c = a.L[l + 1];
+        sweep(f, 0, 1);
+        sweep(f, 1, 0);
+        for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
+        for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
+            int I = q % c.nx + 1, J = q / c.nx + 1;
+            const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+            T s = T(0);
+            for (int fy = fy0; fy <= fy1; fy++)
+                for (int fx = fx0; fx <= fx1; fx++)
+                    if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
+            c.rhs[(size_t)J * c.P + I] = s;
+        }
+        __syncthreads();
+    }
+    {   // coarsest level: a single node is solved exactly by one red sweep;
+        // otherwise symmetric sweeps, the palindrome (RB)^10 (BR)^10
+        const LevelT<T> &c = a.L[a.nl - 1];
+        sweep(c, 0, 1);
+        if (c.nx * c.ny > 1) {
+            sweep(c, 1, 0);
+            for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
+            for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+        }
+    }
+    for (int l = a.nl - 2; l >= a.lb; l--) {
+        const LevelT<T> &f = a.L[l], &c = a.L[l + 1];
+        for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
+            int I = q % f.nx + 1, J = q / f.nx + 1;
+            f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+        }
+        __syncthreads();
+        for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
+    }
+}
+
+// grid-stride loop over the interior nodes; o is the node's field offset
+#define CG_NODES(a, ...)                                                                   \
+    for (long q_ = blockIdx.x * 256L + threadIdx.x; q_ < (long)(a).nx * (a).ny;           \
+         q_ += (long)gridDim.x * 256L) {                                                   \
+        const size_t o = (size_t)(q_ / (a).nx + 1) * (a).P + (size_t)(q_ % (a).nx + 1);   \
+        __VA_ARGS__                                                                        \
+    }
+
+// phi(interior) += d ; ph_mi = phi (lapl_lib.F90:112-119), only after convergence
+__global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, int ny, int P,
+                             const Ctrl *ctrl) {
+    if (!ctrl->cg_done || ctrl->cg_fail) return;
+    size_t n = (size_t)(ny + 2) * P;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
+        int gi = (int)(o % P), gj = (int)(o / P);
+        double v = ph[o];
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) v = v + x[o];
+        ph[o] = v;
+        phm[o] = v;
+    }
+}
+
+inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+template <typename T>
+size_t mg_down_smem(int nu) {
+    size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
+    return (6 * W + MTX * MTY) * sizeof(T);
+}
+template <typename T>
+size_t mg_up_smem(int nu) {
+    size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
+    return 5 * W * sizeof(T);
+}
+
+}  // namespace

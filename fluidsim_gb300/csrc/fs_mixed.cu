@@ -1,0 +1,575 @@
+// fs_mixed.cu -- the particle step in mixed precision (FS_PREC_MIXED).
+//
+// Same algorithm as fs_ptcl.cu (ptclEqn ptcl_lib.F90:99-550, rk_step
+// ptcl_props.F90:71-139, circ_step circ_lib.F90:19-210), with the flux/RHS
+// evaluation in FP32 on densities stored as FP32 log-densities, and FP64 kept
+// for the accepted-state accumulation (n = n3 + dt * sum c_i k_i is formed in
+// FP64 from the FP32 increment) and for the RK-Merson error norm.
+//
+// Log form of the Scharfetter-Gummel flux.  With B(x) = x/(e^x - 1) and the
+// cell Peclet number a = q mu E h / D,
+//   F = (D/h) (B(-a) n_L - B(a) n_R)
+//     = (D/h) B(-a) n_L (1 - exp(l_R - l_L - a))    for a >= 0
+//     = -(D/h) B(a) n_R (1 - exp(l_L - l_R + a))    for a <  0,
+// which is get_Flux (ptcl_props.F90:142-165) rearranged: the difference that
+// cancels near Boltzmann equilibrium is carried by expm1 to full FP32 relative
+// accuracy, and B uses its series 1 - x/2 + x^2/12 near x = 0.  The mean
+// energy is exp(l_t - l_e), and its table abscissa ln(eps) = l_t - l_e + ln(ph0)
+// needs no logarithm.
+#include <cmath>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "fs_internal.h"
+
+#define BX 32
+#define BY 8
+#define NT (BX * BY)
+#define HX (BX + 2)
+#define HY (BY + 2)
+
+namespace {
+
+// B(x) = x/(e^x - 1)
+__device__ __forceinline__ float bern(float x) {
+    if (fabsf(x) < 1e-3f) return 1.0f - 0.5f * x + x * x * (1.0f / 12.0f);
+    return x / expm1f(x);
+}
+
+// SG flux from log densities: (D/h) * [B(-a) n_L - B(a) n_R]
+__device__ __forceinline__ float sg_log(float dh_inv_D, float a, float nl, float nr, float ll, float lr) {
+    if (a >= 0.0f) return dh_inv_D * bern(-a) * nl * (-expm1f(lr - ll - a));
+    return dh_inv_D * bern(a) * nr * expm1f(ll - lr + a);
+}
+
+// -B'(x), the coefficient of dFdPh: dF/dv = -B'(-a) n_L - B'(a) n_R
+__device__ __forceinline__ float mbprime(float x) {
+    if (fabsf(x) < 0.5f) {
+        float x2 = x * x;
+        return 0.5f - x * (1.0f / 6.0f - x2 * (1.0f / 180.0f - x2 * (1.0f / 5040.0f - x2 * (1.0f / 151200.0f))));
+    }
+    if (x > 0.0f) {
+        float em = expf(-x), d = 1.0f - em;
+        return -(em / d - x * em / (d * d));
+    }
+    float ex = expf(x), d = expm1f(x);
+    return -((d - x * ex) / (d * d));
+}
+
+struct FaceMixArgs {
+    PhysParams pp;
+    MeshDev m;
+    const double *ph;
+    double *fx_e, *fy_e;     // FP64 face fields (the assembly's Laplacian needs them)
+    float *f[10];            // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
+};
+
+// Face data while phi is frozen: E (FP64 and FP32), the ion flux
+// coefficients cl = (Di/h) B(-a), cr = (Di/h) B(a) and the ion dFdPh
+// coefficients -B'(-a), -B'(a) (0 where |v| < 1e-12, as dFdPh).
+__device__ __forceinline__ void ion_face32(const PhysParams &pp, double E64, double h, float *out) {
+    const float E = (float)E64, hf = (float)h;
+    const float a = (float)(pp.mui * E64 * h / pp.Di);
+    const float d = (float)(pp.Di / h);
+    out[0] = E;
+    out[1] = d * bern(-a);
+    out[2] = d * bern(a);
+    if (fabs(pp.mui * E64) < 1e-12) {
+        out[3] = out[4] = 0.0f;
+    } else {
+        out[3] = mbprime(-a);
+        out[4] = mbprime(a);
+    }
+    (void)hf;
+}
+
+__global__ void k_faces_mix(const FaceMixArgs a) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x, gj = blockIdx.y * blockDim.y + threadIdx.y;
+    const int nx = a.pp.nx, ny = a.pp.ny, P = a.pp.pitch;
+    if (gi > nx || gj > ny) return;
+    const size_t o = (size_t)gj * P + gi;
+    float v[5];
+    if (gj >= 1) {
+        double E = -(a.ph[o + 1] - a.ph[o]) / a.m.dx[gi];
+        a.fx_e[o] = E;
+        ion_face32(a.pp, E, a.m.dx[gi], v);
+        for (int k = 0; k < 5; k++) a.f[k][o] = v[k];
+    }
+    if (gi >= 1) {
+        double E = -(a.ph[o + P] - a.ph[o]) / a.m.dy[gj];
+        a.fy_e[o] = E;
+        ion_face32(a.pp, E, a.m.dy[gj], v);
+        for (int k = 0; k < 5; k++) a.f[5 + k][o] = v[k];
+    }
+}
+
+// FP32 log-density of a whole field (ghost ring included)
+__global__ void k_log32(const double *n, float *l, size_t cnt) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
+        l[i] = logf(fmaxf((float)n[i], 1e-30f));
+}
+
+// circ_step ghosts in mixed mode: phi ghost and both face fields of the row
+__global__ void k_circ_ghost_mix(double *ph, const int8_t *tx, const double *r, const double *dx,
+                                 double *fx_e64, float *fx_e32, int nx, int ny, int P, double ew, double vd) {
+    int gj = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (gj > ny) return;
+    const size_t o = (size_t)gj * P;
+    if (r[gj] <= ew) {
+        if (tx[(gj - 1) * nx + 0] == -2) {
+            ph[o + 0] = vd / 2.0;
+            double E = -(ph[o + 1] - ph[o + 0]) / dx[0];
+            fx_e64[o + 0] = E;
+            fx_e32[o + 0] = (float)E;
+        }
+        if (tx[(gj - 1) * nx + nx - 1] == 2) {
+            ph[o + nx + 1] = vd / (-2.0);
+            double E = -(ph[o + nx + 1] - ph[o + nx]) / dx[nx];
+            fx_e64[o + nx] = E;
+            fx_e32[o + nx] = (float)E;
+        }
+    }
+}
+
+struct StageMixArgs {
+    PhysParams pp;
+    MeshDev m;
+    const float *tab;               // FP32 table, FS_TAB_STRIDE floats per node
+    const float *lin[FS_MAX_SPECIES];
+    const double *nbase[FS_MAX_SPECIES];
+    double *nout[FS_MAX_SPECIES];   // FP64 output (stages 4 and 5), else null
+    float *lout[FS_MAX_SPECIES];
+    const float *k1[FS_MAX_SPECIES];
+    const float *k3[FS_MAX_SPECIES];
+    const float *k4[FS_MAX_SPECIES];
+    float *kout[FS_MAX_SPECIES];
+    const double *ph;
+    const float *fx_e, *fx_cl, *fx_cr, *fy_e, *fy_cl, *fy_cr;
+    Ctrl *ctrl;
+    double *part;
+    double *rows;
+    int stage;
+    int nblk;
+};
+
+__device__ __forceinline__ void tab32(const StageMixArgs &a, float lneps, int &k, float &w) {
+    float u = (lneps - (float)a.pp.lemin) * (float)a.pp.inv_h;
+    if (!(u >= 0.0f)) u = 0.0f;
+    if (u > (float)(a.pp.ntab - 1)) u = (float)(a.pp.ntab - 1);
+    int i = (int)u;
+    if (i > a.pp.ntab - 2) i = a.pp.ntab - 2;
+    k = i;
+    w = u - (float)i;
+}
+__device__ __forceinline__ float tv32(const float *tab, int k, float w, int row) {
+    const float *t = tab + (size_t)k * FS_TAB_STRIDE;
+    return __ldg(t + row) + w * __ldg(t + 8 + row);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
+    __shared__ float s_l[NS][HY][HX];
+    __shared__ float s_n[NS][HY][HX];
+    __shared__ float s_te[HY][HX], s_mue[HY][HX], s_de[HY][HX];
+    __shared__ float s_w[BY][BX];
+    __shared__ int s_k[BY][BX];
+    __shared__ float s_fx[NS][BY][BX + 1];
+    __shared__ float s_fy[NS][BY + 1][BX];
+    __shared__ float s_ex[BY][BX + 1];
+    __shared__ float s_ey[BY + 1][BX];
+    __shared__ double s_red[NS][NT / 32];
+    __shared__ double s_tm[NT / 32];
+
+    const PhysParams &pp = a.pp;
+    const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
+    const int tid = threadIdx.x;
+    const int gx0 = blockIdx.x * BX + 1, gy0 = blockIdx.y * BY + 1;
+    const float ln_ph0 = (float)log(pp.ph0);
+    const float mui = (float)pp.mui, vi = (float)pp.vi, gam = (float)pp.gam;
+    const float mui_Di = (float)(pp.mui / pp.Di);
+    const float ve_c = (float)pp.ve_coef, t0_x0 = (float)(pp.t0 / pp.x0);
+    unsigned int st = 0;
+
+    for (int q = tid; q < HX * HY; q += NT) {
+        int lx = q % HX, ly = q / HX;
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        bool in = gi <= nx + 1 && gj <= ny + 1;
+        size_t o = (size_t)gj * P + gi;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            float l = in ? a.lin[s][o] : 0.0f;
+            s_l[s][ly][lx] = l;
+            s_n[s][ly][lx] = expf(l);
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < HX * HY; q += NT) {
+        int lx = q % HX, ly = q / HX;
+        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
+        float te = 0, mu = 0, de = 0;
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
+            float dl = s_l[2][ly][lx] - s_l[1][ly][lx];
+            te = expf(dl);
+            int k; float w;
+            tab32(a, dl + ln_ph0, k, w);
+            mu = tv32(a.tab, k, w, 0);
+            de = tv32(a.tab, k, w, 1);
+            if (lx >= 1 && lx <= BX && ly >= 1 && ly <= BY) { s_k[ly - 1][lx - 1] = k; s_w[ly - 1][lx - 1] = w; }
+        }
+        s_te[ly][lx] = te; s_mue[ly][lx] = mu; s_de[ly][lx] = de;
+    }
+    __syncthreads();
+
+    // x faces between gi = gx0-1+c and gi+1
+    for (int q = tid; q < BY * (BX + 1); q += NT) {
+        int c = q % (BX + 1), r = q / (BX + 1);
+        int gi = gx0 - 1 + c, gj = gy0 + r;
+        if (gj > ny || gi > nx) continue;
+        int lx = c, ly = r + 1;
+        const size_t of = (size_t)gj * P + gi;
+        float E = a.fx_e[of];
+        float fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
+        int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;
+        int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;
+        if (gi == 0 && tr == -1) {
+            eu = 0.0f;
+        } else if (gi == nx && tl == 1) {
+            eu = 0.0f;
+        } else if ((gi == 0 && tr == -2) || (gi == nx && tl == 2)) {
+            const bool left = gi == 0;
+            const int lc = left ? lx + 1 : lx;
+            const size_t og = (size_t)gj * P + (left ? 0 : nx + 1), oc = (size_t)gj * P + (left ? 1 : nx);
+            float te = s_te[ly][lc], ni = s_n[0][ly][lc], ne = s_n[1][ly][lc], nt = s_n[2][ly][lc];
+            float aa = (a.ph[og] > a.ph[oc]) ? 1.0f : 0.0f;
+            float mue = s_mue[ly][lc], mut = (5.0f / 3.0f) * mue;
+            float ve = sqrtf(ve_c * te) * t0_x0;
+            float sgn = left ? -1.0f : 1.0f;
+            fi = (1.0f - aa) * mui * E * ni + sgn * (0.25f * vi * ni);
+            fe = -(aa * mue * E * ne) + sgn * (0.25f * ve * ne) - gam * fi;
+            ft = -(aa * mut * E * nt) + sgn * ((1.0f / 3.0f) * ve * nt) - gam * te * fi;
+            if (NS == 4) fm = sgn * (0.5f * vi * s_n[3][ly][lc]);
+        } else {
+            float dh = (float)a.m.dx[gi], idh = (float)a.m.inv_dx[gi];
+            float mue = 0.5f * (s_mue[ly][lx] + s_mue[ly][lx + 1]);
+            float De = 0.5f * (s_de[ly][lx] + s_de[ly][lx + 1]);
+            float ai = E * dh * mui_Di;
+            fi = ai >= 0.0f ? a.fx_cl[of] * s_n[0][ly][lx] * (-expm1f(s_l[0][ly][lx + 1] - s_l[0][ly][lx] - ai))
+                            : a.fx_cr[of] * s_n[0][ly][lx + 1] * expm1f(s_l[0][ly][lx] - s_l[0][ly][lx + 1] + ai);
+            float ae = -mue * E * dh / De, g = De * idh;
+            fe = sg_log(g, ae, s_n[1][ly][lx], s_n[1][ly][lx + 1], s_l[1][ly][lx], s_l[1][ly][lx + 1]);
+            ft = sg_log((5.0f / 3.0f) * g, ae, s_n[2][ly][lx], s_n[2][ly][lx + 1], s_l[2][ly][lx], s_l[2][ly][lx + 1]);
+            if (NS == 4) fm = -(float)pp.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
+            if (a.stage == 5) {
+                if (gi == 1 && a.m.dr_a[gj] != 0.0) a.rows[gj] = a.m.dr_a[gj] * (double)(fi - fe);
+                if (gi == nx - 1 && a.m.dr_c[gj] != 0.0) a.rows[(ny + 2) + gj] = a.m.dr_c[gj] * (double)(fi - fe);
+            }
+        }
+        s_fx[0][r][c] = fi; s_fx[1][r][c] = fe; s_fx[2][r][c] = ft;
+        if (NS == 4) s_fx[3][r][c] = fm;
+        s_ex[r][c] = eu;
+    }
+    __syncthreads();
+    // y faces between gj = gy0-1+r and gj+1
+    for (int q = tid; q < (BY + 1) * BX; q += NT) {
+        int c = q % BX, r = q / BX;
+        int gi = gx0 + c, gj = gy0 - 1 + r;
+        if (gi > nx || gj > ny) continue;
+        int lx = c + 1, ly = r;
+        const size_t of = (size_t)gj * P + gi;
+        float E = a.fy_e[of];
+        float fi = 0, fe = 0, ft = 0, fm = 0, eu = E;
+        int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
+        int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
+        if (gj == 0 && tt == -1) {
+            eu = 0.0f;
+        } else if (gj == 0 && tt == -2) {
+            // no lower y electrode flux in ptclEqn: zero flux, face field kept
+        } else if (gj == ny && tb == 1) {
+            eu = 0.0f;
+        } else if (gj == ny && tb == 2) {
+            const int lc = ly;
+            const size_t og = (size_t)(ny + 1) * P + gi, oc = (size_t)ny * P + gi;
+            float te = s_te[lc][lx], ni = s_n[0][lc][lx], ne = s_n[1][lc][lx], nt = s_n[2][lc][lx];
+            float aa = (a.ph[og] > a.ph[oc]) ? 1.0f : 0.0f;
+            float mue = s_mue[lc][lx], mut = (5.0f / 3.0f) * mue;
+            float ve = sqrtf(ve_c * te) * t0_x0;
+            fi = (1.0f - aa) * mui * E * ni + 0.25f * vi * ni;
+            float fix = s_fx[0][lc - 1][lx];   // x-direction ion flux (ptcl_lib.F90:427-433)
+            fe = -(aa * mue * E * ne) + 0.25f * ve * ne - gam * fix;
+            ft = -(aa * mut * E * nt) + (1.0f / 3.0f) * ve * nt - gam * te * fix;
+            if (NS == 4) fm = 0.5f * vi * s_n[3][lc][lx];
+        } else {
+            float dh = (float)a.m.dy[gj], idh = (float)a.m.inv_dy[gj];
+            float mue = 0.5f * (s_mue[ly][lx] + s_mue[ly + 1][lx]);
+            float De = 0.5f * (s_de[ly][lx] + s_de[ly + 1][lx]);
+            float ai = E * dh * mui_Di;
+            fi = ai >= 0.0f ? a.fy_cl[of] * s_n[0][ly][lx] * (-expm1f(s_l[0][ly + 1][lx] - s_l[0][ly][lx] - ai))
+                            : a.fy_cr[of] * s_n[0][ly + 1][lx] * expm1f(s_l[0][ly][lx] - s_l[0][ly + 1][lx] + ai);
+            float ae = -mue * E * dh / De, g = De * idh;
+            fe = sg_log(g, ae, s_n[1][ly][lx], s_n[1][ly + 1][lx], s_l[1][ly][lx], s_l[1][ly + 1][lx]);
+            ft = sg_log((5.0f / 3.0f) * g, ae, s_n[2][ly][lx], s_n[2][ly + 1][lx], s_l[2][ly][lx], s_l[2][ly + 1][lx]);
+            if (NS == 4) fm = -(float)pp.Dm * (s_n[3][ly + 1][lx] - s_n[3][ly][lx]) * idh;
+        }
+        s_fy[0][r][c] = fi; s_fy[1][r][c] = fe; s_fy[2][r][c] = ft;
+        if (NS == 4) s_fy[3][r][c] = fm;
+        s_ey[r][c] = eu;
+    }
+    __syncthreads();
+
+    const int lx = tid % BX, ly = tid / BX;
+    const int gi = gx0 + lx, gj = gy0 + ly;
+    double qerr[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) qerr[s] = 0.0;
+    double tm = 1e300;
+    if (gi <= nx && gj <= ny) {
+        const size_t o = (size_t)gj * P + gi;
+        const int hx = lx + 1, hy = ly + 1;
+        const float te = s_te[hy][hx];
+        const float ni = s_n[0][hy][hx], ne = s_n[1][hy][hx];
+        const float nm = NS == 4 ? s_n[3][hy][hx] : 0.0f;
+        const int kk = s_k[ly][lx];
+        const float w = s_w[ly][lx];
+        const float k_ir = tv32(a.tab, kk, w, 2), k_ex = tv32(a.tab, kk, w, 3);
+        const float nu = tv32(a.tab, kk, w, 4), beta = tv32(a.tab, kk, w, 5);
+        const float idlx = (float)a.m.inv_dlx[gi - 1], idly = (float)a.m.inv_dly[gj - 1];
+        float dfdx[NS], dfdy[NS];
+        if (pp.cyl) {
+            const float r0 = (float)a.m.r[gj], rp = (float)(a.m.r[gj + 1] + a.m.r[gj]), rm = (float)(a.m.r[gj] + a.m.r[gj - 1]);
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                dfdx[s] = (s_fx[s][ly][lx + 1] - s_fx[s][ly][lx]) * idlx;
+                dfdy[s] = (s_fy[s][ly + 1][lx] * rp * 0.5f - s_fy[s][ly][lx] * rm * 0.5f) * idly / r0;
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                dfdx[s] = (s_fx[s][ly][lx + 1] - s_fx[s][ly][lx]) * idlx;
+                dfdy[s] = (s_fy[s][ly + 1][lx] - s_fy[s][ly][lx]) * idly;
+            }
+        }
+        const float fex = (s_fx[1][ly][lx + 1] + s_fx[1][ly][lx]) * 0.5f;
+        const float exa = (s_ex[ly][lx] + s_ex[ly][lx + 1]) * 0.5f;
+        const float fey = (s_fy[1][ly + 1][lx] + s_fy[1][ly][lx]) * 0.5f;
+        const float eya = (s_ey[ly][lx] + s_ey[ly + 1][lx]) * 0.5f;
+        const float ninf = (float)pp.ninf;
+        float term_sie = k_ir * ninf * ne - beta * ni * ne;
+        float k_si = 0.0f, k_sc = 0.0f;
+        if (NS == 4) {
+            k_sc = tv32(a.tab, kk, w, 6);
+            k_si = tv32(a.tab, kk, w, 7);
+            term_sie = term_sie + k_si * nm * ne + (float)pp.k_mp * (nm * nm);
+        }
+        const float term_st1 = -(fex * exa + fey * eya);
+        const float term_st2 = -(ne * nu * (float)(pp.me / pp.mi) * (te / 1.5f - (float)(pp.tg * pp.kb / pp.e / pp.ph0)));
+        const float term_st3 = -((float)pp.h_ir * k_ir * ninf * ne) - (float)pp.h_si * k_si * nm * ne
+                             - (float)pp.h_ex * k_ex * ninf * ne;
+        float kv[NS];
+        kv[0] = -dfdx[0] - dfdy[0] + term_sie;
+        kv[1] = -dfdx[1] - dfdy[1] + term_sie;
+        kv[2] = -dfdx[2] - dfdy[2] + term_st1 + term_st2 + term_st3;
+        if (NS == 4) {
+            float term_sm = k_ex * ninf * ne - k_si * nm * ne - k_sc * nm * ne - (float)pp.k_r * nm * ne
+                          - 2.0f * (float)pp.k_mp * (nm * nm) - (float)pp.k_2q * ninf * nm
+                          - (float)(pp.k_3q * pp.ninf * pp.ninf) * nm;
+            kv[3] = -dfdx[3] - dfdy[3] + term_sm;
+        }
+        const double dt = a.ctrl->dt;
+        const float dtf = (float)dt;
+        const int stg = a.stage;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            if (isnan(kv[s])) st |= FS_ST_NAN;
+            if (a.kout[s]) a.kout[s][o] = kv[s];
+            float comb;
+            if (stg == 1) comb = kv[s] * (1.0f / 3.0f);
+            else if (stg == 2) comb = (a.k1[s][o] + kv[s]) * (1.0f / 6.0f);
+            else if (stg == 3) comb = (a.k1[s][o] + kv[s] * 3.0f) * 0.125f;
+            else if (stg == 4) comb = (a.k1[s][o] - a.k3[s][o] * 3.0f + kv[s] * 4.0f) * 0.5f;
+            else comb = (a.k1[s][o] + a.k4[s][o] * 4.0f + kv[s]) * (1.0f / 6.0f);
+            const double n3 = a.nbase[s][o];
+            const double v = fmax(n3 + (double)(dtf * comb), pp.nmin[s]);   // FP64 accumulation
+            a.lout[s][o] = logf((float)v);
+            if (a.nout[s]) a.nout[s][o] = v;
+            if (stg == 5) {
+                const double k1 = a.k1[s][o], k3 = a.k3[s][o], k4 = a.k4[s][o];
+                double err = fabs(dt * (k1 * (2.0 / 30.0) - k3 * (3.0 / 10.0) + k4 * (4.0 / 15.0)
+                                        - (double)kv[s] * (1.0 / 30.0)));
+                double qq = err / (pp.abs_tol + pp.rel_tol * fabs(n3));
+                qerr[s] = qq * qq;
+            }
+        }
+        if (stg == 5) {
+            const int ty = a.m.ty[(gj - 1) * nx + gi - 1], tx = a.m.tx[(gj - 1) * nx + gi - 1];
+            float mue2;
+            if (ty == 0 || ty < 0) mue2 = 0.5f * (s_mue[hy][hx] + s_mue[hy + 1][hx]);
+            else if (ty == 1 && (tx == 0 || tx < 0)) mue2 = 0.5f * (s_mue[hy][hx] + s_mue[hy][hx + 1]);
+            else mue2 = s_mue[hy][hx];
+            tm = 1.0 / ((double)mue2 * ne + pp.mui * ni);
+        }
+    }
+    if (st) atomicOr(&a.ctrl->status, st);
+    if (a.stage == 5) {
+        const int wid = tid >> 5, lane = tid & 31;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            double v = warp_sum(qerr[s]);
+            if (lane == 0) s_red[s][wid] = v;
+        }
+        for (int o = 16; o > 0; o >>= 1) tm = fmin(tm, __shfl_down_sync(0xffffffffu, tm, o));
+        if (lane == 0) s_tm[wid] = tm;
+        __syncthreads();
+        if (tid < NS) {
+            double v = 0.0;
+            for (int wv = 0; wv < NT / 32; wv++) v += s_red[tid][wv];
+            a.part[(size_t)tid * a.nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+        }
+        if (tid == 0) {
+            double m = s_tm[0];
+            for (int wv = 1; wv < NT / 32; wv++) m = fmin(m, s_tm[wv]);
+            if (m > 0.0 && m < 1e300)
+                atomicMin((unsigned long long *)&a.ctrl->t_m, (unsigned long long)__double_as_longlong(m));
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int fs_mixed_alloc(fs_ctx *c, const std::vector<double> &rows) {
+    const size_t n = c->field_elems;
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < c->cfg.nspecies && e == cudaSuccess; s++) {
+        for (int b = 0; b < FS_NBUF && e == cudaSuccess; b++) e = cudaMalloc(&c->lbuf[s][b], n * sizeof(float));
+        for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+            e = cudaMalloc(&c->k32[s][k], n * sizeof(float));
+            if (e == cudaSuccess) e = cudaMemset(c->k32[s][k], 0, n * sizeof(float));
+        }
+    }
+    for (int f = 0; f < 10 && e == cudaSuccess; f++) {
+        e = cudaMalloc(&c->f32[f], n * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(c->f32[f], 0, n * sizeof(float));
+    }
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (mixed)");
+    const int nt = c->cfg.table_n;
+    std::vector<float> t((size_t)nt * FS_TAB_STRIDE, 0.0f);
+    for (int i = 0; i < nt; i++)
+        for (int r = 0; r < 8; r++) {
+            t[(size_t)i * FS_TAB_STRIDE + r] = (float)rows[(size_t)r * nt + i];
+            t[(size_t)i * FS_TAB_STRIDE + 8 + r] =
+                i + 1 < nt ? (float)(rows[(size_t)r * nt + i + 1] - rows[(size_t)r * nt + i]) : 0.0f;
+        }
+    e = cudaMalloc(&c->d_tab32, t.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_tab32, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice);
+    return fs_cuda_check(c, e, "mixed table");
+}
+
+void fs_mixed_free(fs_ctx *c) {
+    for (int s = 0; s < FS_MAX_SPECIES; s++) {
+        for (int b = 0; b < FS_NBUF; b++) cudaFree(c->lbuf[s][b]);
+        for (int k = 0; k < 3; k++) cudaFree(c->k32[s][k]);
+    }
+    for (int f = 0; f < 10; f++) cudaFree(c->f32[f]);
+    cudaFree(c->d_tab32);
+}
+
+int fs_mixed_sync_logs(fs_ctx *c) {
+    for (int s = 0; s < c->cfg.nspecies; s++)
+        for (int b = 0; b < FS_NBUF; b++) {
+            c->launches++;
+            k_log32<<<2 * c->nsm, 256, 0, c->stream>>>(c->sp[s].buf[b], c->lbuf[s][b], c->field_elems);
+        }
+    return fs_cuda_check(c, cudaGetLastError(), "log densities");
+}
+
+void fs_faces_update_mixed(fs_ctx *c) {
+    if (c->faces_valid) return;
+    FaceMixArgs f;
+    f.pp = c->pp;
+    f.m = c->mesh;
+    f.ph = c->ph;
+    f.fx_e = c->fx_e;
+    f.fy_e = c->fy_e;
+    for (int k = 0; k < 10; k++) f.f[k] = c->f32[k];
+    dim3 b(32, 8), g((c->nx + 1 + 31) / 32, (c->ny + 1 + 7) / 8);
+    fs_prof_begin(c, PROF_OTHER);
+    k_faces_mix<<<g, b, 0, c->stream>>>(f);
+    fs_prof_end(c);
+    c->faces_valid = 1;
+}
+
+// ptcl_step in mixed precision: buffer handling as fs_ptcl_step_impl; stages
+// 1-3 only produce the FP32 log state, stages 4 and 5 also the FP64 one.
+int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
+    const int ns = c->cfg.nspecies;
+    const int L2 = c->lev[1], L3 = c->lev[2];
+    int freeb[FS_NBUF], nf = 0;
+    for (int b = 0; b < FS_NBUF; b++)
+        if (b != L2 && b != L3) freeb[nf++] = b;
+    const int SA = freeb[0], SB = freeb[1], OUT = freeb[2];
+    int in1 = L2;
+    int attempts = 0;
+    fs_ptcl_reset(c);
+    fs_faces_update_mixed(c);
+    dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
+    for (;;) {
+        attempts++;
+        StageMixArgs a;
+        memset(&a, 0, sizeof(a));
+        a.pp = c->pp;
+        a.m = c->mesh;
+        a.tab = c->d_tab32;
+        a.ph = c->ph;
+        a.fx_e = c->f32[0]; a.fx_cl = c->f32[1]; a.fx_cr = c->f32[2];
+        a.fy_e = c->f32[5]; a.fy_cl = c->f32[6]; a.fy_cr = c->f32[7];
+        a.ctrl = c->d_ctrl;
+        a.part = c->d_part;
+        a.rows = c->d_rows;
+        a.nblk = c->nblk_stage;
+        const int ins[5] = {in1, SA, SB, SA, SB};
+        const int outs[5] = {SA, SB, SA, SB, OUT};
+        for (int stg = 1; stg <= 5; stg++) {
+            a.stage = stg;
+            for (int s = 0; s < ns; s++) {
+                a.lin[s] = c->lbuf[s][ins[stg - 1]];
+                a.nbase[s] = c->sp[s].buf[L3];
+                a.lout[s] = c->lbuf[s][outs[stg - 1]];
+                a.nout[s] = stg >= 4 ? c->sp[s].buf[outs[stg - 1]] : nullptr;
+                a.k1[s] = c->k32[s][0];
+                a.k3[s] = c->k32[s][1];
+                a.k4[s] = c->k32[s][2];
+                a.kout[s] = stg == 1 ? c->k32[s][0] : stg == 3 ? c->k32[s][1] : stg == 4 ? c->k32[s][2] : nullptr;
+            }
+            fs_prof_begin(c, PROF_STAGE);
+            if (ns == 4) k_stage_mix<4><<<grid, NT, 0, c->stream>>>(a);
+            else k_stage_mix<3><<<grid, NT, 0, c->stream>>>(a);
+            fs_prof_end(c);
+            if (stg == 1) {
+                c->launches++;
+                k_circ_ghost_mix<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
+                    c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->f32[0], c->nx, c->ny, c->pitch,
+                    c->cfg.ew, c->Vsrc);
+            }
+        }
+        int rc = fs_ptcl_control(c);
+        if (rc) return rc;
+        c->Vd_pl = c->Vd_mi = c->Vsrc;
+        if (!c->h_ctrl->rejected) break;
+        c->st.rk_rejects++;
+        c->Vd_pl = c->Vd_or;
+        c->Vd_mi = c->Vd_or;
+        in1 = L3;
+        if (attempts > 100000) return fs_set_error(c, FS_ERR_MIN_DT, "RK restart limit");
+    }
+    c->lev[0] = OUT;
+    c->lev[1] = SB;
+    c->dt = c->h_ctrl->dt;
+    c->st.attempts += attempts;
+    if (attempts_out) *attempts_out = attempts;
+    return FS_OK;
+}

@@ -549,6 +549,27 @@ static void launch_stage(fs_ctx *c, StageArgs &a) {
     else k_stage<3><<<grid, NT, 0, c->stream>>>(a);
 }
 
+// Start of a particle step: t_m, status and the current rows reset on the device.
+void fs_ptcl_reset(fs_ctx *c) {
+    c->launches++;
+    k_reset_step<<<(2 * (c->ny + 2) + 255) / 256, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, 2 * (c->ny + 2));
+}
+
+// End of one five-stage attempt: the controller, then the host reads the
+// control block and turns its status bits into errors.
+int fs_ptcl_control(fs_ctx *c) {
+    c->launches++;
+    k_controller<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_part, c->nblk_stage, c->cfg.nspecies, c->d_rows,
+                                           c->ny, c->cfg.adaptive, c->cfg.dt_min);
+    int rc = fs_sync_ctrl(c);
+    if (rc) return rc;
+    const Ctrl &h = *c->h_ctrl;
+    if (h.status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
+    if (h.status & FS_ST_NAN) return fs_set_error(c, FS_ERR_NAN, "NaN in particle right-hand side");
+    if (h.min_dt) return fs_set_error(c, FS_ERR_MIN_DT, "minimum timestep reached");
+    return FS_OK;
+}
+
 // ptcl_step: five stages, restart on rejection (ptcl_lib.F90:32-97).
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     const int ns = c->cfg.nspecies;
@@ -560,8 +581,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     int in1 = L2;
     int attempts = 0;
 
-    c->launches++;
-    k_reset_step<<<(2 * (c->ny + 2) + 255) / 256, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, 2 * (c->ny + 2));
+    fs_ptcl_reset(c);
     fs_faces_update(c);
     for (;;) {
         attempts++;
@@ -599,15 +619,9 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
                     c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->nx, c->ny, c->pitch, c->cfg.ew,
                     c->Vsrc);
         }
-        c->launches++;
-        k_controller<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_part, c->nblk_stage, ns, c->d_rows,
-                                               c->ny, c->cfg.adaptive, c->cfg.dt_min);
-        int rc = fs_sync_ctrl(c);
+        int rc = fs_ptcl_control(c);
         if (rc) return rc;
         const Ctrl &h = *c->h_ctrl;
-        if (h.status & FS_ST_NEG_DENSITY) return fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te");
-        if (h.status & FS_ST_NAN) return fs_set_error(c, FS_ERR_NAN, "NaN in particle right-hand side");
-        if (h.min_dt) return fs_set_error(c, FS_ERR_MIN_DT, "minimum timestep reached");
         c->Vd_pl = c->Vd_mi = c->Vsrc;
         if (!h.rejected) break;
         c->st.rk_rejects++;

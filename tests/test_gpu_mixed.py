@@ -1,0 +1,88 @@
+"""Mixed-precision path (FS_PREC_MIXED) against the FP64 oracle and the FP64
+GPU path on identical seeded inputs (needs a GB300).
+
+Bars: densities within 1e-5 relative to the FP64 result (L-infinity over the
+interior with the density floor as absolute guard, and L2), phi within 1e-5
+relative to max|phi|; every Poisson solve converged to the same relative
+residual as the FP64 solver (lapl_rtol, here 1e-8), with the residual formed
+in FP64.
+"""
+import numpy as np
+import pytest
+
+from tests._util import field_errors
+
+pytestmark = pytest.mark.gpu
+
+DENS_BAR = 1e-5
+
+
+def _setup(n, seed=7, **kw):
+    from fluidsim_gb300 import abi, api, config, grid
+    cfg = config.glow(n, lapl_rtol=1e-8, **kw)
+    mesh = cfg.mesh()
+    k = api.constants(cfg)
+    st = grid.blob_state(mesh, k, noise=0.01, seed=seed, vl=cfg.vl)
+    return cfg, cfg.replace(precision=abi.FS_PREC_MIXED), mesh, k, st
+
+
+def _l2(a, b):
+    a = np.asarray(a)[1:-1, 1:-1]
+    b = np.asarray(b)[1:-1, 1:-1]
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _errors(g, r, k):
+    e = field_errors(g, r, k["n_zero"])
+    for f in ("ni", "ne", "nt"):
+        e[f + "_l2"] = _l2(g[f], r[f])
+    return e
+
+
+def test_mixed_vs_oracle_adaptive(built):
+    """Mixed steps follow the FP64 oracle step for step on a 48x40 grid."""
+    from fluidsim_gb300 import api
+    from oracle import oracle
+    cfg, cfgm, mesh, k, st = _setup(48, ny=40)
+    gpu = api.Discharge(cfgm, mesh, st)
+    ref = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_DIRECT)
+    for s in range(12):
+        gi, ri = gpu.step(), ref.step()
+        assert gi["lerr"] == 0 and ri["lerr"] == 0
+        assert gi["attempts"] == ri["attempts"], (s, gi, ri)
+        assert gi["dt"] == pytest.approx(ri["dt"], rel=1e-3), (s, gi, ri)
+    e = _errors(gpu.download(), ref.download(), k)
+    assert max(e.values()) < DENS_BAR, e
+
+
+@pytest.mark.parametrize("n,steps", [(128, 40), (256, 20)])
+def test_mixed_vs_fp64_gpu(built, n, steps):
+    """Same seeded run in both precisions through the C ABI; the FP64 GPU path
+    stands for the oracle here (it matches the oracle to 1e-10)."""
+    from fluidsim_gb300 import api
+    cfg, cfgm, mesh, k, st = _setup(n)
+    a, b = api.Discharge(cfg, mesh, st), api.Discharge(cfgm, mesh, st)
+    for s in range(steps):
+        ga, gb = a.step(), b.step()
+        assert ga["lerr"] == 0 and gb["lerr"] == 0, (s, ga, gb)
+        assert gb["relres"] <= cfg.lapl_rtol
+        assert ga["attempts"] == gb["attempts"], (s, ga, gb)
+    assert b.t == pytest.approx(a.t, rel=1e-3)
+    e = _errors(b.download(), a.download(), k)
+    assert max(e.values()) < DENS_BAR, e
+
+
+def test_mixed_poisson_residual(built):
+    """One mixed Poisson solve reaches the FP64 solver's relative residual in
+    a comparable number of iterations, and its correction matches."""
+    from fluidsim_gb300 import api
+    cfg, cfgm, mesh, k, st = _setup(256)
+    cfg = cfg.replace(lapl_rtol=1e-10)
+    cfgm = cfgm.replace(lapl_rtol=1e-10)
+    a, b = api.Discharge(cfg, mesh, st), api.Discharge(cfgm, mesh, st)
+    ra, rb = a.lapl_solve(), b.lapl_solve()
+    assert ra["lerr"] == 0 and rb["lerr"] == 0
+    assert rb["relres"] <= 1e-10
+    assert rb["iters"] <= ra["iters"] + 4, (ra, rb)
+    pa, pb = a.download()["ph"], b.download()["ph"]
+    assert np.max(np.abs(pa - pb)) <= 1e-6 * np.max(np.abs(pa))
