@@ -104,10 +104,11 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(n, dt_mode, rtol=1e-8):
-    from fluidsim_gb300 import config
+def workload(n, dt_mode, rtol=1e-8, precision="fp64"):
+    from fluidsim_gb300 import abi, config
     cfg = config.glow(n, adaptive=1 if dt_mode == "adaptive" else 0, lapl_rtol=rtol,
-                      lapl_maxit=500)
+                      lapl_maxit=500,
+                      precision=abi.FS_PREC_MIXED if precision == "mixed" else abi.FS_PREC_FP64)
     return cfg
 
 
@@ -200,7 +201,7 @@ def run_gpu(args):
     from fluidsim_gb300 import api
     torch.cuda.init()
 
-    cfg = workload(args.n, args.dt)
+    cfg = workload(args.n, args.dt, precision=args.precision)
     mesh = cfg.mesh()
     k = api.constants(cfg)
     st0 = initial_state(cfg, mesh, k)
@@ -348,6 +349,7 @@ def main():
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--dt", default="adaptive", choices=("adaptive", "fixed"))
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -81,7 +81,7 @@ class FsStats(C.Structure):
         ("lapl_relres", C.c_double),
         ("steps", C.c_int64), ("attempts", C.c_int64), ("rk_rejects", C.c_int64),
         ("lapl_rejects", C.c_int64), ("lapl_iters", C.c_int64),
-        ("last_lapl_iters", C.c_int32), ("lerr", C.c_int32),
+        ("last_lapl_iters", C.c_int32), ("lerr", C.c_int32), ("dt_step", C.c_double),
     ]
 
     def as_dict(self):

@@ -535,6 +535,7 @@ int fs_get_stats(fs_ctx *c, fs_stats *out) {
     c->st.ida = c->h_ctrl->ida;
     c->st.idc = c->h_ctrl->idc;
     c->st.err_cur = c->h_ctrl->err_cur;
+    c->st.dt_step = c->h_ctrl->dt_step;
     c->st.steps = c->ts;
     *out = c->st;
     return FS_OK;

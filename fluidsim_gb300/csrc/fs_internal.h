@@ -58,6 +58,7 @@ struct Ctrl {
     double t_m;           // running min over stage-5 cells
     double ida, idc;
     double scfac;
+    double dt_step;       // dt of the last attempt, before the controller's update
     unsigned int status;  // FS_ST_* bits
     int rejected;         // last attempt rejected by the error norm
     int min_dt;           // dt fell to dt_min

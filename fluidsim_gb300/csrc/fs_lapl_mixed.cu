@@ -136,11 +136,18 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         s_ne[ly][lx] = ne;
         float te = 0, mu = 0, de = 0;
         if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
-            float nte = (float)a.nt[o];
-            if ((nte >= 0.0f) && (ne >= 0.0f)) te = nte / ne;
-            else { st |= FS_ST_NEG_DENSITY; te = 1e-8f; }
+            const double nt64 = a.nt[o], ne64 = a.ne[o];
+            float lneps;
+            if ((nt64 >= 0.0) && (ne64 >= 0.0)) {
+                te = (float)(nt64 / ne64);
+                lneps = logf((float)(nt64 * pp.ph0 / ne64));   // ln(mean energy in eV)
+            } else {
+                st |= FS_ST_NEG_DENSITY;
+                te = 1e-8f;
+                lneps = logf(1e-8f) + ln_ph0;
+            }
             int k; float w;
-            tab32(pp, logf(te) + ln_ph0, k, w);
+            tab32(pp, lneps, k, w);
             mu = tv32(a.tab, k, w, 0);
             de = tv32(a.tab, k, w, 1);
         }
@@ -307,7 +314,7 @@ struct CgmArgs {
     dim3 grid;
     double *x, *r, *p, *q, *rhs, *dinv, *part;
     float *z, *r32;
-    const float *mc, *ce, *cn;
+    const float *mc, *ce, *cn, *extra;
     Ctrl *ctrl;
     double rtol;
     int maxit;
@@ -400,15 +407,19 @@ __global__ void __launch_bounds__(256) k_cgm_rz(const CgmArgs a) {
 }
 
 // p = z + beta p ; q = M z + beta q ; pq = p.q ; alpha = rz / pq (FP64
-// arithmetic on the FP32 preconditioned residual and coefficients)
+// arithmetic on the FP32 preconditioned residual and coefficients).  M is
+// applied as its face conductances, sum_f c_f (z_i - z_j) + extra_i z_i, so the
+// FP64 operator is exactly the M-matrix of the FP32 conductances; a stored
+// FP32 diagonal would differ from their sum by a rounding of size eps*M_ii,
+// which acts like a spurious reaction term and costs ~cond(M)*eps.
 __global__ void __launch_bounds__(256) k_cgm_pq(const CgmArgs a) {
     double v = 0.0;
     const double be = a.ctrl->beta;
     CG_NODES(a, {
         const double zc = a.z[o];
-        double mz = (double)a.mc[o] * zc - (double)a.ce[o] * (double)a.z[o + 1]
-                  - (double)a.ce[o - 1] * (double)a.z[o - 1] - (double)a.cn[o] * (double)a.z[o + a.P]
-                  - (double)a.cn[o - a.P] * (double)a.z[o - a.P];
+        double mz = (double)a.ce[o] * (zc - (double)a.z[o + 1]) + (double)a.ce[o - 1] * (zc - (double)a.z[o - 1])
+                  + (double)a.cn[o] * (zc - (double)a.z[o + a.P]) + (double)a.cn[o - a.P] * (zc - (double)a.z[o - a.P])
+                  + (double)a.extra[o] * zc;
         double pn = zc + be * a.p[o];
         double qn = mz + be * a.q[o];
         a.p[o] = pn;
@@ -670,7 +681,7 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.x = c->xs; ca.r = c->r; ca.p = c->p; ca.q = c->q;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
     ca.z = m0.x; ca.r32 = m0.rhs;
-    ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
+    ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
     ca.maxit = c->cfg.lapl_maxit;

@@ -13,9 +13,14 @@
 //     = -(D/h) B(a) n_R (1 - exp(l_L - l_R + a))    for a <  0,
 // which is get_Flux (ptcl_props.F90:142-165) rearranged: the difference that
 // cancels near Boltzmann equilibrium is carried by expm1 to full FP32 relative
-// accuracy, and B uses its series 1 - x/2 + x^2/12 near x = 0.  The mean
-// energy is exp(l_t - l_e), and its table abscissa ln(eps) = l_t - l_e + ln(ph0)
-// needs no logarithm.
+// accuracy, and B uses its series 1 - x/2 + x^2/12 near x = 0.
+//
+// Stored FP32 fields: ln n_i, ln n_e and, for the energy density, the log of
+// the mean energy in eV, ln(n_eps ph0 / n_e), with ln n_eps recovered as
+// ln n_e + that - ln ph0.  The mean energy indexes the rate table, whose
+// Arrhenius-like rates amplify an error in ln(eps) by ~15.8/eps; stored this
+// way it has the rounding of a number of magnitude |ln eps_eV| < 4 instead
+// of that of ln n_eps (up to ~13).
 #include <cmath>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -103,10 +108,14 @@ __global__ void k_faces_mix(const FaceMixArgs a) {
     }
 }
 
-// FP32 log-density of a whole field (ghost ring included)
-__global__ void k_log32(const double *n, float *l, size_t cnt) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
-        l[i] = logf(fmaxf((float)n[i], 1e-30f));
+// FP32 log companion of a whole field (ghost ring included): ln n, or with a
+// denominator field ln(scale * n / den) -- the energy density is kept as the
+// log of the mean energy in eV, ln(n_eps ph0 / n_e)
+__global__ void k_log32(const double *n, const double *den, double scale, float *l, size_t cnt) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x) {
+        double v = den ? scale * n[i] / den[i] : n[i];
+        l[i] = logf(fmaxf((float)v, 1e-30f));
+    }
 }
 
 // circ_step ghosts in mixed mode: phi ghost and both face fields of the row
@@ -195,28 +204,28 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
     const float ve_c = (float)pp.ve_coef, t0_x0 = (float)(pp.t0 / pp.x0);
     unsigned int st = 0;
 
+    // tile + halo: log densities, densities, mean energy and its table coefficients
     for (int q = tid; q < HX * HY; q += NT) {
         int lx = q % HX, ly = q / HX;
         int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
         bool in = gi <= nx + 1 && gj <= ny + 1;
         size_t o = (size_t)gj * P + gi;
+        float lw = 0.0f;
 #pragma unroll
         for (int s = 0; s < NS; s++) {
             float l = in ? a.lin[s][o] : 0.0f;
+            if (s == 2) {                   // stored: ln(mean energy in eV)
+                lw = l;
+                l = s_l[1][ly][lx] + lw - ln_ph0;
+            }
             s_l[s][ly][lx] = l;
             s_n[s][ly][lx] = expf(l);
         }
-    }
-    __syncthreads();
-    for (int q = tid; q < HX * HY; q += NT) {
-        int lx = q % HX, ly = q / HX;
-        int gi = gx0 - 1 + lx, gj = gy0 - 1 + ly;
         float te = 0, mu = 0, de = 0;
         if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
-            float dl = s_l[2][ly][lx] - s_l[1][ly][lx];
-            te = expf(dl);
+            te = expf(lw - ln_ph0);
             int k; float w;
-            tab32(a, dl + ln_ph0, k, w);
+            tab32(a, lw, k, w);
             mu = tv32(a.tab, k, w, 0);
             de = tv32(a.tab, k, w, 1);
             if (lx >= 1 && lx <= BX && ly >= 1 && ly <= BY) { s_k[ly - 1][lx - 1] = k; s_w[ly - 1][lx - 1] = w; }
@@ -380,8 +389,8 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
             kv[3] = -dfdx[3] - dfdy[3] + term_sm;
         }
         const double dt = a.ctrl->dt;
-        const float dtf = (float)dt;
         const int stg = a.stage;
+        double vn[NS];
 #pragma unroll
         for (int s = 0; s < NS; s++) {
             if (isnan(kv[s])) st |= FS_ST_NAN;
@@ -393,8 +402,8 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
             else if (stg == 4) comb = (a.k1[s][o] - a.k3[s][o] * 3.0f + kv[s] * 4.0f) * 0.5f;
             else comb = (a.k1[s][o] + a.k4[s][o] * 4.0f + kv[s]) * (1.0f / 6.0f);
             const double n3 = a.nbase[s][o];
-            const double v = fmax(n3 + (double)(dtf * comb), pp.nmin[s]);   // FP64 accumulation
-            a.lout[s][o] = logf((float)v);
+            const double v = fmax(n3 + dt * (double)comb, pp.nmin[s]);   // FP64 accumulation
+            vn[s] = v;
             if (a.nout[s]) a.nout[s][o] = v;
             if (stg == 5) {
                 const double k1 = a.k1[s][o], k3 = a.k3[s][o], k4 = a.k4[s][o];
@@ -404,6 +413,9 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
                 qerr[s] = qq * qq;
             }
         }
+#pragma unroll
+        for (int s = 0; s < NS; s++)
+            a.lout[s][o] = s == 2 ? logf((float)(vn[2] * pp.ph0 / vn[1])) : logf((float)vn[s]);
         if (stg == 5) {
             const int ty = a.m.ty[(gj - 1) * nx + gi - 1], tx = a.m.tx[(gj - 1) * nx + gi - 1];
             float mue2;
@@ -482,7 +494,8 @@ int fs_mixed_sync_logs(fs_ctx *c) {
     for (int s = 0; s < c->cfg.nspecies; s++)
         for (int b = 0; b < FS_NBUF; b++) {
             c->launches++;
-            k_log32<<<2 * c->nsm, 256, 0, c->stream>>>(c->sp[s].buf[b], c->lbuf[s][b], c->field_elems);
+            k_log32<<<2 * c->nsm, 256, 0, c->stream>>>(c->sp[s].buf[b], s == 2 ? c->sp[1].buf[b] : nullptr,
+                                                        c->pp.ph0, c->lbuf[s][b], c->field_elems);
         }
     return fs_cuda_check(c, cudaGetLastError(), "log densities");
 }

@@ -494,6 +494,7 @@ __global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part,
     double e_ni = s[0][0], e_ne = s[1][0], e_nt = s[2][0], e_nm = ns == 4 ? s[3][0] : 0.0;
     double err_cur = sqrt(e_ni + e_ne + e_nm + e_nt);
     c->err_cur = err_cur;
+    c->dt_step = c->dt;
     c->ida = s[FS_MAX_SPECIES][0];
     c->idc = s[FS_MAX_SPECIES + 1][0];
     c->rejected = 0;

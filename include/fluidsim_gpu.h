@@ -135,6 +135,8 @@ typedef struct fs_stats {
     int64_t lapl_iters;     /* total Krylov iterations                                */
     int32_t last_lapl_iters;
     int32_t lerr;           /* lerr of the last Poisson solve                         */
+    double  dt_step;        /* dt of the last accepted RK attempt (before the
+                               controller's update of g%dt, ptcl_lib.F90:59-95)       */
 } fs_stats;
 
 typedef struct fs_ctx fs_ctx;

@@ -292,6 +292,7 @@ struct or_ctx {
     double err_prev = 1.0, t_m = 1e9;
     double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or, Ida = 0, Idc = 0;
     double err_cur = 0;
+    double dt_step = 0;
     long ts = 0;
     fs_stats st;
     std::string err;
@@ -749,6 +750,7 @@ int ptcl_step(or_ctx &c, int &attempts) {
         if (stage == 5) {
             double err_cur = std::sqrt(e_ni + e_ne + e_nm + e_nt);
             c.err_cur = err_cur;
+            c.dt_step = c.dt;
             if (!c.cfg.adaptive) break;
             double scfac = 8e-1 * std::pow(err_cur, -7e-1 / 4.0) * std::pow(c.err_prev, 4e-1 / 4.0);
             scfac = std::min(2.5, std::max(3e-1, scfac));
@@ -1530,6 +1532,7 @@ int or_get_stats(or_ctx *c, fs_stats *out) {
     c->st.ida = c->Ida;
     c->st.idc = c->Idc;
     c->st.err_cur = c->err_cur;
+    c->st.dt_step = c->dt_step;
     c->st.steps = c->ts;
     *out = c->st;
     return FS_OK;

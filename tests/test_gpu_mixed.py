@@ -6,6 +6,14 @@ interior with the density floor as absolute guard, and L2), phi within 1e-5
 relative to max|phi|; every Poisson solve converged to the same relative
 residual as the FP64 solver (lapl_rtol, here 1e-8), with the residual formed
 in FP64.
+
+Both runs take the same steps.  With the adaptive controller the FP32
+right-hand side moves the Merson error estimate (a difference of stage
+derivatives that cancels to O(dt^4)) by ~1e-4 relative, so two adaptive runs
+drift apart in dt and, after tens of steps, sit at different times; that is a
+different trajectory, not an arithmetic error.  The adaptive comparison
+therefore replays the mixed run's accepted step sizes in an FP64 run with the
+controller off.
 """
 import numpy as np
 import pytest
@@ -39,35 +47,63 @@ def _errors(g, r, k):
     return e
 
 
-def test_mixed_vs_oracle_adaptive(built):
-    """Mixed steps follow the FP64 oracle step for step on a 48x40 grid."""
+def test_mixed_fixed_dt_vs_oracle(built):
+    """20 fixed-dt steps on a 48x40 grid against the FP64 oracle."""
     from fluidsim_gb300 import api
     from oracle import oracle
-    cfg, cfgm, mesh, k, st = _setup(48, ny=40)
+    cfg, cfgm, mesh, k, st = _setup(48, ny=40, adaptive=0)
+    cfg, cfgm = cfg.replace(dt0=cfg.dt0 / 4), cfgm.replace(dt0=cfg.dt0 / 4)
     gpu = api.Discharge(cfgm, mesh, st)
     ref = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_DIRECT)
-    for s in range(12):
+    for s in range(20):
         gi, ri = gpu.step(), ref.step()
         assert gi["lerr"] == 0 and ri["lerr"] == 0
-        assert gi["attempts"] == ri["attempts"], (s, gi, ri)
-        assert gi["dt"] == pytest.approx(ri["dt"], rel=1e-3), (s, gi, ri)
+        assert gi["relres"] <= cfg.lapl_rtol
     e = _errors(gpu.download(), ref.download(), k)
     assert max(e.values()) < DENS_BAR, e
 
 
-@pytest.mark.parametrize("n,steps", [(128, 40), (256, 20)])
-def test_mixed_vs_fp64_gpu(built, n, steps):
-    """Same seeded run in both precisions through the C ABI; the FP64 GPU path
+@pytest.mark.parametrize("n,steps", [(128, 200), (256, 100)])
+def test_mixed_fixed_dt_vs_fp64_gpu(built, n, steps):
+    """Fixed-dt runs in both precisions through the C ABI; the FP64 GPU path
     stands for the oracle here (it matches the oracle to 1e-10)."""
     from fluidsim_gb300 import api
-    cfg, cfgm, mesh, k, st = _setup(n)
+    cfg, cfgm, mesh, k, st = _setup(n, adaptive=0)
+    cfg, cfgm = cfg.replace(dt0=cfg.dt0 / 4), cfgm.replace(dt0=cfg.dt0 / 4)
     a, b = api.Discharge(cfg, mesh, st), api.Discharge(cfgm, mesh, st)
     for s in range(steps):
         ga, gb = a.step(), b.step()
         assert ga["lerr"] == 0 and gb["lerr"] == 0, (s, ga, gb)
         assert gb["relres"] <= cfg.lapl_rtol
-        assert ga["attempts"] == gb["attempts"], (s, ga, gb)
-    assert b.t == pytest.approx(a.t, rel=1e-3)
+    e = _errors(b.download(), a.download(), k)
+    assert max(e.values()) < DENS_BAR, e
+
+
+def _replay(a, b, steps):
+    """Step b (mixed, adaptive) and replay its step sizes in a (FP64, controller
+    off).  The reference's loop runs lapl_solve with the dt the controller has
+    already updated and advances t by it (main.F90:75-90), so a takes the
+    attempt's dt in ptcl_step and b's updated dt in lapl_solve."""
+    for s in range(steps):
+        gb = b.step()
+        assert gb["lerr"] == 0 and gb["relres"] <= b.cfg.lapl_rtol, (s, gb)
+        if a.ts > 1:
+            a.dt = b.stats()["dt_step"]   # the accepted attempt's dt
+            a.ptcl_step()
+        a.dt = b.dt
+        ga = a.lapl_solve()
+        assert ga["lerr"] == 0, (s, ga)
+        a.accept()
+    assert a.t == pytest.approx(b.t, rel=1e-14)
+
+
+@pytest.mark.parametrize("n,steps", [(64, 150), (256, 60)])
+def test_mixed_adaptive_replay(built, n, steps):
+    from fluidsim_gb300 import api
+    cfg, cfgm, mesh, k, st = _setup(n)
+    a = api.Discharge(cfg.replace(adaptive=0), mesh, st)
+    b = api.Discharge(cfgm, mesh, st)
+    _replay(a, b, steps)
     e = _errors(b.download(), a.download(), k)
     assert max(e.values()) < DENS_BAR, e
 
