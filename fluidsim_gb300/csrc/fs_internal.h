@@ -39,6 +39,21 @@ struct PhysParams {
     double e100;                   // exp(-100): the SG exponent clamp
 };
 
+// FP32 copies of the constants the mixed-precision kernels use, formed once on
+// the host so that no kernel converts or divides FP64 parameters per thread.
+struct PhysF {
+    float ph0, ln_ph0, mui, vi, gam, Di, mui_Di, ve_c, t0_x0, Dm, ninf, me_mi, tg_term;
+    float h_ir, h_ex, h_si, k_mp, k_r, k_2q, k_3q_ninf2;
+    float lemin, inv_h, ntab_m1;
+    float abs_tol, rel_tol;
+    float nmin[FS_MAX_SPECIES];
+};
+
+// FP32 copy of the mesh arrays (same layout as MeshDev's blob).
+struct MeshF {
+    const float *dx, *dy, *inv_dx, *inv_dy, *dlx, *dly, *inv_dlx, *inv_dly, *r;
+};
+
 // Mesh arrays on the device (all FP64, 0-based).
 struct MeshDev {
     const double *dx, *dy;         // nx+1, ny+1: face spacings (Fortran dx(1..nx+1))
@@ -66,6 +81,8 @@ struct Ctrl {
     // Krylov scalars
     double rz, rz_old, pq, alpha, beta, rnorm2, bnorm2, relres;
     int cg_done, cg_iters, cg_fail, pad2;
+    double r0in2;              // mixed solver: inner residual norm^2 at the last refinement
+    int inner_it, refine;      // mixed solver: inner iterations since it, refinement due
     unsigned int counter[8];   // last-block-done counters of grid reductions
     double host_result;        // host-side landing slot of single-value results
 };
@@ -163,11 +180,15 @@ struct fs_ctx {
     // state buffers, FP32 stage derivatives, FP32 face data and table, FP32
     // multigrid hierarchy
     int mixed;
+    PhysF pf;
+    MeshF meshf;
+    float *d_meshf;
     float *lbuf[FS_MAX_SPECIES][FS_NBUF];
     float *k32[FS_MAX_SPECIES][3];
     float *f32[10];              // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
     float *d_tab32;
     MGLevelF mgf[FS_MG_MAX_LEVELS];
+    float *p32, *q32;            // FP32 inner CG vectors
     cudaGraph_t cgm_graph;
     cudaGraphExec_t cgm_exec;
     int cgm_graph_built;

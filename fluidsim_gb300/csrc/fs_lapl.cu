@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
 __global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a) {
     double v = 0.0;
     CG_NODES(a, {
-        const int I = (int)(q_ % a.nx) + 1, J = (int)(q_ / a.nx) + 1;
+        const int J = (int)j_ + 1, I = (int)(q_ - j_ * (unsigned)a.nx) + 1;
         double z = L.x[o];
         if (((I + J) & 1) == 0) {
             z = gs_node(L, o);
@@ -519,6 +519,16 @@ int fs_lapl_alloc(fs_ctx *c) {
     c->mg_fused = c->cfg.mg_smooth == 2;
     cudaFuncSetAttribute(k_mg_down<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<double>(2));
     cudaFuncSetAttribute(k_mg_up<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<double>(2));
+    {
+        BottomArgs<double> ba;
+        ba.nl = nl;
+        ba.lb = 0;
+        while (ba.lb < nl && (c->mg[ba.lb].nx > BOTTOM_N || c->mg[ba.lb].ny > BOTTOM_N)) ba.lb++;
+        for (int l = 0; l < nl; l++) { ba.L[l].nx = c->mg[l].nx; ba.L[l].ny = c->mg[l].ny; }
+        cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(6 * sizeof(double) * bottom_smem_elems(ba)));
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
+    }
     size_t n0 = (size_t)(c->ny + 2) * c->pitch;
     double **vecs[] = {&c->p, &c->q, &c->z, &c->r, &c->xs, &c->bs, &c->dinv};
     for (double **v : vecs) {
@@ -588,7 +598,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     ba.nl = nl;
     ba.nu = nu;
     fs_prof_begin(c, PROF_BOTTOM);
-    k_bottom<<<1, BOTTOM_THREADS, 0, c->stream>>>(ba);
+    k_bottom_smem<double><<<1, BOTTOM_THREADS, 6 * sizeof(double) * bottom_smem_elems(ba), c->stream>>>(ba);
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);

@@ -33,43 +33,48 @@ namespace {
 //   bm = B(-a), bp = B(a), dm = -B'(-a), dp = -B'(a);  dm + dp = 1.
 __device__ __forceinline__ void bern4(float a, float &bm, float &bp, float &dm, float &dp) {
     const float x = fabsf(a);
-    float b_neg, b_pos, d_pos;   // B(-x), B(x), -B'(x) for x >= 0
+    const float d = -expm1f(-x);          // 1 - e^-x
+    const float em = 1.0f - d;
+    float b_neg, b_pos, d_pos;            // B(-x), B(x), -B'(x) for x >= 0
     if (x < 1e-3f) {
         b_neg = 1.0f + 0.5f * x + x * x * (1.0f / 12.0f);
         b_pos = 1.0f - 0.5f * x + x * x * (1.0f / 12.0f);
     } else {
-        const float d = -expm1f(-x);      // 1 - e^-x
         b_neg = x / d;
-        b_pos = b_neg * (1.0f - d);
+        b_pos = b_neg * em;
     }
     if (x < 0.5f) {
         const float x2 = x * x;
         d_pos = 0.5f - x * (1.0f / 6.0f - x2 * (1.0f / 180.0f - x2 * (1.0f / 5040.0f - x2 * (1.0f / 151200.0f))));
     } else {
-        const float d = -expm1f(-x), em = 1.0f - d;
         d_pos = em * (x - d) / (d * d);
     }
-    if (a >= 0.0f) { bm = b_neg; bp = b_pos; dp = d_pos; dm = 1.0f - d_pos; }
-    else { bm = b_pos; bp = b_neg; dm = d_pos; dp = 1.0f - d_pos; }
+    const bool pos = a >= 0.0f;
+    bm = pos ? b_neg : b_pos;
+    bp = pos ? b_pos : b_neg;
+    dp = pos ? d_pos : 1.0f - d_pos;
+    dm = pos ? 1.0f - d_pos : d_pos;
 }
 
 struct AsmMixArgs {
     PhysParams pp;
+    PhysF f;
     MeshDev m;
+    MeshF mf;
     const float *tab;
     const double *ni, *ne, *nt, *ph, *phm;
     const double *fx_e, *fy_e;
-    const float *f[10];
+    const float *f32[10];
     const Ctrl *ctrl;
     Ctrl *ctrl_w;
     float *mc, *ce, *cn, *extra, *inv_mc;
-    double *rhs, *dinv;
+    double *rhs;
 };
 
-__device__ __forceinline__ void tab32(const PhysParams &pp, float lneps, int &k, float &w) {
-    float u = (lneps - (float)pp.lemin) * (float)pp.inv_h;
+__device__ __forceinline__ void tab32(const PhysParams &pp, const PhysF &pf, float lneps, int &k, float &w) {
+    float u = (lneps - pf.lemin) * pf.inv_h;
     if (!(u >= 0.0f)) u = 0.0f;
-    if (u > (float)(pp.ntab - 1)) u = (float)(pp.ntab - 1);
+    if (u > pf.ntab_m1) u = pf.ntab_m1;
     int i = (int)u;
     if (i > pp.ntab - 2) i = pp.ntab - 2;
     k = i;
@@ -82,19 +87,19 @@ __device__ __forceinline__ float tv32(const float *tab, int k, float w, int row)
 
 // Interior face: ion and electron fluxes and the face conductance
 // 1/h + dt (mui/h dFi + mue/h dFe).
-__device__ __forceinline__ void sg_face_mix(const PhysParams &pp, const float *fc, size_t of, float E,
+__device__ __forceinline__ void sg_face_mix(const PhysF &pf, const float *fc, size_t of, float E,
                                             float Emi, bool same, float dh, float idh, float mue, float De,
                                             float nil, float nir, float nel, float ner, float dt,
                                             float &fi, float &fe, float &cf) {
-    const float mui = (float)pp.mui;
+    const float mui = pf.mui;
     fi = fc[1] * nil - fc[2] * nir;
     float dFi;
     if (same) {
         dFi = fc[3] * nil + fc[4] * nir;
     } else {
         float bm, bp, dm, dp;
-        bern4(mui * Emi * dh / (float)pp.Di, bm, bp, dm, dp);
-        dFi = fabs(pp.mui * (double)Emi) < 1e-12 ? 0.0f : dm * nil + dp * nir;
+        bern4(pf.mui_Di * Emi * dh, bm, bp, dm, dp);
+        dFi = fabsf(mui * Emi) < 1e-12f ? 0.0f : dm * nil + dp * nir;
     }
     float bm, bp, dm, dp;
     const float ae = -mue * E * dh / De;
@@ -122,9 +127,10 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
     const int gx0 = blockIdx.x * ABX + 1, gy0 = blockIdx.y * ABY + 1;
     const double dt = a.ctrl->dt;
     const float dtf = (float)dt;
-    const float ln_ph0 = (float)log(pp.ph0);
-    const float mui = (float)pp.mui, vi = (float)pp.vi, gam = (float)pp.gam;
-    const float ve_c = (float)pp.ve_coef, t0_x0 = (float)(pp.t0 / pp.x0);
+    const PhysF &pf = a.f;
+    const float ln_ph0 = pf.ln_ph0;
+    const float mui = pf.mui, vi = pf.vi, gam = pf.gam;
+    const float ve_c = pf.ve_c, t0_x0 = pf.t0_x0;
     unsigned int st = 0;
     for (int q = tid; q < (ABX + 2) * (ABY + 2); q += ANT) {
         int lx = q % (ABX + 2), ly = q / (ABX + 2);
@@ -136,18 +142,18 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         s_ne[ly][lx] = ne;
         float te = 0, mu = 0, de = 0;
         if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) {
-            const double nt64 = a.nt[o], ne64 = a.ne[o];
+            const float nt32 = (float)a.nt[o];
             float lneps;
-            if ((nt64 >= 0.0) && (ne64 >= 0.0)) {
-                te = (float)(nt64 / ne64);
-                lneps = logf((float)(nt64 * pp.ph0 / ne64));   // ln(mean energy in eV)
+            if ((nt32 >= 0.0f) && (ne >= 0.0f)) {
+                te = nt32 / ne;
+                lneps = logf(nt32 * pf.ph0 / ne);   // ln(mean energy in eV)
             } else {
                 st |= FS_ST_NEG_DENSITY;
                 te = 1e-8f;
                 lneps = logf(1e-8f) + ln_ph0;
             }
             int k; float w;
-            tab32(pp, lneps, k, w);
+            tab32(pp, pf, lneps, k, w);
             mu = tv32(a.tab, k, w, 0);
             de = tv32(a.tab, k, w, 1);
         }
@@ -161,9 +167,9 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         if (gj > ny || gi > nx) continue;
         int lx = c, ly = r + 1;
         const size_t of = (size_t)gj * P + gi;
-        const float dh = (float)a.m.dx[gi], idh = (float)a.m.inv_dx[gi];
+        const float dh = a.mf.dx[gi], idh = a.mf.inv_dx[gi];
         const double E64 = a.fx_e[of];
-        const float E = a.f[0][of];
+        const float E = a.f32[0][of];
         int tl = gi >= 1 ? a.m.tx[(gj - 1) * nx + gi - 1] : 0;
         int tr = gi + 1 <= nx ? a.m.tx[(gj - 1) * nx + gi] : 0;
         float fi = 0, fe = 0, cf = 0;
@@ -198,9 +204,9 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
             const float De = 0.5f * (s_de[ly][lx] + s_de[ly][lx + 1]);
             const size_t ol = (size_t)gj * P + gi;
             const bool same = a.phm[ol] == a.ph[ol] && a.phm[ol + 1] == a.ph[ol + 1];
-            const float Emi = same ? E : (float)(-(a.phm[ol + 1] - a.phm[ol]) / a.m.dx[gi]);
-            const float fc[5] = {E, a.f[1][of], a.f[2][of], a.f[3][of], a.f[4][of]};
-            sg_face_mix(pp, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly][lx + 1],
+            const float Emi = same ? E : (float)(-(a.phm[ol + 1] - a.phm[ol]) * a.m.inv_dx[gi]);
+            const float fc[5] = {E, a.f32[1][of], a.f32[2][of], a.f32[3][of], a.f32[4][of]};
+            sg_face_mix(pf, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly][lx + 1],
                         s_ne[ly][lx], s_ne[ly][lx + 1], dtf, fi, fe, cf);
             if (isnan(cf)) st |= FS_ST_DFDPH_NAN;
         }
@@ -213,9 +219,9 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         if (gi > nx || gj > ny) continue;
         int lx = c + 1, ly = r;
         const size_t of = (size_t)gj * P + gi;
-        const float dh = (float)a.m.dy[gj], idh = (float)a.m.inv_dy[gj];
+        const float dh = a.mf.dy[gj], idh = a.mf.inv_dy[gj];
         const double E64 = a.fy_e[of];
-        const float E = a.f[5][of];
+        const float E = a.f32[5][of];
         int tb = gj >= 1 ? a.m.ty[(gj - 1) * nx + gi - 1] : 0;
         int tt = gj + 1 <= ny ? a.m.ty[gj * nx + gi - 1] : 0;
         float fi = 0, fe = 0, cf = 0;
@@ -248,9 +254,9 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
             const float De = 0.5f * (s_de[ly][lx] + s_de[ly + 1][lx]);
             const size_t ol = (size_t)gj * P + gi;
             const bool same = a.phm[ol] == a.ph[ol] && a.phm[ol + P] == a.ph[ol + P];
-            const float Emi = same ? E : (float)(-(a.phm[ol + P] - a.phm[ol]) / a.m.dy[gj]);
-            const float fc[5] = {E, a.f[6][of], a.f[7][of], a.f[8][of], a.f[9][of]};
-            sg_face_mix(pp, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly + 1][lx],
+            const float Emi = same ? E : (float)(-(a.phm[ol + P] - a.phm[ol]) * a.m.inv_dy[gj]);
+            const float fc[5] = {E, a.f32[6][of], a.f32[7][of], a.f32[8][of], a.f32[9][of]};
+            sg_face_mix(pf, fc, of, E, Emi, same, dh, idh, mue, De, s_ni[ly][lx], s_ni[ly + 1][lx],
                         s_ne[ly][lx], s_ne[ly + 1][lx], dtf, fi, fe, cf);
             if (isnan(cf)) st |= FS_ST_DFDPH_NAN;
         }
@@ -261,26 +267,32 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
     const int gi = gx0 + lx, gj = gy0 + ly;
     if (gi <= nx && gj <= ny) {
         const size_t o = (size_t)gj * P + gi;
-        const double dlx = a.m.dlx[gi - 1], dly = a.m.dly[gj - 1];
-        const double idlx = a.m.inv_dlx[gi - 1], idly = a.m.inv_dly[gj - 1];
         const int tx = a.m.tx[(gj - 1) * nx + gi - 1], ty = a.m.ty[(gj - 1) * nx + gi - 1];
-        const double wr = pp.cyl ? a.m.r[gj] : 1.0;
-        const double wn = pp.cyl ? (a.m.r[gj + 1] + a.m.r[gj]) / 2.0 : 1.0;
-        const double ws = pp.cyl ? (a.m.r[gj] + a.m.r[gj - 1]) / 2.0 : 1.0;
         // Gauss-law part in FP64
+        const double idlx = a.m.inv_dlx[gi - 1];
         double dfdx = -(s_xe[ly][lx + 1] - s_xe[ly][lx]) * idlx;
-        double dfdy = pp.cyl ? -(s_ye[ly + 1][lx] * wn - s_ye[ly][lx] * ws) / dly / wr
-                             : -(s_ye[ly + 1][lx] - s_ye[ly][lx]) * idly;
-        // flux divergence in FP32
-        const float fidlx = (float)idlx, fidly = (float)idly;
-        float div = ((s_xfi[ly][lx + 1] - s_xfi[ly][lx]) - (s_xfe[ly][lx + 1] - s_xfe[ly][lx])) * fidlx;
+        double dfdy;
         if (pp.cyl) {
-            const float fwn = (float)wn, fws = (float)ws, fwr = (float)wr;
+            const double wr = a.m.r[gj], wn = (a.m.r[gj + 1] + wr) / 2.0, ws = (wr + a.m.r[gj - 1]) / 2.0;
+            dfdy = -(s_ye[ly + 1][lx] * wn - s_ye[ly][lx] * ws) / a.m.dly[gj - 1] / wr;
+        } else {
+            dfdy = -(s_ye[ly + 1][lx] - s_ye[ly][lx]) * a.m.inv_dly[gj - 1];
+        }
+        // flux divergence and the conductances in FP32
+        const float fdlx = a.mf.dlx[gi - 1], fdly = a.mf.dly[gj - 1];
+        const float fidlx = a.mf.inv_dlx[gi - 1], fidly = a.mf.inv_dly[gj - 1];
+        float fwr = 1.0f, fwn = 1.0f, fws = 1.0f;
+        if (pp.cyl) {
+            fwr = a.mf.r[gj];
+            fwn = 0.5f * (a.mf.r[gj + 1] + fwr);
+            fws = 0.5f * (fwr + a.mf.r[gj - 1]);
+        }
+        float div = ((s_xfi[ly][lx + 1] - s_xfi[ly][lx]) - (s_xfe[ly][lx + 1] - s_xfe[ly][lx])) * fidlx;
+        if (pp.cyl)
             div += ((s_yfi[ly + 1][lx] * fwn - s_yfi[ly][lx] * fws) - (s_yfe[ly + 1][lx] * fwn - s_yfe[ly][lx] * fws))
                    * fidly / fwr;
-        } else {
+        else
             div += ((s_yfi[ly + 1][lx] - s_yfi[ly][lx]) - (s_yfe[ly + 1][lx] - s_yfe[ly][lx])) * fidly;
-        }
         double b = dfdx + dfdy + (a.ni[o] - a.ne[o]) - dt * (double)div;
         if (isnan(b)) st |= FS_ST_BNAN;
         const float cw = s_xc[ly][lx], cee = s_xc[ly][lx + 1], cs = s_yc[ly][lx], cnn = s_yc[ly + 1][lx];
@@ -291,65 +303,59 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         if (gi == nx && tx == 2) gx += cee;
         if (gj == 1 && ty == -2) gys += cs;
         if (gj == ny && ty == 2) gyn += cnn;
-        if (gi == 1 && tx == -1) gx += (float)(1.0 / a.m.dx[0] - 1.0 / a.m.dx[1]);
-        if (gj == 1 && ty == -1) gyn += (float)(1.0 / a.m.dy[0] - 1.0 / a.m.dy[1]);
-        const float sx = (float)(dly * wr), fdlx = (float)dlx, fwn = (float)wn, fws = (float)ws;
+        if (gi == 1 && tx == -1) gx += a.mf.inv_dx[0] - a.mf.inv_dx[1];
+        if (gj == 1 && ty == -1) gyn += a.mf.inv_dy[0] - a.mf.inv_dy[1];
+        const float sx = fdly * fwr;
         const float extra = gx * sx + (gys * fws + gyn * fwn) * fdlx;
         const float mc = (offw + offe) * sx + (offs * fws + offn * fwn) * fdlx + extra;
-        const double D = dlx * dly * wr;
         a.mc[o] = mc;
         a.inv_mc[o] = 1.0f / mc;
         a.extra[o] = extra;
         a.ce[o] = offe * sx;
         a.cn[o] = offn * fwn * fdlx;
-        a.rhs[o] = b * D;
-        a.dinv[o] = 1.0 / D;
+        // the CG runs on M d = D b, D = dlx dly r; 1/D is written by k_dinv once
+        a.rhs[o] = b * (a.m.dlx[gi - 1] * a.m.dly[gj - 1] * (pp.cyl ? a.m.r[gj] : 1.0));
     }
     if (st) atomicOr(&a.ctrl_w->status, st);
 }
 
-// ---------------------------------------------------------------- FP64 CG
+// 1/D of the row scaling D = dlx dly r (a property of the mesh)
+__global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *dinv) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x + 1, gj = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (gi > nx || gj > ny) return;
+    dinv[(size_t)gj * P + gi] = 1.0 / (m.dlx[gi - 1] * m.dly[gj - 1] * (cyl ? m.r[gj] : 1.0));
+}
+
+// --------------------------------------------- FP32 CG under FP64 refinement
+// Outer loop (FP64): r = D b - M x, ||r|| / ||b|| checked against lapl_rtol.
+// Inner loop: flexible PCG with FP32 vectors and the FP32 V-cycle on the
+// current residual, the iterate accumulated in FP64, run until its FP32
+// recurrence residual has fallen by inner_tol (or just enough to reach
+// lapl_rtol, or inner_max iterations); then the refinement recomputes the
+// true residual in FP64 and restarts the inner loop from it.  The FP32
+// recurrence drifts from the true residual (rounding of the FP32 vectors and
+// operator products); the refinement removes the drift, so the converged
+// residual is the true FP64 one.  Dot products: FP32 products summed per thread, then FP64 across
+// threads and CTAs in a fixed order.
 struct CgmArgs {
     int nx, ny, P, nblk;
     dim3 grid;
-    double *x, *r, *p, *q, *rhs, *dinv, *part;
-    float *z, *r32;
-    const float *mc, *ce, *cn, *extra;
+    double *x, *r, *rhs, *dinv, *part;   // FP64: iterate, true residual, D b, 1/D
+    float *z, *r32, *p, *q;              // FP32 inner vectors (z, r32 are level 0 of the V-cycle)
+    const float *ce, *cn, *extra;
     Ctrl *ctrl;
-    double rtol;
-    int maxit;
+    double rtol, inner_tol2;
+    int maxit, inner_max;
     int use_cond;
     cudaGraphConditionalHandle cond;
 };
 
-__global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
-    double v = 0.0;
-    CG_NODES(a, {
-        const double b = a.rhs[o];
-        a.x[o] = 0.0;
-        a.r[o] = b;
-        a.r32[o] = (float)b;
-        a.p[o] = 0.0;
-        a.q[o] = 0.0;
-        double u = b * a.dinv[o];
-        v += u * u;
-    })
-    double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[0], a.nblk, &out) && threadIdx.x == 0) {
-        a.ctrl->bnorm2 = out;
-        a.ctrl->rnorm2 = out;
-        a.ctrl->relres = out > 0.0 ? 1.0 : 0.0;
-        a.ctrl->cg_done = out == 0.0 ? 1 : 0;
-        a.ctrl->cg_iters = 0;
-        a.ctrl->cg_fail = 0;
-        a.ctrl->rz = 0.0;
-    }
-}
-
-// rz = r.z and z.q (q = M p of the previous direction) in one pass, then the
-// flexible beta = -alpha z.q / rz_old (0 on the first iteration).
-__device__ __forceinline__ double block_sum2(double v, double w, double &wsum) {
+// Fixed-order sum of two per-thread values over the grid; true in the last
+// CTA (thread 0 holds the sums).  part needs 2 * nblk entries.
+__device__ bool grid_sum2(double v, double w, double *part, unsigned int *counter, int nblk, double &sv,
+                          double &sw) {
     __shared__ double s_a[8], s_b[8];
+    __shared__ bool s_last;
     for (int o = 16; o > 0; o >>= 1) {
         v += __shfl_down_sync(0xffffffffu, v, o);
         w += __shfl_down_sync(0xffffffffu, w, o);
@@ -357,107 +363,218 @@ __device__ __forceinline__ double block_sum2(double v, double w, double &wsum) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) { s_a[wid] = v; s_b[wid] = w; }
     __syncthreads();
-    double ra = 0.0, rb = 0.0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 8; k++) { ra += s_a[k]; rb += s_b[k]; }
-    wsum = rb;
-    return ra;
-}
-
-__global__ void __launch_bounds__(256) k_cgm_rz(const CgmArgs a) {
-    double v = 0.0, w = 0.0;
-    CG_NODES(a, {
-        const double z = a.z[o];
-        v += a.r[o] * z;
-        w += z * a.q[o];
-    })
-    double ws;
-    double vs = block_sum2(v, w, ws);
-    __shared__ bool s_last;
     if (threadIdx.x == 0) {
-        a.part[blockIdx.x] = vs;
-        a.part[a.nblk + blockIdx.x] = ws;
+        double ra = 0.0, rb = 0.0;
+        for (int k = 0; k < 8; k++) { ra += s_a[k]; rb += s_b[k]; }
+        part[blockIdx.x] = ra;
+        part[nblk + blockIdx.x] = rb;
         __threadfence();
-        unsigned int prev = atomicAdd(&a.ctrl->counter[1], 1u);
-        s_last = prev == (unsigned int)a.nblk - 1u;
+        s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
     }
     __syncthreads();
-    if (!s_last) return;
+    if (!s_last) return false;
     __threadfence();
     __shared__ double s_r[256], s_w[256];
-    double sv = 0.0, sw = 0.0;
-    for (int b = threadIdx.x; b < a.nblk; b += 256) {
-        sv += ((volatile double *)a.part)[b];
-        sw += ((volatile double *)a.part)[a.nblk + b];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < nblk; k += 256) {
+        a += ((volatile double *)part)[k];
+        b += ((volatile double *)part)[nblk + k];
     }
-    s_r[threadIdx.x] = sv;
-    s_w[threadIdx.x] = sw;
+    s_r[threadIdx.x] = a;
+    s_w[threadIdx.x] = b;
     __syncthreads();
     for (int k = 128; k > 0; k >>= 1) {
         if (threadIdx.x < k) { s_r[threadIdx.x] += s_r[threadIdx.x + k]; s_w[threadIdx.x] += s_w[threadIdx.x + k]; }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    sv = s_r[0];
+    sw = s_w[0];
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
+// x = 0, r = D b (FP64), r32 = r; ||b||, ||r32||
+__global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
+    double v = 0.0, w = 0.0;
+    CG_NODES(a, {
+        const double b = a.rhs[o];
+        const float b32 = (float)b;
+        a.x[o] = 0.0;
+        a.r[o] = b;
+        a.r32[o] = b32;
+        a.p[o] = 0.0f;
+        a.q[o] = 0.0f;
+        const double u = b * a.dinv[o];
+        v += u * u;
+        w += (double)(b32 * b32);
+    })
+    double sv, sw;
+    if (grid_sum2(v, w, a.part, &a.ctrl->counter[0], a.nblk, sv, sw) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
-        c->counter[1] = 0u;
-        c->rz_old = c->rz;
-        c->rz = s_r[0];
-        c->beta = c->cg_iters == 0 ? 0.0 : -c->alpha * s_w[0] / c->rz_old;
+        c->bnorm2 = sv;
+        c->rnorm2 = sv;
+        c->r0in2 = sw;
+        c->relres = sv > 0.0 ? 1.0 : 0.0;
+        c->cg_done = sv == 0.0 ? 1 : 0;
+        c->cg_iters = 0;
+        c->cg_fail = 0;
+        c->inner_it = 0;
+        c->refine = 0;
+        c->rz = 0.0;
+        c->alpha = 0.0;
     }
 }
 
-// p = z + beta p ; q = M z + beta q ; pq = p.q ; alpha = rz / pq (FP64
-// arithmetic on the FP32 preconditioned residual and coefficients).  M is
-// applied as its face conductances, sum_f c_f (z_i - z_j) + extra_i z_i, so the
-// FP64 operator is exactly the M-matrix of the FP32 conductances; a stored
-// FP32 diagonal would differ from their sum by a rounding of size eps*M_ii,
-// which acts like a spurious reaction term and costs ~cond(M)*eps.
+__device__ __forceinline__ float4 ld4(const float *p, size_t o) { return *reinterpret_cast<const float4 *>(p + o); }
+__device__ __forceinline__ void st4(float *p, size_t o, float4 v) { *reinterpret_cast<float4 *>(p + o) = v; }
+__device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+
+// The inner-loop kernels stream whole rows 1..ny in float4 steps: every
+// inner vector and coefficient is zero on the ghost ring and the row padding,
+// so those lanes add nothing to the dot products and stay zero.
+
+// after the V-cycle: rz = r32.z, flexible beta = -alpha z.q / rz_old
+__global__ void __launch_bounds__(256) k_cgm_rz(const CgmArgs a) {
+    if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
+    float v = 0.0f, w = 0.0f;
+    CG_VEC4(a, {
+        const float4 z = ld4(a.z, o);
+        v += dot4(ld4(a.r32, o), z);
+        w += dot4(z, ld4(a.q, o));
+    })
+    double sv, sw;
+    if (grid_sum2((double)v, (double)w, a.part, &a.ctrl->counter[1], a.nblk, sv, sw) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->rz_old = c->rz;
+        c->rz = sv;
+        c->beta = c->inner_it == 0 ? 0.0 : -c->alpha * sw / c->rz_old;
+    }
+}
+
+// M z at one node in float-float arithmetic: each face term c (z_i - z_j) is
+// formed exactly (the difference of neighbouring, similar values is exact,
+// the product's rounding error is recovered with an FMA) and the terms are
+// summed with error-free additions, so the FP32 result carries an error of
+// ~eps |M z| instead of ~eps sum_f |c_f (z_i - z_j)|.  For the smooth
+// corrections of the first refinement cycle the face terms are ~1e3 times
+// larger than their sum, and a plainly rounded M z lets the FP32 residual
+// drift away from the true one by ~5e-4 relative within a few iterations.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float p, float pe) {
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+__device__ __forceinline__ float mz_ff(float z, float ze, float zw, float zn, float zs, float ce, float cw, float cn,
+                                       float cs, float ex) {
+    float hi = 0.0f, lo = 0.0f;
+    float d, p;
+    d = __fsub_rn(z, ze); p = __fmul_rn(ce, d); ff_add(hi, lo, p, __fmaf_rn(ce, d, -p));
+    d = __fsub_rn(z, zw); p = __fmul_rn(cw, d); ff_add(hi, lo, p, __fmaf_rn(cw, d, -p));
+    d = __fsub_rn(z, zn); p = __fmul_rn(cn, d); ff_add(hi, lo, p, __fmaf_rn(cn, d, -p));
+    d = __fsub_rn(z, zs); p = __fmul_rn(cs, d); ff_add(hi, lo, p, __fmaf_rn(cs, d, -p));
+    p = __fmul_rn(ex, z); ff_add(hi, lo, p, __fmaf_rn(ex, z, -p));
+    return __fadd_rn(hi, lo);
+}
+
+// p = z + beta p ; q = M z + beta q ; alpha = rz / p.q
 __global__ void __launch_bounds__(256) k_cgm_pq(const CgmArgs a) {
-    double v = 0.0;
-    const double be = a.ctrl->beta;
-    CG_NODES(a, {
-        const double zc = a.z[o];
-        double mz = (double)a.ce[o] * (zc - (double)a.z[o + 1]) + (double)a.ce[o - 1] * (zc - (double)a.z[o - 1])
-                  + (double)a.cn[o] * (zc - (double)a.z[o + a.P]) + (double)a.cn[o - a.P] * (zc - (double)a.z[o - a.P])
-                  + (double)a.extra[o] * zc;
-        double pn = zc + be * a.p[o];
-        double qn = mz + be * a.q[o];
-        a.p[o] = pn;
-        a.q[o] = qn;
-        v += pn * qn;
+    if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
+    const float be = (float)a.ctrl->beta;
+    const int P = a.P;
+    float v = 0.0f;
+    CG_VEC4(a, {
+        const float4 z = ld4(a.z, o), zn = ld4(a.z, o + P), zs = ld4(a.z, o - P);
+        const float zw = a.z[o - 1], ze = a.z[o + 4];
+        const float4 ce = ld4(a.ce, o), cn = ld4(a.cn, o), cs = ld4(a.cn, o - P), ex = ld4(a.extra, o);
+        const float cw = a.ce[o - 1];
+        float4 mz;
+        mz.x = mz_ff(z.x, z.y, zw, zn.x, zs.x, ce.x, cw, cn.x, cs.x, ex.x);
+        mz.y = mz_ff(z.y, z.z, z.x, zn.y, zs.y, ce.y, ce.x, cn.y, cs.y, ex.y);
+        mz.z = mz_ff(z.z, z.w, z.y, zn.z, zs.z, ce.z, ce.y, cn.z, cs.z, ex.z);
+        mz.w = mz_ff(z.w, ze, z.z, zn.w, zs.w, ce.w, ce.z, cn.w, cs.w, ex.w);
+        const float4 p0 = ld4(a.p, o), q0 = ld4(a.q, o);
+        const float4 pn = make_float4(z.x + be * p0.x, z.y + be * p0.y, z.z + be * p0.z, z.w + be * p0.w);
+        const float4 qn = make_float4(mz.x + be * q0.x, mz.y + be * q0.y, mz.z + be * q0.z, mz.w + be * q0.w);
+        st4(a.p, o, pn);
+        st4(a.q, o, qn);
+        v += dot4(pn, qn);
     })
     double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
+    if (grid_sum<256>((double)v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
         c->pq = out;
-        if (c->cg_done) c->alpha = 0.0;
-        else if (!(out > 0.0)) { c->cg_fail = 1; c->alpha = 0.0; }
-        else c->alpha = c->rz / out;
+        c->alpha = out > 0.0 ? c->rz / out : 0.0;
     }
 }
 
-// x += alpha p ; r -= alpha q (FP64) ; r32 = r for the next V-cycle
+// x += alpha p in FP64 ; r32 -= alpha q ; ||r32|| decides when the next
+// refinement runs.  x is accumulated in FP64: an FP32 correction would carry
+// a rounding of ~eps |d| that M amplifies by its condition number (~5e-4
+// relative residual at 1024^2), the floor no inner iteration can get below.
 __global__ void __launch_bounds__(256) k_cgm_xr(const CgmArgs a) {
-    double v = 0.0;
-    const double al = a.ctrl->alpha;
-    CG_NODES(a, {
-        a.x[o] += al * a.p[o];
-        double rr = a.r[o] - al * a.q[o];
-        a.r[o] = rr;
-        a.r32[o] = (float)rr;
-        double u = rr * a.dinv[o];
-        v += u * u;
+    if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
+    const double ald = a.ctrl->alpha;
+    const float al = (float)ald;
+    float v = 0.0f;
+    CG_VEC4(a, {
+        const float4 p = ld4(a.p, o), q = ld4(a.q, o);
+        double2 *x2 = reinterpret_cast<double2 *>(a.x + o);
+        double2 x01 = x2[0], x23 = x2[1];
+        x01.x += ald * (double)p.x; x01.y += ald * (double)p.y;
+        x23.x += ald * (double)p.z; x23.y += ald * (double)p.w;
+        x2[0] = x01;
+        x2[1] = x23;
+        float4 r = ld4(a.r32, o);
+        r.x -= al * q.x; r.y -= al * q.y; r.z -= al * q.z; r.w -= al * q.w;
+        st4(a.r32, o, r);
+        v += dot4(r, r);
     })
     double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
+    if (grid_sum<256>((double)v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
-        c->rnorm2 = out;
         c->cg_iters += 1;
-        c->relres = c->bnorm2 > 0.0 ? sqrt(out / c->bnorm2) : 0.0;
+        c->inner_it += 1;
+        c->rnorm2 = out;   // inner recurrence residual (diagnostic)
+        // this cycle's target: inner_tol, or just enough to reach rtol overall
+        const double need = 0.3 * a.rtol / fmax(c->relres, 1e-300);
+        const double tgt2 = fmax(a.inner_tol2, need * need);
+        if (!(c->pq > 0.0) || out <= tgt2 * c->r0in2 || c->inner_it >= a.inner_max ||
+            c->cg_iters >= a.maxit || isnan(out))
+            c->refine = 1;
+    }
+}
+
+// refinement: r = D b - M x in FP64, r32 = r; convergence on the FP64 residual
+__global__ void __launch_bounds__(256) k_cgm_refine(const CgmArgs a) {
+    if (!a.ctrl->refine || a.ctrl->cg_done || a.ctrl->cg_fail) return;
+    double v = 0.0, w = 0.0;
+    CG_NODES(a, {
+        const double xc = a.x[o];
+        const double mx = (double)a.ce[o] * (xc - a.x[o + 1]) + (double)a.ce[o - 1] * (xc - a.x[o - 1])
+                        + (double)a.cn[o] * (xc - a.x[o + a.P]) + (double)a.cn[o - a.P] * (xc - a.x[o - a.P])
+                        + (double)a.extra[o] * xc;
+        const double rr = a.rhs[o] - mx;
+        a.r[o] = rr;
+        const float r32 = (float)rr;
+        a.r32[o] = r32;
+        const double u = rr * a.dinv[o];
+        v += u * u;
+        w += (double)(r32 * r32);
+    })
+    double sv, sw;
+    if (grid_sum2(v, w, a.part, &a.ctrl->counter[4], a.nblk, sv, sw) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        const double prev = c->relres;
+        c->rnorm2 = sv;
+        c->r0in2 = sw;
+        c->relres = c->bnorm2 > 0.0 ? sqrt(sv / c->bnorm2) : 0.0;
+        c->inner_it = 0;
+        c->refine = 0;
         if (c->relres <= a.rtol) c->cg_done = 1;
-        if (isnan(out)) c->cg_fail = 1;
-        if (a.use_cond && (c->cg_done || c->cg_fail || c->cg_iters >= a.maxit))
-            cudaGraphSetConditional(a.cond, 0u);
+        else if (isnan(sv) || c->cg_iters >= a.maxit || !(c->relres < prev)) c->cg_fail = 1;
+        if (a.use_cond && (c->cg_done || c->cg_fail)) cudaGraphSetConditional(a.cond, 0u);
     }
 }
 
@@ -493,6 +610,12 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         }
         m.res = nullptr;
     }
+    float **vecs[] = {&c->p32, &c->q32};
+    for (float **v : vecs) {
+        cudaError_t e = cudaMalloc(v, c->field_elems * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(*v, 0, c->field_elems * sizeof(float));
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 CG vectors)");
+    }
     if (c->cg_nblk < 2 * 4 * c->nsm) {   // k_cgm_rz keeps two partials per CTA
         cudaFree(c->d_cg_part);
         cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * 2 * 4 * c->nsm);
@@ -501,7 +624,20 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
     }
     cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<float>(2));
     cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
-    return FS_OK;
+    {
+        BottomArgs<float> ba;
+        ba.nl = c->mg_nlev;
+        ba.lb = 0;
+        while (ba.lb < ba.nl && (c->mgf[ba.lb].nx > BOTTOM_N || c->mgf[ba.lb].ny > BOTTOM_N)) ba.lb++;
+        for (int l = 0; l < ba.nl; l++) { ba.L[l].nx = c->mgf[l].nx; ba.L[l].ny = c->mgf[l].ny; }
+        cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(6 * sizeof(float) * bottom_smem_elems(ba)));
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
+    }
+    c->launches++;
+    k_dinv<<<grid2(c->nx, c->ny, dim3(32, 8)), dim3(32, 8), 0, c->stream>>>(c->mesh, c->nx, c->ny, c->pitch,
+                                                                           c->cfg.cyl, c->dinv);
+    return fs_cuda_check(c, cudaGetLastError(), "row scaling");
 }
 
 void fs_lapl_free_mixed(fs_ctx *c) {
@@ -516,6 +652,8 @@ void fs_lapl_free_mixed(fs_ctx *c) {
         for (float *f : fs) cudaFree(f);
         memset(&m, 0, sizeof(m));
     }
+    cudaFree(c->p32);
+    cudaFree(c->q32);
 }
 
 // FP32 V-cycle on the correction equation: mgf[0].rhs holds the FP64
@@ -554,7 +692,7 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     ba.nl = nl;
     ba.nu = nu;
     fs_prof_begin(c, PROF_BOTTOM);
-    k_bottom<float><<<1, BOTTOM_THREADS, 0, c->stream>>>(ba);
+    k_bottom_smem<float><<<1, BOTTOM_THREADS, 6 * sizeof(float) * bottom_smem_elems(ba), c->stream>>>(ba);
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
@@ -590,6 +728,9 @@ static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
     fs_prof_end(c);
     fs_prof_begin(c, PROF_CG);
     k_cgm_xr<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_refine<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
 }
 
@@ -641,7 +782,9 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_faces_update_mixed(c);
     AsmMixArgs a;
     a.pp = c->pp;
+    a.f = c->pf;
     a.m = c->mesh;
+    a.mf = c->meshf;
     a.tab = c->d_tab32;
     a.ni = c->sp[0].buf[c->lev[0]];
     a.ne = c->sp[1].buf[c->lev[0]];
@@ -650,13 +793,12 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.phm = c->ph_mi;
     a.fx_e = c->fx_e;
     a.fy_e = c->fy_e;
-    for (int k = 0; k < 10; k++) a.f[k] = c->f32[k];
+    for (int k = 0; k < 10; k++) a.f32[k] = c->f32[k];
     a.ctrl = c->d_ctrl;
     a.ctrl_w = c->d_ctrl;
     MGLevelF &m0 = c->mgf[0];
     a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
     a.rhs = c->bs;
-    a.dinv = c->dinv;
     cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);
     fs_prof_begin(c, PROF_ASSEMBLE);
     k_assemble_mix<<<grid2(c->nx, c->ny, dim3(ABX, ABY)), ANT, 0, c->stream>>>(a);
@@ -678,12 +820,14 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         ca.nblk = (int)(nb < cap ? nb : cap);
         ca.grid = dim3(ca.nblk);
     }
-    ca.x = c->xs; ca.r = c->r; ca.p = c->p; ca.q = c->q;
+    ca.x = c->xs; ca.r = c->r;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
-    ca.z = m0.x; ca.r32 = m0.rhs;
-    ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
+    ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32;
+    ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
+    ca.inner_tol2 = 1e-5 * 1e-5;
+    ca.inner_max = 16;
     ca.maxit = c->cfg.lapl_maxit;
     ca.use_cond = 0;
     ca.cond = 0;
@@ -716,11 +860,16 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         return FS_OK;
     }
     int it = 0;
+    static const bool trace = getenv("FS_TRACE_CG") != nullptr;
     while (!ok && it < c->cfg.lapl_maxit) {
         cg_iteration_mixed(c, ca);
         rc = fs_sync_ctrl(c);
         if (rc) return rc;
         it = c->h_ctrl->cg_iters;
+        if (trace)
+            fprintf(stderr, "cgm %d inner %d relres %.3e inner_r2 %.3e r0in2 %.3e pq %.3e alpha %.3e beta %.3e\n",
+                    it, c->h_ctrl->inner_it, c->h_ctrl->relres, c->h_ctrl->rnorm2, c->h_ctrl->r0in2, c->h_ctrl->pq,
+                    c->h_ctrl->alpha, c->h_ctrl->beta);
         if (c->h_ctrl->cg_fail) break;
         ok = c->h_ctrl->cg_done != 0;
     }

@@ -343,11 +343,113 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a
     }
 }
 
+// The same V-cycle over levels [lb, nl) with every level held in shared
+// memory: the levels' operators and the intermediate right-hand sides and
+// iterates never leave the SM, so each of the ~60 dependent half sweeps costs
+// a shared-memory round trip instead of an L2 one.  Only the top level's
+// right-hand side is read from, and its iterate written to, global memory.
+// Arithmetic and order are those of k_bottom, so the results are identical.
+template <typename T>
+__host__ __device__ inline int bottom_smem_elems(const BottomArgs<T> &a) {
+    int n = 0;
+    for (int l = a.lb; l < a.nl; l++) n += (a.L[l].nx + 2) * (a.L[l].ny + 2);
+    return n;
+}
+template <typename T>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int t = threadIdx.x;
+    const int tot = bottom_smem_elems(a);
+    T *base = (T *)sm_raw;
+    LevelT<T> S[FS_MG_MAX_LEVELS];
+    {
+        int off = 0;
+        for (int l = a.lb; l < a.nl; l++) {
+            const LevelT<T> &G = a.L[l];
+            LevelT<T> &L = S[l];
+            L.nx = G.nx; L.ny = G.ny; L.P = G.nx + 2;
+            L.mc = base + off; L.ce = base + tot + off; L.cn = base + 2 * tot + off;
+            L.inv_mc = base + 3 * tot + off; L.rhs = base + 4 * tot + off; L.x = base + 5 * tot + off;
+            L.extra = nullptr; L.res = nullptr;
+            const int n = (G.nx + 2) * (G.ny + 2);
+            for (int q = t; q < n; q += BOTTOM_THREADS) {
+                const int i = q % (G.nx + 2), j = q / (G.nx + 2);
+                const size_t o = (size_t)j * G.P + i;
+                L.mc[q] = G.mc[o]; L.ce[q] = G.ce[o]; L.cn[q] = G.cn[o]; L.inv_mc[q] = G.inv_mc[o];
+                L.rhs[q] = l == a.lb ? G.rhs[o] : T(0);
+                L.x[q] = T(0);
+            }
+            off += n;
+        }
+    }
+    __syncthreads();
+    auto sweep = [&](const LevelT<T> &L, int color, int zero) {
+        for (int q = t; q < L.nx * L.ny; q += BOTTOM_THREADS) {
+            int I = q % L.nx + 1, J = q / L.nx + 1;
+            int o = J * L.P + I;
+            if (((I + J) & 1) == color) L.x[o] = zero ? L.rhs[o] * L.inv_mc[o] : gs_node(L, (size_t)o);
+            else if (zero) L.x[o] = T(0);
+        }
+        __syncthreads();
+    };
+    for (int l = a.lb; l < a.nl - 1; l++) {
+        const LevelT<T> f = S[l], c = S[l + 1];
+        sweep(f, 0, 1);
+        sweep(f, 1, 0);
+        for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
+        for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
+            int I = q % c.nx + 1, J = q / c.nx + 1;
+            const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+            T s = T(0);
+            for (int fy = fy0; fy <= fy1; fy++)
+                for (int fx = fx0; fx <= fx1; fx++)
+                    if (((fx + fy) & 1) == 0) s += resid(f, (size_t)(fy * f.P + fx));
+            c.rhs[J * c.P + I] = s;
+        }
+        __syncthreads();
+    }
+    {
+        const LevelT<T> c = S[a.nl - 1];
+        sweep(c, 0, 1);
+        if (c.nx * c.ny > 1) {
+            sweep(c, 1, 0);
+            for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
+            for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+        }
+    }
+    for (int l = a.nl - 2; l >= a.lb; l--) {
+        const LevelT<T> f = S[l], c = S[l + 1];
+        for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
+            int I = q % f.nx + 1, J = q / f.nx + 1;
+            f.x[J * f.P + I] += c.x[((J + 1) / 2) * c.P + (I + 1) / 2];
+        }
+        __syncthreads();
+        for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
+    }
+    const LevelT<T> G = a.L[a.lb], L = S[a.lb];
+    for (int q = t; q < G.nx * G.ny; q += BOTTOM_THREADS) {
+        int I = q % G.nx + 1, J = q / G.nx + 1;
+        G.x[(size_t)J * G.P + I] = L.x[J * L.P + I];
+    }
+}
+
 // grid-stride loop over the interior nodes; o is the node's field offset
+// (32-bit index arithmetic: grids are limited to 2^28 nodes)
 #define CG_NODES(a, ...)                                                                   \
-    for (long q_ = blockIdx.x * 256L + threadIdx.x; q_ < (long)(a).nx * (a).ny;           \
-         q_ += (long)gridDim.x * 256L) {                                                   \
-        const size_t o = (size_t)(q_ / (a).nx + 1) * (a).P + (size_t)(q_ % (a).nx + 1);   \
+    for (unsigned q_ = blockIdx.x * 256u + threadIdx.x; q_ < (unsigned)((a).nx * (a).ny); \
+         q_ += gridDim.x * 256u) {                                                         \
+        const unsigned j_ = q_ / (unsigned)(a).nx;                                         \
+        const size_t o = (size_t)(j_ + 1) * (a).P + (q_ - j_ * (unsigned)(a).nx + 1);      \
+        __VA_ARGS__                                                                        \
+    }
+
+// grid-stride loop over rows 1..ny of a pitched FP32 field in float4 steps
+// (ghost columns and row padding included; o is the offset of the first of
+// the four elements, a multiple of 4 since the pitch is a multiple of 32)
+#define CG_VEC4(a, ...)                                                                    \
+    for (unsigned t4_ = blockIdx.x * 256u + threadIdx.x; t4_ < (unsigned)((a).ny * (a).P / 4); \
+         t4_ += gridDim.x * 256u) {                                                        \
+        const size_t o = (size_t)(a).P + 4 * (size_t)t4_;                                  \
         __VA_ARGS__                                                                        \
     }
 

@@ -41,10 +41,25 @@ __device__ __forceinline__ float bern(float x) {
     return x / expm1f(x);
 }
 
-// SG flux from log densities: (D/h) * [B(-a) n_L - B(a) n_R]
-__device__ __forceinline__ float sg_log(float dh_inv_D, float a, float nl, float nr, float ll, float lr) {
-    if (a >= 0.0f) return dh_inv_D * bern(-a) * nl * (-expm1f(lr - ll - a));
-    return dh_inv_D * bern(a) * nr * expm1f(ll - lr + a);
+// The three Scharfetter-Gummel fluxes of one face from log densities, branch
+// free.  With s = sign(a) and the upwind node u (left for a >= 0):
+//   F = s C_u n_u (1 - exp(s (l_R - l_L) - |a|)),
+// C_u = (D/h) B(-|a|) -- for the ions the precomputed cl (a >= 0) or cr.
+// The electron and energy fluxes share a = -mue E h / De and B(-|a|)
+// (mut/Dt = mue/De, ptcl_lib.F90:142-143).
+__device__ __forceinline__ void sg3(float ai, float cl, float cr, float ae, float g, float niL, float niR, float liL,
+                                    float liR, float neL, float neR, float leL, float leR, float ntL, float ntR,
+                                    float ltL, float ltR, float &fi, float &fe, float &ft) {
+    const bool ui = ai >= 0.0f;
+    const float si = ui ? 1.0f : -1.0f;
+    fi = si * (ui ? cl * niL : cr * niR) * (-expm1f(si * (liR - liL) - fabsf(ai)));
+    const float x = fabsf(ae);
+    const float b = x < 1e-3f ? 1.0f + 0.5f * x + x * x * (1.0f / 12.0f) : x / (-expm1f(-x));
+    const bool ue = ae >= 0.0f;
+    const float gb = (ue ? g : -g) * b;
+    const float se = ue ? 1.0f : -1.0f;
+    fe = gb * (ue ? neL : neR) * (-expm1f(se * (leR - leL) - x));
+    ft = (5.0f / 3.0f) * gb * (ue ? ntL : ntR) * (-expm1f(se * (ltR - ltL) - x));
 }
 
 // -B'(x), the coefficient of dFdPh: dF/dv = -B'(-a) n_L - B'(a) n_R
@@ -63,29 +78,29 @@ __device__ __forceinline__ float mbprime(float x) {
 
 struct FaceMixArgs {
     PhysParams pp;
+    PhysF f;
     MeshDev m;
+    MeshF mf;
     const double *ph;
     double *fx_e, *fy_e;     // FP64 face fields (the assembly's Laplacian needs them)
-    float *f[10];            // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
+    float *f32[10];          // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
 };
 
 // Face data while phi is frozen: E (FP64 and FP32), the ion flux
 // coefficients cl = (Di/h) B(-a), cr = (Di/h) B(a) and the ion dFdPh
-// coefficients -B'(-a), -B'(a) (0 where |v| < 1e-12, as dFdPh).
-__device__ __forceinline__ void ion_face32(const PhysParams &pp, double E64, double h, float *out) {
-    const float E = (float)E64, hf = (float)h;
-    const float a = (float)(pp.mui * E64 * h / pp.Di);
-    const float d = (float)(pp.Di / h);
+// coefficients -B'(-a), -B'(a) (0 where |mui E| < 1e-12, as dFdPh).
+__device__ __forceinline__ void ion_face32(const PhysF &pf, float E, float h, float ih, float *out) {
+    const float a = pf.mui_Di * E * h;
+    const float d = pf.Di * ih;
     out[0] = E;
     out[1] = d * bern(-a);
     out[2] = d * bern(a);
-    if (fabs(pp.mui * E64) < 1e-12) {
+    if (fabsf(pf.mui * E) < 1e-12f) {
         out[3] = out[4] = 0.0f;
     } else {
         out[3] = mbprime(-a);
         out[4] = mbprime(a);
     }
-    (void)hf;
 }
 
 __global__ void k_faces_mix(const FaceMixArgs a) {
@@ -95,16 +110,16 @@ __global__ void k_faces_mix(const FaceMixArgs a) {
     const size_t o = (size_t)gj * P + gi;
     float v[5];
     if (gj >= 1) {
-        double E = -(a.ph[o + 1] - a.ph[o]) / a.m.dx[gi];
+        double E = -(a.ph[o + 1] - a.ph[o]) * a.m.inv_dx[gi];
         a.fx_e[o] = E;
-        ion_face32(a.pp, E, a.m.dx[gi], v);
-        for (int k = 0; k < 5; k++) a.f[k][o] = v[k];
+        ion_face32(a.f, (float)E, a.mf.dx[gi], a.mf.inv_dx[gi], v);
+        for (int k = 0; k < 5; k++) a.f32[k][o] = v[k];
     }
     if (gi >= 1) {
-        double E = -(a.ph[o + P] - a.ph[o]) / a.m.dy[gj];
+        double E = -(a.ph[o + P] - a.ph[o]) * a.m.inv_dy[gj];
         a.fy_e[o] = E;
-        ion_face32(a.pp, E, a.m.dy[gj], v);
-        for (int k = 0; k < 5; k++) a.f[5 + k][o] = v[k];
+        ion_face32(a.f, (float)E, a.mf.dy[gj], a.mf.inv_dy[gj], v);
+        for (int k = 0; k < 5; k++) a.f32[5 + k][o] = v[k];
     }
 }
 
@@ -116,6 +131,11 @@ __global__ void k_log32(const double *n, const double *den, double scale, float 
         double v = den ? scale * n[i] / den[i] : n[i];
         l[i] = logf(fmaxf((float)v, 1e-30f));
     }
+}
+
+__global__ void k_d2f(const double *in, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
 }
 
 // circ_step ghosts in mixed mode: phi ghost and both face fields of the row
@@ -142,9 +162,12 @@ __global__ void k_circ_ghost_mix(double *ph, const int8_t *tx, const double *r, 
 
 struct StageMixArgs {
     PhysParams pp;
+    PhysF f;
     MeshDev m;
+    MeshF mf;
     const float *tab;               // FP32 table, FS_TAB_STRIDE floats per node
     const float *lin[FS_MAX_SPECIES];
+    const float *lbase[FS_MAX_SPECIES];     // FP32 log companions of the base state
     const double *nbase[FS_MAX_SPECIES];
     double *nout[FS_MAX_SPECIES];   // FP64 output (stages 4 and 5), else null
     float *lout[FS_MAX_SPECIES];
@@ -162,9 +185,9 @@ struct StageMixArgs {
 };
 
 __device__ __forceinline__ void tab32(const StageMixArgs &a, float lneps, int &k, float &w) {
-    float u = (lneps - (float)a.pp.lemin) * (float)a.pp.inv_h;
+    float u = (lneps - a.f.lemin) * a.f.inv_h;
     if (!(u >= 0.0f)) u = 0.0f;
-    if (u > (float)(a.pp.ntab - 1)) u = (float)(a.pp.ntab - 1);
+    if (u > a.f.ntab_m1) u = a.f.ntab_m1;
     int i = (int)u;
     if (i > a.pp.ntab - 2) i = a.pp.ntab - 2;
     k = i;
@@ -181,7 +204,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 template <int NS>
-__global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
+__global__ void __launch_bounds__(NT, 4) k_stage_mix(const StageMixArgs a) {
     __shared__ float s_l[NS][HY][HX];
     __shared__ float s_n[NS][HY][HX];
     __shared__ float s_te[HY][HX], s_mue[HY][HX], s_de[HY][HX];
@@ -198,10 +221,11 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
     const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
     const int tid = threadIdx.x;
     const int gx0 = blockIdx.x * BX + 1, gy0 = blockIdx.y * BY + 1;
-    const float ln_ph0 = (float)log(pp.ph0);
-    const float mui = (float)pp.mui, vi = (float)pp.vi, gam = (float)pp.gam;
-    const float mui_Di = (float)(pp.mui / pp.Di);
-    const float ve_c = (float)pp.ve_coef, t0_x0 = (float)(pp.t0 / pp.x0);
+    const PhysF &pf = a.f;
+    const float ln_ph0 = pf.ln_ph0;
+    const float mui = pf.mui, vi = pf.vi, gam = pf.gam;
+    const float mui_Di = pf.mui_Di;
+    const float ve_c = pf.ve_c, t0_x0 = pf.t0_x0;
     unsigned int st = 0;
 
     // tile + halo: log densities, densities, mean energy and its table coefficients
@@ -263,16 +287,15 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
             ft = -(aa * mut * E * nt) + sgn * ((1.0f / 3.0f) * ve * nt) - gam * te * fi;
             if (NS == 4) fm = sgn * (0.5f * vi * s_n[3][ly][lc]);
         } else {
-            float dh = (float)a.m.dx[gi], idh = (float)a.m.inv_dx[gi];
+            float dh = a.mf.dx[gi], idh = a.mf.inv_dx[gi];
             float mue = 0.5f * (s_mue[ly][lx] + s_mue[ly][lx + 1]);
             float De = 0.5f * (s_de[ly][lx] + s_de[ly][lx + 1]);
             float ai = E * dh * mui_Di;
-            fi = ai >= 0.0f ? a.fx_cl[of] * s_n[0][ly][lx] * (-expm1f(s_l[0][ly][lx + 1] - s_l[0][ly][lx] - ai))
-                            : a.fx_cr[of] * s_n[0][ly][lx + 1] * expm1f(s_l[0][ly][lx] - s_l[0][ly][lx + 1] + ai);
             float ae = -mue * E * dh / De, g = De * idh;
-            fe = sg_log(g, ae, s_n[1][ly][lx], s_n[1][ly][lx + 1], s_l[1][ly][lx], s_l[1][ly][lx + 1]);
-            ft = sg_log((5.0f / 3.0f) * g, ae, s_n[2][ly][lx], s_n[2][ly][lx + 1], s_l[2][ly][lx], s_l[2][ly][lx + 1]);
-            if (NS == 4) fm = -(float)pp.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
+            sg3(ai, a.fx_cl[of], a.fx_cr[of], ae, g, s_n[0][ly][lx], s_n[0][ly][lx + 1], s_l[0][ly][lx],
+                s_l[0][ly][lx + 1], s_n[1][ly][lx], s_n[1][ly][lx + 1], s_l[1][ly][lx], s_l[1][ly][lx + 1],
+                s_n[2][ly][lx], s_n[2][ly][lx + 1], s_l[2][ly][lx], s_l[2][ly][lx + 1], fi, fe, ft);
+            if (NS == 4) fm = -pf.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
             if (a.stage == 5) {
                 if (gi == 1 && a.m.dr_a[gj] != 0.0) a.rows[gj] = a.m.dr_a[gj] * (double)(fi - fe);
                 if (gi == nx - 1 && a.m.dr_c[gj] != 0.0) a.rows[(ny + 2) + gj] = a.m.dr_c[gj] * (double)(fi - fe);
@@ -313,16 +336,15 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
             ft = -(aa * mut * E * nt) + (1.0f / 3.0f) * ve * nt - gam * te * fix;
             if (NS == 4) fm = 0.5f * vi * s_n[3][lc][lx];
         } else {
-            float dh = (float)a.m.dy[gj], idh = (float)a.m.inv_dy[gj];
+            float dh = a.mf.dy[gj], idh = a.mf.inv_dy[gj];
             float mue = 0.5f * (s_mue[ly][lx] + s_mue[ly + 1][lx]);
             float De = 0.5f * (s_de[ly][lx] + s_de[ly + 1][lx]);
             float ai = E * dh * mui_Di;
-            fi = ai >= 0.0f ? a.fy_cl[of] * s_n[0][ly][lx] * (-expm1f(s_l[0][ly + 1][lx] - s_l[0][ly][lx] - ai))
-                            : a.fy_cr[of] * s_n[0][ly + 1][lx] * expm1f(s_l[0][ly][lx] - s_l[0][ly + 1][lx] + ai);
             float ae = -mue * E * dh / De, g = De * idh;
-            fe = sg_log(g, ae, s_n[1][ly][lx], s_n[1][ly + 1][lx], s_l[1][ly][lx], s_l[1][ly + 1][lx]);
-            ft = sg_log((5.0f / 3.0f) * g, ae, s_n[2][ly][lx], s_n[2][ly + 1][lx], s_l[2][ly][lx], s_l[2][ly + 1][lx]);
-            if (NS == 4) fm = -(float)pp.Dm * (s_n[3][ly + 1][lx] - s_n[3][ly][lx]) * idh;
+            sg3(ai, a.fy_cl[of], a.fy_cr[of], ae, g, s_n[0][ly][lx], s_n[0][ly + 1][lx], s_l[0][ly][lx],
+                s_l[0][ly + 1][lx], s_n[1][ly][lx], s_n[1][ly + 1][lx], s_l[1][ly][lx], s_l[1][ly + 1][lx],
+                s_n[2][ly][lx], s_n[2][ly + 1][lx], s_l[2][ly][lx], s_l[2][ly + 1][lx], fi, fe, ft);
+            if (NS == 4) fm = -pf.Dm * (s_n[3][ly + 1][lx] - s_n[3][ly][lx]) * idh;
         }
         s_fy[0][r][c] = fi; s_fy[1][r][c] = fe; s_fy[2][r][c] = ft;
         if (NS == 4) s_fy[3][r][c] = fm;
@@ -346,10 +368,10 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
         const float w = s_w[ly][lx];
         const float k_ir = tv32(a.tab, kk, w, 2), k_ex = tv32(a.tab, kk, w, 3);
         const float nu = tv32(a.tab, kk, w, 4), beta = tv32(a.tab, kk, w, 5);
-        const float idlx = (float)a.m.inv_dlx[gi - 1], idly = (float)a.m.inv_dly[gj - 1];
+        const float idlx = a.mf.inv_dlx[gi - 1], idly = a.mf.inv_dly[gj - 1];
         float dfdx[NS], dfdy[NS];
         if (pp.cyl) {
-            const float r0 = (float)a.m.r[gj], rp = (float)(a.m.r[gj + 1] + a.m.r[gj]), rm = (float)(a.m.r[gj] + a.m.r[gj - 1]);
+            const float r0 = a.mf.r[gj], rp = a.mf.r[gj + 1] + r0, rm = r0 + a.mf.r[gj - 1];
 #pragma unroll
             for (int s = 0; s < NS; s++) {
                 dfdx[s] = (s_fx[s][ly][lx + 1] - s_fx[s][ly][lx]) * idlx;
@@ -366,31 +388,37 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
         const float exa = (s_ex[ly][lx] + s_ex[ly][lx + 1]) * 0.5f;
         const float fey = (s_fy[1][ly + 1][lx] + s_fy[1][ly][lx]) * 0.5f;
         const float eya = (s_ey[ly][lx] + s_ey[ly + 1][lx]) * 0.5f;
-        const float ninf = (float)pp.ninf;
+        const float ninf = pf.ninf;
         float term_sie = k_ir * ninf * ne - beta * ni * ne;
         float k_si = 0.0f, k_sc = 0.0f;
         if (NS == 4) {
             k_sc = tv32(a.tab, kk, w, 6);
             k_si = tv32(a.tab, kk, w, 7);
-            term_sie = term_sie + k_si * nm * ne + (float)pp.k_mp * (nm * nm);
+            term_sie = term_sie + k_si * nm * ne + pf.k_mp * (nm * nm);
         }
         const float term_st1 = -(fex * exa + fey * eya);
-        const float term_st2 = -(ne * nu * (float)(pp.me / pp.mi) * (te / 1.5f - (float)(pp.tg * pp.kb / pp.e / pp.ph0)));
-        const float term_st3 = -((float)pp.h_ir * k_ir * ninf * ne) - (float)pp.h_si * k_si * nm * ne
-                             - (float)pp.h_ex * k_ex * ninf * ne;
+        const float term_st2 = -(ne * nu * pf.me_mi * (te / 1.5f - pf.tg_term));
+        const float term_st3 = -(pf.h_ir * k_ir * ninf * ne) - pf.h_si * k_si * nm * ne
+                             - pf.h_ex * k_ex * ninf * ne;
         float kv[NS];
         kv[0] = -dfdx[0] - dfdy[0] + term_sie;
         kv[1] = -dfdx[1] - dfdy[1] + term_sie;
         kv[2] = -dfdx[2] - dfdy[2] + term_st1 + term_st2 + term_st3;
         if (NS == 4) {
-            float term_sm = k_ex * ninf * ne - k_si * nm * ne - k_sc * nm * ne - (float)pp.k_r * nm * ne
-                          - 2.0f * (float)pp.k_mp * (nm * nm) - (float)pp.k_2q * ninf * nm
-                          - (float)(pp.k_3q * pp.ninf * pp.ninf) * nm;
+            float term_sm = k_ex * ninf * ne - k_si * nm * ne - k_sc * nm * ne - pf.k_r * nm * ne
+                          - 2.0f * pf.k_mp * (nm * nm) - pf.k_2q * ninf * nm
+                          - pf.k_3q_ninf2 * nm;
             kv[3] = -dfdx[3] - dfdy[3] + term_sm;
         }
         const double dt = a.ctrl->dt;
+        const float dtf = (float)dt;
         const int stg = a.stage;
-        double vn[NS];
+        float vf[NS];
+        float lb[NS];
+        if (stg <= 3) {   // intermediate stage states: FP32 from the FP32 log base
+#pragma unroll
+            for (int s = 0; s < NS; s++) lb[s] = a.lbase[s][o];
+        }
 #pragma unroll
         for (int s = 0; s < NS; s++) {
             if (isnan(kv[s])) st |= FS_ST_NAN;
@@ -401,28 +429,35 @@ __global__ void __launch_bounds__(NT, 3) k_stage_mix(const StageMixArgs a) {
             else if (stg == 3) comb = (a.k1[s][o] + kv[s] * 3.0f) * 0.125f;
             else if (stg == 4) comb = (a.k1[s][o] - a.k3[s][o] * 3.0f + kv[s] * 4.0f) * 0.5f;
             else comb = (a.k1[s][o] + a.k4[s][o] * 4.0f + kv[s]) * (1.0f / 6.0f);
+            if (stg <= 3) {
+                const float n3 = expf(s == 2 ? lb[1] + lb[2] - ln_ph0 : lb[s]);
+                vf[s] = fmaxf(n3 + dtf * comb, pf.nmin[s]);
+                continue;
+            }
+            // stages 4 and 5 produce the states the step keeps: FP64 accumulation
             const double n3 = a.nbase[s][o];
-            const double v = fmax(n3 + dt * (double)comb, pp.nmin[s]);   // FP64 accumulation
-            vn[s] = v;
-            if (a.nout[s]) a.nout[s][o] = v;
+            const double v = fmax(n3 + dt * (double)comb, pp.nmin[s]);
+            vf[s] = (float)v;
+            a.nout[s][o] = v;
             if (stg == 5) {
                 const double k1 = a.k1[s][o], k3 = a.k3[s][o], k4 = a.k4[s][o];
-                double err = fabs(dt * (k1 * (2.0 / 30.0) - k3 * (3.0 / 10.0) + k4 * (4.0 / 15.0)
-                                        - (double)kv[s] * (1.0 / 30.0)));
-                double qq = err / (pp.abs_tol + pp.rel_tol * fabs(n3));
-                qerr[s] = qq * qq;
+                // the Merson combination cancels to O(dt^4): formed in FP64
+                const float err = (float)fabs(dt * (k1 * (2.0 / 30.0) - k3 * (3.0 / 10.0) + k4 * (4.0 / 15.0)
+                                                    - (double)kv[s] * (1.0 / 30.0)));
+                const float qq = err / (pf.abs_tol + pf.rel_tol * fabsf((float)n3));
+                qerr[s] = (double)(qq * qq);
             }
         }
 #pragma unroll
         for (int s = 0; s < NS; s++)
-            a.lout[s][o] = s == 2 ? logf((float)(vn[2] * pp.ph0 / vn[1])) : logf((float)vn[s]);
+            a.lout[s][o] = s == 2 ? logf(vf[2] * pf.ph0 / vf[1]) : logf(vf[s]);
         if (stg == 5) {
             const int ty = a.m.ty[(gj - 1) * nx + gi - 1], tx = a.m.tx[(gj - 1) * nx + gi - 1];
             float mue2;
             if (ty == 0 || ty < 0) mue2 = 0.5f * (s_mue[hy][hx] + s_mue[hy + 1][hx]);
             else if (ty == 1 && (tx == 0 || tx < 0)) mue2 = 0.5f * (s_mue[hy][hx] + s_mue[hy][hx + 1]);
             else mue2 = s_mue[hy][hx];
-            tm = 1.0 / ((double)mue2 * ne + pp.mui * ni);
+            tm = (double)(1.0f / (mue2 * ne + mui * ni));
         }
     }
     if (st) atomicOr(&a.ctrl->status, st);
@@ -478,7 +513,35 @@ int fs_mixed_alloc(fs_ctx *c, const std::vector<double> &rows) {
         }
     e = cudaMalloc(&c->d_tab32, t.size() * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpy(c->d_tab32, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice);
-    return fs_cuda_check(c, e, "mixed table");
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "mixed table");
+
+    // FP32 constants
+    const PhysParams &p = c->pp;
+    PhysF &f = c->pf;
+    f.ph0 = (float)p.ph0; f.ln_ph0 = (float)std::log(p.ph0);
+    f.mui = (float)p.mui; f.vi = (float)p.vi; f.gam = (float)p.gam; f.Di = (float)p.Di;
+    f.mui_Di = (float)(p.mui / p.Di);
+    f.ve_c = (float)p.ve_coef; f.t0_x0 = (float)(p.t0 / p.x0);
+    f.Dm = (float)p.Dm; f.ninf = (float)p.ninf; f.me_mi = (float)(p.me / p.mi);
+    f.tg_term = (float)(p.tg * p.kb / p.e / p.ph0);
+    f.h_ir = (float)p.h_ir; f.h_ex = (float)p.h_ex; f.h_si = (float)p.h_si;
+    f.k_mp = (float)p.k_mp; f.k_r = (float)p.k_r; f.k_2q = (float)p.k_2q;
+    f.k_3q_ninf2 = (float)(p.k_3q * p.ninf * p.ninf);
+    f.lemin = (float)p.lemin; f.inv_h = (float)p.inv_h; f.ntab_m1 = (float)(p.ntab - 1);
+    f.abs_tol = (float)p.abs_tol; f.rel_tol = (float)p.rel_tol;
+    for (int q = 0; q < FS_MAX_SPECIES; q++) f.nmin[q] = (float)p.nmin[q];
+    // FP32 mesh: the FP64 blob converted element by element, same offsets
+    const size_t nblob = (size_t)(c->mesh.dr_c - c->d_mesh_blob) + c->ny + 2;
+    e = cudaMalloc(&c->d_meshf, nblob * sizeof(float));
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 mesh)");
+    c->launches++;
+    k_d2f<<<64, 256, 0, c->stream>>>(c->d_mesh_blob, c->d_meshf, nblob);
+    auto fp = [&](const double *d) { return (const float *)(c->d_meshf + (d - c->d_mesh_blob)); };
+    MeshF &m = c->meshf;
+    m.dx = fp(c->mesh.dx); m.dy = fp(c->mesh.dy); m.inv_dx = fp(c->mesh.inv_dx); m.inv_dy = fp(c->mesh.inv_dy);
+    m.dlx = fp(c->mesh.dlx); m.dly = fp(c->mesh.dly); m.inv_dlx = fp(c->mesh.inv_dlx);
+    m.inv_dly = fp(c->mesh.inv_dly); m.r = fp(c->mesh.r);
+    return fs_cuda_check(c, cudaGetLastError(), "FP32 mesh");
 }
 
 void fs_mixed_free(fs_ctx *c) {
@@ -488,6 +551,7 @@ void fs_mixed_free(fs_ctx *c) {
     }
     for (int f = 0; f < 10; f++) cudaFree(c->f32[f]);
     cudaFree(c->d_tab32);
+    cudaFree(c->d_meshf);
 }
 
 int fs_mixed_sync_logs(fs_ctx *c) {
@@ -504,11 +568,13 @@ void fs_faces_update_mixed(fs_ctx *c) {
     if (c->faces_valid) return;
     FaceMixArgs f;
     f.pp = c->pp;
+    f.f = c->pf;
     f.m = c->mesh;
+    f.mf = c->meshf;
     f.ph = c->ph;
     f.fx_e = c->fx_e;
     f.fy_e = c->fy_e;
-    for (int k = 0; k < 10; k++) f.f[k] = c->f32[k];
+    for (int k = 0; k < 10; k++) f.f32[k] = c->f32[k];
     dim3 b(32, 8), g((c->nx + 1 + 31) / 32, (c->ny + 1 + 7) / 8);
     fs_prof_begin(c, PROF_OTHER);
     k_faces_mix<<<g, b, 0, c->stream>>>(f);
@@ -535,7 +601,9 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
         StageMixArgs a;
         memset(&a, 0, sizeof(a));
         a.pp = c->pp;
+        a.f = c->pf;
         a.m = c->mesh;
+        a.mf = c->meshf;
         a.tab = c->d_tab32;
         a.ph = c->ph;
         a.fx_e = c->f32[0]; a.fx_cl = c->f32[1]; a.fx_cr = c->f32[2];
@@ -551,6 +619,7 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
             for (int s = 0; s < ns; s++) {
                 a.lin[s] = c->lbuf[s][ins[stg - 1]];
                 a.nbase[s] = c->sp[s].buf[L3];
+                a.lbase[s] = c->lbuf[s][L3];
                 a.lout[s] = c->lbuf[s][outs[stg - 1]];
                 a.nout[s] = stg >= 4 ? c->sp[s].buf[outs[stg - 1]] : nullptr;
                 a.k1[s] = c->k32[s][0];
