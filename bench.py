@@ -186,6 +186,55 @@ def run_reference(args):
     return 0
 
 
+def measure_variant(cfg, mesh, st0, args, barrier):
+    """Device-resident and end-to-end steps/s of one solver variant on the
+    same workload (fresh context, same warm-up), for the comparison keys."""
+    import torch
+    from fluidsim_gb300 import api
+    d = api.Discharge(cfg, mesh, st0)
+    stream = torch.cuda.ExternalStream(d.stream_handle())
+    d.run(2 + args.warmup)
+    warm_state = d.download(nlev=3)
+    warm_t, warm_dt, warm_ts = d.t, d.dt, d.ts
+    w = d.stats()
+    l0 = d.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s = d.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = d.launch_count() - l0
+    pinned = {}
+    for key in ("ni", "ne", "nt", "ph"):
+        t = torch.empty(warm_state[key].shape[::-1], dtype=torch.float64, pin_memory=True)
+        v = t.numpy().T
+        v[...] = warm_state[key]
+        pinned[key] = v
+    d.set_time(warm_t, warm_dt)
+    d.ts = warm_ts
+    barrier()
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    d.upload(pinned)
+    for _ in range(args.steps):
+        d.step()
+    fin = d.download(nlev=3)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3)
+    d.close()
+    return {"value": args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+            "e2e": args.steps / (ms_e2e * 1e-3),
+            "cg_iters_per_step": (s["lapl_iters"] - w["lapl_iters"]) / args.steps,
+            "rk_attempts": s["attempts"] - w["attempts"], "gpu_launches": launches,
+            "h2d_bytes_per_step": sum(a.nbytes for a in pinned.values()) / args.steps,
+            "d2h_bytes_per_step": 3 * sum(a.nbytes for a in pinned.values()) / args.steps}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -309,6 +358,15 @@ def run_gpu(args):
                "sample": "%d main-loop steps of the %dx%d workload from the warmed-up state "
                          "(C++ oracle, OpenMP, BiCGStab+ILU(0))" % (steps_c, args.n, args.n)}
 
+    # ---- the mixed-precision solver on the same workload ---------------------
+    variants = {}
+    if args.precision == "fp64" and not args.no_variants:
+        cfgm = workload(args.n, args.dt, precision="mixed")
+        vm = measure_variant(cfgm, mesh, st0, args, barrier)
+        vm["speedup_vs_plain"] = vm["value"] / (args.steps / (ms * 1e-3))
+        vm["e2e_speedup_vs_plain"] = vm["e2e"] / (args.steps / (ms_e2e * 1e-3))
+        variants["mixed"] = vm
+
     if rank == 0:
         total_ms = {kk: v[0] for kk, v in breakdown.items()}
         line = {
@@ -330,6 +388,7 @@ def run_gpu(args):
                          "stage_ms": stage_ms},
             "kernel_ms_per_step": {kk: v / args.steps for kk, v in total_ms.items()},
             "cpu_baseline": cpu,
+            "variants": variants,
             "clocks": clocks,
             "gpu_launches": launches,
         }
@@ -352,6 +411,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the mixed-precision comparison run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
