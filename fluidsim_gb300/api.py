@@ -53,6 +53,17 @@ def load_library():
     lib.fs_profile_read.restype = C.c_int
     lib.fs_launch_count.argtypes = [C.c_void_p]
     lib.fs_launch_count.restype = C.c_int64
+    fp, i32, vp = C.POINTER(C.c_float), C.c_int32, C.c_void_p
+    for name, args in (("fs_lpc_init", [vp, i32, i32, i32, C.c_uint64]),
+                       ("fs_lpc_harvest", [vp, i32, C.POINTER(i32)]),
+                       ("fs_lpc_train", [vp, i32, i32, C.c_float, C.c_uint64, fp]),
+                       ("fs_lpc_use", [vp, i32]),
+                       ("fs_lpc_weights", [vp, fp, C.c_int64, i32]),
+                       ("fs_lpc_grad", [vp, fp, fp, fp, i32, fp, fp, fp]),
+                       ("fs_lpc_info", [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                                        C.POINTER(C.c_int64), C.POINTER(i32)])):
+        getattr(lib, name).argtypes = args
+        getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
 
@@ -243,3 +254,52 @@ class Discharge(Handle):
         v = C.c_double()
         self.check(self._lib.fs_max_ne(self.ctx, C.byref(v)))
         return v.value
+
+    # -- learned Poisson preconditioner (mixed contexts) -----------------------
+    def lpc_init(self, level=3, max_batch=16, max_samples=512, seed=0):
+        self.check(self._lib.fs_lpc_init(self.ctx, level, max_batch, max_samples, seed))
+
+    def lpc_info(self):
+        h, w, n, off = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        npar = C.c_int64()
+        self.check(self._lib.fs_lpc_info(self.ctx, C.byref(h), C.byref(w), C.byref(n), C.byref(npar),
+                                         C.byref(off)))
+        return dict(h=h.value, w=w.value, samples=n.value, nparam=npar.value, off=off.value)
+
+    def lpc_harvest(self, per_solve=4):
+        a = C.c_int32()
+        self.check(self._lib.fs_lpc_harvest(self.ctx, per_solve, C.byref(a)))
+        return a.value
+
+    def lpc_train(self, iters, batch, lr=1e-3, seed=0):
+        hist = np.zeros(max(iters, 1), dtype=np.float32)
+        self.check(self._lib.fs_lpc_train(self.ctx, iters, batch, lr, seed,
+                                          hist.ctypes.data_as(C.POINTER(C.c_float))))
+        return hist[:iters]
+
+    def lpc_use(self, on=True):
+        self.check(self._lib.fs_lpc_use(self.ctx, 1 if on else 0))
+
+    def lpc_weights(self, w=None):
+        """Get the FP32 parameters, or set them when w is given."""
+        n = self.lpc_info()["nparam"]
+        if w is None:
+            out = np.zeros(n, dtype=np.float32)
+            self.check(self._lib.fs_lpc_weights(self.ctx, out.ctypes.data_as(C.POINTER(C.c_float)), n, 0))
+            return out
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self.check(self._lib.fs_lpc_weights(self.ctx, w.ctypes.data_as(C.POINTER(C.c_float)), n, 1))
+
+    def lpc_grad(self, feat, tgt, mask):
+        """Loss, gradient and predictions of the network for feat [B][h][w][4]."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        tgt = np.ascontiguousarray(tgt, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.float32)
+        n = self.lpc_info()["nparam"]
+        g = np.zeros(n, dtype=np.float32)
+        pred = np.zeros(tgt.shape, dtype=np.float32)
+        loss = C.c_float()
+        f = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self.check(self._lib.fs_lpc_grad(self.ctx, f(feat), f(tgt), f(mask), feat.shape[0], f(g),
+                                         C.byref(loss), f(pred)))
+        return loss.value, g, pred

@@ -172,6 +172,7 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
 
 void free_ctx(fs_ctx *c) {
     if (!c) return;
+    fs_lpc_free_impl(c);
     fs_lapl_free(c);
     if (c->mixed) {
         fs_lapl_free_mixed(c);
@@ -640,3 +641,74 @@ extern "C" int fs_max_ne_noalloc(fs_ctx *c, double *out) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ learned Poisson preconditioner
+#include "fs_lpc.cuh"
+
+int fs_lpc_init(fs_ctx *c, int32_t level, int32_t max_batch, int32_t max_samples, uint64_t seed) {
+    if (!c) return FS_ERR_INVALID;
+    return fs_lpc_init_impl(c, level, max_batch, max_samples, seed);
+}
+
+int fs_lpc_harvest(fs_ctx *c, int32_t per_solve, int32_t *added) {
+    if (!c) return FS_ERR_INVALID;
+    int a = 0;
+    int rc = fs_lpc_harvest_impl(c, per_solve, &a);
+    if (added) *added = a;
+    return rc;
+}
+
+int fs_lpc_train(fs_ctx *c, int32_t iters, int32_t batch, float lr, uint64_t seed, float *loss_hist) {
+    if (!c) return FS_ERR_INVALID;
+    if (iters < 0) return fs_set_error(c, FS_ERR_INVALID, "iters must be >= 0");
+    return fs_lpc_train_impl(c, iters, batch, lr, seed, loss_hist);
+}
+
+int fs_lpc_use(fs_ctx *c, int32_t on) {
+    if (!c) return FS_ERR_INVALID;
+    if (on && !c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    if ((on != 0) != (c->lpc_on != 0) && c->cgm_graph_built) {   // the CG graph bakes the choice in
+        cudaStreamSynchronize(c->stream);
+        cudaGraphExecDestroy(c->cgm_exec);
+        cudaGraphDestroy(c->cgm_graph);
+        c->cgm_graph_built = 0;
+    }
+    c->lpc_on = on != 0;
+    return FS_OK;
+}
+
+int fs_lpc_weights(fs_ctx *c, float *w, int64_t n, int32_t to_device) {
+    if (!c || !w) return FS_ERR_INVALID;
+    if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    LpcState *L = c->lpc;
+    if ((size_t)n != L->net.nparam) return fs_set_error(c, FS_ERR_INVALID, "expected %zu parameters", L->net.nparam);
+    cudaError_t e;
+    if (to_device) {
+        e = cudaMemcpyAsync(L->w, w, n * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(L->m, 0, n * sizeof(float), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(L->v, 0, n * sizeof(float), c->stream);
+        L->adam_t = 0;
+        if (e == cudaSuccess) lpc_refresh(L, c->stream);
+    } else {
+        e = cudaMemcpyAsync(w, L->w, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "learned preconditioner weights");
+}
+
+int fs_lpc_grad(fs_ctx *c, const float *feat, const float *tgt, const float *mask, int32_t batch, float *grad,
+                float *loss, float *pred) {
+    if (!c || !feat || !tgt || !mask) return FS_ERR_INVALID;
+    return fs_lpc_grad_impl(c, feat, tgt, mask, batch, grad, loss, pred);
+}
+
+int fs_lpc_info(fs_ctx *c, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off) {
+    if (!c) return FS_ERR_INVALID;
+    if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    if (h) *h = c->lpc->Hn;
+    if (w) *w = c->lpc->Wn;
+    if (nsamples) *nsamples = c->lpc->nsamp < c->lpc->Nmax ? c->lpc->nsamp : c->lpc->Nmax;
+    if (nparam) *nparam = (int64_t)c->lpc->net.nparam;
+    if (off) *off = c->h_ctrl->lpc_off;
+    return FS_OK;
+}

@@ -83,6 +83,9 @@ struct Ctrl {
     int cg_done, cg_iters, cg_fail, pad2;
     double r0in2;              // mixed solver: inner residual norm^2 at the last refinement
     int inner_it, refine;      // mixed solver: inner iterations since it, refinement due
+    double rr_prev;            // mixed solver: previous inner residual norm^2
+    double lpc_s, lpc_mcm;     // learned correction: residual scale, mean level diagonal
+    int lpc_off, pad3;         // learned correction switched off for this solve (stall)
     unsigned int counter[8];   // last-block-done counters of grid reductions
     double host_result;        // host-side landing slot of single-value results
 };
@@ -189,6 +192,14 @@ struct fs_ctx {
     float *d_tab32;
     MGLevelF mgf[FS_MG_MAX_LEVELS];
     float *p32, *q32;            // FP32 inner CG vectors
+    // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
+    struct LpcState *lpc;
+    int lpc_on, lpc_level;
+    float *lpc_op;               // [Hn][Wn][3] operator features of the level (per solve)
+    float *lpc_rr;               // [Hn][Wn] restricted residual
+    double *lpc_rhs64;           // fine right-hand side of a harvest solve
+    float *lpc_snap;             // harvested residual snapshots (fine FP32 fields)
+    int lpc_snap_max;
     cudaGraph_t cgm_graph;
     cudaGraphExec_t cgm_exec;
     int cgm_graph_built;
@@ -225,6 +236,13 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
 // mixed-precision Poisson (fs_lapl_mixed.cu)
 int fs_lapl_alloc_mixed(fs_ctx *c);
 void fs_lapl_free_mixed(fs_ctx *c);
+// learned preconditioner (fs_lapl_mixed.cu, network in fs_lpc.cu)
+int fs_lpc_init_impl(fs_ctx *c, int level, int max_batch, int max_samples, uint64_t seed);
+void fs_lpc_free_impl(fs_ctx *c);
+int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added);
+int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, float *loss_hist);
+int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float *mask, int batch, float *grad,
+                     float *loss, float *pred);
 // misc device helpers (fs_api.cu)
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
 int fs_sync_ctrl(fs_ctx *c);

@@ -17,10 +17,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
+#include "fs_lpc.cuh"
 #include "fs_mg.cuh"
 
 #define ABX 32
@@ -346,6 +349,7 @@ struct CgmArgs {
     Ctrl *ctrl;
     double rtol, inner_tol2;
     int maxit, inner_max;
+    int lpc;                             // the learned correction is part of the preconditioner
     int use_cond;
     cudaGraphConditionalHandle cond;
 };
@@ -422,6 +426,8 @@ __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
         c->refine = 0;
         c->rz = 0.0;
         c->alpha = 0.0;
+        c->rr_prev = sw;
+        c->lpc_off = 0;
     }
 }
 
@@ -534,6 +540,9 @@ __global__ void __launch_bounds__(256) k_cgm_xr(const CgmArgs a) {
     double out;
     if (grid_sum<256>((double)v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
+        // the learned correction stalls the iteration: plain MG-PCG for the rest of the solve
+        if (a.lpc && c->inner_it > 0 && out > 0.25 * c->rr_prev) c->lpc_off = 1;
+        c->rr_prev = out;
         c->cg_iters += 1;
         c->inner_it += 1;
         c->rnorm2 = out;   // inner recurrence residual (diagnostic)
@@ -572,10 +581,153 @@ __global__ void __launch_bounds__(256) k_cgm_refine(const CgmArgs a) {
         c->relres = c->bnorm2 > 0.0 ? sqrt(sv / c->bnorm2) : 0.0;
         c->inner_it = 0;
         c->refine = 0;
+        c->rr_prev = sw;
         if (c->relres <= a.rtol) c->cg_done = 1;
         else if (isnan(sv) || c->cg_iters >= a.maxit || !(c->relres < prev)) c->cg_fail = 1;
         if (a.use_cond && (c->cg_done || c->cg_fail)) cudaGraphSetConditional(a.cond, 0u);
     }
+}
+
+// ------------------------------------------- learned correction (inference)
+// The network works on the grid of MG level lev (aggregates of 2^lev x 2^lev
+// fine nodes; NN cell (I, J), 1-based, covers fine i in (I-1) 2^lev + 1 ..
+// I 2^lev).  Inputs per cell: the aggregated residual R (r - M z) after the
+// V-cycle, scaled by its RMS s, and the level operator's ce/mc, cn/mc,
+// extra/mc.  Output y: the aggregate mean of the remaining error
+// M^-1 (r - M z), scaled by mcm/s (mcm the mean level diagonal); it is
+// interpolated bilinearly (cell centred) to the fine grid and added to z.
+struct LpcArgs {
+    int lev, nxl, nyl, Hn, Wn;
+    const float *mc, *ce, *cn, *extra;   // level operator
+    int Pl;                              // level pitch
+    float *op, *rr;
+    __nv_bfloat16 *x0;
+    const float *y;
+    double *rhs64;                       // harvest: fine r - M z in FP64 (or null)
+    float *tgt;                          // harvest: target slot
+    const double *e;                     // harvest: solution of M e = r - M z
+};
+
+__global__ void __launch_bounds__(256) k_lpc_opfeat(const LpcArgs l, const CgmArgs a) {
+    double v = 0.0;
+    const int n = l.nxl * l.nyl;
+    for (int q = blockIdx.x * 256 + threadIdx.x; q < n; q += gridDim.x * 256) {
+        const int J = q / l.nxl + 1, I = q - (J - 1) * l.nxl + 1;
+        const size_t o = (size_t)J * l.Pl + I;
+        const float mc = l.mc[o], im = mc > 0.0f ? 1.0f / mc : 0.0f;
+        float *f = l.op + ((size_t)(J - 1) * l.Wn + (I - 1)) * 3;
+        f[0] = l.ce[o] * im;
+        f[1] = l.cn[o] * im;
+        f[2] = l.extra[o] * im;
+        v += (double)mc;
+    }
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[5], a.nblk, &out) && threadIdx.x == 0)
+        a.ctrl->lpc_mcm = out / (double)n;
+}
+
+// R (r32 - M z) per NN cell (aggregates of s x s fine nodes, s = 2, 4 or 8);
+// for a harvest also r - M z in FP64.  A CTA takes a 32 x 8 tile of fine
+// nodes (whole cells, since s divides both), one node per thread; the cell
+// sums are formed in shared memory in a fixed order.
+__global__ void __launch_bounds__(256) k_lpc_resid(const LpcArgs l, const CgmArgs a) {
+    __shared__ float v[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
+    float r1 = 0.0f;
+    if (i <= a.nx && j <= a.ny) {
+        const size_t o = (size_t)j * a.P + i;
+        r1 = a.r32[o] - mz_ff(a.z[o], a.z[o + 1], a.z[o - 1], a.z[o + a.P], a.z[o - a.P], a.ce[o], a.ce[o - 1],
+                              a.cn[o], a.cn[o - a.P], a.extra[o]);
+        if (l.rhs64) l.rhs64[o] = (double)r1;
+    }
+    v[ty][tx] = r1;
+    __syncthreads();
+    const int s = 1 << l.lev;
+    if ((tx % s) == 0 && (ty % s) == 0) {
+        const int I = (i - 1) / s, J = (j - 1) / s;   // 0-based cell
+        if (I < l.nxl && J < l.nyl) {
+            float acc = 0.0f;
+            for (int dy = 0; dy < s && ty + dy < 8; dy++)
+                for (int dx = 0; dx < s; dx++) acc += v[ty + dy][tx + dx];
+            l.rr[(size_t)J * l.Wn + I] = acc;
+        }
+    }
+}
+
+// network input [Hn][Wn][16] BF16 (channels 4..15 stay zero), the residual
+// channel scaled by its RMS s over the level's cells.  One CTA, fixed order.
+__global__ void __launch_bounds__(1024) k_lpc_x0(const LpcArgs l, Ctrl *ctrl) {
+    __shared__ double red[1024];
+    const int n = l.nxl * l.nyl;
+    double acc = 0.0;
+    for (int q = threadIdx.x; q < n; q += 1024) {
+        const int J = q / l.nxl, I = q - J * l.nxl;
+        const double r = l.rr[(size_t)J * l.Wn + I];
+        acc += r * r;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = 512; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    const double s = sqrt(red[0] / (double)n);
+    if (threadIdx.x == 0) ctrl->lpc_s = s;
+    const float is = s > 0.0 ? (float)(1.0 / s) : 0.0f;
+    for (int p = threadIdx.x; p < l.Hn * l.Wn; p += 1024) {
+        const int J = p / l.Wn, I = p - J * l.Wn;
+        const bool ok = J < l.nyl && I < l.nxl;
+        __nv_bfloat16 *x = l.x0 + (size_t)p * LPC_CIN0;
+        x[0] = __float2bfloat16_rn(ok ? l.rr[p] * is : 0.0f);
+        x[1] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 0] : 0.0f);
+        x[2] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 1] : 0.0f);
+        x[3] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 2] : 0.0f);
+    }
+}
+
+// bilinear, cell-centred interpolation of the NN grid value to fine node (i, j)
+__device__ __forceinline__ float lpc_interp(const LpcArgs &l, const float *y, int stride, int i, int j) {
+    const float h = (float)(1 << l.lev);
+    float u = ((float)i - 0.5f) / h - 0.5f, w = ((float)j - 0.5f) / h - 0.5f;
+    u = fminf(fmaxf(u, 0.0f), (float)(l.nxl - 1));
+    w = fminf(fmaxf(w, 0.0f), (float)(l.nyl - 1));
+    const int i0 = min((int)u, l.nxl - 1), j0 = min((int)w, l.nyl - 1);
+    const int i1 = min(i0 + 1, l.nxl - 1), j1 = min(j0 + 1, l.nyl - 1);
+    const float fu = u - (float)i0, fw = w - (float)j0;
+    const float y00 = y[((size_t)j0 * l.Wn + i0) * stride], y01 = y[((size_t)j0 * l.Wn + i1) * stride];
+    const float y10 = y[((size_t)j1 * l.Wn + i0) * stride], y11 = y[((size_t)j1 * l.Wn + i1) * stride];
+    return (1.0f - fw) * ((1.0f - fu) * y00 + fu * y01) + fw * ((1.0f - fu) * y10 + fu * y11);
+}
+
+// z += interp(y) * s / mcm, unless the correction is switched off
+__global__ void __launch_bounds__(256) k_lpc_prolong(const LpcArgs l, const CgmArgs a) {
+    Ctrl *c = a.ctrl;
+    if (c->lpc_off || c->cg_done || c->cg_fail) return;
+    const float sc = c->lpc_mcm > 0.0 ? (float)(c->lpc_s / c->lpc_mcm) : 0.0f;
+    CG_NODES(a, {
+        const int j = (int)j_ + 1, i = (int)(q_ - j_ * (unsigned)a.nx) + 1;
+        const float v = lpc_interp(l, l.y, LPC_COUT_LAST, i, j) * sc;
+        if (isfinite(v)) a.z[o] += v;
+        else c->lpc_off = 1;
+    })
+}
+
+// harvest target: aggregate mean of e, times mcm / s
+__global__ void k_lpc_target(const LpcArgs l, const CgmArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= l.Hn * l.Wn) return;
+    const int J = p / l.Wn + 1, I = p - (J - 1) * l.Wn + 1, s = 1 << l.lev;
+    float v = 0.0f;
+    if (J <= l.nyl && I <= l.nxl) {
+        double acc = 0.0;
+        int cnt = 0;
+        for (int j = (J - 1) * s + 1; j <= min(J * s, a.ny); j++)
+            for (int i = (I - 1) * s + 1; i <= min(I * s, a.nx); i++) { acc += l.e[(size_t)j * a.P + i]; cnt++; }
+        const double sc = a.ctrl->lpc_s > 0.0 ? a.ctrl->lpc_mcm / a.ctrl->lpc_s : 0.0;
+        v = (float)(acc / cnt * sc);
+    }
+    l.tgt[p] = v;
 }
 
 LevelT<float> level_f(const MGLevelF &m) {
@@ -716,13 +868,42 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
             fs_prof_end(c);
         }
     }
-    fs_prof_begin(c, PROF_CG);
-    k_cgm_rz<<<ca.grid, 256, 0, c->stream>>>(ca);
+}
+
+static LpcArgs lpc_args(fs_ctx *c) {
+    LpcArgs l = {};
+    const MGLevelF &m = c->mgf[c->lpc_level];
+    l.lev = c->lpc_level; l.nxl = m.nx; l.nyl = m.ny; l.Hn = c->lpc->Hn; l.Wn = c->lpc->Wn;
+    l.mc = m.mc; l.ce = m.ce; l.cn = m.cn; l.extra = m.extra; l.Pl = m.pitch;
+    l.op = c->lpc_op; l.rr = c->lpc_rr; l.x0 = c->lpc->x0; l.y = c->lpc->y;
+    return l;
+}
+
+// z += learned correction of the V-cycle's remaining error
+static void lpc_apply(fs_ctx *c, const CgmArgs &ca) {
+    LpcArgs l = lpc_args(c);
+    fs_prof_begin(c, PROF_OTHER);
+    k_lpc_resid<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(l, ca);
+    k_lpc_x0<<<1, 1024, 0, c->stream>>>(l, c->d_ctrl);
+    lpc_forward(c->lpc, 1, c->stream);
+    k_lpc_prolong<<<ca.grid, 256, 0, c->stream>>>(l, ca);
+    // one black-red Gauss-Seidel pass removes the cell-scale error the
+    // interpolated correction brings in (as post-smoothing does after a
+    // coarse-grid correction)
+    LevelT<float> f0 = level_f(c->mgf[0]);
+    dim3 b(32, 8), gh = grid2((f0.nx + 1) / 2, f0.ny, b);
+    k_rb<float><<<gh, b, 0, c->stream>>>(f0, 1, 0);
+    k_rb<float><<<gh, b, 0, c->stream>>>(f0, 0, 0);
     fs_prof_end(c);
+    c->launches += 3 + 13 + 2;   // feature, input and prolongation kernels, the network, the sweep
 }
 
 static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
     vcycle_mixed(c, ca);
+    if (ca.lpc) lpc_apply(c, ca);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_rz<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
     fs_prof_begin(c, PROF_CG);
     k_cgm_pq<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
@@ -778,6 +959,30 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     return FS_OK;
 }
 
+static CgmArgs cgm_args(fs_ctx *c) {
+    MGLevelF &m0 = c->mgf[0];
+    CgmArgs ca;
+    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;
+    {
+        long nb = ((long)c->nx * c->ny + 255) / 256, cap = 4L * c->nsm;
+        ca.nblk = (int)(nb < cap ? nb : cap);
+        ca.grid = dim3(ca.nblk);
+    }
+    ca.x = c->xs; ca.r = c->r;
+    ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
+    ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32;
+    ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
+    ca.ctrl = c->d_ctrl;
+    ca.rtol = c->cfg.lapl_rtol;
+    ca.inner_tol2 = 1e-5 * 1e-5;
+    ca.inner_max = 16;
+    ca.maxit = c->cfg.lapl_maxit;
+    ca.lpc = c->lpc_on && c->lpc;
+    ca.use_cond = 0;
+    ca.cond = 0;
+    return ca;
+}
+
 int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_faces_update_mixed(c);
     AsmMixArgs a;
@@ -813,24 +1018,12 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         k_coarsen_diag<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
         fs_prof_end(c);
     }
-    CgmArgs ca;
-    ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;
-    {
-        long nb = ((long)c->nx * c->ny + 255) / 256, cap = 4L * c->nsm;
-        ca.nblk = (int)(nb < cap ? nb : cap);
-        ca.grid = dim3(ca.nblk);
+    CgmArgs ca = cgm_args(c);
+    if (c->lpc_on) {
+        LpcArgs l = lpc_args(c);
+        c->launches++;
+        k_lpc_opfeat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
     }
-    ca.x = c->xs; ca.r = c->r;
-    ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
-    ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32;
-    ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
-    ca.ctrl = c->d_ctrl;
-    ca.rtol = c->cfg.lapl_rtol;
-    ca.inner_tol2 = 1e-5 * 1e-5;
-    ca.inner_max = 16;
-    ca.maxit = c->cfg.lapl_maxit;
-    ca.use_cond = 0;
-    ca.cond = 0;
     fs_prof_begin(c, PROF_CG);
     k_cgm_init<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
@@ -886,4 +1079,180 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels (mixed)");
     return FS_OK;
+}
+
+// ---------------------------------------------------- learned preconditioner
+static int round4(int v) { return (v + 3) / 4 * 4; }
+
+int fs_lpc_init_impl(fs_ctx *c, int level, int max_batch, int max_samples, uint64_t seed) {
+    if (!c->mixed) return fs_set_error(c, FS_ERR_UNSUPPORTED, "the learned preconditioner needs the mixed solver");
+    if (level < 1 || level > 3 || level >= c->mg_nlev)
+        return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner level %d outside 1..%d", level,
+                            c->mg_nlev - 1 < 3 ? c->mg_nlev - 1 : 3);
+    if (max_batch < 1 || max_samples < 1) return fs_set_error(c, FS_ERR_INVALID, "batch and sample counts must be positive");
+    fs_lpc_free_impl(c);
+    const MGLevelF &m = c->mgf[level];
+    const int Hn = round4(m.ny), Wn = round4(m.nx);
+    LpcState *L = nullptr;
+    int e = lpc_alloc(&L, Hn, Wn, max_batch, max_samples, seed, c->stream);
+    if (e) return fs_cuda_check(c, (cudaError_t)e, "learned preconditioner buffers");
+    L->level = level;
+    c->lpc = L;
+    c->lpc_level = level;
+    c->lpc_snap_max = 8;
+    cudaError_t ce = cudaMalloc(&c->lpc_op, (size_t)Hn * Wn * 3 * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_op, 0, (size_t)Hn * Wn * 3 * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_rr, (size_t)Hn * Wn * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_rr, 0, (size_t)Hn * Wn * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_rhs64, c->field_elems * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_rhs64, 0, c->field_elems * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_snap, (size_t)c->lpc_snap_max * c->field_elems * sizeof(float));
+    if (ce != cudaSuccess) { fs_lpc_free_impl(c); return fs_cuda_check(c, ce, "learned preconditioner buffers"); }
+    // valid cells of the padded NN grid
+    std::vector<float> mk((size_t)Hn * Wn, 0.0f);
+    for (int j = 0; j < m.ny; j++)
+        for (int i = 0; i < m.nx; i++) mk[(size_t)j * Wn + i] = 1.0f;
+    ce = cudaMemcpyAsync(L->mask, mk.data(), mk.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, ce, "learned preconditioner init");
+}
+
+void fs_lpc_free_impl(fs_ctx *c) {
+    if (c->cgm_graph_built) {   // the graph may hold the network's kernels
+        cudaGraphExecDestroy(c->cgm_exec);
+        cudaGraphDestroy(c->cgm_graph);
+        c->cgm_graph_built = 0;
+    }
+    lpc_free(c->lpc);
+    c->lpc = nullptr;
+    c->lpc_on = 0;
+    cudaFree(c->lpc_op); cudaFree(c->lpc_rr); cudaFree(c->lpc_rhs64); cudaFree(c->lpc_snap);
+    c->lpc_op = c->lpc_rr = nullptr; c->lpc_rhs64 = nullptr; c->lpc_snap = nullptr;
+}
+
+// Host-driven solve of the current (assembled) system with the plain mixed
+// MG-PCG to lapl_rtol; returns the iterations, or a negative error.
+static int solve_plain(fs_ctx *c, CgmArgs ca, std::vector<int> *snap_iters) {
+    ca.lpc = 0;
+    k_cgm_init<<<ca.grid, 256, 0, c->stream>>>(ca);
+    int rc = fs_sync_ctrl(c);
+    if (rc) return rc;
+    int taken = 0;
+    for (int it = 0; !c->h_ctrl->cg_done && !c->h_ctrl->cg_fail && it < c->cfg.lapl_maxit; it++) {
+        if (snap_iters && taken < c->lpc_snap_max && it % 2 == 0) {   // the residual the preconditioner sees
+            cudaMemcpyAsync(c->lpc_snap + (size_t)taken * c->field_elems, ca.r32, c->field_elems * sizeof(float),
+                            cudaMemcpyDeviceToDevice, c->stream);
+            snap_iters->push_back(it);
+            taken++;
+        }
+        cg_iteration_mixed(c, ca);
+        if ((rc = fs_sync_ctrl(c))) return rc;
+    }
+    if (!c->h_ctrl->cg_done) return fs_set_error(c, FS_ERR_INVALID, "harvest solve did not converge");
+    return c->h_ctrl->cg_iters;
+}
+
+int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added) {
+    if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    LpcState *L = c->lpc;
+    *added = 0;
+    CgmArgs ca = cgm_args(c);
+    LpcArgs l = lpc_args(c);
+    k_lpc_opfeat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
+    std::vector<int> its;
+    int rc = solve_plain(c, ca, &its);
+    if (rc < 0) return rc;
+    const size_t px = (size_t)L->Hn * L->Wn;
+    const int n = std::min((int)its.size(), std::min(per_solve, c->lpc_snap_max));
+    for (int k = 0; k < n; k++) {
+        const int slot = L->nsamp % L->Nmax;
+        // r: a residual of the plain solve; z = V(r); features of R (r - M z)
+        cudaMemcpyAsync(ca.r32, c->lpc_snap + (size_t)k * c->field_elems, c->field_elems * sizeof(float),
+                        cudaMemcpyDeviceToDevice, c->stream);
+        vcycle_mixed(c, ca);
+        LpcArgs lh = l;
+        lh.rhs64 = c->lpc_rhs64;
+        k_lpc_resid<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(lh, ca);
+        k_lpc_x0<<<1, 1024, 0, c->stream>>>(lh, c->d_ctrl);
+        cudaMemcpyAsync(L->dfeat + slot * px * LPC_CIN0, L->x0, px * LPC_CIN0 * sizeof(__nv_bfloat16),
+                        cudaMemcpyDeviceToDevice, c->stream);
+        if ((rc = fs_sync_ctrl(c))) return rc;
+        const double s = c->h_ctrl->lpc_s, mcm = c->h_ctrl->lpc_mcm;
+        // the correction multigrid-PCG gives for that remaining residual
+        CgmArgs ch = ca;
+        ch.rhs = c->lpc_rhs64;
+        rc = solve_plain(c, ch, nullptr);
+        if (rc < 0) return rc;
+        (void)s;
+        (void)mcm;
+        lh.tgt = L->dtgt + slot * px;
+        lh.e = c->xs;
+        k_lpc_target<<<(int)((px + 255) / 256), 256, 0, c->stream>>>(lh, ca);
+        L->nsamp++;
+        (*added)++;
+    }
+    return fs_cuda_check(c, cudaStreamSynchronize(c->stream), "harvest");
+}
+
+int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, float *loss_hist) {
+    if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    LpcState *L = c->lpc;
+    const int n = std::min(L->nsamp, L->Nmax);
+    if (n < 1) return fs_set_error(c, FS_ERR_INVALID, "no harvested samples");
+    if (batch < 1 || batch > L->Bmax) return fs_set_error(c, FS_ERR_INVALID, "batch %d outside 1..%d", batch, L->Bmax);
+    uint64_t st = seed * 0x9E3779B97F4A7C15ull + 7;
+    std::vector<int> idx(batch);
+    float *h_loss = nullptr;
+    cudaMallocHost(&h_loss, sizeof(float) * (size_t)iters);
+    for (int it = 0; it < iters; it++) {
+        for (int b = 0; b < batch; b++) {
+            st += 0x9E3779B97F4A7C15ull;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            idx[b] = (int)((z ^ (z >> 31)) % (uint64_t)n);
+        }
+        lpc_gather(L, idx.data(), batch, c->stream);
+        lpc_forward(L, batch, c->stream);
+        int e = lpc_loss_backward(L, batch, c->stream);
+        if (e) { cudaFreeHost(h_loss); return fs_cuda_check(c, (cudaError_t)e, "training step"); }
+        cudaMemcpyAsync(h_loss + it, L->d_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+        lpc_adam(L, lr, c->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && loss_hist) memcpy(loss_hist, h_loss, sizeof(float) * (size_t)iters);
+    cudaFreeHost(h_loss);
+    return fs_cuda_check(c, e, "training");
+}
+
+// loss and gradient of given features/targets (host arrays), for checks
+int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float *mask, int batch, float *grad,
+                     float *loss, float *pred) {
+    if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
+    LpcState *L = c->lpc;
+    if (batch < 1 || batch > L->Bmax) return fs_set_error(c, FS_ERR_INVALID, "batch %d outside 1..%d", batch, L->Bmax);
+    const size_t px = (size_t)L->Hn * L->Wn, P = px * batch;
+    std::vector<__nv_bfloat16> x0(P * LPC_CIN0, __float2bfloat16(0.0f));
+    for (size_t p = 0; p < P; p++)
+        for (int k = 0; k < LPC_NFEAT; k++) x0[p * LPC_CIN0 + k] = __float2bfloat16(feat[p * LPC_NFEAT + k]);
+    std::vector<float> bm(P);
+    for (size_t p = 0; p < P; p++) bm[p] = mask[p % px];
+    cudaError_t e = cudaMemcpyAsync(L->x0, x0.data(), x0.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L->btgt, tgt, P * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L->bmask, bm.data(), P * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "gradient inputs");
+    lpc_forward(L, batch, c->stream);
+    int r = lpc_loss_backward(L, batch, c->stream);
+    if (r) return fs_cuda_check(c, (cudaError_t)r, "gradient");
+    if (grad) e = cudaMemcpyAsync(grad, L->g, L->net.nparam * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, L->d_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    std::vector<float> y;
+    if (e == cudaSuccess && pred) {
+        y.resize(P * LPC_COUT_LAST);
+        e = cudaMemcpyAsync(y.data(), L->y, y.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && pred)
+        for (size_t p = 0; p < P; p++) pred[p] = y[p * LPC_COUT_LAST];
+    return fs_cuda_check(c, e, "gradient outputs");
 }

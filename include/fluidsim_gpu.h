@@ -237,6 +237,47 @@ int64_t fs_launch_count(fs_ctx *ctx);
  * GPU work overlaps race on it.  ctx's device must be current. */
 int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
 
+/* ---- Learned Poisson preconditioner (FS_PREC_MIXED contexts only).  No
+ * counterpart in the reference, which hands the system to PETSc
+ * (lapl_lib.F90:83-104).  A small BF16 convolutional network (~250k
+ * parameters, two-level U-Net, tensor cores with FP32 accumulation) on the
+ * grid of multigrid level `level` predicts the error the V-cycle leaves; its
+ * interpolated prediction is added to each V-cycle's result inside the
+ * flexible CG.  The FP64 refinement of the mixed solver judges convergence,
+ * so every solve reaches lapl_rtol exactly as without the network, and if an
+ * iteration stalls (inner residual falling by less than 2x) the network is
+ * switched off for the rest of that solve.
+ *
+ * fs_lpc_init      allocate the network (seeded He init), its training state
+ *                  and a ring of up to max_samples training pairs; batches up
+ *                  to max_batch.
+ * fs_lpc_harvest   after fs_lapl_solve: re-solve the step's assembled system
+ *                  with the plain multigrid-PCG, take up to per_solve of its
+ *                  residuals r, and store for each the pair (features of the
+ *                  residual left by one V-cycle, aggregate means of the
+ *                  correction multigrid-PCG computes for it).  phi is not
+ *                  changed.
+ * fs_lpc_train     iters Adam steps (lr) on random batches of the stored
+ *                  pairs (seeded); loss_hist (may be NULL) gets each step's
+ *                  training loss.
+ * fs_lpc_use       1: the solver uses the network; 0: plain multigrid-PCG.
+ * fs_lpc_weights   copy the FP32 parameters out (to_device = 0) or in
+ *                  (to_device = 1, Adam state reset); n must equal nparam.
+ * fs_lpc_grad      loss and parameter gradient for given inputs: feat
+ *                  [batch][h][w][4], tgt [batch][h][w], mask [h][w]; pred
+ *                  (may be NULL) gets the predictions [batch][h][w].
+ * fs_lpc_info      NN grid size (h, w, padded to multiples of 4), stored
+ *                  pairs, parameter count; off = 1 if the last solve switched
+ *                  the network off. */
+int fs_lpc_init(fs_ctx *ctx, int32_t level, int32_t max_batch, int32_t max_samples, uint64_t seed);
+int fs_lpc_harvest(fs_ctx *ctx, int32_t per_solve, int32_t *added);
+int fs_lpc_train(fs_ctx *ctx, int32_t iters, int32_t batch, float lr, uint64_t seed, float *loss_hist);
+int fs_lpc_use(fs_ctx *ctx, int32_t on);
+int fs_lpc_weights(fs_ctx *ctx, float *w, int64_t n, int32_t to_device);
+int fs_lpc_grad(fs_ctx *ctx, const float *feat, const float *tgt, const float *mask, int32_t batch, float *grad,
+                float *loss, float *pred);
+int fs_lpc_info(fs_ctx *ctx, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off);
+
 #ifdef __cplusplus
 }
 #endif
