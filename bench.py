@@ -13,7 +13,12 @@ The gb300 arm prints one JSON line with the device-resident throughput
 (`value`), the end-to-end throughput through the C ABI with host buffers
 (`e2e`), a roofline object for the dominant kernel (the RK stage kernel),
 the CPU oracle timed on the host cores (`cpu_baseline`), SM clocks sampled
-during the timed region and the number of kernels launched.
+during the timed region and the number of kernels launched.  `value` and
+`e2e` are the plain FP64 path (the drop-in); `variants` holds the same two
+numbers for the mixed-precision solver and for the mixed solver with the
+learned Poisson preconditioner (trained first on pairs harvested from the
+run), each with its speed-up over the plain path, all at the same 1e-8
+relative Poisson residual.
 
 The reference arm (--impl reference) times the reference algorithm's CPU
 implementation -- the C++ oracle, a restatement of the Fortran, because the
@@ -39,6 +44,12 @@ UNIT = "steps/s"
 # (stage 1 reads n2, n3, phi and writes k1, n2'; ...; stage 5 reads n2, n3,
 # k1, k3, k4, phi and writes n1), i.e. 640 B per node per attempt, 128 B per stage.
 STAGE_BYTES_PER_NODE = (25 * 3 + 5) * 8 / 5.0
+# measured DRAM traffic of one FP64 stage launch at 1024^2: 113.0 MB read + 26.0 MB written
+STAGE_TRAFFIC_1024 = 139.0e6
+# learned preconditioner variant: training pairs harvested over this many
+# steps (4 per step), then this many Adam steps of batch 16
+LPC_HARVEST = 12
+LPC_ITERS = 400
 
 
 def measured_peaks():
@@ -186,14 +197,31 @@ def run_reference(args):
     return 0
 
 
-def measure_variant(cfg, mesh, st0, args, barrier):
+def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
     """Device-resident and end-to-end steps/s of one solver variant on the
-    same workload (fresh context, same warm-up), for the comparison keys."""
+    same workload (fresh context, same warm-up), for the comparison keys.
+    learned: first harvest training pairs from the plain multigrid-PCG over
+    LPC_HARVEST steps, train the network (LPC_ITERS Adam steps), then time
+    with the network in the solver."""
     import torch
     from fluidsim_gb300 import api
     d = api.Discharge(cfg, mesh, st0)
     stream = torch.cuda.ExternalStream(d.stream_handle())
     d.run(2 + args.warmup)
+    train = None
+    if learned:
+        t0 = time.perf_counter()
+        d.lpc_init(level=3, max_batch=16, max_samples=1024, seed=1)
+        for _ in range(LPC_HARVEST):
+            d.step()
+            d.lpc_harvest(per_solve=4)
+        hist = d.lpc_train(iters=LPC_ITERS, batch=16, lr=1e-3, seed=2)
+        d.lpc_use(True)
+        torch.cuda.synchronize()
+        train = {"pairs": d.lpc_info()["samples"], "adam_steps": LPC_ITERS, "batch": 16,
+                 "loss_first20": float(hist[:20].mean()), "loss_last20": float(hist[-20:].mean()),
+                 "seconds": time.perf_counter() - t0, "nn_grid": [d.lpc_info()["h"], d.lpc_info()["w"]],
+                 "params": d.lpc_info()["nparam"]}
     warm_state = d.download(nlev=3)
     warm_t, warm_dt, warm_ts = d.t, d.dt, d.ts
     w = d.stats()
@@ -226,13 +254,15 @@ def measure_variant(cfg, mesh, st0, args, barrier):
     e3.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e2.elapsed_time(e3)
+    off = d.lpc_info()["off"] if learned else None
     d.close()
     return {"value": args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
             "e2e": args.steps / (ms_e2e * 1e-3),
             "cg_iters_per_step": (s["lapl_iters"] - w["lapl_iters"]) / args.steps,
             "rk_attempts": s["attempts"] - w["attempts"], "gpu_launches": launches,
             "h2d_bytes_per_step": sum(a.nbytes for a in pinned.values()) / args.steps,
-            "d2h_bytes_per_step": 3 * sum(a.nbytes for a in pinned.values()) / args.steps}
+            "d2h_bytes_per_step": 3 * sum(a.nbytes for a in pinned.values()) / args.steps,
+            "training": train, "network_switched_off_in_last_solve": off}
 
 
 def run_gpu(args):
@@ -342,11 +372,9 @@ def run_gpu(args):
     nodes = cfg.nx * cfg.ny
     stage_ms = st_ms / max(st_n, 1)
     achieved = STAGE_BYTES_PER_NODE * nodes / (stage_ms * 1e-3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get("bytes_per_launch_%d" % args.n)
+    # DRAM bytes of one stage launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    # from one ncu capture of the 1024^2 workload; scaled by nodes elsewhere
+    traffic = STAGE_TRAFFIC_1024 * nodes / (1024.0 * 1024.0)
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample ---------
     cpu = None
@@ -366,6 +394,10 @@ def run_gpu(args):
         vm["speedup_vs_plain"] = vm["value"] / (args.steps / (ms * 1e-3))
         vm["e2e_speedup_vs_plain"] = vm["e2e"] / (args.steps / (ms_e2e * 1e-3))
         variants["mixed"] = vm
+        vl = measure_variant(cfgm, mesh, st0, args, barrier, learned=True)
+        vl["speedup_vs_plain"] = vl["value"] / (args.steps / (ms * 1e-3))
+        vl["e2e_speedup_vs_plain"] = vl["e2e"] / (args.steps / (ms_e2e * 1e-3))
+        variants["mixed+learned-PC"] = vl
 
     if rank == 0:
         total_ms = {kk: v[0] for kk, v in breakdown.items()}

@@ -667,13 +667,9 @@ int fs_lpc_train(fs_ctx *c, int32_t iters, int32_t batch, float lr, uint64_t see
 int fs_lpc_use(fs_ctx *c, int32_t on) {
     if (!c) return FS_ERR_INVALID;
     if (on && !c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
-    if ((on != 0) != (c->lpc_on != 0) && c->cgm_graph_built) {   // the CG graph bakes the choice in
-        cudaStreamSynchronize(c->stream);
-        cudaGraphExecDestroy(c->cgm_exec);
-        cudaGraphDestroy(c->cgm_graph);
-        c->cgm_graph_built = 0;
-    }
-    c->lpc_on = on != 0;
+    c->lpc_on = on != 0;   // the solver keeps one CG graph with and one without the network
+    c->lpc_strikes = 0;
+    c->lpc_skip = 0;
     return FS_OK;
 }
 

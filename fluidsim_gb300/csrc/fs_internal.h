@@ -195,15 +195,16 @@ struct fs_ctx {
     // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
     struct LpcState *lpc;
     int lpc_on, lpc_level;
+    int lpc_strikes, lpc_skip;   // solves in a row the network stalled; solves left without it
     float *lpc_op;               // [Hn][Wn][3] operator features of the level (per solve)
     float *lpc_rr;               // [Hn][Wn] restricted residual
     double *lpc_rhs64;           // fine right-hand side of a harvest solve
     float *lpc_snap;             // harvested residual snapshots (fine FP32 fields)
     int lpc_snap_max;
-    cudaGraph_t cgm_graph;
-    cudaGraphExec_t cgm_exec;
-    int cgm_graph_built;
-    int cgm_body_kernels;
+    cudaGraph_t cgm_graph[2];    // [0] plain MG-PCG, [1] with the learned correction
+    cudaGraphExec_t cgm_exec[2];
+    int cgm_graph_built[2];
+    int cgm_body_kernels[2];
 
     // host mirrors of scalar state
     double t, dt;

@@ -747,6 +747,15 @@ LvT<float> lvt_f(const MGLevelF &m) {
 }  // namespace
 
 // ------------------------------------------------------------------ host side
+static void destroy_cgm_graphs(fs_ctx *c) {
+    for (int v = 0; v < 2; v++)
+        if (c->cgm_graph_built[v]) {
+            cudaGraphExecDestroy(c->cgm_exec[v]);
+            cudaGraphDestroy(c->cgm_graph[v]);
+            c->cgm_graph_built[v] = 0;
+        }
+}
+
 int fs_lapl_alloc_mixed(fs_ctx *c) {
     for (int l = 0; l < c->mg_nlev; l++) {
         MGLevelF &m = c->mgf[l];
@@ -793,11 +802,7 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
 }
 
 void fs_lapl_free_mixed(fs_ctx *c) {
-    if (c->cgm_graph_built) {
-        cudaGraphExecDestroy(c->cgm_exec);
-        cudaGraphDestroy(c->cgm_graph);
-        c->cgm_graph_built = 0;
-    }
+    destroy_cgm_graphs(c);
     for (int l = 0; l < FS_MG_MAX_LEVELS; l++) {
         MGLevelF &m = c->mgf[l];
         float *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.rhs, m.x};
@@ -940,7 +945,8 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
         cg_iteration_mixed(c, ca);
         e = cudaStreamEndCapture(c->stream, &body);
     }
-    c->cgm_body_kernels = (int)(c->launches - l0);
+    const int v = ca.lpc ? 1 : 0;
+    c->cgm_body_kernels[v] = (int)(c->launches - l0);
     if (e == cudaSuccess)
         e = cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -949,14 +955,29 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     }
     c->launches = l0;
     c->prof_on = prof;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cgm_exec, g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cgm_exec[v], g, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(g);
         return fs_cuda_check(c, e, "CG graph capture");
     }
-    c->cgm_graph = g;
-    c->cgm_graph_built = 1;
+    c->cgm_graph[v] = g;
+    c->cgm_graph_built[v] = 1;
     return FS_OK;
+}
+
+// Solve-level fallback: a network that stalled two solves in a row sits out
+// the next 50 solves (plain multigrid-PCG), then gets another try.
+static void lpc_account(fs_ctx *c, const CgmArgs &ca) {
+    if (!c->lpc_on) return;
+    if (!ca.lpc) {
+        if (c->lpc_skip > 0) c->lpc_skip--;
+        return;
+    }
+    if (c->h_ctrl->lpc_off) {
+        if (++c->lpc_strikes >= 2) { c->lpc_skip = 50; c->lpc_strikes = 0; }
+    } else {
+        c->lpc_strikes = 0;
+    }
 }
 
 static CgmArgs cgm_args(fs_ctx *c) {
@@ -977,7 +998,7 @@ static CgmArgs cgm_args(fs_ctx *c) {
     ca.inner_tol2 = 1e-5 * 1e-5;
     ca.inner_max = 16;
     ca.maxit = c->cfg.lapl_maxit;
-    ca.lpc = c->lpc_on && c->lpc;
+    ca.lpc = c->lpc_on && c->lpc && c->lpc_skip == 0;
     ca.use_cond = 0;
     ca.cond = 0;
     return ca;
@@ -1039,12 +1060,14 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     static const bool no_graph = getenv("FS_NO_GRAPH") != nullptr;
     const int poisson_classes = (1 << PROF_SMOOTH) | (1 << PROF_TRANSFER) | (1 << PROF_BOTTOM) | (1 << PROF_CG);
     if (!ok && !no_graph && !(c->prof_on & poisson_classes)) {
-        if (!c->cgm_graph_built && (rc = build_cgm_graph(c, ca))) return rc;
-        cudaError_t e = cudaGraphLaunch(c->cgm_exec, c->stream);
+        const int v = ca.lpc ? 1 : 0;
+        if (!c->cgm_graph_built[v] && (rc = build_cgm_graph(c, ca))) return rc;
+        cudaError_t e = cudaGraphLaunch(c->cgm_exec[v], c->stream);
         if (e != cudaSuccess) return fs_cuda_check(c, e, "CG graph launch");
         rc = fs_sync_ctrl(c);
         if (rc) return rc;
-        c->launches += (int64_t)c->h_ctrl->cg_iters * c->cgm_body_kernels + 1;
+        c->launches += (int64_t)c->h_ctrl->cg_iters * c->cgm_body_kernels[v] + 1;
+        lpc_account(c, ca);
         *iters = c->h_ctrl->cg_iters;
         *relres = c->h_ctrl->relres;
         bool conv = c->h_ctrl->cg_done && !c->h_ctrl->cg_fail;
@@ -1066,6 +1089,7 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         if (c->h_ctrl->cg_fail) break;
         ok = c->h_ctrl->cg_done != 0;
     }
+    lpc_account(c, ca);
     *iters = c->h_ctrl->cg_iters;
     *relres = c->h_ctrl->relres;
     if (!ok) {
@@ -1118,11 +1142,7 @@ int fs_lpc_init_impl(fs_ctx *c, int level, int max_batch, int max_samples, uint6
 }
 
 void fs_lpc_free_impl(fs_ctx *c) {
-    if (c->cgm_graph_built) {   // the graph may hold the network's kernels
-        cudaGraphExecDestroy(c->cgm_exec);
-        cudaGraphDestroy(c->cgm_graph);
-        c->cgm_graph_built = 0;
-    }
+    destroy_cgm_graphs(c);   // a graph may hold the network's kernels
     lpc_free(c->lpc);
     c->lpc = nullptr;
     c->lpc_on = 0;

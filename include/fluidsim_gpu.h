@@ -246,7 +246,8 @@ int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
  * flexible CG.  The FP64 refinement of the mixed solver judges convergence,
  * so every solve reaches lapl_rtol exactly as without the network, and if an
  * iteration stalls (inner residual falling by less than 2x) the network is
- * switched off for the rest of that solve.
+ * switched off for the rest of that solve; after two such solves in a row
+ * the next 50 solves run without it.
  *
  * fs_lpc_init      allocate the network (seeded He init), its training state
  *                  and a ring of up to max_samples training pairs; batches up
