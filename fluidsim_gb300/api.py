@@ -277,8 +277,10 @@ class Discharge(Handle):
                                           hist.ctypes.data_as(C.POINTER(C.c_float))))
         return hist[:iters]
 
-    def lpc_use(self, on=True):
-        self.check(self._lib.fs_lpc_use(self.ctx, 1 if on else 0))
+    def lpc_use(self, mode=1):
+        """0: plain multigrid-PCG; 1 (or True): the network where it is faster;
+        2: the network in every solve."""
+        self.check(self._lib.fs_lpc_use(self.ctx, int(mode)))
 
     def lpc_weights(self, w=None):
         """Get the FP32 parameters, or set them when w is given."""

@@ -667,9 +667,12 @@ int fs_lpc_train(fs_ctx *c, int32_t iters, int32_t batch, float lr, uint64_t see
 int fs_lpc_use(fs_ctx *c, int32_t on) {
     if (!c) return FS_ERR_INVALID;
     if (on && !c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
-    c->lpc_on = on != 0;   // the solver keeps one CG graph with and one without the network
-    c->lpc_strikes = 0;
-    c->lpc_skip = 0;
+    if (on < 0 || on > 2) return fs_set_error(c, FS_ERR_INVALID, "fs_lpc_use mode %d not 0, 1 or 2", on);
+    c->lpc_on = on;   // the solver keeps one CG graph with and one without the network
+    c->lpc_t_nn = -1.0;
+    c->lpc_t_plain = -1.0;
+    c->lpc_use_next = 1;
+    c->lpc_since_probe = 0;
     return FS_OK;
 }
 

@@ -163,6 +163,9 @@ struct fs_ctx {
     MGLevel mg[FS_MG_MAX_LEVELS];
     int mg_nlev;
     int mg_fused;                // coarse launched levels use the fused kernels
+    int mg_lb, mg_dl;            // first level of the one-CTA bottom solver; its dense level
+    double *d_ainv64;            // dense inverse of level mg_dl (FP64 solver)
+    float *d_ainv32;             // dense inverse of level mg_dl (mixed solver)
     double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D
     double *d_cg_part;
     int cg_nblk;
@@ -195,7 +198,9 @@ struct fs_ctx {
     // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
     struct LpcState *lpc;
     int lpc_on, lpc_level;
-    int lpc_strikes, lpc_skip;   // solves in a row the network stalled; solves left without it
+    // choice between the two solvers, judged on measured solve time
+    double lpc_t_nn, lpc_t_plain;   // moving averages of the solve time (ms), < 0: none yet
+    int lpc_use_next, lpc_since_probe;
     float *lpc_op;               // [Hn][Wn][3] operator features of the level (per solve)
     float *lpc_rr;               // [Hn][Wn] restricted residual
     double *lpc_rhs64;           // fine right-hand side of a harvest solve

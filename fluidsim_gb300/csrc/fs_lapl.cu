@@ -525,9 +525,14 @@ int fs_lapl_alloc(fs_ctx *c) {
         ba.lb = 0;
         while (ba.lb < nl && (c->mg[ba.lb].nx > BOTTOM_N || c->mg[ba.lb].ny > BOTTOM_N)) ba.lb++;
         for (int l = 0; l < nl; l++) { ba.L[l].nx = c->mg[l].nx; ba.L[l].ny = c->mg[l].ny; }
+        ba.dl = bottom_dense_level(ba);
+        c->mg_lb = ba.lb;
+        c->mg_dl = ba.dl;
         cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(6 * sizeof(double) * bottom_smem_elems(ba)));
+                                             (int)bottom_smem_bytes(ba));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
+        if ((e = cudaMalloc(&c->d_ainv64, 64 * 64 * sizeof(double))) != cudaSuccess)
+            return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
     }
     size_t n0 = (size_t)(c->ny + 2) * c->pitch;
     double **vecs[] = {&c->p, &c->q, &c->z, &c->r, &c->xs, &c->bs, &c->dinv};
@@ -554,7 +559,7 @@ void fs_lapl_free(fs_ctx *c) {
         for (double *f : fs) cudaFree(f);
         if (l > 0) { cudaFree(m.rhs); cudaFree(m.x); }
     }
-    double *vs[] = {c->p, c->q, c->z, c->r, c->xs, c->bs, c->dinv, c->d_cg_part};
+    double *vs[] = {c->p, c->q, c->z, c->r, c->xs, c->bs, c->dinv, c->d_cg_part, c->d_ainv64};
     for (double *v : vs) cudaFree(v);
     c->mg_nlev = 0;
 }
@@ -597,8 +602,10 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     ba.lb = lb;
     ba.nl = nl;
     ba.nu = nu;
+    ba.dl = c->mg_dl;
+    ba.ainv = c->d_ainv64;
     fs_prof_begin(c, PROF_BOTTOM);
-    k_bottom_smem<double><<<1, BOTTOM_THREADS, 6 * sizeof(double) * bottom_smem_elems(ba), c->stream>>>(ba);
+    k_bottom_smem<double><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
@@ -726,6 +733,9 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
         k_coarsen_diag<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
         fs_prof_end(c);
     }
+    fs_prof_begin(c, PROF_COARSEN);
+    k_dense_inv<double><<<1, 1024, 0, c->stream>>>(level_dev(c->mg[c->mg_dl]), c->d_ainv64);
+    fs_prof_end(c);
     // CG on M d = D b
     CgArgs ca;
     ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <vector>
 #include <cuda_runtime.h>
@@ -777,11 +778,14 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         if (e == cudaSuccess) e = cudaMemset(*v, 0, c->field_elems * sizeof(float));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 CG vectors)");
     }
-    if (c->cg_nblk < 2 * 4 * c->nsm) {   // k_cgm_rz keeps two partials per CTA
-        cudaFree(c->d_cg_part);
-        cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * 2 * 4 * c->nsm);
-        if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (CG partials)");
-        c->cg_nblk = 2 * 4 * c->nsm;
+    {   // two partials per CTA of the CG reductions (<= 4 CTAs per SM)
+        const int need = 2 * 4 * c->nsm;
+        if (c->cg_nblk < need) {
+            cudaFree(c->d_cg_part);
+            cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * need);
+            if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (CG partials)");
+            c->cg_nblk = need;
+        }
     }
     cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<float>(2));
     cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
@@ -791,9 +795,12 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         ba.lb = 0;
         while (ba.lb < ba.nl && (c->mgf[ba.lb].nx > BOTTOM_N || c->mgf[ba.lb].ny > BOTTOM_N)) ba.lb++;
         for (int l = 0; l < ba.nl; l++) { ba.L[l].nx = c->mgf[l].nx; ba.L[l].ny = c->mgf[l].ny; }
+        ba.dl = bottom_dense_level(ba);
         cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(6 * sizeof(float) * bottom_smem_elems(ba)));
+                                             (int)bottom_smem_bytes(ba));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
+        if ((e = cudaMalloc(&c->d_ainv32, 64 * 64 * sizeof(float))) != cudaSuccess)
+            return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
     }
     c->launches++;
     k_dinv<<<grid2(c->nx, c->ny, dim3(32, 8)), dim3(32, 8), 0, c->stream>>>(c->mesh, c->nx, c->ny, c->pitch,
@@ -811,6 +818,7 @@ void fs_lapl_free_mixed(fs_ctx *c) {
     }
     cudaFree(c->p32);
     cudaFree(c->q32);
+    cudaFree(c->d_ainv32);
 }
 
 // FP32 V-cycle on the correction equation: mgf[0].rhs holds the FP64
@@ -848,15 +856,17 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     ba.lb = lb;
     ba.nl = nl;
     ba.nu = nu;
+    ba.dl = c->mg_dl;
+    ba.ainv = c->d_ainv32;
     fs_prof_begin(c, PROF_BOTTOM);
-    k_bottom_smem<float><<<1, BOTTOM_THREADS, 6 * sizeof(float) * bottom_smem_elems(ba), c->stream>>>(ba);
+    k_bottom_smem<float><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
         if (fused) {
             fs_prof_begin(c, PROF_SMOOTH);
-            k_mg_up<float, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_up_smem<float>(2), c->stream>>>(
-                lvt_f(c->mgf[l]), lvt_f(c->mgf[l + 1]));
+            const dim3 g = grid2(f.nx, f.ny, dim3(MTX, MTY));
+            k_mg_up<float, 2><<<g, 256, mg_up_smem<float>(2), c->stream>>>(lvt_f(c->mgf[l]), lvt_f(c->mgf[l + 1]));
             fs_prof_end(c);
             continue;
         }
@@ -900,7 +910,7 @@ static void lpc_apply(fs_ctx *c, const CgmArgs &ca) {
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 1, 0);
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 0, 0);
     fs_prof_end(c);
-    c->launches += 3 + 13 + 2;   // feature, input and prolongation kernels, the network, the sweep
+    c->launches += 3 + 13 + 2 - 1;   // feature, input, prolongation, network, sweep (one counted above)
 }
 
 static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
@@ -965,19 +975,28 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     return FS_OK;
 }
 
-// Solve-level fallback: a network that stalled two solves in a row sits out
-// the next 50 solves (plain multigrid-PCG), then gets another try.
-static void lpc_account(fs_ctx *c, const CgmArgs &ca) {
+// Solve-level choice with the plain multigrid-PCG as the judge: the host keeps
+// moving averages of the wall time of solves with and without the network
+// (a solve in which the network stalled counts double) and runs the next
+// solve with the faster one; every 25 solves it tries the other once.
+static void lpc_account(fs_ctx *c, const CgmArgs &ca, double ms) {
     if (!c->lpc_on) return;
-    if (!ca.lpc) {
-        if (c->lpc_skip > 0) c->lpc_skip--;
-        return;
-    }
-    if (c->h_ctrl->lpc_off) {
-        if (++c->lpc_strikes >= 2) { c->lpc_skip = 50; c->lpc_strikes = 0; }
+    const double a = 0.3;
+    if (ca.lpc) {
+        const double t = c->h_ctrl->lpc_off ? 2.0 * ms : ms;
+        c->lpc_t_nn = c->lpc_t_nn < 0.0 ? t : (1.0 - a) * c->lpc_t_nn + a * t;
     } else {
-        c->lpc_strikes = 0;
+        c->lpc_t_plain = c->lpc_t_plain < 0.0 ? ms : (1.0 - a) * c->lpc_t_plain + a * ms;
     }
+    int next;
+    if (c->lpc_t_nn < 0.0) next = 1;
+    else if (c->lpc_t_plain < 0.0) next = 0;
+    else next = c->lpc_t_nn <= c->lpc_t_plain ? 1 : 0;
+    if (++c->lpc_since_probe >= 25) {
+        next = !next;
+        c->lpc_since_probe = 0;
+    }
+    c->lpc_use_next = next;
 }
 
 static CgmArgs cgm_args(fs_ctx *c) {
@@ -998,13 +1017,17 @@ static CgmArgs cgm_args(fs_ctx *c) {
     ca.inner_tol2 = 1e-5 * 1e-5;
     ca.inner_max = 16;
     ca.maxit = c->cfg.lapl_maxit;
-    ca.lpc = c->lpc_on && c->lpc && c->lpc_skip == 0;
+    ca.lpc = c->lpc && (c->lpc_on == 2 || (c->lpc_on == 1 && c->lpc_use_next));
     ca.use_cond = 0;
     ca.cond = 0;
     return ca;
 }
 
 int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
+    const auto t_start = std::chrono::steady_clock::now();
+    auto elapsed_ms = [&]() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    };
     fs_faces_update_mixed(c);
     AsmMixArgs a;
     a.pp = c->pp;
@@ -1039,6 +1062,9 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         k_coarsen_diag<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
         fs_prof_end(c);
     }
+    fs_prof_begin(c, PROF_COARSEN);
+    k_dense_inv<float><<<1, 1024, 0, c->stream>>>(level_f(c->mgf[c->mg_dl]), c->d_ainv32);
+    fs_prof_end(c);
     CgmArgs ca = cgm_args(c);
     if (c->lpc_on) {
         LpcArgs l = lpc_args(c);
@@ -1067,7 +1093,7 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         rc = fs_sync_ctrl(c);
         if (rc) return rc;
         c->launches += (int64_t)c->h_ctrl->cg_iters * c->cgm_body_kernels[v] + 1;
-        lpc_account(c, ca);
+        lpc_account(c, ca, elapsed_ms());
         *iters = c->h_ctrl->cg_iters;
         *relres = c->h_ctrl->relres;
         bool conv = c->h_ctrl->cg_done && !c->h_ctrl->cg_fail;
@@ -1089,7 +1115,7 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         if (c->h_ctrl->cg_fail) break;
         ok = c->h_ctrl->cg_done != 0;
     }
-    lpc_account(c, ca);
+    lpc_account(c, ca, elapsed_ms());
     *iters = c->h_ctrl->cg_iters;
     *relres = c->h_ctrl->relres;
     if (!ok) {
@@ -1167,8 +1193,15 @@ static int solve_plain(fs_ctx *c, CgmArgs ca, std::vector<int> *snap_iters) {
         }
         cg_iteration_mixed(c, ca);
         if ((rc = fs_sync_ctrl(c))) return rc;
+        static const bool trace = getenv("FS_TRACE_CG") != nullptr;
+        if (trace)
+            fprintf(stderr, "harvest cg %d inner %d relres %.3e inner_r2 %.3e r0in2 %.3e pq %.3e fail %d\n",
+                    c->h_ctrl->cg_iters, c->h_ctrl->inner_it, c->h_ctrl->relres, c->h_ctrl->rnorm2,
+                    c->h_ctrl->r0in2, c->h_ctrl->pq, c->h_ctrl->cg_fail);
     }
-    if (!c->h_ctrl->cg_done) return fs_set_error(c, FS_ERR_INVALID, "harvest solve did not converge");
+    if (!c->h_ctrl->cg_done)
+        return fs_set_error(c, FS_ERR_INVALID, "harvest solve did not converge (relres %.3e after %d iterations)",
+                            c->h_ctrl->relres, c->h_ctrl->cg_iters);
     return c->h_ctrl->cg_iters;
 }
 

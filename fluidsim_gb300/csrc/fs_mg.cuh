@@ -293,6 +293,8 @@ template <typename T>
 struct BottomArgs {
     LevelT<T> L[FS_MG_MAX_LEVELS];
     int lb, nl, nu;
+    int dl;              // k_bottom_smem: level solved exactly with the dense inverse ainv
+    const T *ainv;       // (nx*ny)^2 of level dl, row-major over the compact index (J-1)*nx + I-1
 };
 template <typename T>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a) {
@@ -343,17 +345,77 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a
     }
 }
 
-// The same V-cycle over levels [lb, nl) with every level held in shared
-// memory: the levels' operators and the intermediate right-hand sides and
-// iterates never leave the SM, so each of the ~60 dependent half sweeps costs
-// a shared-memory round trip instead of an L2 one.  Only the top level's
-// right-hand side is read from, and its iterate written to, global memory.
-// Arithmetic and order are those of k_bottom, so the results are identical.
+// The V-cycle over levels [lb, dl] with every level held in shared memory
+// (operators, right-hand sides, iterates), and level dl -- the first with at
+// most 64 unknowns -- solved exactly with its dense inverse (k_dense_inv, once
+// per solve) instead of recursing further: ~20 dependent phases instead of
+// ~50.  Only the top level's right-hand side is read from, and its iterate
+// written to, global memory.
 template <typename T>
 __host__ __device__ inline int bottom_smem_elems(const BottomArgs<T> &a) {
     int n = 0;
-    for (int l = a.lb; l < a.nl; l++) n += (a.L[l].nx + 2) * (a.L[l].ny + 2);
+    for (int l = a.lb; l <= a.dl; l++) n += (a.L[l].nx + 2) * (a.L[l].ny + 2);
     return n;
+}
+// shared memory of k_bottom_smem: six arrays per level and the dense inverse
+template <typename T>
+inline size_t bottom_smem_bytes(const BottomArgs<T> &a) {
+    const size_t nd = (size_t)a.L[a.dl].nx * a.L[a.dl].ny;
+    return (6 * (size_t)bottom_smem_elems(a) + nd * nd) * sizeof(T);
+}
+// first level at or below lb with at most 64 unknowns (the coarsest is 1 x 1)
+template <typename T>
+inline int bottom_dense_level(const BottomArgs<T> &a) {
+    int l = a.lb;
+    while (l < a.nl - 1 && a.L[l].nx * a.L[l].ny > 64) l++;
+    return l;
+}
+
+// Exact inverse of the level operator (at most 64 unknowns), once per solve:
+// in-place Gauss-Jordan without pivoting (the operator is symmetric positive
+// definite), one CTA.  A node without a positive pivot gets x = 0.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_dense_inv(const LevelT<T> L, T *ainv) {
+    __shared__ T A[64 * 64];
+    __shared__ T col[64];
+    __shared__ T s_piv;
+    const int nx = L.nx, n = L.nx * L.ny, t = threadIdx.x;
+    for (int q = t; q < n * n; q += 1024) {
+        const int r = q / n, cidx = q - r * n;
+        const int I = r % nx + 1, J = r / nx + 1;
+        const size_t o = (size_t)J * L.P + I;
+        T v = T(0);
+        if (cidx == r) v = L.mc[o];
+        else if (cidx == r + 1 && I < nx) v = -L.ce[o];
+        else if (cidx == r - 1 && I > 1) v = -L.ce[o - 1];
+        else if (cidx == r + nx) v = -L.cn[o];
+        else if (cidx == r - nx) v = -L.cn[o - L.P];
+        A[q] = v;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        // column k as it stands, and the pivot, before anything changes
+        if (t < n) col[t] = A[t * n + k];
+        if (t == 0) s_piv = A[k * n + k];
+        __syncthreads();
+        const T piv = s_piv;
+        const bool ok = piv > T(0);
+        // row k: A[k][j] /= piv, with A[k][k] = 1/piv
+        for (int j = t; j < n; j += 1024) {
+            if (!ok) A[k * n + j] = T(0);
+            else A[k * n + j] = (j == k ? T(1) : A[k * n + j]) / piv;
+        }
+        __syncthreads();
+        // other rows: A[i][j] -= col_i A[k][j] (j != k), A[i][k] = -col_i A[k][k]
+        for (int q = t; q < n * n; q += 1024) {
+            const int i = q / n, j = q - i * n;
+            if (i == k) continue;
+            if (j == k) A[q] = -col[i] * A[k * n + k];
+            else A[q] = A[q] - col[i] * A[k * n + j];
+        }
+        __syncthreads();
+    }
+    for (int q = t; q < n * n; q += 1024) ainv[q] = A[q];
 }
 template <typename T>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs<T> a) {
@@ -361,10 +423,12 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
     const int t = threadIdx.x;
     const int tot = bottom_smem_elems(a);
     T *base = (T *)sm_raw;
+    const int nd = a.L[a.dl].nx * a.L[a.dl].ny;
+    T *sinv = base + 6 * tot;
     LevelT<T> S[FS_MG_MAX_LEVELS];
     {
         int off = 0;
-        for (int l = a.lb; l < a.nl; l++) {
+        for (int l = a.lb; l <= a.dl; l++) {
             const LevelT<T> &G = a.L[l];
             LevelT<T> &L = S[l];
             L.nx = G.nx; L.ny = G.ny; L.P = G.nx + 2;
@@ -381,6 +445,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
             }
             off += n;
         }
+        for (int q = t; q < nd * nd; q += BOTTOM_THREADS) sinv[q] = a.ainv[q];
     }
     __syncthreads();
     auto sweep = [&](const LevelT<T> &L, int color, int zero) {
@@ -392,7 +457,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         }
         __syncthreads();
     };
-    for (int l = a.lb; l < a.nl - 1; l++) {
+    for (int l = a.lb; l < a.dl; l++) {
         const LevelT<T> f = S[l], c = S[l + 1];
         sweep(f, 0, 1);
         sweep(f, 1, 0);
@@ -408,16 +473,16 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         }
         __syncthreads();
     }
-    {
-        const LevelT<T> c = S[a.nl - 1];
-        sweep(c, 0, 1);
-        if (c.nx * c.ny > 1) {
-            sweep(c, 1, 0);
-            for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
-            for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
+    {   // level dl: x = A^-1 rhs with the precomputed dense inverse
+        const LevelT<T> c = S[a.dl];
+        if (t < nd) {
+            T acc = T(0);
+            for (int j = 0; j < nd; j++) acc += sinv[t * nd + j] * c.rhs[(j / c.nx + 1) * c.P + j % c.nx + 1];
+            c.x[(t / c.nx + 1) * c.P + t % c.nx + 1] = acc;
         }
+        __syncthreads();
     }
-    for (int l = a.nl - 2; l >= a.lb; l--) {
+    for (int l = a.dl - 1; l >= a.lb; l--) {
         const LevelT<T> f = S[l], c = S[l + 1];
         for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
             int I = q % f.nx + 1, J = q / f.nx + 1;

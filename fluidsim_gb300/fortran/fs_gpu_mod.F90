@@ -80,6 +80,33 @@ module fs_gpu_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: v
     end function
+    ! learned Poisson preconditioner of the mixed solver (no reference counterpart)
+    integer(c_int) function fs_lpc_init(ctx, level, max_batch, max_samples, seed) &
+        bind(C, name="fs_lpc_init")
+      import :: c_ptr, c_int, c_int32_t, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: level, max_batch, max_samples
+      integer(c_int64_t), value :: seed
+    end function
+    integer(c_int) function fs_lpc_harvest(ctx, per_solve, added) bind(C, name="fs_lpc_harvest")
+      import :: c_ptr, c_int, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: per_solve
+      integer(c_int32_t), intent(out) :: added
+    end function
+    integer(c_int) function fs_lpc_train(ctx, iters, batch, lr, seed, loss_hist) bind(C, name="fs_lpc_train")
+      import :: c_ptr, c_int, c_int32_t, c_int64_t, c_float
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: iters, batch
+      real(c_float), value :: lr
+      integer(c_int64_t), value :: seed
+      type(c_ptr), value :: loss_hist
+    end function
+    integer(c_int) function fs_lpc_use(ctx, mode) bind(C, name="fs_lpc_use")
+      import :: c_ptr, c_int, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: mode
+    end function
     type(c_ptr) function fs_last_error(ctx) bind(C, name="fs_last_error")
       import :: c_ptr
       type(c_ptr), value :: ctx

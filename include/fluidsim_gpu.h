@@ -246,8 +246,10 @@ int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
  * flexible CG.  The FP64 refinement of the mixed solver judges convergence,
  * so every solve reaches lapl_rtol exactly as without the network, and if an
  * iteration stalls (inner residual falling by less than 2x) the network is
- * switched off for the rest of that solve; after two such solves in a row
- * the next 50 solves run without it.
+ * switched off for the rest of that solve.  In mode 1 the
+ * library times every solve and runs each next one with whichever of the
+ * two -- with or without the network -- has been faster on average (a
+ * stalled solve counts double), trying the other one every 25 solves.
  *
  * fs_lpc_init      allocate the network (seeded He init), its training state
  *                  and a ring of up to max_samples training pairs; batches up
@@ -261,7 +263,8 @@ int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
  * fs_lpc_train     iters Adam steps (lr) on random batches of the stored
  *                  pairs (seeded); loss_hist (may be NULL) gets each step's
  *                  training loss.
- * fs_lpc_use       1: the solver uses the network; 0: plain multigrid-PCG.
+ * fs_lpc_use       0: plain multigrid-PCG; 1: the network where it pays off
+ *                  (see below); 2: the network in every solve.
  * fs_lpc_weights   copy the FP32 parameters out (to_device = 0) or in
  *                  (to_device = 1, Adam state reset); n must equal nparam.
  * fs_lpc_grad      loss and parameter gradient for given inputs: feat

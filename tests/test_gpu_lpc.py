@@ -88,7 +88,7 @@ def test_lpc_training_and_solver(built):
         e.ts = ts
         e.lpc_init(level=3, max_batch=1, max_samples=1, seed=0)
         e.lpc_weights(w)
-        e.lpc_use(use)
+        e.lpc_use(2 if use else 0)
         its = []
         for _ in range(6):
             info = e.step()
