@@ -360,8 +360,7 @@ __host__ __device__ inline int bottom_smem_elems(const BottomArgs<T> &a) {
 // shared memory of k_bottom_smem: six arrays per level and the dense inverse
 template <typename T>
 inline size_t bottom_smem_bytes(const BottomArgs<T> &a) {
-    const size_t nd = (size_t)a.L[a.dl].nx * a.L[a.dl].ny;
-    return (6 * (size_t)bottom_smem_elems(a) + nd * nd) * sizeof(T);
+    return (6 * (size_t)bottom_smem_elems(a) + 64 * 64) * sizeof(T);
 }
 // first level at or below lb with at most 64 unknowns (the coarsest is 1 x 1)
 template <typename T>
@@ -373,49 +372,55 @@ inline int bottom_dense_level(const BottomArgs<T> &a) {
 
 // Exact inverse of the level operator (at most 64 unknowns), once per solve:
 // in-place Gauss-Jordan without pivoting (the operator is symmetric positive
-// definite), one CTA.  A node without a positive pivot gets x = 0.
+// definite), one CTA, on a 64 x 64 matrix (identity beyond the n unknowns) so
+// that every index is a shift.  A node without a positive pivot gets x = 0.
+// ainv is 64 x 64, row-major over the compact index (J-1)*nx + I-1.
+#define DENSE_N 64
 template <typename T>
 __global__ void __launch_bounds__(1024) k_dense_inv(const LevelT<T> L, T *ainv) {
-    __shared__ T A[64 * 64];
-    __shared__ T col[64];
-    __shared__ T s_piv;
+    __shared__ T A[DENSE_N * DENSE_N];
+    __shared__ T col[DENSE_N];
     const int nx = L.nx, n = L.nx * L.ny, t = threadIdx.x;
-    for (int q = t; q < n * n; q += 1024) {
-        const int r = q / n, cidx = q - r * n;
-        const int I = r % nx + 1, J = r / nx + 1;
-        const size_t o = (size_t)J * L.P + I;
+    for (int q = t; q < DENSE_N * DENSE_N; q += 1024) {
+        const int r = q >> 6, cidx = q & (DENSE_N - 1);
         T v = T(0);
-        if (cidx == r) v = L.mc[o];
-        else if (cidx == r + 1 && I < nx) v = -L.ce[o];
-        else if (cidx == r - 1 && I > 1) v = -L.ce[o - 1];
-        else if (cidx == r + nx) v = -L.cn[o];
-        else if (cidx == r - nx) v = -L.cn[o - L.P];
+        if (r >= n || cidx >= n) {
+            v = r == cidx ? T(1) : T(0);
+        } else {
+            const int I = r % nx + 1, J = r / nx + 1;
+            const size_t o = (size_t)J * L.P + I;
+            if (cidx == r) v = L.mc[o];
+            else if (cidx == r + 1 && I < nx) v = -L.ce[o];
+            else if (cidx == r - 1 && I > 1) v = -L.ce[o - 1];
+            else if (cidx == r + nx) v = -L.cn[o];
+            else if (cidx == r - nx) v = -L.cn[o - L.P];
+        }
         A[q] = v;
     }
     __syncthreads();
+    const int j = t & (DENSE_N - 1), i0 = t >> 6;   // this thread's column, first row
     for (int k = 0; k < n; k++) {
-        // column k as it stands, and the pivot, before anything changes
-        if (t < n) col[t] = A[t * n + k];
-        if (t == 0) s_piv = A[k * n + k];
+        // column k and the pivot as they stand
+        if (t < DENSE_N) col[t] = A[(t << 6) + k];
         __syncthreads();
-        const T piv = s_piv;
+        const T piv = col[k];
         const bool ok = piv > T(0);
-        // row k: A[k][j] /= piv, with A[k][k] = 1/piv
-        for (int j = t; j < n; j += 1024) {
-            if (!ok) A[k * n + j] = T(0);
-            else A[k * n + j] = (j == k ? T(1) : A[k * n + j]) / piv;
+        // row k: A[k][j] /= piv, with A[k][k] = 1/piv (64 threads)
+        if (t < DENSE_N) {
+            const int jj = t;
+            A[(k << 6) + jj] = ok ? (jj == k ? T(1) : A[(k << 6) + jj]) / piv : T(0);
         }
         __syncthreads();
         // other rows: A[i][j] -= col_i A[k][j] (j != k), A[i][k] = -col_i A[k][k]
-        for (int q = t; q < n * n; q += 1024) {
-            const int i = q / n, j = q - i * n;
+        const T akj = A[(k << 6) + j];
+        for (int i = i0; i < DENSE_N; i += 1024 / DENSE_N) {
             if (i == k) continue;
-            if (j == k) A[q] = -col[i] * A[k * n + k];
-            else A[q] = A[q] - col[i] * A[k * n + j];
+            const int q = (i << 6) + j;
+            A[q] = j == k ? -col[i] * akj : A[q] - col[i] * akj;
         }
         __syncthreads();
     }
-    for (int q = t; q < n * n; q += 1024) ainv[q] = A[q];
+    for (int q = t; q < DENSE_N * DENSE_N; q += 1024) ainv[q] = A[q];
 }
 template <typename T>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs<T> a) {
@@ -424,7 +429,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
     const int tot = bottom_smem_elems(a);
     T *base = (T *)sm_raw;
     const int nd = a.L[a.dl].nx * a.L[a.dl].ny;
-    T *sinv = base + 6 * tot;
+    T *sinv = base + 6 * tot;   // DENSE_N x DENSE_N
     LevelT<T> S[FS_MG_MAX_LEVELS];
     {
         int off = 0;
@@ -445,7 +450,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
             }
             off += n;
         }
-        for (int q = t; q < nd * nd; q += BOTTOM_THREADS) sinv[q] = a.ainv[q];
+        for (int q = t; q < DENSE_N * DENSE_N; q += BOTTOM_THREADS) sinv[q] = a.ainv[q];
     }
     __syncthreads();
     auto sweep = [&](const LevelT<T> &L, int color, int zero) {
@@ -477,7 +482,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         const LevelT<T> c = S[a.dl];
         if (t < nd) {
             T acc = T(0);
-            for (int j = 0; j < nd; j++) acc += sinv[t * nd + j] * c.rhs[(j / c.nx + 1) * c.P + j % c.nx + 1];
+            for (int j = 0; j < nd; j++) acc += sinv[t * DENSE_N + j] * c.rhs[(j / c.nx + 1) * c.P + j % c.nx + 1];
             c.x[(t / c.nx + 1) * c.P + t % c.nx + 1] = acc;
         }
         __syncthreads();
