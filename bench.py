@@ -265,6 +265,54 @@ def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
             "training": train, "network_switched_off_in_last_solve": off}
 
 
+def run_sweep(args):
+    """--sweep: the batched uneven sweep.  Aggregate steps/s of `sweep_count`
+    independent discharges (grid sizes 64..512 squared, voltage, pressure and
+    gamma drawn from a seed), each advanced `sweep_steps` main-loop iterations:
+    one after another (the sequential baseline), all together through the
+    batch driver with the fixed smoother schedule, and all together with the
+    schedule the autotuner picks per grid size."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from fluidsim_gb300 import abi, sweep
+    specs = sweep.sweep_specs(args.sweep_count, seed=0)
+    res = {}
+    t0 = time.perf_counter()
+    choice, table = sweep.autotune(specs, abi.FS_PREC_FP64, nthreads=args.sweep_threads)
+    t_tune = time.perf_counter() - t0
+    for name, threads, sched in (("sequential_fixed", 1, None), ("batched_fixed", args.sweep_threads, None),
+                                 ("batched_autotuned", args.sweep_threads, choice)):
+        ds = sweep.make_discharges(specs, abi.FS_PREC_FP64, sched)
+        try:
+            rate, el, stats, rcs = sweep.run(ds, args.sweep_steps, threads)
+        finally:
+            sweep.close(ds)
+        res[name] = {"steps_per_s": rate, "seconds": el, "failed": [i for i, r in enumerate(rcs) if r != 0],
+                     "idc_first8": [s["idc"] for s in stats[:8]]}
+    line = {
+        "metric": "aggregate steps/s, %d-discharge uneven sweep (grids 64-512^2)" % args.sweep_count,
+        "value": res["batched_autotuned"]["steps_per_s"], "unit": UNIT, "n_gpus": 1,
+        "steps": args.sweep_steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic: seeded sweep of V ~ U(150,400) V, p ~ logU(0.5,10) Torr, "
+                                "gamma ~ U(0.03,0.12), Gaussian-blob initial states",
+        "config": {"workload": "batched uneven sweep", "instances": args.sweep_count,
+                   "steps_per_instance": args.sweep_steps, "host_threads": args.sweep_threads,
+                   "sizes": {str(n): sum(1 for s in specs if s["n"] == n) for n in sweep.SIZES}},
+        "runs": res,
+        "speedup_batched_autotuned_vs_sequential": res["batched_autotuned"]["steps_per_s"]
+                                                   / res["sequential_fixed"]["steps_per_s"],
+        "speedup_autotuned_vs_fixed": res["batched_autotuned"]["steps_per_s"]
+                                      / res["batched_fixed"]["steps_per_s"],
+        "autotune": {"mg_smooth_by_size": {str(k): v for k, v in choice.items()},
+                     "steps_per_s_by_size": {str(k): {str(nu): r for nu, r in v.items()} for k, v in table.items()},
+                     "seconds": t_tune},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -445,11 +493,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the mixed-precision comparison run")
+    ap.add_argument("--sweep", action="store_true", help="the batched uneven sweep instead")
+    ap.add_argument("--sweep-count", type=int, default=192)
+    ap.add_argument("--sweep-steps", type=int, default=40)
+    ap.add_argument("--sweep-threads", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.sweep:
+        return run_sweep(args)
     return run_gpu(args)
 
 

@@ -64,6 +64,9 @@ def load_library():
                                         C.POINTER(C.c_int64), C.POINTER(i32)])):
         getattr(lib, name).argtypes = args
         getattr(lib, name).restype = C.c_int
+    lib.fs_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                 C.POINTER(abi.FsStats), C.POINTER(C.c_int32)]
+    lib.fs_batch_run.restype = C.c_int
     _lib = lib
     return lib
 
@@ -305,3 +308,24 @@ class Discharge(Handle):
         self.check(self._lib.fs_lpc_grad(self.ctx, f(feat), f(tgt), f(mask), feat.shape[0], f(g),
                                          C.byref(loss), f(pred)))
         return loss.value, g, pred
+
+
+def batch_run(discharges, steps, t_end=0.0, nthreads=32, check=True):
+    """Advance independent discharges concurrently in the library (fs_batch_run):
+    `steps` main-loop iterations each, or until t >= t_end (nondimensional,
+    0 = no limit).  Returns (stats dicts, return codes); with check, raises
+    if any instance failed."""
+    lib = load_library()
+    n = len(discharges)
+    arr = (C.c_void_p * n)(*[d.ctx for d in discharges])
+    st = (abi.FsStats * n)()
+    rcs = (C.c_int32 * n)()
+    rc = lib.fs_batch_run(arr, n, int(steps), float(t_end), int(nthreads), st, rcs)
+    out = [st[i].as_dict() for i in range(n)]
+    for d, s in zip(discharges, out):
+        d.t, d.dt, d.ts = s["t"], s["dt"], s["steps"]
+    if rc != abi.FS_OK and check:
+        bad = [i for i in range(n) if rcs[i] != 0]
+        raise FluidsimError(rc, "batch: instances %s failed (first: %s)" % (
+            bad[:8], discharges[bad[0]].last_error() if bad else ""))
+    return out, list(rcs)

@@ -250,6 +250,7 @@ int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, 
 int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float *mask, int batch, float *grad,
                      float *loss, float *pred);
 // misc device helpers (fs_api.cu)
+int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out);
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
 int fs_sync_ctrl(fs_ctx *c);
 // profiler: bracket one launch; drained at every fs_sync_ctrl

@@ -1,0 +1,82 @@
+"""Sweeps of the 2D argon DC glow: many independent discharges of uneven grid
+sizes (the voltage / pressure runs behind the reference's I-V curves,
+plot-idvd.py), advanced together by the library's batch driver, and a small
+autotuner that picks the multigrid smoother schedule per grid size.
+
+Workload: `count` discharges with grid sizes drawn uniformly from SIZES
+(squared), cathode voltage uniform in 150-400 V, pressure log-uniform in
+0.5-10 Torr and secondary-emission coefficient uniform in 0.03-0.12, each from
+its own seeded Gaussian-blob initial state with 1% noise.
+"""
+import time
+
+import numpy as np
+
+from . import abi, api, config, grid
+
+SIZES = (64, 96, 128, 192, 256, 384, 512)
+
+
+def sweep_specs(count=192, seed=0):
+    """The seeded draw of the sweep's instances: list of dicts."""
+    rng = np.random.default_rng(seed)
+    n = rng.choice(SIZES, size=count)
+    v = rng.uniform(150.0, 400.0, size=count)
+    p = np.exp(rng.uniform(np.log(0.5), np.log(10.0), size=count))
+    g = rng.uniform(0.03, 0.12, size=count)
+    return [dict(n=int(n[i]), volts=float(v[i]), p_torr=float(p[i]), gam=float(g[i]), seed=int(seed * 1000 + i))
+            for i in range(count)]
+
+
+def make_config(spec, precision=abi.FS_PREC_FP64, mg_smooth=2, rtol=1e-8):
+    return config.glow(spec["n"], p_torr=spec["p_torr"], gam=spec["gam"], vl=-spec["volts"] / config.PH0,
+                       lapl_rtol=rtol, lapl_maxit=500, precision=precision, mg_smooth=mg_smooth)
+
+
+def make_discharges(specs, precision=abi.FS_PREC_FP64, schedule=None):
+    """One context per spec; schedule maps grid size -> mg_smooth (default 2)."""
+    out = []
+    for s in specs:
+        nu = (schedule or {}).get(s["n"], 2)
+        cfg = make_config(s, precision, nu)
+        mesh = cfg.mesh()
+        k = api.constants(cfg)
+        st = grid.blob_state(mesh, k, noise=0.01, seed=s["seed"], vl=cfg.vl)
+        out.append(api.Discharge(cfg, mesh, st))
+    return out
+
+
+def run(discharges, steps, nthreads, warm=3):
+    """Warm up (start-up iterations and `warm` steps, untimed), then time
+    `steps` main-loop iterations of every discharge with `nthreads` host
+    threads.  Returns (aggregate steps/s, seconds, stats, return codes)."""
+    api.batch_run(discharges, 2 + warm, nthreads=nthreads, check=False)
+    t0 = time.perf_counter()
+    stats, rcs = api.batch_run(discharges, steps, nthreads=nthreads, check=False)
+    el = time.perf_counter() - t0
+    ok = sum(1 for r in rcs if r == 0)
+    return ok * steps / el, el, stats, rcs
+
+
+def close(discharges):
+    for d in discharges:
+        d.close()
+
+
+def autotune(specs, precision=abi.FS_PREC_FP64, candidates=(1, 2, 3), per_size=4, steps=6, nthreads=32):
+    """For every grid size in specs, time up to `per_size` of its instances
+    with each smoother schedule (mg_smooth = pre- and post-sweeps per level)
+    and keep the fastest.  Returns ({size: mg_smooth}, {size: {nu: steps/s}})."""
+    choice, table = {}, {}
+    for n in sorted({s["n"] for s in specs}):
+        sub = [s for s in specs if s["n"] == n][:per_size]
+        table[n] = {}
+        for nu in candidates:
+            ds = make_discharges(sub, precision, {n: nu})
+            try:
+                rate, _, _, rcs = run(ds, steps, nthreads, warm=2)
+                table[n][nu] = rate if all(r == 0 for r in rcs) else 0.0
+            finally:
+                close(ds)
+        choice[n] = max(table[n], key=table[n].get)
+    return choice, table

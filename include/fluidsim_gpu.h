@@ -237,6 +237,20 @@ int64_t fs_launch_count(fs_ctx *ctx);
  * GPU work overlaps race on it.  ctx's device must be current. */
 int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
 
+/* ---- Many independent discharges (voltage / pressure sweeps).  No single
+ * counterpart in the reference, which runs one discharge per invocation
+ * (main.F90) and builds I-V curves from many runs.  Advances the n contexts
+ * concurrently with nthreads host threads (one discharge per thread at a
+ * time, largest grids first): each runs `steps` main-loop iterations as
+ * fs_run does, stopping early once its time reaches t_end (t_end <= 0: no
+ * limit).  Contexts keep their own adaptive dt and convergence.  out[i]
+ * (may be NULL) gets instance i's statistics -- its electrode currents are
+ * the last step's -- and rc_out[i] (may be NULL) its return code; the call
+ * returns the first nonzero code, or FS_OK.  No context may be used by
+ * another thread during the call. */
+int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
+                 int32_t *rc_out);
+
 /* ---- Learned Poisson preconditioner (FS_PREC_MIXED contexts only).  No
  * counterpart in the reference, which hands the system to PETSc
  * (lapl_lib.F90:83-104).  A small BF16 convolutional network (~250k
