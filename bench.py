@@ -265,6 +265,62 @@ def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
             "training": train, "network_switched_off_in_last_solve": off}
 
 
+def run_accuracy(args):
+    """--accuracy: per-field error of the mixed-precision path against the FP64
+    path after `acc_steps` adaptive steps of the workload.  The FP64 run
+    replays the mixed run's accepted step sizes with the controller off, so
+    both integrate the same step sequence (two adaptive runs choose slightly
+    different dt and drift apart in time); the FP64 GPU path matches the CPU
+    oracle to 1e-10 (64x64: 4e-14 after 2000 fixed-dt steps)."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from fluidsim_gb300 import abi, api
+    cfg = workload(args.n, "adaptive")
+    cfgm = workload(args.n, "adaptive", precision="mixed")
+    mesh = cfg.mesh()
+    k = api.constants(cfg)
+    st = initial_state(cfg, mesh, k)
+    a = api.Discharge(cfg.replace(adaptive=0), mesh, st)
+    b = api.Discharge(cfgm, mesh, st)
+
+    def errs(gm, gf):
+        out = {}
+        for f in ("ni", "ne", "nt"):
+            x, y = np.asarray(gm[f])[1:-1, 1:-1], np.asarray(gf[f])[1:-1, 1:-1]
+            out[f] = {"linf_rel": float(np.max(np.abs(x - y) / (np.abs(y) + k["n_zero"]))),
+                      "l2_rel": float(np.linalg.norm(x - y) / np.linalg.norm(y))}
+        x, y = np.asarray(gm["ph"])[1:-1, 1:-1], np.asarray(gf["ph"])[1:-1, 1:-1]
+        out["ph"] = {"linf_rel": float(np.max(np.abs(x - y)) / np.max(np.abs(y))),
+                     "l2_rel": float(np.linalg.norm(x - y) / np.linalg.norm(y))}
+        return out
+
+    marks = sorted({m for m in (10, 100, 500, 1000, args.acc_steps) if m <= args.acc_steps})
+    rows = []
+    max_relres = 0.0
+    for s in range(1, args.acc_steps + 1):
+        gb = b.step()
+        if gb["lerr"]:
+            raise RuntimeError("mixed Poisson solve failed at step %d" % s)
+        max_relres = max(max_relres, gb["relres"])
+        if a.ts > 1:
+            a.dt = b.stats()["dt_step"]
+            a.ptcl_step()
+        a.dt = b.dt
+        if a.lapl_solve()["lerr"]:
+            raise RuntimeError("FP64 Poisson solve failed at step %d" % s)
+        a.accept()
+        if s in marks:
+            rows.append({"step": s, "t_s": b.t * 1e-6, "errors": errs(b.download(), a.download())})
+    line = {"metric": "per-field relative error, mixed vs FP64, %dx%d glow" % (args.n, args.n),
+            "steps": args.acc_steps, "max_mixed_relres": max_relres, "poisson_rtol": cfg.lapl_rtol,
+            "checkpoints": rows}
+    print(json.dumps(line))
+    return 0
+
+
 def run_sweep(args):
     """--sweep: the batched uneven sweep.  Aggregate steps/s of `sweep_count`
     independent discharges (grid sizes 64..512 squared, voltage, pressure and
@@ -494,6 +550,9 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the mixed-precision comparison run")
     ap.add_argument("--sweep", action="store_true", help="the batched uneven sweep instead")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="per-field error of the mixed path against the FP64 path instead")
+    ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--sweep-count", type=int, default=192)
     ap.add_argument("--sweep-steps", type=int, default=40)
     ap.add_argument("--sweep-threads", type=int, default=32)
@@ -504,6 +563,8 @@ def main():
         return run_reference(args)
     if args.sweep:
         return run_sweep(args)
+    if args.accuracy:
+        return run_accuracy(args)
     return run_gpu(args)
 
 
