@@ -152,8 +152,10 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
     if ((long)cfg->nx * cfg->ny > (1L << 28))
         return fs_set_error(nullptr, FS_ERR_INVALID, "grid too large");
     if (cfg->nspecies != 3 && cfg->nspecies != 4) return fs_set_error(nullptr, FS_ERR_INVALID, "nspecies must be 3 or 4");
-    if (cfg->coef_mode != FS_COEF_TABLE)
-        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the tabulated coefficient mode runs on the GPU");
+    if (cfg->coef_mode != FS_COEF_TABLE && cfg->coef_mode != FS_COEF_FITS)
+        return fs_set_error(nullptr, FS_ERR_INVALID, "unknown coefficient mode %d", cfg->coef_mode);
+    if (cfg->coef_mode == FS_COEF_FITS && cfg->precision != FS_PREC_FP64)
+        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "the fit coefficient mode runs on the FP64 path only");
     if (cfg->table_n < 2 || !(cfg->table_emax_ev > cfg->table_emin_ev) || !(cfg->table_emin_ev > 0))
         return fs_set_error(nullptr, FS_ERR_INVALID, "bad coefficient table range");
     if (cfg->rf != 0) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the DC source (rf = 0) is implemented");
@@ -280,6 +282,8 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     pp.ve_coef = (16.0 * k.e * k.ph0) / (3.0 * k.pi * k.me);
     pp.tg_term = k.tg * k.kb / k.e / k.ph0;
     pp.e100 = std::exp(-100.0);
+    pp.fits = cfg->coef_mode == FS_COEF_FITS;
+    pp.fit = fs_fit_eval(k);
 
     // mesh blob: dx, inv_dx (nx+1), dy, inv_dy (ny+1), dlx, inv_dlx (nx), dly, inv_dly (ny),
     // r (ny+2), dr_a, dr_c (ny+2)

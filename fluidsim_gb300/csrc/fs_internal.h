@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/fluidsim_gpu.h"
+#include "fs_fits.h"
 
 #define FS_MAX_SPECIES 4
 #define FS_NBUF 5            // level/stage buffers per species
@@ -37,6 +38,8 @@ struct PhysParams {
     double ve_coef;                // (16 e ph0)/(3 pi me): ve = sqrt(ve_coef*Te)*t0/x0
     double tg_term;                // Tg*kb/e/ph0 (ptcl_lib.F90:508)
     double e100;                   // exp(-100): the SG exponent clamp
+    int fits;                      // coefficients from the fits per node (FS_COEF_FITS) instead of the table
+    FitEval fit;
 };
 
 // FP32 copies of the constants the mixed-precision kernels use, formed once on

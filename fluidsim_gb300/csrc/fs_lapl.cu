@@ -167,9 +167,14 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
             if ((nte >= 0.0) && (nee >= 0.0)) te = nte / nee;
             else { st |= FS_ST_NEG_DENSITY; te = 1e-8; }
             int k; double w;
-            tab_index(pp, te, k, w);
-            mu = tab_val(a.tab, k, w, 0);
-            de = tab_val(a.tab, k, w, 1);
+            if (pp.fits) {
+                mu = pp.fit.mue(te);
+                de = pp.fit.De(te);
+            } else {
+                tab_index(pp, te, k, w);
+                mu = tab_val(a.tab, k, w, 0);
+                de = tab_val(a.tab, k, w, 1);
+            }
         }
         s_te[ly][lx] = te; s_mu[ly][lx] = mu; s_de[ly][lx] = de;
     }

@@ -176,9 +176,15 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             if ((nte >= 0.0) && (nee >= 0.0)) te = nte / nee;
             else { st |= FS_ST_NEG_DENSITY; te = 1e-8; }
             int k; double w;
-            tab_index(pp, te, k, w);
-            mu = tab_val(a.tab, k, w, 0);
-            de = tab_val(a.tab, k, w, 1);
+            if (pp.fits) {
+                k = 0; w = 0.0;
+                mu = pp.fit.mue(te);
+                de = pp.fit.De(te);
+            } else {
+                tab_index(pp, te, k, w);
+                mu = tab_val(a.tab, k, w, 0);
+                de = tab_val(a.tab, k, w, 1);
+            }
             if (lx >= 1 && lx <= BX && ly >= 1 && ly <= BY) { s_k[ly - 1][lx - 1] = k; s_w[ly - 1][lx - 1] = w; }
         }
         s_te[ly][lx] = te; s_mue[ly][lx] = mu; s_de[ly][lx] = de;
@@ -294,8 +300,11 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         const double nm = NS == 4 ? s_n[3][hy][hx] : 0.0;
         const int kk = s_k[ly][lx];
         const double w = s_w[ly][lx];
-        const double k_ir = tab_val(a.tab, kk, w, 2), k_ex = tab_val(a.tab, kk, w, 3);
-        const double nu = tab_val(a.tab, kk, w, 4), beta = tab_val(a.tab, kk, w, 5);
+        const bool fits = pp.fits;
+        const double k_ir = fits ? pp.fit.k_ir_fit(te) : tab_val(a.tab, kk, w, 2);
+        const double k_ex = fits ? pp.fit.k_ex(te) : tab_val(a.tab, kk, w, 3);
+        const double nu = fits ? pp.fit.nu(te) : tab_val(a.tab, kk, w, 4);
+        const double beta = fits ? pp.fit.beta(te) : tab_val(a.tab, kk, w, 5);
         const double idlx = a.m.inv_dlx[gi - 1], idly = a.m.inv_dly[gj - 1];
         double dfdx[NS], dfdy[NS];
         if (pp.cyl) {
@@ -319,8 +328,8 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         double term_sie = k_ir * pp.ninf * ne - beta * ni * ne;
         double k_si = 0, k_sc = 0;
         if (NS == 4) {
-            k_sc = tab_val(a.tab, kk, w, 6);
-            k_si = tab_val(a.tab, kk, w, 7);
+            k_sc = fits ? pp.fit.k_sc(te) : tab_val(a.tab, kk, w, 6);
+            k_si = fits ? pp.fit.k_si(te) : tab_val(a.tab, kk, w, 7);
             term_sie = term_sie + k_si * nm * ne + pp.k_mp * (nm * nm);
         }
         const double term_st1 = -(fex * exa + fey * eya);
