@@ -67,6 +67,8 @@ def load_library():
     lib.fs_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                  C.POINTER(abi.FsStats), C.POINTER(C.c_int32)]
     lib.fs_batch_run.restype = C.c_int
+    lib.fs_write_output.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
+    lib.fs_write_output.restype = C.c_int
     _lib = lib
     return lib
 
@@ -257,6 +259,10 @@ class Discharge(Handle):
         v = C.c_double()
         self.check(self._lib.fs_max_ne(self.ctx, C.byref(v)))
         return v.value
+
+    def write_output(self, directory, init=False):
+        """The reference's output files in `directory` (see fs_write_output)."""
+        self.check(self._lib.fs_write_output(self.ctx, os.fsencode(directory), 1 if init else 0))
 
     # -- learned Poisson preconditioner (mixed contexts) -----------------------
     def lpc_init(self, level=3, max_batch=16, max_samples=512, seed=0):

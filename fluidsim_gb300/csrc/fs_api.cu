@@ -294,6 +294,11 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     for (int j = 0; j <= ny; j++) inv_dy[j] = 1.0 / m->dy[j];
     for (int i = 0; i < nx; i++) inv_dlx[i] = 1.0 / m->dlx[i];
     for (int j = 0; j < ny; j++) inv_dly[j] = 1.0 / m->dly[j];
+    // node coordinates for the output writer: x(1) = 0, x(i+1) = x(i) + dx(i)
+    c->h_x.assign(nx + 2, 0.0);
+    c->h_y.assign(ny + 2, 0.0);
+    for (int i = 0; i <= nx; i++) c->h_x[i + 1] = c->h_x[i] + m->dx[i];
+    for (int j = 0; j <= ny; j++) c->h_y[j + 1] = c->h_y[j] + m->dy[j];
     // circ_step current weights per row (circ_lib.F90:87-151)
     c->h_dr_a.assign(ny + 2, 0.0);
     c->h_dr_c.assign(ny + 2, 0.0);

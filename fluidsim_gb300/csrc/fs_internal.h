@@ -141,6 +141,7 @@ struct fs_ctx {
     std::vector<double> h_dr_a, h_dr_c;
     std::vector<int32_t> h_tx, h_ty;
     std::vector<double> h_r;
+    std::vector<double> h_x, h_y;   // node coordinates, ghost ring included (x(1) = y(1) = 0)
 
     // table
     double *d_tab;

@@ -237,6 +237,14 @@ int64_t fs_launch_count(fs_ctx *ctx);
  * GPU work overlaps race on it.  ctx's device must be current. */
 int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
 
+/* The reference's output files (props.F90:239-320 set-up, writeOut
+ * main.F90:297-333), written into directory dir: init = 1 creates
+ * meshx.dat / meshy.dat and empties f1..f5.dat, time.dat, vd.dat, ida.dat,
+ * idc.dat, dt.dat, flx.dat; init = 0 appends the current state -- raw native
+ * FP64, same units and layout as the reference, so its save.py reads them.
+ * With three species f5.dat gets zeros; flx.dat (the EM flux) gets 0. */
+int fs_write_output(fs_ctx *ctx, const char *dir, int32_t init);
+
 /* ---- Many independent discharges (voltage / pressure sweeps).  No single
  * counterpart in the reference, which runs one discharge per invocation
  * (main.F90) and builds I-V curves from many runs.  Advances the n contexts
