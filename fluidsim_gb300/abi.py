@@ -121,6 +121,8 @@ def declare_api(lib, prefix):
         "reject": ([vp], C.c_int),
         "run": ([vp, C.c_int32, P(FsStats)], C.c_int),
         "get_stats": ([vp, P(FsStats)], C.c_int),
+        "get_surface_charge": ([vp, dp, dp, dp], C.c_int),
+        "set_surface_charge": ([vp, dp, dp, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, prefix + name)

@@ -155,6 +155,20 @@ class Handle:
             abi.dptr(out["nm"]), abi.dptr(out["ph"]), self.nx + 2, nlev))
         return out
 
+    def surface_charge(self):
+        """sfc_lib's sig_pl, sig_mi, sig_or (nx+2 entries each, Fortran index
+        i at [i-1]): the charge of the dielectric wall (type_y == 3) nodes."""
+        out = [np.zeros(self.nx + 2) for _ in range(3)]
+        self.check(self._f("get_surface_charge")(self.ctx, *[abi.dptr(a) for a in out]))
+        return dict(zip(("sig_pl", "sig_mi", "sig_or"), out))
+
+    def set_surface_charge(self, sig_pl=None, sig_mi=None, sig_or=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (sig_pl, sig_mi, sig_or)]
+        for a in arrs:
+            if a is not None and a.shape != (self.nx + 2,):
+                raise ValueError("surface charge arrays have nx+2 entries")
+        self.check(self._f("set_surface_charge")(self.ctx, *[abi.dptr(a) for a in arrs]))
+
     # -- the reference's subroutines -----------------------------------------
     def ptcl_step(self):
         dt = C.c_double(self.dt)

@@ -55,6 +55,7 @@ class RunConfig:
     mesh_law: str = "geometric"
     mesh_ratio: float = 1.05
     mesh_cap: float = 4.0
+    rwall: bool = False                  # dielectric upper wall (type_y = 3) instead of Neumann
     dt0: float = 1e-12 / T0
 
     def c_struct(self):
@@ -68,7 +69,7 @@ class RunConfig:
 
     def mesh(self):
         return make_mesh(self.nx, self.ny, self.l, self.w, self.ew, self.gap,
-                         self.mesh_law, self.mesh_ratio, self.mesh_cap)
+                         self.mesh_law, self.mesh_ratio, self.mesh_cap, self.rwall)
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)

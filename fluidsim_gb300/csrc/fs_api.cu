@@ -165,9 +165,12 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
     if (cfg->lapl_maxit < 1) return fs_set_error(nullptr, FS_ERR_INVALID, "lapl_maxit must be positive");
     for (long q = 0; q < (long)cfg->nx * cfg->ny; q++) {
         int tx = m->type_x[q], ty = m->type_y[q];
-        if (tx < -2 || tx > 2 || ty < -2 || ty > 2)
-            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "node type (%d,%d) at %ld not supported "
-                                "(dielectric walls need the surface-charge model)", tx, ty, q);
+        if (tx < -2 || tx > 2 || ty < -2 || ty > 3)
+            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "node type (%d,%d) at %ld not supported", tx, ty, q);
+        if (ty == 3 && q / cfg->nx != cfg->ny - 1)   // g_init puts the wall on the last row only
+            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "dielectric wall node off the last row at %ld", q);
+        if (ty == 3 && cfg->precision != FS_PREC_FP64)
+            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "the dielectric wall runs on the FP64 path only");
     }
     return FS_OK;
 }
@@ -188,6 +191,7 @@ void free_ctx(fs_ctx *c) {
     cudaFree(c->ph_mi);
     cudaFree(c->d_part);
     cudaFree(c->d_rows);
+    cudaFree(c->d_sig);
     double *faces[] = {c->fx_e, c->fx_cl, c->fx_cr, c->fy_e, c->fy_cl, c->fy_cr,
                        c->fx_dl, c->fx_dr, c->fy_dl, c->fy_dr};
     for (double *f : faces) cudaFree(f);
@@ -319,6 +323,7 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     for (size_t q = 0; q < (size_t)nx * ny; q++) {
         types[q] = (int8_t)m->type_x[q];
         types[(size_t)nx * ny + q] = (int8_t)m->type_y[q];
+        if (m->type_y[q] == 3) c->rwall = 1;
     }
     CK(cudaMalloc(&c->d_types, types.size()), "cudaMalloc types");
     CK(cudaMemcpy(c->d_types, types.data(), types.size(), cudaMemcpyHostToDevice), "types upload");
@@ -498,6 +503,13 @@ int fs_accept(fs_ctx *c) {
     c->lev[1] = c->lev[0];   // n2 <- n1
     c->Vd_or = c->Vd_mi;
     c->Vd_mi = c->Vd_pl;
+    if (c->rwall) {   // sig_or <- sig_mi, sig_mi <- sig_pl: rotate the slots, sig_pl keeps its values
+        const int pl = c->sig_slot[0], mi = c->sig_slot[1], orr = c->sig_slot[2];
+        c->sig_slot[2] = mi;
+        c->sig_slot[1] = pl;
+        c->sig_slot[0] = orr;
+        return fs_sig_copy(c, 0, 1);
+    }
     return FS_OK;
 }
 
@@ -507,6 +519,8 @@ int fs_reject(fs_ctx *c) {
     c->lev[1] = c->lev[2];   // n2 <- n3
     c->Vd_pl = c->Vd_or;
     c->Vd_mi = c->Vd_or;
+    int rc;
+    if (c->rwall && ((rc = fs_sig_copy(c, 0, 2)) || (rc = fs_sig_copy(c, 1, 2)))) return rc;
     return set_dt_dev(c, c->dt / 2.0);
 }
 
@@ -534,6 +548,32 @@ int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out) {
         }
     }
     return fs_get_stats(c, out);
+}
+
+int fs_get_surface_charge(fs_ctx *c, double *sig_pl, double *sig_mi, double *sig_or) {
+    if (!c) return FS_ERR_INVALID;
+    double *dst[3] = {sig_pl, sig_mi, sig_or};
+    for (int q = 0; q < 3; q++) {
+        if (!dst[q]) continue;
+        cudaError_t e = cudaMemcpyAsync(dst[q], fs_sig(c, q), sizeof(double) * (c->nx + 2), cudaMemcpyDeviceToHost,
+                                        c->stream);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "surface charge download");
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "surface charge download");
+}
+
+int fs_set_surface_charge(fs_ctx *c, const double *sig_pl, const double *sig_mi, const double *sig_or) {
+    if (!c) return FS_ERR_INVALID;
+    const double *src[3] = {sig_pl, sig_mi, sig_or};
+    for (int q = 0; q < 3; q++) {
+        if (!src[q]) continue;
+        cudaError_t e = cudaMemcpyAsync(fs_sig(c, q), src[q], sizeof(double) * (c->nx + 2), cudaMemcpyHostToDevice,
+                                        c->stream);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "surface charge upload");
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "surface charge upload");
 }
 
 int fs_get_stats(fs_ctx *c, fs_stats *out) {

@@ -40,6 +40,26 @@ struct FitEval {
               + FS_F32(-3.57242763244f) * q3(x) + FS_F32(0.486276623664f) * q4(x) + FS_F32(-0.0259045697422f) * q5(x);
         return exp(s) * x0 / ninf * t0 * ph0;
     }
+    // get_mut (ptcl_props.F90:223-250): same range and branch point as get_mue
+    FS_HD double mut(double T) const {
+        double x = clog(2.34e-1, 1.57e2, T), s;
+        if (x < th_mue)
+            s = FS_F32(58.1354622038f) + FS_F32(-1.29918391109f) * x + FS_F32(-0.106559658509f) * q2(x)
+              + FS_F32(-0.0202265418394f) * q3(x) + FS_F32(-0.0286667333915f) * q4(x) + FS_F32(0.022457210094f) * q5(x);
+        else
+            s = FS_F32(68.2627663433f) + FS_F32(-19.3524000831f) * x + FS_F32(11.3251980583f) * q2(x)
+              + FS_F32(-3.24070386509f) * q3(x) + FS_F32(0.449848156054f) * q4(x) + FS_F32(-0.0242585762405f) * q5(x);
+        return exp(s) * x0 / ninf * t0 * ph0;
+    }
+    // get_Dt (ptcl_props.F90:293-316)
+    FS_HD double Dt(double T) const {
+        double x = clog(2.34e-1, 1.57e2, T);
+        double s = FS_F32(57.7214952841f) + FS_F32(-0.353731464348f) * x + FS_F32(-0.00505156731795f) * q2(x)
+                 + FS_F32(0.161173720584f) * q3(x) + FS_F32(-0.196610345869f) * q4(x) + FS_F32(-0.0719115643218f) * q5(x)
+                 + FS_F32(0.11874085868f) * q6(x) + FS_F32(-0.00669712724784f) * q7(x) + FS_F32(-0.0236445308504f) * q8(x)
+                 + FS_F32(0.00917326671764f) * q9(x) + FS_F32(-0.00135453096483f) * q10(x) + FS_F32(7.26379684461e-05f) * q11(x);
+        return exp(s) * x0 / ninf * t0;
+    }
     FS_HD double De(double T) const {
         double x = clog(2.34e-1, 1.57e2, T);
         double s = FS_F32(57.7067018813f) + FS_F32(-0.0699892875381f) * x + FS_F32(-0.117645585949f) * q2(x)

@@ -153,6 +153,12 @@ struct fs_ctx {
     double *d_part;              // per-block partial sums (4 species)
     int nblk_stage;              // blocks of one stage launch
     double *d_rows;              // per-row current contributions (2*(ny+2))
+    // sfc_lib state (dielectric wall, type_y == 3 on the last row): three
+    // slots of nx+2 charges (Fortran sig(i) at [i-1]) holding sig_pl, sig_mi,
+    // sig_or by sig_slot[0..2], then the five Merson slopes ks(:, stage)
+    double *d_sig;
+    int sig_slot[3];
+    int rwall;
     // per-step face data (phi is frozen during ptcl_step): field E and the
     // ion SG flux coefficients, flux = cl*n_left - cr*n_right, for the x face
     // east of node (gi,gj) and the y face north of it
@@ -238,6 +244,10 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres);
 int fs_ptcl_alloc(fs_ctx *c);
 void fs_ptcl_reset(fs_ctx *c);     // t_m, status and current rows of a new step
 int fs_ptcl_control(fs_ctx *c);   // controller + status check after five stages
+// surface charge slot `which` (0 sig_pl, 1 sig_mi, 2 sig_or) and the slopes
+inline double *fs_sig(fs_ctx *c, int which) { return c->d_sig + (size_t)c->sig_slot[which] * (c->nx + 2); }
+inline double *fs_sig_ks(fs_ctx *c) { return c->d_sig + (size_t)3 * (c->nx + 2); }
+int fs_sig_copy(fs_ctx *c, int dst, int src);   // slot dst <- slot src, on the stream
 void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);

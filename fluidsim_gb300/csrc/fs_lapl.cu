@@ -29,6 +29,7 @@
 #include "fs_internal.h"
 
 #include "fs_mg.cuh"
+#include "fs_sg.cuh"
 
 #define LBX 32
 #define LBY 8
@@ -45,6 +46,7 @@ struct AsmArgs {
     const double *fx_e, *fx_cl, *fx_cr, *fx_dl, *fx_dr, *fy_e, *fy_cl, *fy_cr, *fy_dl, *fy_dr;
     const Ctrl *ctrl;
     Ctrl *ctrl_w;
+    const double *sig;   // sig_pl of the dielectric wall, nx+2
     double *mc, *ce, *cn, *extra, *inv_mc, *rhs, *dinv;
 };
 
@@ -262,6 +264,18 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
             cf = 1.0 / dh + dt * (dfi - dfe);
         } else if (gj == ny && tb == 1) {
             eu = 0.0;
+        } else if (gj == ny && tb == 3) {
+            // dielectric wall: field -sig (lapl_lib.F90:72-76,263-265), fluxes into an
+            // empty wall node with the node's own coefficients (:322-331); laplJ
+            // sets no column and no flux derivative for it (:548-559) but keeps
+            // the interior form of the diagonal (:590-600): a boundary
+            // conductance of 1/dy without dt terms
+            const int lc = ly;
+            E = -a.sig[gi];
+            eu = E;
+            fi = fs_sg_flux(1.0, E, dh, pp.mui, pp.Di, s_ni[lc][lx], 0.0);
+            fe = fs_sg_flux(-1.0, E, dh, s_mu[lc][lx], s_de[lc][lx], s_ne[lc][lx], 0.0);
+            cf = idh;
         } else if (gj == ny && tb == 2) {
             int lc = ly;
             double te = s_te[lc][lx], ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
@@ -334,7 +348,7 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         if (gi == 1 && tx == -2) gx += cw;
         if (gi == nx && tx == 2) gx += cee;
         if (gj == 1 && ty == -2) gys += cs;
-        if (gj == ny && ty == 2) gyn += cnn;
+        if (gj == ny && (ty == 2 || ty == 3)) gyn += cnn;
         // lower Neumann rows: the reference's diagonal takes the ghost spacing
         // dx(i-1) / dy(j-1) where the off-diagonal takes dx(i) / dy(j)
         if (gi == 1 && tx == -1) gx += 1.0 / a.m.dx[0] - 1.0 / a.m.dx[1];
@@ -717,6 +731,7 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.fy_e = c->fy_e; a.fy_cl = c->fy_cl; a.fy_cr = c->fy_cr; a.fy_dl = c->fy_dl; a.fy_dr = c->fy_dr;
     a.ctrl = c->d_ctrl;
     a.ctrl_w = c->d_ctrl;
+    a.sig = fs_sig(c, 0);
     MGLevel &m0 = c->mg[0];
     a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
     a.rhs = c->bs;   // scaled right-hand side D b

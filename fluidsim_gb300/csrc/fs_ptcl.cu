@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
+#include "fs_sg.cuh"
 
 #define BX 32
 #define BY 8
@@ -47,6 +48,8 @@ struct StageArgs {
     Ctrl *ctrl;
     double *part;     // [species][nblk] partial error sums
     double *rows;     // [2][ny+2] current rows
+    double *sig_mi, *sig_pl, *ks;   // dielectric wall charge (nx+2 each) and its 5 stage slopes
+    const double *sig_or;
     int stage;
     int nblk;
 };
@@ -131,6 +134,54 @@ __device__ __forceinline__ void sg_elec(double E, double dh, double inv_dh, doub
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Dielectric wall face of column gi (type_y == 3 on the last row): field
+// -sig_mi(i) (ptcl_lib.F90:292-294), fluxes into an empty wall node with the
+// node's own coefficients and get_mut / get_Dt for the energy (:392-406).
+// The calling thread is the only reader and writer of column gi's charge, so
+// sfc_step (sfc_lib.F90:19-80) runs here too: its slope from the same stage
+// state, then the Merson combination into sig_mi (stages 1-4) or sig_pl
+// (stage 5).  Returns the face field.  Kept out of line: it runs on one row.
+template <int NS>
+__device__ __noinline__ double wall_face(const StageArgs &a, int gi, double te, double ni, double ne, double nt,
+                                         double nm, double mue, double de, double &fi, double &fe, double &ft,
+                                         double &fm, unsigned int &st) {
+    const PhysParams &pp = a.pp;
+    const int ny = pp.ny;
+    const double E = -a.sig_mi[gi];
+    const double dh = a.m.dy[ny];
+    fi = fs_sg_flux(1.0, E, dh, pp.mui, pp.Di, ni, 0.0);
+    fe = fs_sg_flux(-1.0, E, dh, mue, de, ne, 0.0);
+    ft = fs_sg_flux(-1.0, E, dh, pp.fit.mut(te), pp.fit.Dt(te), nt, 0.0);
+    fm = NS == 4 ? pp.Dm * nm / dh : 0.0;
+    // sfc_step receives (ni, ne, nt) in its (ne, ni, nt) arguments
+    // (ptcl_lib.F90:52): its mean energy is nt/ni, its "ion" flux carries n_e
+    // and its "electron" flux n_i
+    double tes;
+    if ((nt >= 0.0) && (ni >= 0.0)) tes = nt / ni;
+    else { st |= FS_ST_NEG_DENSITY; tes = 1e-8; }
+    double mus, des;
+    if (pp.fits) {
+        mus = pp.fit.mue(tes);
+        des = pp.fit.De(tes);
+    } else {
+        int kq; double wq;
+        tab_index(pp, tes, kq, wq);
+        mus = tab_val(a.tab, kq, wq, 0);
+        des = tab_val(a.tab, kq, wq, 1);
+    }
+    const double ksv = fs_sg_flux(1.0, E, dh, pp.mui, pp.Di, ne, 0.0) - fs_sg_flux(-1.0, E, dh, mus, des, ni, 0.0);
+    const int W = pp.nx + 2, stg = a.stage;
+    a.ks[(size_t)(stg - 1) * W + gi] = ksv;
+    const double dt = a.ctrl->dt, so = a.sig_or[gi];
+    const double k1 = stg > 1 ? a.ks[gi] : ksv;
+    if (stg == 1) a.sig_mi[gi] = so + dt * k1 / 3.0;
+    else if (stg == 2) a.sig_mi[gi] = so + dt * (k1 + ksv) / 6.0;
+    else if (stg == 3) a.sig_mi[gi] = so + dt * (k1 + ksv * 3.0) / 8.0;
+    else if (stg == 4) a.sig_mi[gi] = so + dt * (k1 - a.ks[(size_t)2 * W + gi] * 3.0 + ksv * 4.0) / 2.0;
+    else a.sig_pl[gi] = so + dt * (k1 + a.ks[(size_t)3 * W + gi] * 4.0 + ksv) / 6.0;
+    return E;
 }
 
 template <int NS>
@@ -254,6 +305,10 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             // ptclEqn has no lower y electrode: zero flux, face field kept (ptcl_lib.F90:287-367)
         } else if (gj == ny && tb == 1) {
             eu = 0.0;
+        } else if (gj == ny && tb == 3) {
+            const int lc = ly;
+            eu = wall_face<NS>(a, gi, s_te[lc][lx], s_n[0][lc][lx], s_n[1][lc][lx], s_n[2][lc][lx],
+                               NS == 4 ? s_n[3][lc][lx] : 0.0, s_mue[lc][lx], s_de[lc][lx], fi, fe, ft, fm, st);
         } else if (gj == ny && tb == 2) {
             const bool low = false;
             const int lc = low ? ly + 1 : ly;
@@ -535,10 +590,20 @@ void fs_faces_update(fs_ctx *c) {
     c->faces_valid = 1;
 }
 
+int fs_sig_copy(fs_ctx *c, int dst, int src) {
+    cudaError_t e = cudaMemcpyAsync(fs_sig(c, dst), fs_sig(c, src), sizeof(double) * (c->nx + 2),
+                                    cudaMemcpyDeviceToDevice, c->stream);
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "surface charge copy");
+}
+
 int fs_ptcl_alloc(fs_ctx *c) {
     dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
     c->nblk_stage = grid.x * grid.y;
-    cudaError_t e = cudaMalloc(&c->d_part, sizeof(double) * FS_MAX_SPECIES * c->nblk_stage);
+    cudaError_t e = cudaMalloc(&c->d_sig, sizeof(double) * 8 * (c->nx + 2));
+    if (e == cudaSuccess) e = cudaMemset(c->d_sig, 0, sizeof(double) * 8 * (c->nx + 2));
+    if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc surface charge");
+    for (int q = 0; q < 3; q++) c->sig_slot[q] = q;
+    e = cudaMalloc(&c->d_part, sizeof(double) * FS_MAX_SPECIES * c->nblk_stage);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc partials");
     e = cudaMalloc(&c->d_rows, sizeof(double) * 2 * (c->ny + 2));
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc rows");
@@ -606,6 +671,10 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
         a.ctrl = c->d_ctrl;
         a.part = c->d_part;
         a.rows = c->d_rows;
+        a.sig_pl = fs_sig(c, 0);
+        a.sig_mi = fs_sig(c, 1);
+        a.sig_or = fs_sig(c, 2);
+        a.ks = fs_sig_ks(c);
         a.nblk = c->nblk_stage;
         const int ins[5] = {in1, SA, SB, SA, SB};
         const int outs[5] = {SA, SB, SA, SB, OUT};
@@ -637,6 +706,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
         c->st.rk_rejects++;
         c->Vd_pl = c->Vd_or;
         c->Vd_mi = c->Vd_or;
+        if (c->rwall && ((rc = fs_sig_copy(c, 0, 2)) || (rc = fs_sig_copy(c, 1, 2)))) return rc;
         in1 = L3;   // n(:,:,1) = n(:,:,2) = n(:,:,3): restart from the base state
         if (attempts > 100000) return fs_set_error(c, FS_ERR_MIN_DT, "RK restart limit");
     }

@@ -99,12 +99,12 @@ def node_types(nx, ny, y, ew, gap, rwall=False):
     return tx, ty
 
 
-def make_mesh(nx, ny, l, w, ew, gap, law="geometric", ratio=1.05, cap=4.0):
+def make_mesh(nx, ny, l, w, ew, gap, law="geometric", ratio=1.05, cap=4.0, rwall=False):
     if nx < 3 or ny < 2:
         raise ValueError("nx >= 3 and ny >= 2 are required")
     x = x_nodes(nx, l, law, ratio, cap)
     y = y_nodes(ny, w)
-    tx, ty = node_types(nx, ny, y, ew, gap)
+    tx, ty = node_types(nx, ny, y, ew, gap, rwall)
     return Mesh(nx, ny, x, y, tx, ty)
 
 

@@ -24,6 +24,8 @@
  *   module arrays ni/ne/nt/nm (ptcl_lib.F90:7-10),
  *     ph (lapl_lib.F90:14)                         fs_upload_state / fs_download_state
  *   maxval(ne)  main.F90:131                       fs_max_ne
+ *   module arrays sig_pl/sig_mi/sig_or
+ *     (sfc_lib.F90:7)                              fs_get_surface_charge / fs_set_surface_charge
  *   KSPDestroy/VecDestroy/MatDestroy main.F90:159  fs_destroy
  *
  * Array layout at the boundary is the reference's: Fortran column-major
@@ -190,10 +192,22 @@ int fs_ptcl_step(fs_ctx *ctx, double *dt_inout, double *t_m_out,
 int fs_lapl_solve(fs_ctx *ctx, double dt, int32_t *lerr_out,
                   int32_t *iters_out, double *relres_out);
 
-/* Level rotation of main.F90:83-101 (accept: t += dt, n3 <- n2, n2 <- n1)
- * and main.F90:103-121 (reject: dt /= 2, n1 <- n3, n2 <- n3). */
+/* Level rotation of main.F90:83-101 (accept: t += dt, n3 <- n2, n2 <- n1,
+ * sig_or <- sig_mi, sig_mi <- sig_pl) and main.F90:103-121 (reject: dt /= 2,
+ * n1 <- n3, n2 <- n3, sig_pl = sig_mi = sig_or). */
 int fs_accept(fs_ctx *ctx);
 int fs_reject(fs_ctx *ctx);
+
+/* sfc_lib's module arrays sig_pl, sig_mi, sig_or (sfc_lib.F90:7): the
+ * surface charge of the dielectric wall, nx+2 entries each with Fortran index
+ * i at [i-1]; a NULL pointer skips that array.  A mesh whose last row has
+ * type_y == 3 nodes (the reference's rwall, props.F90:191-195) turns the
+ * wall on: fs_ptcl_step advances the charge with sfc_step's Merson stages
+ * (sfc_lib.F90:19-80) and fs_lapl_solve reads sig_pl as lapl_solve's sig.
+ * The charge starts at zero (sfc_init, sfc_lib.F90:84-90).  FP64 contexts. */
+int fs_get_surface_charge(fs_ctx *ctx, double *sig_pl, double *sig_mi, double *sig_or);
+int fs_set_surface_charge(fs_ctx *ctx, const double *sig_pl, const double *sig_mi,
+                          const double *sig_or);
 
 /* nsteps iterations of the main.F90:68-121 loop body on the device:
  * ptcl_step (when ts > 1), lapl_solve, accept or reject.  Host work per

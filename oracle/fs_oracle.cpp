@@ -291,6 +291,10 @@ struct or_ctx {
     F2 ph, ph_mi;
     double err_prev = 1.0, t_m = 1e9;
     double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or, Ida = 0, Idc = 0;
+    // sfc_lib module state (sfc_lib.F90:7): surface charge of the dielectric
+    // wall per column, 1-based (1..bx+2), and its Merson stage slopes
+    std::vector<double> sig_pl, sig_mi, sig_or, ks;   // ks(i, stage) at i + (stage - 1) * (bx + 3)
+    bool rwall = false;                                // some node has type_y == 3
     double err_cur = 0;
     double dt_step = 0;
     long ts = 0;
@@ -494,7 +498,7 @@ void ptclEqn(or_ctx &c, int i, int j, int stage, Flags &fl, double &t_m_loc) {
         Ey[1] = 0.0;
     } else if (ty == 3) {
         Ey[0] = -(ph(i, j) - ph(i, j - 1)) / c.DY(j - 1);
-        Ey[1] = 0.0;   // -sig_mi(i): dielectric surface charge, zero without rwall
+        Ey[1] = -c.sig_mi[i];   // dielectric surface charge (:292-294)
     } else {
         Ey[0] = -(ph(i, j) - ph(i, j - 1)) / c.DY(j - 1);
         Ey[1] = -(ph(i, j + 1) - ph(i, j)) / c.DY(j);
@@ -707,6 +711,44 @@ void circ_step(or_ctx &c, int stage, Flags &fl) {
     }
 }
 
+// sfc_step, sfc_lib.F90:19-80: Merson stages of the wall charge on the last
+// interior row.  Two points where the oracle has to choose:
+//  * ptcl_step passes (ni, ne, nt) to the dummy arguments (ne, ni, nt)
+//    (ptcl_lib.F90:52 against sfc_lib.F90:19-23), so the routine's "ne" is
+//    the ion density and its "ni" the electron density; kept as written;
+//  * the routine tests type_y(i-1, by+1), one column past the end of
+//    type_y(bx, by), whose value is whatever memory follows the array; the
+//    oracle tests the wall row type_y(i-1, by), as ptclEqn does for the same
+//    nodes (ptcl_lib.F90:292).
+void sfc_step(or_ctx &c, int stage, Flags &fl) {
+    const Consts &k = c.k;
+    const int j = c.by + 1, ld = c.bx + 3;
+    for (int i = 2; i <= c.bx + 1; i++) {
+        if (c.type_y(i - 1, j - 1) == 3) {
+            const double ne_a = c.ni(i, j, 2), ni_a = c.ne(i, j, 2), nt_a = c.nt(i, j, 2);
+            double Te = get_Te(nt_a, ne_a, fl);
+            double mue = c.get_mue(Te);
+            double De = c.get_De(Te);
+            double fluxi = get_flux(-c.sig_mi[i], c.DY(j), 1, k.mui, k.Di, ni_a, 0.0);
+            double fluxe = get_flux(-c.sig_mi[i], c.DY(j), -1, mue, De, ne_a, 0.0);
+            c.ks[i + (stage - 1) * ld] = fluxi - fluxe;
+        }
+    }
+    auto K = [&](int i, int s) { return c.ks[i + (s - 1) * ld]; };
+    const double dt = c.dt;
+    for (int i = 2; i <= c.bx + 1; i++) {
+        if (c.type_y(i - 1, j - 1) == 3) {
+            if (stage == 1) c.sig_mi[i] = c.sig_or[i] + dt * K(i, 1) / 3.0;
+            else if (stage == 2) c.sig_mi[i] = c.sig_or[i] + dt * (K(i, 1) + K(i, 2)) / 6.0;
+            else if (stage == 3) c.sig_mi[i] = c.sig_or[i] + dt * (K(i, 1) + K(i, 3) * 3.0) / 8.0;
+            else if (stage == 4) c.sig_mi[i] = c.sig_or[i] + dt * (K(i, 1) - K(i, 3) * 3.0 + K(i, 4) * 4.0) / 2.0;
+            else c.sig_pl[i] = c.sig_or[i] + dt * (K(i, 1) + K(i, 4) * 4.0 + K(i, 5)) / 6.0;
+        }
+    }
+    // the east/west exchange of the ghost entries (:57-70) has no neighbour
+    // on a single block: sig(1) and sig(bx+2) keep their values
+}
+
 int flags_to_code(or_ctx &c, const Flags &fl) {
     if (fl.neg) { c.err = "negative density in get_Te"; return FS_ERR_NEG_DENSITY; }
     if (fl.nan) { c.err = "NaN in particle right-hand side"; return FS_ERR_NAN; }
@@ -741,6 +783,7 @@ int ptcl_step(or_ctx &c, int &attempts) {
         int rc = flags_to_code(c, fl);
         if (rc) return rc;
         circ_step(c, stage, fl);
+        if (c.rwall) sfc_step(c, stage, fl);
         rc = flags_to_code(c, fl);
         if (rc) return rc;
         double e_ni = rk_step(c, c.ni, c.ki, stage, c.dt, c.k.n_zero);
@@ -767,6 +810,8 @@ int ptcl_step(or_ctx &c, int &attempts) {
                 if (four) { c.nm.copy_level(1, 3); c.nm.copy_level(2, 3); }
                 c.Vd_pl = c.Vd_or;
                 c.Vd_mi = c.Vd_or;
+                c.sig_pl = c.sig_or;
+                c.sig_mi = c.sig_or;
             }
         }
     }
@@ -851,7 +896,7 @@ double laplEqn(const or_ctx &c, int i, int j, double dt, Flags &fl) {
         Ey[1] = 0.0;
     } else if (ty == 3) {
         Ey[0] = -(ph(i, j) - ph(i, j - 1)) / c.DY(j - 1);
-        Ey[1] = -0.0;   // -sig, zero without rwall
+        Ey[1] = -c.sig_pl[i];   // sig0 = sig(i) with sig = sig_pl (lapl_lib.F90:72-76, main.F90:80)
     } else {
         Ey[0] = -(ph(i, j) - ph(i, j - 1)) / c.DY(j - 1);
         Ey[1] = -(ph(i, j + 1) - ph(i, j)) / c.DY(j);
@@ -1298,6 +1343,8 @@ void rotate_accept(or_ctx &c) {    // main.F90:83-101
     }
     c.Vd_or = c.Vd_mi;
     c.Vd_mi = c.Vd_pl;
+    c.sig_or = c.sig_mi;
+    c.sig_mi = c.sig_pl;
 }
 
 void rotate_reject(or_ctx &c) {    // main.F90:103-121
@@ -1310,6 +1357,8 @@ void rotate_reject(or_ctx &c) {    // main.F90:103-121
     }
     c.Vd_pl = c.Vd_or;
     c.Vd_mi = c.Vd_or;
+    c.sig_pl = c.sig_or;
+    c.sig_mi = c.sig_or;
 }
 
 }  // namespace
@@ -1384,6 +1433,10 @@ int or_create(const fs_config *cfg, const fs_mesh *m, int32_t solver, or_ctx **o
     c->ph_mi.init(ld, by + 2, 0.0);
     // circ_init
     c->Vmax = c->Vsrc = c->Vd_pl = c->Vd_mi = c->Vd_or = cfg->vl;
+    // sfc_init (sfc_lib.F90:84-90); rwall is on when the mesh has wall nodes
+    c->sig_pl.assign(bx + 3, 0.0); c->sig_mi.assign(bx + 3, 0.0); c->sig_or.assign(bx + 3, 0.0);
+    c->ks.assign((size_t)(bx + 3) * 5, 0.0);
+    for (int q : c->ty) c->rwall = c->rwall || q == 3;
     std::memset(&c->st, 0, sizeof(c->st));
     *out = c;
     return FS_OK;
@@ -1495,6 +1548,22 @@ int or_lapl_assemble(or_ctx *c, double dt, double *b, double *a5) {
     }
     if (fl.neg) return FS_ERR_NEG_DENSITY;
     if (fl.nan) return FS_ERR_NAN;
+    return FS_OK;
+}
+
+int or_get_surface_charge(or_ctx *c, double *sig_pl, double *sig_mi, double *sig_or) {
+    const std::vector<double> *src[3] = {&c->sig_pl, &c->sig_mi, &c->sig_or};
+    double *dst[3] = {sig_pl, sig_mi, sig_or};
+    for (int q = 0; q < 3; q++)
+        if (dst[q]) std::memcpy(dst[q], src[q]->data() + 1, sizeof(double) * (c->bx + 2));
+    return FS_OK;
+}
+
+int or_set_surface_charge(or_ctx *c, const double *sig_pl, const double *sig_mi, const double *sig_or) {
+    std::vector<double> *dst[3] = {&c->sig_pl, &c->sig_mi, &c->sig_or};
+    const double *src[3] = {sig_pl, sig_mi, sig_or};
+    for (int q = 0; q < 3; q++)
+        if (src[q]) std::memcpy(dst[q]->data() + 1, src[q], sizeof(double) * (c->bx + 2));
     return FS_OK;
 }
 

@@ -54,6 +54,10 @@ int or_lapl_solve(or_ctx *ctx, double dt, int32_t *lerr_out,
  * A per interior node in the order west, east, south, north, centre
  * (0 where the reference sets no column). */
 int or_lapl_assemble(or_ctx *ctx, double dt, double *b, double *a5);
+/* sfc_lib's sig_pl, sig_mi, sig_or (bx+2 entries each; NULL skips one). */
+int or_get_surface_charge(or_ctx *ctx, double *sig_pl, double *sig_mi, double *sig_or);
+int or_set_surface_charge(or_ctx *ctx, const double *sig_pl, const double *sig_mi,
+                          const double *sig_or);
 int or_accept(or_ctx *ctx);
 int or_reject(or_ctx *ctx);
 int or_run(or_ctx *ctx, int32_t nsteps, fs_stats *stats_out);
