@@ -123,6 +123,8 @@ def declare_api(lib, prefix):
         "get_stats": ([vp, P(FsStats)], C.c_int),
         "get_surface_charge": ([vp, dp, dp, dp], C.c_int),
         "set_surface_charge": ([vp, dp, dp, dp], C.c_int),
+        "get_circuit": ([vp, dp], C.c_int),
+        "set_circuit": ([vp, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, prefix + name)

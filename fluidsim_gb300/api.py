@@ -169,6 +169,16 @@ class Handle:
                 raise ValueError("surface charge arrays have nx+2 entries")
         self.check(self._f("set_surface_charge")(self.ctx, *[abi.dptr(a) for a in arrs]))
 
+    def circuit(self):
+        """circ_lib's Vd_pl, Vd_mi, Vd_or and the last source voltage Vsrc."""
+        v = np.zeros(4)
+        self.check(self._f("get_circuit")(self.ctx, abi.dptr(v)))
+        return dict(zip(("vd_pl", "vd_mi", "vd_or", "vsrc"), v.tolist()))
+
+    def set_circuit(self, vd_pl, vd_mi, vd_or):
+        v = np.array([vd_pl, vd_mi, vd_or], dtype=np.float64)
+        self.check(self._f("set_circuit")(self.ctx, abi.dptr(v)))
+
     # -- the reference's subroutines -----------------------------------------
     def ptcl_step(self):
         dt = C.c_double(self.dt)

@@ -158,7 +158,12 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
         return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "the fit coefficient mode runs on the FP64 path only");
     if (cfg->table_n < 2 || !(cfg->table_emax_ev > cfg->table_emin_ev) || !(cfg->table_emin_ev > 0))
         return fs_set_error(nullptr, FS_ERR_INVALID, "bad coefficient table range");
-    if (cfg->rf != 0) return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "only the DC source (rf = 0) is implemented");
+    if (cfg->rf < 0 || cfg->rf > 3)
+        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "rf must be 0 (DC), 1 (AC) or 2, 3 (pulses), got %d", cfg->rf);
+    if (cfg->rf != 0 && cfg->precision != FS_PREC_FP64)
+        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "time-dependent sources run on the FP64 path only");
+    if (cfg->rf == 1 && !(cfg->res > 0))
+        return fs_set_error(nullptr, FS_ERR_INVALID, "the AC source's RC circuit needs res > 0");
     if (cfg->precision != FS_PREC_FP64 && cfg->precision != FS_PREC_MIXED)
         return fs_set_error(nullptr, FS_ERR_INVALID, "unknown precision mode %d", cfg->precision);
     if (cfg->mg_smooth < 1 || cfg->mg_smooth > 8) return fs_set_error(nullptr, FS_ERR_INVALID, "mg_smooth must be 1..8");
@@ -548,6 +553,18 @@ int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out) {
         }
     }
     return fs_get_stats(c, out);
+}
+
+int fs_get_circuit(fs_ctx *c, double *v) {
+    if (!c || !v) return FS_ERR_INVALID;
+    v[0] = c->Vd_pl; v[1] = c->Vd_mi; v[2] = c->Vd_or; v[3] = c->Vsrc;
+    return FS_OK;
+}
+
+int fs_set_circuit(fs_ctx *c, const double *v) {
+    if (!c || !v) return FS_ERR_INVALID;
+    c->Vd_pl = v[0]; c->Vd_mi = v[1]; c->Vd_or = v[2];
+    return FS_OK;
 }
 
 int fs_get_surface_charge(fs_ctx *c, double *sig_pl, double *sig_mi, double *sig_or) {

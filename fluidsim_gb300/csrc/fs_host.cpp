@@ -79,3 +79,22 @@ void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<doub
         rows[7 * (size_t)n + i] = f.k_si(T);
     }
 }
+
+// Source voltage of circ_step (circ_lib.F90:26-50) at nondimensional time t:
+// DC, AC sin(pi t) (a 2 us period), and the two pulse shapes.  x**3 and x**2
+// are products, as gfortran evaluates integer powers.
+double fs_circ_source(const fs_config &cfg, const fs_constants &k, double t) {
+    const double pi = k.pi, V = cfg.vl;
+    switch (cfg.rf) {
+    case 1: return V * std::sin(pi * t);
+    case 2:
+        if (t < 2.5e-1) { double s = std::sin(4 * pi * t); return V * (s * s * s); }
+        return 0.0;
+    case 3:
+        if (t < 2.3e-1) { double s = std::sin(4.0 * pi * t); return V * (s * s); }
+        if (t < 3.35e-1) return V * (std::sin(3.81 * pi * (t + 5.85e-2)) * 7.19e-1 + 2.81e-1);
+        if (t < 8.2e-1) { double s = std::sin(3.81 * pi * (t + 1.2e-1) / 3.5); return V * ((s * s * s) * (-4.38e-1)); }
+        return 0.0;
+    default: return V;
+    }
+}

@@ -89,6 +89,8 @@ struct Ctrl {
     double rr_prev;            // mixed solver: previous inner residual norm^2
     double lpc_s, lpc_mcm;     // learned correction: residual scale, mean level diagonal
     int lpc_off, pad3;         // learned correction switched off for this solve (stall)
+    double vd_pl, vd_mi;       // electrode voltage of the RC circuit (AC source, circ_lib.F90:158-174)
+    double kv[6];              // its Merson slopes kv(1..5)
     unsigned int counter[8];   // last-block-done counters of grid reductions
     double host_result;        // host-side landing slot of single-value results
 };
@@ -232,6 +234,7 @@ struct fs_ctx {
 int fs_set_error(fs_ctx *c, int code, const char *fmt, ...);
 void fs_host_constants(const fs_config &cfg, fs_constants &k);
 void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<double> &rows);
+double fs_circ_source(const fs_config &cfg, const fs_constants &k, double t);   // Vsrc(t), circ_lib.F90:26-50
 
 // particle kernels (fs_ptcl.cu; the mixed-precision step in fs_mixed.cu)
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts);

@@ -50,6 +50,7 @@ struct StageArgs {
     double *rows;     // [2][ny+2] current rows
     double *sig_mi, *sig_pl, *ks;   // dielectric wall charge (nx+2 each) and its 5 stage slopes
     const double *sig_or;
+    int rows_every_stage;   // the RC circuit needs the electrode current after every stage
     int stage;
     int nblk;
 };
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             sg_elec(E, dh, idh, mue, De, s_n[1][ly][lx], s_n[1][ly][lx + 1],
                     s_n[2][ly][lx], s_n[2][ly][lx + 1], fe, ft);
             if (NS == 4) fm = -pp.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
-            if (a.stage == 5) {
+            if (a.stage == 5 || a.rows_every_stage) {
                 if (gi == 1 && a.m.dr_a[gj] != 0.0) a.rows[gj] = a.m.dr_a[gj] * (fi - fe);
                 if (gi == nx - 1 && a.m.dr_c[gj] != 0.0) a.rows[(ny + 2) + gj] = a.m.dr_c[gj] * (fi - fe);
             }
@@ -528,6 +529,61 @@ __global__ void k_circ_ghost(double *ph, const int8_t *tx, const double *r, cons
     }
 }
 
+// RC circuit of circ_step for the AC source (circ_lib.F90:156-198), after each
+// stage: Idc from the stage's current rows (fixed-order sum), the slope
+// kv(stage) = -(Idc - (Vsrc - Vd_mi)/Res)/Cap, the Merson combination into
+// Vd_mi (stages 1-4) or Vd_pl (stage 5), then the ghost potentials +-Vd/2 of
+// the electrode rows and the fields of their electrode faces.  vd_mi0 is
+// Vd_mi at the start of the attempt (a host value); later stages read the
+// device's.
+__global__ void __launch_bounds__(256) k_circuit(Ctrl *c, const double *rows, double *ph, double *fx_e,
+                                                 const int8_t *tx, const double *r, const double *dx, int nx,
+                                                 int ny, int P, double ew, int stage, double vsrc, double vd_or,
+                                                 double vd_mi0, double res, double cap) {
+    __shared__ double s[256];
+    __shared__ double s_vd;
+    const int t = threadIdx.x;
+    double rc = 0.0;
+    for (int j = 1 + t; j <= ny; j += 256) rc += rows[(ny + 2) + j];
+    s[t] = rc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) s[t] += s[t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        const double idc = s[0], dt = c->dt;
+        const double vd_mi = stage == 1 ? vd_mi0 : c->vd_mi;
+        const double kv = -(idc - (vsrc - vd_mi) / res) / cap;
+        c->kv[stage] = kv;
+        const double *k = c->kv;
+        double v;
+        if (stage == 1) v = vd_or + dt * k[1] / 3.0;
+        else if (stage == 2) v = vd_or + dt * (k[1] + k[2]) / 6.0;
+        else if (stage == 3) v = vd_or + dt * (k[1] + k[3] * 3.0) / 8.0;
+        else if (stage == 4) v = vd_or + dt * (k[1] - k[3] * 3.0 + k[4] * 4.0) / 2.0;
+        else v = vd_or + dt * (k[1] + k[4] * 4.0 + k[5]) / 6.0;
+        if (stage == 5) c->vd_pl = v;
+        else c->vd_mi = v;
+        s_vd = v;
+    }
+    __syncthreads();
+    const double vd = s_vd;
+    for (int gj = 1 + t; gj <= ny; gj += 256) {
+        const size_t o = (size_t)gj * P;
+        if (r[gj] <= ew) {
+            if (tx[(gj - 1) * nx + 0] == -2) {
+                ph[o + 0] = vd / 2.0;
+                fx_e[o + 0] = -(ph[o + 1] - ph[o + 0]) / dx[0];
+            }
+            if (tx[(gj - 1) * nx + nx - 1] == 2) {
+                ph[o + nx + 1] = vd / (-2.0);
+                fx_e[o + nx] = -(ph[o + nx + 1] - ph[o + nx]) / dx[nx];
+            }
+        }
+    }
+}
+
 // PI controller of ptcl_lib.F90:59-95 plus the current sums of circ_step.
 // All sums are fixed-order: strided per-thread partials, then a fixed tree.
 __global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part, int nblk, int ns,
@@ -656,6 +712,10 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     int in1 = L2;
     int attempts = 0;
 
+    const bool rc_circuit = c->cfg.rf == 1;
+    // source voltage at the step's time (circ_lib.F90:26-50); without the RC
+    // circuit the electrode voltage is the source's (:176-177)
+    c->Vsrc = fs_circ_source(c->cfg, c->k, c->t);
     fs_ptcl_reset(c);
     fs_faces_update(c);
     for (;;) {
@@ -675,6 +735,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
         a.sig_mi = fs_sig(c, 1);
         a.sig_or = fs_sig(c, 2);
         a.ks = fs_sig_ks(c);
+        a.rows_every_stage = rc_circuit;
         a.nblk = c->nblk_stage;
         const int ins[5] = {in1, SA, SB, SA, SB};
         const int outs[5] = {SA, SB, SA, SB, OUT};
@@ -693,15 +754,26 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
             fs_prof_begin(c, PROF_STAGE);
             launch_stage(c, a);
             fs_prof_end(c);
-            if (stg == 1 && ++c->launches)
+            if (rc_circuit) {
+                c->launches++;
+                k_circuit<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, c->ph, c->fx_e, c->mesh.tx, c->mesh.r,
+                                                    c->mesh.dx, c->nx, c->ny, c->pitch, c->cfg.ew, stg, c->Vsrc,
+                                                    c->Vd_or, c->Vd_mi, c->cfg.res, c->k.cap);
+            } else if (stg == 1 && ++c->launches) {
                 k_circ_ghost<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
                     c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->nx, c->ny, c->pitch, c->cfg.ew,
                     c->Vsrc);
+            }
         }
         int rc = fs_ptcl_control(c);
         if (rc) return rc;
         const Ctrl &h = *c->h_ctrl;
-        c->Vd_pl = c->Vd_mi = c->Vsrc;
+        if (rc_circuit) {
+            c->Vd_pl = h.vd_pl;
+            c->Vd_mi = h.vd_mi;
+        } else {
+            c->Vd_pl = c->Vd_mi = c->Vsrc;
+        }
         if (!h.rejected) break;
         c->st.rk_rejects++;
         c->Vd_pl = c->Vd_or;

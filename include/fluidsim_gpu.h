@@ -77,7 +77,8 @@ typedef struct fs_config {
     int32_t nspecies;       /* 3: ni, ne, nt ; 4: + metastables nm                   */
     int32_t coef_mode;      /* FS_COEF_*                                              */
     int32_t cyl;            /* 1: cylindrical r-weighting in y (props.F90:47)          */
-    int32_t rf;             /* source waveform; 0 = DC is the implemented one          */
+    int32_t rf;             /* source (circ_lib.F90:26-50): 0 DC, 1 AC sin(pi t) through
+                               the RC circuit, 2 and 3 the pulse shapes; rf != 0 FP64 only */
     int32_t adaptive;       /* 1: PI dt controller + reject (reference)               */
                             /* 0: dt held fixed, attempts never rejected              */
     int32_t precision;      /* FS_PREC_*                                              */
@@ -205,6 +206,13 @@ int fs_reject(fs_ctx *ctx);
  * wall on: fs_ptcl_step advances the charge with sfc_step's Merson stages
  * (sfc_lib.F90:19-80) and fs_lapl_solve reads sig_pl as lapl_solve's sig.
  * The charge starts at zero (sfc_init, sfc_lib.F90:84-90).  FP64 contexts. */
+/* circ_lib's module scalars (circ_lib.F90:8): get writes Vd_pl, Vd_mi, Vd_or
+ * and the source voltage Vsrc of the last particle step into v4[0..3]; set
+ * takes Vd_pl, Vd_mi, Vd_or from v3[0..2] (a restart).  Vd_pl is what the
+ * reference writes to vd.dat. */
+int fs_get_circuit(fs_ctx *ctx, double *v4);
+int fs_set_circuit(fs_ctx *ctx, const double *v3);
+
 int fs_get_surface_charge(fs_ctx *ctx, double *sig_pl, double *sig_mi, double *sig_or);
 int fs_set_surface_charge(fs_ctx *ctx, const double *sig_pl, const double *sig_mi,
                           const double *sig_or);

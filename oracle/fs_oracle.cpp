@@ -291,6 +291,7 @@ struct or_ctx {
     F2 ph, ph_mi;
     double err_prev = 1.0, t_m = 1e9;
     double Vmax, Vsrc, Vd_pl, Vd_mi, Vd_or, Ida = 0, Idc = 0;
+    double kv[6] = {0, 0, 0, 0, 0, 0};   // circ_lib.F90:8, kv(1..5)
     // sfc_lib module state (sfc_lib.F90:7): surface charge of the dielectric
     // wall per column, 1-based (1..bx+2), and its Merson stage slopes
     std::vector<double> sig_pl, sig_mi, sig_or, ks;   // ks(i, stage) at i + (stage - 1) * (bx + 3)
@@ -676,10 +677,29 @@ double circ_face(const or_ctx &c, int il, int j, double dh, Flags &fl) {
     return flxi - flxe;
 }
 
-// circ_step, circ_lib.F90:19-210 (DC source, ny > 1)
+// source voltage of circ_step (circ_lib.F90:26-50) at time t
+double circ_source(const or_ctx &c, double t) {
+    const double pi = c.k.pi, V = c.Vmax;
+    switch (c.cfg.rf) {
+    case 1: return V * std::sin(pi * t);                                    // AC
+    case 2: {                                                               // pulse
+        if (t < 2.5e-1) { double s = std::sin(4 * pi * t); return V * (s * s * s); }
+        return 0.0;
+    }
+    case 3: {                                                               // measured pulse shape
+        if (t < 2.3e-1) { double s = std::sin(4.0 * pi * t); return V * (s * s); }
+        if (t < 3.35e-1) return V * (std::sin(3.81 * pi * (t + 5.85e-2)) * 7.19e-1 + 2.81e-1);
+        if (t < 8.2e-1) { double s = std::sin(3.81 * pi * (t + 1.2e-1) / 3.5); return V * ((s * s * s) * (-4.38e-1)); }
+        return 0.0;
+    }
+    default: return V;                                                      // DC
+    }
+}
+
+// circ_step, circ_lib.F90:19-210 (ny > 1)
 void circ_step(or_ctx &c, int stage, Flags &fl) {
     const int bx = c.bx, by = c.by;
-    c.Vsrc = c.Vmax;
+    c.Vsrc = circ_source(c, c.t);
     double dr;
     int i = 3;
     c.Ida = 0;
@@ -699,9 +719,18 @@ void circ_step(or_ctx &c, int stage, Flags &fl) {
             c.Idc = c.Idc + dr * circ_face(c, i, j, c.DX(i), fl);
         }
     }
-    // kv(stage) only drives Vd for rf == 1; for DC Vd_pl = Vd_mi = Vsrc (:176-177)
-    c.Vd_pl = c.Vsrc;
-    c.Vd_mi = c.Vsrc;
+    // RC circuit of the electrode voltage (:156-174); it drives Vd for rf == 1
+    // only, the other sources set Vd_pl = Vd_mi = Vsrc (:176-177)
+    const double dt = c.dt;
+    double *kv = c.kv;
+    kv[stage] = -(c.Idc - (c.Vsrc - c.Vd_mi) / c.cfg.res) / c.k.cap;
+    if (stage == 1) c.Vd_mi = c.Vd_or + dt * kv[1] / 3.0;
+    else if (stage == 2) c.Vd_mi = c.Vd_or + dt * (kv[1] + kv[2]) / 6.0;
+    else if (stage == 3) c.Vd_mi = c.Vd_or + dt * (kv[1] + kv[3] * 3.0) / 8.0;
+    else if (stage == 4) c.Vd_mi = c.Vd_or + dt * (kv[1] - kv[3] * 3.0 + kv[4] * 4.0) / 2.0;
+    else c.Vd_pl = c.Vd_or + dt * (kv[1] + kv[4] * 4.0 + kv[5]) / 6.0;
+    if (c.cfg.rf != 1) c.Vd_pl = c.Vsrc;
+    if (c.cfg.rf != 1) c.Vd_mi = c.Vsrc;
     i = 2;
     for (int j = 2; j <= by + 1; j++) {
         if (c.R(j) <= c.cfg.ew) {
@@ -1402,7 +1431,8 @@ int or_create(const fs_config *cfg, const fs_mesh *m, int32_t solver, or_ctx **o
     if (cfg->abi_version != FS_ABI_VERSION) { g_create_error = "ABI version mismatch"; return FS_ERR_INVALID; }
     if (cfg->nx < 3 || cfg->ny < 2) { g_create_error = "grid must have nx >= 3 and ny >= 2"; return FS_ERR_UNSUPPORTED; }
     if (cfg->nspecies != 3 && cfg->nspecies != 4) { g_create_error = "nspecies must be 3 or 4"; return FS_ERR_INVALID; }
-    if (cfg->rf != 0) { g_create_error = "only the DC source (rf = 0) is implemented"; return FS_ERR_UNSUPPORTED; }
+    if (cfg->rf < 0 || cfg->rf > 3) { g_create_error = "rf must be 0 (DC), 1 (AC), 2 or 3 (pulses)"; return FS_ERR_UNSUPPORTED; }
+    if (cfg->rf == 1 && !(cfg->res > 0)) { g_create_error = "the AC source needs res > 0"; return FS_ERR_INVALID; }
     if (cfg->coef_mode == FS_COEF_TABLE && cfg->table_n < 2) { g_create_error = "table_n < 2"; return FS_ERR_INVALID; }
     or_ctx *c = new or_ctx();
     c->cfg = *cfg;
@@ -1564,6 +1594,16 @@ int or_set_surface_charge(or_ctx *c, const double *sig_pl, const double *sig_mi,
     const double *src[3] = {sig_pl, sig_mi, sig_or};
     for (int q = 0; q < 3; q++)
         if (src[q]) std::memcpy(dst[q]->data() + 1, src[q], sizeof(double) * (c->bx + 2));
+    return FS_OK;
+}
+
+int or_get_circuit(or_ctx *c, double *v) {
+    v[0] = c->Vd_pl; v[1] = c->Vd_mi; v[2] = c->Vd_or; v[3] = c->Vsrc;
+    return FS_OK;
+}
+
+int or_set_circuit(or_ctx *c, const double *v) {
+    c->Vd_pl = v[0]; c->Vd_mi = v[1]; c->Vd_or = v[2];
     return FS_OK;
 }
 

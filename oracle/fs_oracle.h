@@ -58,6 +58,10 @@ int or_lapl_assemble(or_ctx *ctx, double dt, double *b, double *a5);
 int or_get_surface_charge(or_ctx *ctx, double *sig_pl, double *sig_mi, double *sig_or);
 int or_set_surface_charge(or_ctx *ctx, const double *sig_pl, const double *sig_mi,
                           const double *sig_or);
+/* circ_lib's Vd_pl, Vd_mi, Vd_or and the last source voltage Vsrc (get: 4
+ * values; set: the first 3). */
+int or_get_circuit(or_ctx *ctx, double *v4);
+int or_set_circuit(or_ctx *ctx, const double *v3);
 int or_accept(or_ctx *ctx);
 int or_reject(or_ctx *ctx);
 int or_run(or_ctx *ctx, int32_t nsteps, fs_stats *stats_out);

@@ -90,11 +90,3 @@ def test_wall_reject_restores_charge(built):
     s = d.surface_charge()
     assert np.array_equal(s["sig_pl"], orr) and np.array_equal(s["sig_mi"], orr) and np.array_equal(s["sig_or"], orr)
 
-
-def test_mixed_rejects_wall(built):
-    from fluidsim_gb300 import abi, api
-    from fluidsim_gb300.api import FluidsimError
-    cfg = _cfg(0, True, 3, False, 1).replace(precision=abi.FS_PREC_MIXED)
-    with pytest.raises(FluidsimError) as ei:
-        api.Discharge(cfg, cfg.mesh(), None)
-    assert ei.value.code == abi.FS_ERR_UNSUPPORTED
