@@ -69,6 +69,8 @@ def load_library():
     lib.fs_batch_run.restype = C.c_int
     lib.fs_write_output.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
     lib.fs_write_output.restype = C.c_int
+    lib.fs_output_wait.argtypes = [C.c_void_p]
+    lib.fs_output_wait.restype = C.c_int
     _lib = lib
     return lib
 
@@ -285,8 +287,13 @@ class Discharge(Handle):
         return v.value
 
     def write_output(self, directory, init=False):
-        """The reference's output files in `directory` (see fs_write_output)."""
+        """The reference's output files in `directory` (see fs_write_output):
+        a record is appended by a writer thread while stepping continues."""
         self.check(self._lib.fs_write_output(self.ctx, os.fsencode(directory), 1 if init else 0))
+
+    def output_wait(self):
+        """Wait until the last record is on disk."""
+        self.check(self._lib.fs_output_wait(self.ctx))
 
     # -- learned Poisson preconditioner (mixed contexts) -----------------------
     def lpc_init(self, level=3, max_batch=16, max_samples=512, seed=0):

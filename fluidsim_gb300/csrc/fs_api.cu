@@ -182,6 +182,7 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
 
 void free_ctx(fs_ctx *c) {
     if (!c) return;
+    fs_output_free(c);
     fs_lpc_free_impl(c);
     fs_lapl_free(c);
     if (c->mixed) {

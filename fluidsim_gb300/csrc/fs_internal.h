@@ -144,6 +144,7 @@ struct fs_ctx {
     std::vector<int32_t> h_tx, h_ty;
     std::vector<double> h_r;
     std::vector<double> h_x, h_y;   // node coordinates, ghost ring included (x(1) = y(1) = 0)
+    struct fs_output *out;          // asynchronous output writer (fs_output.cpp), on first use
 
     // table
     double *d_tab;
@@ -266,6 +267,8 @@ int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added);
 int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, float *loss_hist);
 int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float *mask, int batch, float *grad,
                      float *loss, float *pred);
+// output writer (fs_output.cpp): waits for the record in flight, stops the thread
+void fs_output_free(fs_ctx *c);
 // misc device helpers (fs_api.cu)
 int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out);
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);

@@ -264,8 +264,15 @@ int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
  * meshx.dat / meshy.dat and empties f1..f5.dat, time.dat, vd.dat, ida.dat,
  * idc.dat, dt.dat, flx.dat; init = 0 appends the current state -- raw native
  * FP64, same units and layout as the reference, so its save.py reads them.
- * With three species f5.dat gets zeros; flx.dat (the EM flux) gets 0. */
+ * With three species f5.dat gets zeros; flx.dat (the EM flux) gets 0.
+ * init = 0 returns once the record's device-to-host copy is queued on the
+ * context's stream: a writer thread appends it to the files while the caller
+ * keeps stepping.  One record is in flight at a time; the next
+ * fs_write_output, fs_output_wait and fs_destroy wait for it, and a write
+ * error surfaces from whichever of the first two comes next. */
 int fs_write_output(fs_ctx *ctx, const char *dir, int32_t init);
+/* Wait until the record in flight is on disk; its status. */
+int fs_output_wait(fs_ctx *ctx);
 
 /* ---- Many independent discharges (voltage / pressure sweeps).  No single
  * counterpart in the reference, which runs one discharge per invocation

@@ -1,6 +1,7 @@
 """The reference's output files written from device state (needs a GB300):
 read back the way the reference's save.py reads them, they hold the
-downloaded fields in the reference's units, one record per call."""
+downloaded fields in the reference's units, one record per call, each the
+state at its call although the files are written while stepping goes on."""
 import os
 
 import numpy as np
@@ -19,9 +20,13 @@ def test_output_files_match_state(built, tmp_path):
     states, times = [], []
     for _ in range(3):
         d.step()
+        # the record is queued; the download and the next steps run while the
+        # writer thread appends it, and it must hold the state of this call
         d.write_output(str(tmp_path))
         states.append(d.download())
         times.append(d.t)
+    d.step()
+    d.output_wait()
     rd = lambda n: np.fromfile(os.path.join(tmp_path, n), dtype=float)
     x, y, t = rd("meshx.dat"), rd("meshy.dat"), rd("time.dat")
     nx, ny, nt = len(x), len(y), len(t)
