@@ -4,7 +4,9 @@
 // Fortran's operation order, on 1-based column-major arrays.  Only the test
 // suite, the smoke check and the benchmark's CPU-baseline leg use it.
 // Parity status: unpinned (no reference tests or fixtures exist, and the
-// reference cannot be compiled: no Fortran compiler, MPI or PETSc).
+// reference cannot be compiled: no Fortran compiler, MPI or PETSc), apart
+// from get_mue, get_De, get_Dt and get_nu, which tests/test_golden_coef.py
+// checks against the reference's own Python copies of those fits.
 //
 // Fortran details kept on purpose:
 //  * literals written without a d exponent are REAL(4) in Fortran and are
@@ -1656,6 +1658,10 @@ double or_dfdph(double E_pl, double E_mi, int32_t q, double mu, double D, double
     return dfdph(E_pl, E_mi, q, mu, D, dx, n1, n2, nullptr);
 }
 
-double or_coef(const or_ctx *c, int32_t which, double T) { return c->coef(which, T); }
+double or_coef(const or_ctx *c, int32_t which, double T) {
+    if (which == 8) return c->get_mut(T);
+    if (which == 9) return c->get_Dt(T);
+    return c->coef(which, T);
+}
 
 }  // extern "C"

@@ -12,10 +12,13 @@
  * solvers: a banded LU (exact to rounding) or BiCGStab with block-Jacobi
  * ILU(0), the PETSc default preconditioner with one block per thread.
  *
- * Parity status: UNPINNED.  The reference has no tests, golden vectors or
- * fixtures, and it cannot be built here or on the GPU host (no Fortran
- * compiler, MPI or PETSc), so this restatement is checked against analytic
- * known-answer tests only (tests/test_oracle_kat.py).
+ * Parity status: UNPINNED apart from the coefficient fits get_mue, get_De,
+ * get_Dt and get_nu, which tests/test_golden_coef.py checks against the
+ * reference's own Python copies of them (coeftest.py, wvgAC.py).  The
+ * reference has no tests, golden vectors or fixtures, and it cannot be built
+ * here or on the GPU host (no Fortran compiler, MPI or PETSc), so the rest of
+ * this restatement is checked against analytic known-answer tests
+ * (tests/test_oracle_kat.py and the wall and circuit tests).
  *
  * The interface mirrors include/fluidsim_gpu.h entry for entry, prefixed or_.
  */
@@ -73,7 +76,8 @@ double or_get_flux(double E, double dh, int32_t q, double mu, double D,
 double or_dfdph(double E_pl, double E_mi, int32_t q, double mu, double D,
                 double dx, double n1, double n2);
 /* coefficient by index (0 mue,1 De,2 k_ir,3 k_ex,4 nu,5 beta,6 k_sc,7 k_si)
- * at nondimensional mean energy T, through the configured mode. */
+ * at nondimensional mean energy T, through the configured mode; 8 get_mut and
+ * 9 get_Dt, always from the fits. */
 double or_coef(const or_ctx *ctx, int32_t which, double T);
 
 #ifdef __cplusplus
