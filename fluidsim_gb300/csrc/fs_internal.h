@@ -106,6 +106,7 @@ struct MGLevelF {
     int nx, ny, pitch;
     float *mc, *ce, *cn, *extra, *inv_mc;
     float *rhs, *x, *res;
+    float *xd;              // iterate after the fused down-smoothing (read by the fused up kernel)
 };
 
 // Multigrid level (FP64 plain path).
@@ -113,6 +114,7 @@ struct MGLevel {
     int nx, ny, pitch;      // interior size; fields are (ny+2) x pitch with ghost ring
     double *mc, *ce, *cn, *extra, *inv_mc;
     double *rhs, *x, *res;
+    double *xd;             // iterate after the fused down-smoothing (read by the fused up kernel)
 };
 
 // Kernel classes timed by the optional per-launch event profiler.

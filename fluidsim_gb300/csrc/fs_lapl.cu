@@ -497,7 +497,7 @@ LevelDev level_dev(const MGLevel &m) {
 LvT<double> lvt(const MGLevel &m) {
     LvT<double> L;
     L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
-    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
     return L;
 }
 
@@ -528,6 +528,7 @@ int fs_lapl_alloc(fs_ctx *c) {
         } else {
             if ((rc = alloc_zero(c, &m.rhs, n))) return rc;
             if ((rc = alloc_zero(c, &m.x, n))) return rc;
+            if ((rc = alloc_zero(c, &m.xd, n))) return rc;   // fused levels (1 and coarser)
         }
         nl++;
         if ((nx == 1 && ny == 1) || nl == FS_MG_MAX_LEVELS) break;
@@ -576,7 +577,7 @@ void fs_lapl_free(fs_ctx *c) {
         MGLevel &m = c->mg[l];
         double *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.res};
         for (double *f : fs) cudaFree(f);
-        if (l > 0) { cudaFree(m.rhs); cudaFree(m.x); }
+        if (l > 0) { cudaFree(m.rhs); cudaFree(m.x); cudaFree(m.xd); }
     }
     double *vs[] = {c->p, c->q, c->z, c->r, c->xs, c->bs, c->dinv, c->d_cg_part, c->d_ainv64};
     for (double *v : vs) cudaFree(v);

@@ -741,7 +741,7 @@ LevelT<float> level_f(const MGLevelF &m) {
 LvT<float> lvt_f(const MGLevelF &m) {
     LvT<float> L;
     L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
-    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
     return L;
 }
 
@@ -764,7 +764,7 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         m.ny = c->mg[l].ny;
         m.pitch = c->mg[l].pitch;
         const size_t n = (size_t)(m.ny + 2) * m.pitch;
-        float **fields[] = {&m.mc, &m.ce, &m.cn, &m.extra, &m.inv_mc, &m.rhs, &m.x};
+        float **fields[] = {&m.mc, &m.ce, &m.cn, &m.extra, &m.inv_mc, &m.rhs, &m.x, &m.xd};
         for (float **f : fields) {
             cudaError_t e = cudaMalloc(f, n * sizeof(float));
             if (e == cudaSuccess) e = cudaMemset(*f, 0, n * sizeof(float));
@@ -812,7 +812,7 @@ void fs_lapl_free_mixed(fs_ctx *c) {
     destroy_cgm_graphs(c);
     for (int l = 0; l < FS_MG_MAX_LEVELS; l++) {
         MGLevelF &m = c->mgf[l];
-        float *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.rhs, m.x};
+        float *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.rhs, m.x, m.xd};
         for (float *f : fs) cudaFree(f);
         memset(&m, 0, sizeof(m));
     }

@@ -183,7 +183,10 @@ __global__ void k_prolong(const LevelT<T> f, const LevelT<T> c) {
 // coarse correction and nu black-red sweeps in one launch.  With x = 0 the
 // first sweep needs no neighbours, and each later sweep updates a region one
 // ring smaller, so after 2*nu sweeps the tile (and, going down, its first
-// ring) holds exactly the values the unfused sweeps produce.
+// ring) holds exactly the values the unfused sweeps produce.  The halo of the
+// up kernel must hold the down-smoothed values of the neighbouring tiles, so
+// down writes its iterate to xd and up reads xd and writes x: no tile reads
+// a value another tile of the same launch writes.
 #define MTX 32
 #define MTY 16
 
@@ -191,7 +194,7 @@ template <typename T>
 struct LvT {
     int nx, ny, P;
     const T *mc, *ce, *cn, *inv_mc;
-    T *rhs, *x;
+    T *rhs, *x, *xd;
 };
 
 template <typename T, int NU>
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c)
             if (((gi + gj) & 1) == 0)   // black residuals vanish after the last (black) sweep
                 r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
                                - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
-            f.x[(size_t)gj * f.P + gi] = sx[k];
+            f.xd[(size_t)gj * f.P + gi] = sx[k];
         }
         sr[q] = r;
     }
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
         const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
         const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
         const size_t o = (size_t)gj * f.P + gi;
-        sx[q] = in ? f.x[o] + c.x[(size_t)((gj + 1) / 2) * c.P + (gi + 1) / 2] : T(0);
+        sx[q] = in ? f.xd[o] + c.x[(size_t)((gj + 1) / 2) * c.P + (gi + 1) / 2] : T(0);
         srhs[q] = in ? f.rhs[o] : T(0);
         simc[q] = in ? f.inv_mc[o] : T(0);
         sce[q] = arr ? f.ce[o] : T(0);
