@@ -169,11 +169,28 @@ __global__ void k_restrict(const LevelT<T> f, const LevelT<T> c) {
             if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
     c.rhs[(size_t)J * c.P + I] = s;
 }
+// Coarse-grid correction at fine node (gi, gj): cell-centred bilinear
+// interpolation of the coarse iterate -- weights 9/16, 3/16, 3/16, 1/16 from
+// the aggregate holding the node and its neighbours on the node's side --
+// constant beyond the coarse grid's edge.  (With piecewise-constant
+// prolongation and restriction the orders add up to the PDE's order and the
+// V-cycle converges slowly; a second-order prolongation fixes that.)
+template <typename T>
+__device__ __forceinline__ T prolong_at(const T *cx, int cP, int cnx, int cny, int gi, int gj) {
+    const int I = (gi + 1) >> 1, J = (gj + 1) >> 1;
+    int In = (gi & 1) ? I - 1 : I + 1, Jn = (gj & 1) ? J - 1 : J + 1;
+    if (In < 1 || In > cnx) In = I;
+    if (Jn < 1 || Jn > cny) Jn = J;
+    const T a = cx[(size_t)J * cP + I], b = cx[(size_t)J * cP + In], d = cx[(size_t)Jn * cP + I],
+            e = cx[(size_t)Jn * cP + In];
+    return T(0.5625) * a + T(0.1875) * (b + d) + T(0.0625) * e;
+}
+
 template <typename T>
 __global__ void k_prolong(const LevelT<T> f, const LevelT<T> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (I > f.nx || J > f.ny) return;
-    f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+    f.x[(size_t)J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
 }
 
 // ---------------------------------------------- fused (temporally blocked) levels
@@ -265,7 +282,7 @@ __global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
         const bool in = gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny;
         const bool arr = gi >= 0 && gj >= 0 && gi <= f.nx + 1 && gj <= f.ny + 1;
         const size_t o = (size_t)gj * f.P + gi;
-        sx[q] = in ? f.xd[o] + c.x[(size_t)((gj + 1) / 2) * c.P + (gi + 1) / 2] : T(0);
+        sx[q] = in ? f.xd[o] + prolong_at(c.x, c.P, c.nx, c.ny, gi, gj) : T(0);
         srhs[q] = in ? f.rhs[o] : T(0);
         simc[q] = in ? f.inv_mc[o] : T(0);
         sce[q] = arr ? f.ce[o] : T(0);
@@ -341,7 +358,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a
         const LevelT<T> &f = a.L[l], &c = a.L[l + 1];
         for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
             int I = q % f.nx + 1, J = q / f.nx + 1;
-            f.x[(size_t)J * f.P + I] += c.x[(size_t)((J + 1) / 2) * c.P + (I + 1) / 2];
+            f.x[(size_t)J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
         }
         __syncthreads();
         for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
@@ -494,7 +511,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         const LevelT<T> f = S[l], c = S[l + 1];
         for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
             int I = q % f.nx + 1, J = q / f.nx + 1;
-            f.x[J * f.P + I] += c.x[((J + 1) / 2) * c.P + (I + 1) / 2];
+            f.x[J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
         }
         __syncthreads();
         for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
