@@ -186,6 +186,17 @@ __device__ __forceinline__ T prolong_at(const T *cx, int cP, int cnx, int cny, i
     return T(0.5625) * a + T(0.1875) * (b + d) + T(0.0625) * e;
 }
 
+// Weight of coarse index I in prolong_at's interpolation at fine index fi
+// (one direction; the 2D weight is the product): restriction with these
+// weights is the transpose of the prolongation.
+template <typename T>
+__device__ __forceinline__ T prolong_w(int fi, int I, int cn) {
+    const int Ic = (fi + 1) >> 1;
+    int In = (fi & 1) ? Ic - 1 : Ic + 1;
+    if (In < 1 || In > cn) In = Ic;
+    return (I == Ic ? T(0.75) : T(0)) + (I == In ? T(0.25) : T(0));
+}
+
 template <typename T>
 __global__ void k_prolong(const LevelT<T> f, const LevelT<T> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -214,9 +225,40 @@ struct LvT {
     T *rhs, *x, *xd;
 };
 
+// Restriction.  The FP64 levels, under the plain (non-flexible) PCG that
+// wants a symmetric preconditioner, restrict with the transpose of the
+// bilinear prolongation (11 instead of 13 CG iterations at 1024^2); the FP32
+// levels under the flexible CG sum the aggregate's residuals, which costs less
+// and needs the same iterations there.  With the transpose the down kernel
+// keeps one more halo ring than the sweeps need, so that the residuals of the
+// tile's first ring, which the transpose reaches, are exact too.
+template <typename T>
+struct RestrictFW { static constexpr bool value = sizeof(T) == 8; };
+
+// coarse right-hand side at (I, J) from the fine residuals (the red ones:
+// black residuals vanish after the last, black, half sweep)
+template <typename T>
+__device__ __forceinline__ T restrict_at(const LevelT<T> &f, const LevelT<T> &c, int I, int J) {
+    T s = T(0);
+    if (RestrictFW<T>::value) {
+        for (int fy = max(2 * J - 2, 1); fy <= min(2 * J + 1, f.ny); fy++)
+            for (int fx = max(2 * I - 2, 1); fx <= min(2 * I + 1, f.nx); fx++)
+                if (((fx + fy) & 1) == 0)
+                    s += prolong_w<T>(fy, J, c.ny) * prolong_w<T>(fx, I, c.nx) * resid(f, (size_t)fy * f.P + fx);
+    } else {
+        for (int fy = 2 * J - 1; fy <= min(2 * J, f.ny); fy++)
+            for (int fx = 2 * I - 1; fx <= min(2 * I, f.nx); fx++)
+                if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
+    }
+    return s;
+}
+
 template <typename T, int NU>
 __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c) {
-    constexpr int H = 2 * NU, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    constexpr bool FW = RestrictFW<T>::value;
+    constexpr int E = FW ? 1 : 0;    // residual ring beyond the tile
+    constexpr int H = 2 * NU + E, WX = MTX + 2 * H, WY = MTY + 2 * H, W = WX * WY;
+    constexpr int RX = MTX + 2 * E;  // residual block: the tile (and its first ring)
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *smc = simc + W, *sce = smc + W,
       *scn = sce + W, *sr = scn + W;
@@ -248,16 +290,16 @@ __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c)
         }
         __syncthreads();
     }
-    for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
-        const int tx = q % MTX, ty = q / MTX, lx = H + tx, ly = H + ty;
+    for (int q = threadIdx.x; q < RX * (MTY + 2 * E); q += blockDim.x) {
+        const int tx = q % RX - E, ty = q / RX - E, lx = H + tx, ly = H + ty;
         const int gi = gx0 + tx, gj = gy0 + ty;
         const int k = ly * WX + lx;
         T r = T(0);
-        if (gi <= f.nx && gj <= f.ny) {
+        if (gi >= 1 && gj >= 1 && gi <= f.nx && gj <= f.ny) {
             if (((gi + gj) & 1) == 0)   // black residuals vanish after the last (black) sweep
                 r = srhs[k] - (smc[k] * sx[k] - sce[k] * sx[k + 1] - sce[k - 1] * sx[k - 1]
                                - scn[k] * sx[k + WX] - scn[k - WX] * sx[k - WX]);
-            f.xd[(size_t)gj * f.P + gi] = sx[k];
+            if (tx >= 0 && ty >= 0 && tx < MTX && ty < MTY) f.xd[(size_t)gj * f.P + gi] = sx[k];
         }
         sr[q] = r;
     }
@@ -266,8 +308,23 @@ __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c)
         const int ci = q % (MTX / 2), cj = q / (MTX / 2);
         const int I = (gx0 - 1) / 2 + 1 + ci, J = (gy0 - 1) / 2 + 1 + cj;
         if (I > c.nx || J > c.ny) continue;
-        const int t0 = (2 * cj) * MTX + 2 * ci;
-        c.rhs[(size_t)J * c.P + I] = sr[t0] + sr[t0 + 1] + sr[t0 + MTX] + sr[t0 + MTX + 1];
+        if (!FW) {
+            const int t0 = (2 * cj) * MTX + 2 * ci;
+            c.rhs[(size_t)J * c.P + I] = sr[t0] + sr[t0 + 1] + sr[t0 + MTX] + sr[t0 + MTX + 1];
+            continue;
+        }
+        T acc = T(0);
+        for (int dy = -1; dy <= 2; dy++) {
+            const int fy = 2 * J - 1 + dy;
+            if (fy < 1 || fy > f.ny) continue;
+            const T wy = prolong_w<T>(fy, J, c.ny);
+            for (int dx = -1; dx <= 2; dx++) {
+                const int fx = 2 * I - 1 + dx;
+                if (fx < 1 || fx > f.nx) continue;
+                acc += wy * prolong_w<T>(fx, I, c.nx) * sr[(2 * cj + dy + 1) * RX + 2 * ci + dx + 1];
+            }
+        }
+        c.rhs[(size_t)J * c.P + I] = acc;
     }
 }
 
@@ -335,12 +392,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a
         for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
         for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
             int I = q % c.nx + 1, J = q / c.nx + 1;
-            const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
-            T s = T(0);
-            for (int fy = fy0; fy <= fy1; fy++)
-                for (int fx = fx0; fx <= fx1; fx++)
-                    if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
-            c.rhs[(size_t)J * c.P + I] = s;
+            c.rhs[(size_t)J * c.P + I] = restrict_at(f, c, I, J);
         }
         __syncthreads();
     }
@@ -489,12 +541,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
         for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
             int I = q % c.nx + 1, J = q / c.nx + 1;
-            const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
-            T s = T(0);
-            for (int fy = fy0; fy <= fy1; fy++)
-                for (int fx = fx0; fx <= fx1; fx++)
-                    if (((fx + fy) & 1) == 0) s += resid(f, (size_t)(fy * f.P + fx));
-            c.rhs[J * c.P + I] = s;
+            c.rhs[J * c.P + I] = restrict_at(f, c, I, J);
         }
         __syncthreads();
     }
@@ -561,8 +608,9 @@ inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (n
 
 template <typename T>
 size_t mg_down_smem(int nu) {
-    size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
-    return (6 * W + MTX * MTY) * sizeof(T);
+    const int e = RestrictFW<T>::value ? 1 : 0;
+    size_t W = (size_t)(MTX + 4 * nu + 2 * e) * (MTY + 4 * nu + 2 * e);
+    return (6 * W + (size_t)(MTX + 2 * e) * (MTY + 2 * e)) * sizeof(T);
 }
 template <typename T>
 size_t mg_up_smem(int nu) {
