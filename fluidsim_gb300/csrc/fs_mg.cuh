@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
     }
 }
 
-// V-cycle over levels [lb, nl) inside one CTA (levels of at most 32x32 nodes).
+// V-cycle over levels [lb, dl] inside one CTA (levels of at most 32x32 nodes).
 template <typename T>
 struct BottomArgs {
     LevelT<T> L[FS_MG_MAX_LEVELS];
@@ -373,50 +373,6 @@ struct BottomArgs {
     int dl;              // k_bottom_smem: level solved exactly with the dense inverse ainv
     const T *ainv;       // (nx*ny)^2 of level dl, row-major over the compact index (J-1)*nx + I-1
 };
-template <typename T>
-__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(const BottomArgs<T> a) {
-    const int t = threadIdx.x;
-    auto sweep = [&](const LevelT<T> &L, int color, int zero) {
-        for (int q = t; q < L.nx * L.ny; q += BOTTOM_THREADS) {
-            int I = q % L.nx + 1, J = q / L.nx + 1;
-            size_t o = (size_t)J * L.P + I;
-            if (((I + J) & 1) == color) L.x[o] = zero ? L.rhs[o] * L.inv_mc[o] : gs_node(L, o);
-            else if (zero) L.x[o] = T(0);
-        }
-        __syncthreads();
-    };
-    for (int l = a.lb; l < a.nl - 1; l++) {
-        const LevelT<T> &f = a.L[l], &c = a.L[l + 1];
-        sweep(f, 0, 1);
-        sweep(f, 1, 0);
-        for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
-        for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
-            int I = q % c.nx + 1, J = q / c.nx + 1;
-            c.rhs[(size_t)J * c.P + I] = restrict_at(f, c, I, J);
-        }
-        __syncthreads();
-    }
-    {   // coarsest level: a single node is solved exactly by one red sweep;
-        // otherwise symmetric sweeps, the palindrome (RB)^10 (BR)^10
-        const LevelT<T> &c = a.L[a.nl - 1];
-        sweep(c, 0, 1);
-        if (c.nx * c.ny > 1) {
-            sweep(c, 1, 0);
-            for (int it = 1; it < 10; it++) { sweep(c, 0, 0); sweep(c, 1, 0); }
-            for (int it = 0; it < 10; it++) { sweep(c, 1, 0); sweep(c, 0, 0); }
-        }
-    }
-    for (int l = a.nl - 2; l >= a.lb; l--) {
-        const LevelT<T> &f = a.L[l], &c = a.L[l + 1];
-        for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
-            int I = q % f.nx + 1, J = q / f.nx + 1;
-            f.x[(size_t)J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
-        }
-        __syncthreads();
-        for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0); sweep(f, 0, 0); }
-    }
-}
-
 // The V-cycle over levels [lb, dl] with every level held in shared memory
 // (operators, right-hand sides, iterates), and level dl -- the first with at
 // most 64 unknowns -- solved exactly with its dense inverse (k_dense_inv, once
@@ -429,10 +385,11 @@ __host__ __device__ inline int bottom_smem_elems(const BottomArgs<T> &a) {
     for (int l = a.lb; l <= a.dl; l++) n += (a.L[l].nx + 2) * (a.L[l].ny + 2);
     return n;
 }
-// shared memory of k_bottom_smem: six arrays per level and the dense inverse
+// shared memory of k_bottom_smem: six arrays per level, the dense inverse and
+// the residuals of the top level (the largest)
 template <typename T>
 inline size_t bottom_smem_bytes(const BottomArgs<T> &a) {
-    return (6 * (size_t)bottom_smem_elems(a) + 64 * 64) * sizeof(T);
+    return (6 * (size_t)bottom_smem_elems(a) + 64 * 64 + (size_t)(a.L[a.lb].nx + 2) * (a.L[a.lb].ny + 2)) * sizeof(T);
 }
 // first level at or below lb with at most 64 unknowns (the coarsest is 1 x 1)
 template <typename T>
@@ -502,6 +459,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
     T *base = (T *)sm_raw;
     const int nd = a.L[a.dl].nx * a.L[a.dl].ny;
     T *sinv = base + 6 * tot;   // DENSE_N x DENSE_N
+    T *sres = sinv + DENSE_N * DENSE_N;   // fine residuals of the level being restricted
     LevelT<T> S[FS_MG_MAX_LEVELS];
     {
         int off = 0;
@@ -539,9 +497,27 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         sweep(f, 0, 1);
         sweep(f, 1, 0);
         for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0); sweep(f, 1, 0); }
-        for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
-            int I = q % c.nx + 1, J = q / c.nx + 1;
-            c.rhs[J * c.P + I] = restrict_at(f, c, I, J);
+        if (RestrictFW<T>::value) {   // each fine residual once, then the transpose weights
+            for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
+                const int I = q % f.nx + 1, J = q / f.nx + 1, o = J * f.P + I;
+                sres[o] = ((I + J) & 1) == 0 ? resid(f, (size_t)o) : T(0);
+            }
+            __syncthreads();
+            for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
+                const int I = q % c.nx + 1, J = q / c.nx + 1;
+                T s = T(0);
+                for (int fy = max(2 * J - 2, 1); fy <= min(2 * J + 1, f.ny); fy++) {
+                    const T wy = prolong_w<T>(fy, J, c.ny);
+                    for (int fx = max(2 * I - 2, 1); fx <= min(2 * I + 1, f.nx); fx++)
+                        s += wy * prolong_w<T>(fx, I, c.nx) * sres[fy * f.P + fx];
+                }
+                c.rhs[J * c.P + I] = s;
+            }
+        } else {
+            for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
+                int I = q % c.nx + 1, J = q / c.nx + 1;
+                c.rhs[J * c.P + I] = restrict_at(f, c, I, J);
+            }
         }
         __syncthreads();
     }
