@@ -209,7 +209,7 @@ struct fs_ctx {
     float *f32[10];              // fx_e, fx_cl, fx_cr, fx_dl, fx_dr, fy_e, fy_cl, fy_cr, fy_dl, fy_dr
     float *d_tab32;
     MGLevelF mgf[FS_MG_MAX_LEVELS];
-    float *p32, *q32;            // FP32 inner CG vectors
+    float *p32, *q32, *w32;      // FP32 inner CG vectors (w = M z)
     // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
     struct LpcState *lpc;
     int lpc_on, lpc_level;

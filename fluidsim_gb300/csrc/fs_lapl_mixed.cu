@@ -345,7 +345,7 @@ struct CgmArgs {
     int nx, ny, P, nblk;
     dim3 grid;
     double *x, *r, *rhs, *dinv, *part;   // FP64: iterate, true residual, D b, 1/D
-    float *z, *r32, *p, *q;              // FP32 inner vectors (z, r32 are level 0 of the V-cycle)
+    float *z, *r32, *p, *q, *w;          // FP32 inner vectors (z, r32 are level 0 of the V-cycle; w = M z)
     const float *ce, *cn, *extra;
     Ctrl *ctrl;
     double rtol, inner_tol2;
@@ -398,6 +398,48 @@ __device__ bool grid_sum2(double v, double w, double *part, unsigned int *counte
     return true;
 }
 
+// Fixed-order sums of three per-thread values; part needs 3 * nblk entries.
+__device__ bool grid_sum3(double v0, double v1, double v2, double *part, unsigned int *counter, int nblk,
+                          double out[3]) {
+    __shared__ double s_p[3][8];
+    __shared__ bool s_last;
+    double v[3] = {v0, v1, v2};
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 3; k++) s_p[k][wid] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; k++) {
+            double r = 0.0;
+            for (int wv = 0; wv < 8; wv++) r += s_p[k][wv];
+            part[(size_t)k * nblk + blockIdx.x] = r;
+        }
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    __shared__ double s_r[3][256];
+    for (int k = 0; k < 3; k++) {
+        double a = 0.0;
+        for (int b = threadIdx.x; b < nblk; b += 256) a += ((volatile double *)part)[(size_t)k * nblk + b];
+        s_r[k][threadIdx.x] = a;
+    }
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 3; k++) s_r[k][threadIdx.x] += s_r[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    for (int k = 0; k < 3; k++) out[k] = s_r[k][0];
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
 // x = 0, r = D b (FP64), r32 = r; ||b||, ||r32||
 __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
     double v = 0.0, w = 0.0;
@@ -440,24 +482,6 @@ __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a
 // inner vector and coefficient is zero on the ghost ring and the row padding,
 // so those lanes add nothing to the dot products and stay zero.
 
-// after the V-cycle: rz = r32.z, flexible beta = -alpha z.q / rz_old
-__global__ void __launch_bounds__(256) k_cgm_rz(const CgmArgs a) {
-    if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
-    float v = 0.0f, w = 0.0f;
-    CG_VEC4(a, {
-        const float4 z = ld4(a.z, o);
-        v += dot4(ld4(a.r32, o), z);
-        w += dot4(z, ld4(a.q, o));
-    })
-    double sv, sw;
-    if (grid_sum2((double)v, (double)w, a.part, &a.ctrl->counter[1], a.nblk, sv, sw) && threadIdx.x == 0) {
-        Ctrl *c = a.ctrl;
-        c->rz_old = c->rz;
-        c->rz = sv;
-        c->beta = c->inner_it == 0 ? 0.0 : -c->alpha * sw / c->rz_old;
-    }
-}
-
 // M z at one node in float-float arithmetic: each face term c (z_i - z_j) is
 // formed exactly (the difference of neighbouring, similar values is exact,
 // the product's rounding error is recovered with an FMA) and the terms are
@@ -485,12 +509,17 @@ __device__ __forceinline__ float mz_ff(float z, float ze, float zw, float zn, fl
     return __fadd_rn(hi, lo);
 }
 
-// p = z + beta p ; q = M z + beta q ; alpha = rz / p.q
-__global__ void __launch_bounds__(256) k_cgm_pq(const CgmArgs a) {
+// After the V-cycle, one pass and one reduction (the Chronopoulos-Gear
+// arrangement of the iteration): w = M z (float-float stencil), rz = r32.z,
+// zq = z.q and zw = z.w.  The flexible beta = -alpha z.q / rz_old (Notay's
+// FCG(1): -z.(M p_old) / p_old.(M p_old)), and p.q of the new directions
+// p = z + beta p_old, q = w + beta q_old follows from the same sums:
+// p.q = z.w + 2 beta z.q + beta^2 (p_old.q_old), with p_old.(M z) = q_old.z
+// for the symmetric M.  alpha = rz / p.q.
+__global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
     if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
-    const float be = (float)a.ctrl->beta;
     const int P = a.P;
-    float v = 0.0f;
+    float v = 0.0f, u = 0.0f, t = 0.0f;
     CG_VEC4(a, {
         const float4 z = ld4(a.z, o), zn = ld4(a.z, o + P), zs = ld4(a.z, o - P);
         const float zw = a.z[o - 1], ze = a.z[o + 4];
@@ -501,32 +530,41 @@ __global__ void __launch_bounds__(256) k_cgm_pq(const CgmArgs a) {
         mz.y = mz_ff(z.y, z.z, z.x, zn.y, zs.y, ce.y, ce.x, cn.y, cs.y, ex.y);
         mz.z = mz_ff(z.z, z.w, z.y, zn.z, zs.z, ce.z, ce.y, cn.z, cs.z, ex.z);
         mz.w = mz_ff(z.w, ze, z.z, zn.w, zs.w, ce.w, ce.z, cn.w, cs.w, ex.w);
-        const float4 p0 = ld4(a.p, o), q0 = ld4(a.q, o);
-        const float4 pn = make_float4(z.x + be * p0.x, z.y + be * p0.y, z.z + be * p0.z, z.w + be * p0.w);
-        const float4 qn = make_float4(mz.x + be * q0.x, mz.y + be * q0.y, mz.z + be * q0.z, mz.w + be * q0.w);
-        st4(a.p, o, pn);
-        st4(a.q, o, qn);
-        v += dot4(pn, qn);
+        st4(a.w, o, mz);
+        v += dot4(ld4(a.r32, o), z);
+        u += dot4(z, ld4(a.q, o));
+        t += dot4(z, mz);
     })
-    double out;
-    if (grid_sum<256>((double)v, a.part, &a.ctrl->counter[2], a.nblk, &out) && threadIdx.x == 0) {
+    double s[3];
+    if (grid_sum3((double)v, (double)u, (double)t, a.part, &a.ctrl->counter[1], a.nblk, s) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
-        c->pq = out;
-        c->alpha = out > 0.0 ? c->rz / out : 0.0;
+        c->rz_old = c->rz;
+        c->rz = s[0];
+        const double be = c->inner_it == 0 ? 0.0 : -c->alpha * s[1] / c->rz_old;
+        c->beta = be;
+        const double pq = c->inner_it == 0 ? s[2] : s[2] + 2.0 * be * s[1] + be * be * c->pq;
+        c->pq = pq;
+        c->alpha = pq > 0.0 ? c->rz / pq : 0.0;
     }
 }
 
-// x += alpha p in FP64 ; r32 -= alpha q ; ||r32|| decides when the next
-// refinement runs.  x is accumulated in FP64: an FP32 correction would carry
-// a rounding of ~eps |d| that M amplifies by its condition number (~5e-4
-// relative residual at 1024^2), the floor no inner iteration can get below.
-__global__ void __launch_bounds__(256) k_cgm_xr(const CgmArgs a) {
+// p = z + beta p ; q = w + beta q ; x += alpha p in FP64 ; r32 -= alpha q ;
+// ||r32|| decides when the next refinement runs.  x is accumulated in FP64:
+// an FP32 correction would carry a rounding of ~eps |d| that M amplifies by
+// its condition number (~5e-4 relative residual at 1024^2), the floor no
+// inner iteration can get below.
+__global__ void __launch_bounds__(256) k_cgm_upd(const CgmArgs a) {
     if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
+    const float be = (float)a.ctrl->beta;
     const double ald = a.ctrl->alpha;
     const float al = (float)ald;
     float v = 0.0f;
     CG_VEC4(a, {
-        const float4 p = ld4(a.p, o), q = ld4(a.q, o);
+        const float4 z = ld4(a.z, o), w = ld4(a.w, o), p0 = ld4(a.p, o), q0 = ld4(a.q, o);
+        const float4 p = make_float4(z.x + be * p0.x, z.y + be * p0.y, z.z + be * p0.z, z.w + be * p0.w);
+        const float4 q = make_float4(w.x + be * q0.x, w.y + be * q0.y, w.z + be * q0.z, w.w + be * q0.w);
+        st4(a.p, o, p);
+        st4(a.q, o, q);
         double2 *x2 = reinterpret_cast<double2 *>(a.x + o);
         double2 x01 = x2[0], x23 = x2[1];
         x01.x += ald * (double)p.x; x01.y += ald * (double)p.y;
@@ -772,14 +810,14 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         }
         m.res = nullptr;
     }
-    float **vecs[] = {&c->p32, &c->q32};
+    float **vecs[] = {&c->p32, &c->q32, &c->w32};
     for (float **v : vecs) {
         cudaError_t e = cudaMalloc(v, c->field_elems * sizeof(float));
         if (e == cudaSuccess) e = cudaMemset(*v, 0, c->field_elems * sizeof(float));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 CG vectors)");
     }
-    {   // two partials per CTA of the CG reductions (<= 4 CTAs per SM)
-        const int need = 2 * 4 * c->nsm;
+    {   // three partials per CTA of the CG reductions (<= 4 CTAs per SM)
+        const int need = 3 * 4 * c->nsm;
         if (c->cg_nblk < need) {
             cudaFree(c->d_cg_part);
             cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * need);
@@ -818,6 +856,7 @@ void fs_lapl_free_mixed(fs_ctx *c) {
     }
     cudaFree(c->p32);
     cudaFree(c->q32);
+    cudaFree(c->w32);
     cudaFree(c->d_ainv32);
 }
 
@@ -917,13 +956,10 @@ static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
     vcycle_mixed(c, ca);
     if (ca.lpc) lpc_apply(c, ca);
     fs_prof_begin(c, PROF_CG);
-    k_cgm_rz<<<ca.grid, 256, 0, c->stream>>>(ca);
+    k_cgm_rzw<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     fs_prof_begin(c, PROF_CG);
-    k_cgm_pq<<<ca.grid, 256, 0, c->stream>>>(ca);
-    fs_prof_end(c);
-    fs_prof_begin(c, PROF_CG);
-    k_cgm_xr<<<ca.grid, 256, 0, c->stream>>>(ca);
+    k_cgm_upd<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     fs_prof_begin(c, PROF_CG);
     k_cgm_refine<<<ca.grid, 256, 0, c->stream>>>(ca);
@@ -1010,7 +1046,7 @@ static CgmArgs cgm_args(fs_ctx *c) {
     }
     ca.x = c->xs; ca.r = c->r;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
-    ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32;
+    ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32; ca.w = c->w32;
     ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
