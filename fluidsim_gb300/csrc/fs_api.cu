@@ -282,7 +282,7 @@ int fs_create(const fs_config *cfg, const fs_mesh *m, fs_ctx **out) {
     pp.ntab = cfg->table_n;
     pp.ph0 = k.ph0; pp.e = k.e; pp.pi = k.pi; pp.me = k.me; pp.t0 = k.t0; pp.x0 = k.x0;
     pp.mui = k.mui; pp.Di = k.Di; pp.vi = k.vi; pp.Dm = k.Dm; pp.gam = k.gam; pp.ninf = k.ninf;
-    pp.tg = k.tg; pp.kb = k.kb; pp.mi = k.mi;
+    pp.tg = k.tg; pp.kb = k.kb; pp.mi = k.mi; pp.inv_mi = 1.0 / k.mi;
     pp.h_ir = k.h_ir; pp.h_ex = k.h_ex; pp.h_si = k.h_si;
     pp.k_mp = k.k_mp; pp.k_r = k.k_r; pp.k_2q = k.k_2q; pp.k_3q = k.k_3q;
     pp.nmin[0] = k.n_zero; pp.nmin[1] = k.n_zero; pp.nmin[2] = k.nmin_nt; pp.nmin[3] = k.n_zero;

@@ -30,7 +30,7 @@ struct PhysParams {
     int nx, ny, pitch, nspecies, cyl;
     int ntab;
     double ph0, e, pi, me, t0, x0;
-    double mui, Di, vi, Dm, gam, ninf, tg, kb, mi;
+    double mui, Di, vi, Dm, gam, ninf, tg, kb, mi, inv_mi;
     double h_ir, h_ex, h_si, k_mp, k_r, k_2q, k_3q;
     double nmin[FS_MAX_SPECIES];   // floors: n_zero, n_zero, n_zero/ph0/1e2, n_zero
     double abs_tol, rel_tol;

@@ -389,7 +389,9 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
             term_sie = term_sie + k_si * nm * ne + pp.k_mp * (nm * nm);
         }
         const double term_st1 = -(fex * exa + fey * eya);
-        const double term_st2 = -(ne * nu * pp.me / pp.mi * (te / 1.5 - pp.tg * pp.kb / pp.e / pp.ph0));
+        // Tg kb / e / ph0 folded on the host (same operations, same value); the
+        // divisions by mi and by 1.5 as products with reciprocals (<= 1 ulp each)
+        const double term_st2 = -(ne * nu * pp.me * pp.inv_mi * (te * (2.0 / 3.0) - pp.tg_term));
         double term_st3 = -(pp.h_ir * k_ir * pp.ninf * ne) - pp.h_si * k_si * nm * ne
                         - pp.h_ex * k_ex * pp.ninf * ne;
         double kv[NS];
