@@ -740,6 +740,8 @@ int fs_lpc_use(fs_ctx *c, int32_t on) {
     c->lpc_t_plain = -1.0;
     c->lpc_use_next = 1;
     c->lpc_since_probe = 0;
+    c->lpc_probe_every = 25;
+    c->lpc_probe_pending = 0;
     return FS_OK;
 }
 

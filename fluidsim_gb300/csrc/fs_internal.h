@@ -216,6 +216,7 @@ struct fs_ctx {
     // choice between the two solvers, judged on measured solve time
     double lpc_t_nn, lpc_t_plain;   // moving averages of the solve time (ms), < 0: none yet
     int lpc_use_next, lpc_since_probe;
+    int lpc_probe_every, lpc_probe_pending;   // probe interval of the other choice, last solve was a probe
     float *lpc_op;               // [Hn][Wn][3] operator features of the level (per solve)
     float *lpc_rr;               // [Hn][Wn] restricted residual
     double *lpc_rhs64;           // fine right-hand side of a harvest solve

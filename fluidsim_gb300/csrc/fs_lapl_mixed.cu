@@ -1014,7 +1014,9 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
 // Solve-level choice with the plain multigrid-PCG as the judge: the host keeps
 // moving averages of the wall time of solves with and without the network
 // (a solve in which the network stalled counts double) and runs the next
-// solve with the faster one; every 25 solves it tries the other once.
+// solve with the faster one.  Every lpc_probe_every solves it tries the other
+// once: 25 to start with and after a probe that changed the choice, doubled
+// (up to 400) after each probe that did not.
 static void lpc_account(fs_ctx *c, const CgmArgs &ca, double ms) {
     if (!c->lpc_on) return;
     const double a = 0.3;
@@ -1024,13 +1026,20 @@ static void lpc_account(fs_ctx *c, const CgmArgs &ca, double ms) {
     } else {
         c->lpc_t_plain = c->lpc_t_plain < 0.0 ? ms : (1.0 - a) * c->lpc_t_plain + a * ms;
     }
-    int next;
-    if (c->lpc_t_nn < 0.0) next = 1;
-    else if (c->lpc_t_plain < 0.0) next = 0;
-    else next = c->lpc_t_nn <= c->lpc_t_plain ? 1 : 0;
-    if (++c->lpc_since_probe >= 25) {
-        next = !next;
+    int pref;
+    if (c->lpc_t_nn < 0.0) pref = 1;
+    else if (c->lpc_t_plain < 0.0) pref = 0;
+    else pref = c->lpc_t_nn <= c->lpc_t_plain ? 1 : 0;
+    if (c->lpc_probe_pending) {
+        c->lpc_probe_pending = 0;
+        if (pref == (ca.lpc ? 1 : 0)) c->lpc_probe_every = 25;
+        else c->lpc_probe_every = std::min(2 * c->lpc_probe_every, 400);
+    }
+    int next = pref;
+    if (++c->lpc_since_probe >= c->lpc_probe_every) {
+        next = !pref;
         c->lpc_since_probe = 0;
+        c->lpc_probe_pending = 1;
     }
     c->lpc_use_next = next;
 }
@@ -1102,7 +1111,7 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     k_dense_inv<float><<<1, 1024, 0, c->stream>>>(level_f(c->mgf[c->mg_dl]), c->d_ainv32);
     fs_prof_end(c);
     CgmArgs ca = cgm_args(c);
-    if (c->lpc_on) {
+    if (ca.lpc) {   // the network's operator features, only for a solve that runs it
         LpcArgs l = lpc_args(c);
         c->launches++;
         k_lpc_opfeat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
