@@ -44,8 +44,8 @@ UNIT = "steps/s"
 # (stage 1 reads n2, n3, phi and writes k1, n2'; ...; stage 5 reads n2, n3,
 # k1, k3, k4, phi and writes n1), i.e. 640 B per node per attempt, 128 B per stage.
 STAGE_BYTES_PER_NODE = (25 * 3 + 5) * 8 / 5.0
-# measured DRAM traffic of one FP64 stage launch at 1024^2: 113.0 MB read + 26.0 MB written
-STAGE_TRAFFIC_1024 = 139.0e6
+# measured DRAM traffic of one FP64 stage launch at 1024^2: 113.0 MB read + 27.8 MB written
+STAGE_TRAFFIC_1024 = 140.7e6
 # learned preconditioner variant: training pairs harvested over this many
 # steps (4 per step), then this many Adam steps of batch 16
 LPC_HARVEST = 12
