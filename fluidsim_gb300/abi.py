@@ -123,6 +123,8 @@ def declare_api(lib, prefix):
         "get_stats": ([vp, P(FsStats)], C.c_int),
         "get_surface_charge": ([vp, dp, dp, dp], C.c_int),
         "set_surface_charge": ([vp, dp, dp, dp], C.c_int),
+        "get_controller": ([vp, dp, P(C.c_int64)], C.c_int),
+        "set_controller": ([vp, C.c_double, C.c_int64], C.c_int),
         "get_circuit": ([vp, dp], C.c_int),
         "set_circuit": ([vp, dp], C.c_int),
     }

@@ -171,6 +171,31 @@ class Handle:
                 raise ValueError("surface charge arrays have nx+2 entries")
         self.check(self._f("set_surface_charge")(self.ctx, *[abi.dptr(a) for a in arrs]))
 
+    def controller(self):
+        """ptcl_step's err_prev and main's step counter ts."""
+        e, ts = C.c_double(), C.c_int64()
+        self.check(self._f("get_controller")(self.ctx, C.byref(e), C.byref(ts)))
+        return dict(err_prev=e.value, ts=ts.value)
+
+    def set_controller(self, err_prev, ts):
+        self.check(self._f("set_controller")(self.ctx, float(err_prev), int(ts)))
+        self.ts = int(ts)
+
+    def checkpoint(self):
+        """Everything a restart needs: the three-level state, phi, time, dt,
+        the controller, the circuit and the wall charge (host copies)."""
+        return dict(state=self.download(nlev=3), t=self.t, dt=self.dt, controller=self.controller(),
+                    circuit=self.circuit(), surface_charge=self.surface_charge())
+
+    def restore(self, ck):
+        self.upload(ck["state"])
+        self.set_time(ck["t"], ck["dt"])
+        self.set_controller(ck["controller"]["err_prev"], ck["controller"]["ts"])
+        c = ck["circuit"]
+        self.set_circuit(c["vd_pl"], c["vd_mi"], c["vd_or"])
+        sc = ck["surface_charge"]
+        self.set_surface_charge(sc["sig_pl"], sc["sig_mi"], sc["sig_or"])
+
     def circuit(self):
         """circ_lib's Vd_pl, Vd_mi, Vd_or and the last source voltage Vsrc."""
         v = np.zeros(4)
@@ -218,6 +243,38 @@ class Handle:
         else:
             self.reject()
         return info
+
+    def run_logged(self, nsteps, log, every=1):
+        """nsteps main-loop iterations through the separate calls, with one
+        JSON line per `every` steps written to `log` (a path or a file
+        object): the figures the reference prints every few seconds
+        (main.F90:124-138: step, t, dt, t_m, Vd, Ida, Idc, max n_e) plus RK
+        attempts, CG iterations and residual, and the wall time per step."""
+        import json
+        import time
+        own = isinstance(log, (str, bytes, os.PathLike))
+        f = open(log, "a") if own else log
+        try:
+            last, since = time.perf_counter(), 0
+            for s in range(nsteps):
+                info = self.step()
+                since += 1
+                if since < every and s + 1 != nsteps:
+                    continue
+                now = time.perf_counter()
+                rec = {"step": self.ts, "t": self.t, "dt": self.dt, "lerr": info["lerr"],
+                       "attempts": info.get("attempts", 0), "cg_iters": info["iters"],
+                       "relres": info["relres"], "t_m": info.get("t_m"), "ida": info.get("ida"),
+                       "idc": info.get("idc"), "vd": self.circuit()["vd_pl"],
+                       "wall_s_per_step": (now - last) / since}
+                if hasattr(self, "max_ne"):
+                    rec["max_ne"] = self.max_ne()
+                f.write(json.dumps(rec) + "\n")
+                last, since = now, 0
+            f.flush()
+        finally:
+            if own:
+                f.close()
 
     def run(self, nsteps):
         """nsteps main-loop iterations inside the library (fs_run)."""

@@ -74,6 +74,33 @@ class RunConfig:
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)
 
+    # -- JSON files: every field by name; a file may name a subset, the rest
+    # keeps its default (the reference takes its run parameters as CLI pairs,
+    # main.F90:172-248, and its physics as compile-time constants)
+    def to_json(self, path=None):
+        import json
+        text = json.dumps(dataclasses.asdict(self), indent=1, sort_keys=True)
+        if path:
+            with open(path, "w") as f:
+                f.write(text + "\n")
+        return text
+
+    @classmethod
+    def from_json(cls, src):
+        """A RunConfig from a JSON file path or a JSON string; unknown keys are an error."""
+        import json
+        import os
+        if isinstance(src, str) and os.path.exists(src):
+            with open(src) as f:
+                d = json.load(f)
+        else:
+            d = json.loads(src)
+        names = {fl.name for fl in dataclasses.fields(cls)}
+        unknown = sorted(set(d) - names)
+        if unknown:
+            raise ValueError("unknown configuration keys: %s" % ", ".join(unknown))
+        return cls(**d)
+
 
 def glow(n=64, **kw):
     """2D Cartesian argon DC glow: square 1 cm gap, n x n nodes, 1 Torr, 300 K,

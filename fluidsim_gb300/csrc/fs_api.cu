@@ -9,9 +9,18 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "fs_internal.h"
 
 static thread_local std::string g_err;
+
+// NVTX range over one reference routine (ptcl_step, lapl_solve, the main-loop
+// body), visible to profilers that attach; a no-op without one
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
 
 int fs_set_error(fs_ctx *c, int code, const char *fmt, ...) {
     char buf[512];
@@ -412,6 +421,25 @@ int fs_set_time(fs_ctx *c, double t, double dt) {
     return set_dt_dev(c, dt);
 }
 
+int fs_get_controller(fs_ctx *c, double *err_prev, int64_t *ts) {
+    if (!c) return FS_ERR_INVALID;
+    int rc = fs_sync_ctrl(c);
+    if (rc) return rc;
+    if (err_prev) *err_prev = c->h_ctrl->err_prev;
+    if (ts) *ts = c->ts;
+    return FS_OK;
+}
+
+int fs_set_controller(fs_ctx *c, double err_prev, int64_t ts) {
+    if (!c) return FS_ERR_INVALID;
+    if (!(err_prev > 0.0)) return fs_set_error(c, FS_ERR_INVALID, "err_prev must be positive");
+    c->ts = ts;
+    cudaError_t e = cudaMemcpyAsync(&c->d_ctrl->err_prev, &err_prev, sizeof(double), cudaMemcpyHostToDevice,
+                                    c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "set controller");
+}
+
 int fs_upload_state(fs_ctx *c, const double *ni, const double *ne, const double *nt, const double *nm,
                     const double *ph, int32_t ld, int32_t nlev) {
     if (!c) return FS_ERR_INVALID;
@@ -472,6 +500,7 @@ int fs_download_state(fs_ctx *c, double *ni, double *ne, double *nt, double *nm,
 int fs_ptcl_step(fs_ctx *c, double *dt_inout, double *t_m_out, double *ida_out, double *idc_out,
                  int32_t *attempts_out) {
     if (!c) return FS_ERR_INVALID;
+    NvtxRange range("ptcl_step");
     int rc;
     if (dt_inout && (rc = set_dt_dev(c, *dt_inout))) return rc;
     int attempts = 0;
@@ -486,6 +515,7 @@ int fs_ptcl_step(fs_ctx *c, double *dt_inout, double *t_m_out, double *ida_out, 
 
 int fs_lapl_solve(fs_ctx *c, double dt, int32_t *lerr_out, int32_t *iters_out, double *relres_out) {
     if (!c) return FS_ERR_INVALID;
+    NvtxRange range("lapl_solve");
     int rc = set_dt_dev(c, dt);
     if (rc) return rc;
     int lerr = 1, iters = 0;
@@ -533,22 +563,28 @@ int fs_reject(fs_ctx *c) {
 int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out) {
     if (!c) return FS_ERR_INVALID;
     for (int s = 0; s < nsteps; s++) {
+        NvtxRange step("main loop step");
         int rc;
         if (c->ts > 1) {
+            NvtxRange range("ptcl_step");
             int att = 0;
             if ((rc = c->mixed ? fs_ptcl_step_mixed(c, &att) : fs_ptcl_step_impl(c, &att))) return rc;
         }
         int lerr = 1, iters = 0;
         double relres = 0;
-        if ((rc = c->mixed ? fs_lapl_solve_mixed(c, &lerr, &iters, &relres)
-                           : fs_lapl_solve_impl(c, &lerr, &iters, &relres)))
-            return rc;
+        {
+            NvtxRange range("lapl_solve");
+            if ((rc = c->mixed ? fs_lapl_solve_mixed(c, &lerr, &iters, &relres)
+                               : fs_lapl_solve_impl(c, &lerr, &iters, &relres)))
+                return rc;
+        }
         c->st.lapl_iters += iters;
         c->st.last_lapl_iters = iters;
         c->st.lapl_relres = relres;
         c->st.lerr = lerr;
-        if (lerr == 0) fs_accept(c);
-        else {
+        if (lerr == 0) {
+            if ((rc = fs_accept(c))) return rc;
+        } else {
             c->st.lapl_rejects++;
             if ((rc = fs_reject(c))) return rc;
         }

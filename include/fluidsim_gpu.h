@@ -168,6 +168,14 @@ const char *fs_last_error(const fs_ctx *ctx);
 /* g%t and g%dt. */
 int fs_set_time(fs_ctx *ctx, double t, double dt);
 
+/* The rest of the step state a restart needs (with the three-level densities,
+ * phi, g%t, g%dt, the circuit and the wall charge): ptcl_step's err_prev
+ * (ptcl_lib.F90:11), the PI controller's memory, and main's step counter ts
+ * (main.F90:12; ptcl_step runs once ts > 1).  A context restored from these
+ * continues bit for bit as the one they were read from. */
+int fs_get_controller(fs_ctx *ctx, double *err_prev, int64_t *ts);
+int fs_set_controller(fs_ctx *ctx, double err_prev, int64_t ts);
+
 /* Module arrays <-> device.  Species arrays are (ld, ny+2, nlev) column-major
  * like ni(bx+2,by+2,3); nlev = 3 (all RK levels) or 1 (the one array is used
  * for every level).  nm may be NULL when nspecies == 3.  ph is (ld, ny+2).

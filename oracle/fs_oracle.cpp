@@ -1480,6 +1480,18 @@ const char *or_last_error(const or_ctx *c) { return c ? c->err.c_str() : g_creat
 
 int or_set_time(or_ctx *c, double t, double dt) { c->t = t; c->dt = dt; return FS_OK; }
 
+int or_get_controller(or_ctx *c, double *err_prev, int64_t *ts) {
+    if (err_prev) *err_prev = c->err_prev;
+    if (ts) *ts = c->ts;
+    return FS_OK;
+}
+
+int or_set_controller(or_ctx *c, double err_prev, int64_t ts) {
+    c->err_prev = err_prev;
+    c->ts = ts;
+    return FS_OK;
+}
+
 static void copy_in(F3 &f, const double *src, int ld, int nlev, int bx, int by) {
     for (int l = 1; l <= 3; l++) {
         int sl = nlev == 1 ? 1 : l;

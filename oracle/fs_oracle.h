@@ -42,6 +42,8 @@ void or_destroy(or_ctx *ctx);
 const char *or_last_error(const or_ctx *ctx);
 int or_set_threads(int32_t nthreads);
 int or_set_time(or_ctx *ctx, double t, double dt);
+int or_get_controller(or_ctx *ctx, double *err_prev, int64_t *ts);
+int or_set_controller(or_ctx *ctx, double err_prev, int64_t ts);
 int or_upload_state(or_ctx *ctx, const double *ni, const double *ne,
                     const double *nt, const double *nm, const double *ph,
                     int32_t ld, int32_t nlev);

@@ -77,3 +77,31 @@ def test_uniform_pm1_range_and_mean():
     u = grid.uniform_pm1(1, 0, 200000)
     assert u.min() >= -1 and u.max() < 1
     assert abs(u.mean()) < 0.01
+
+
+def test_config_json_roundtrip(tmp_path):
+    from fluidsim_gb300 import config
+    cfg = config.glow(48, ny=40, rf=2, rwall=True, gam=0.09)
+    p = tmp_path / "run.json"
+    cfg.to_json(str(p))
+    back = config.RunConfig.from_json(str(p))
+    assert back == cfg
+    part = config.RunConfig.from_json('{"nx": 32, "ny": 16, "p_torr": 2.0}')
+    assert (part.nx, part.ny, part.p_torr) == (32, 16, 2.0) and part.gam == config.RunConfig().gam
+    with pytest.raises(ValueError):
+        config.RunConfig.from_json('{"nx": 8, "bogus": 1}')
+
+
+def test_run_log_lines(tmp_path):
+    import json
+    from fluidsim_gb300 import api, config, grid
+    from oracle import oracle
+    cfg = config.glow(12, ny=10, lapl_rtol=1e-12)
+    mesh = cfg.mesh()
+    st = grid.blob_state(mesh, api.constants(cfg, oracle.load(), "or_"), noise=0.01, seed=1, vl=cfg.vl)
+    o = oracle.OracleDischarge(cfg, mesh, st)
+    p = tmp_path / "run.jsonl"
+    o.run_logged(7, str(p), every=3)
+    lines = [json.loads(x) for x in open(p)]
+    assert [r["step"] for r in lines] == [3, 6, 7]
+    assert all(r["lerr"] == 0 and r["cg_iters"] >= 1 and r["wall_s_per_step"] > 0 for r in lines)
