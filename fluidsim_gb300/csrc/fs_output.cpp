@@ -39,6 +39,7 @@ struct fs_output {
     double *stage = nullptr;     // pinned: ni, ne, nt, nm, ph at (nx+2, ny+2) each
     cudaEvent_t ev = nullptr;
     int nx = 0, ny = 0, ns = 3;
+    int device = 0;
     double x0 = 0, ph0 = 0;
 };
 
@@ -85,6 +86,7 @@ int write_record(fs_output &o) {
 }
 
 void writer_loop(fs_output *o) {
+    cudaSetDevice(o->device);   // the context's device, for the event waits
     std::unique_lock<std::mutex> lk(o->m);
     for (;;) {
         o->cv.wait(lk, [o] { return o->quit || o->busy; });
@@ -125,6 +127,7 @@ int start(fs_ctx *c) {
     fs_output *o = new fs_output();
     o->nx = c->nx;
     o->ny = c->ny;
+    o->device = c->device;
     o->ns = c->cfg.nspecies;
     o->x0 = c->k.x0;
     o->ph0 = c->k.ph0;

@@ -111,6 +111,55 @@ module fs_gpu_mod
       import :: c_ptr
       type(c_ptr), value :: ctx
     end function
+    ! g_init output set-up (init = 1) and writeOut (init = 0), props.F90:239-320,
+    ! main.F90:297-333; dir is a NUL-terminated path
+    integer(c_int) function fs_write_output(ctx, dir, init) bind(C, name="fs_write_output")
+      import :: c_ptr, c_int, c_int32_t, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: dir(*)
+      integer(c_int32_t), value :: init
+    end function
+    integer(c_int) function fs_output_wait(ctx) bind(C, name="fs_output_wait")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+    end function
+    ! circ_lib's Vd_pl, Vd_mi, Vd_or and Vsrc (get), Vd_pl, Vd_mi, Vd_or (set)
+    integer(c_int) function fs_get_circuit(ctx, v4) bind(C, name="fs_get_circuit")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: v4(4)
+    end function
+    integer(c_int) function fs_set_circuit(ctx, v3) bind(C, name="fs_set_circuit")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: v3(3)
+    end function
+    ! sfc_lib's sig_pl, sig_mi, sig_or (bx+2 each)
+    integer(c_int) function fs_get_surface_charge(ctx, sig_pl, sig_mi, sig_or) &
+        bind(C, name="fs_get_surface_charge")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: sig_pl(*), sig_mi(*), sig_or(*)
+    end function
+    integer(c_int) function fs_set_surface_charge(ctx, sig_pl, sig_mi, sig_or) &
+        bind(C, name="fs_set_surface_charge")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: sig_pl(*), sig_mi(*), sig_or(*)
+    end function
+    ! ptcl_step's err_prev and main's ts (restart)
+    integer(c_int) function fs_get_controller(ctx, err_prev, ts) bind(C, name="fs_get_controller")
+      import :: c_ptr, c_int, c_double, c_int64_t
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: err_prev
+      integer(c_int64_t), intent(out) :: ts
+    end function
+    integer(c_int) function fs_set_controller(ctx, err_prev, ts) bind(C, name="fs_set_controller")
+      import :: c_ptr, c_int, c_double, c_int64_t
+      type(c_ptr), value :: ctx
+      real(c_double), value :: err_prev
+      integer(c_int64_t), value :: ts
+    end function
   end interface
 
   type(c_ptr), save :: fs_ctx = c_null_ptr
@@ -142,6 +191,21 @@ contains
     call fs_check(fs_ptcl_step(fs_ctx, dt, tm, ida, idc, att))
     t_m = min(t_m, tm)
   end subroutine
+
+  ! writeOut (main.F90:297-333): the record is appended by the library's
+  ! writer thread; the g_init set-up passes init = 1 once
+  subroutine write_out_gpu(path, init)
+    character(len=*), intent(in) :: path
+    integer, intent(in) :: init
+    call fs_check(fs_write_output(fs_ctx, trim(path)//c_null_char, int(init, c_int32_t)))
+  end subroutine
+
+  ! Vd_pl, the electrode voltage main prints and writes (circ_lib.F90:8)
+  real(8) function vd_gpu()
+    real(c_double) :: v(4)
+    call fs_check(fs_get_circuit(fs_ctx, v))
+    vd_gpu = v(1)
+  end function
 
   ! lapl_solve(g, ne(:,:,1), ni(:,:,1), nt(:,:,1), sig, lerr)
   subroutine lapl_solve_gpu(dt, lerr)
