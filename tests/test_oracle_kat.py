@@ -7,7 +7,9 @@ reference has no tests or golden data of its own):
     of a uniform plasma between zero-flux walls, and leaves it uniform;
   * the Poisson system (lapl_lib.F90:123-609) reproduces a linear potential
     exactly, converges at 2nd order on a manufactured solution, and is
-    symmetric after scaling each row by its control volume.
+    symmetric after scaling each row by its control volume;
+  * the anode and cathode currents of circ_step (circ_lib.F90:87-151) come
+    together as a discharge approaches steady state (current continuity).
 """
 import math
 
@@ -224,3 +226,24 @@ def test_dfdph_matches_high_precision(a):
     exact = mp.diff(F, mp.mpf(mu) * mp.mpf(E))
     got = oracle.dfdph(E, E, 1, mu, D, dx, n1, n2)
     assert abs(got - float(exact)) <= 1e-12 * float(abs(exact)), (got, exact)
+
+
+def test_current_continuity_approaching_steady_state(built):
+    """Ida = Idc at steady state (current continuity): a 1D-like 400 V
+    discharge (32 x 2 nodes, electrodes on every row with current weight)
+    grows from the seed blob; the anode and cathode conduction currents,
+    far apart while the space charge builds up, agree to 1 % after ~2.7 us
+    (60,000 adaptive steps) and the difference keeps falling."""
+    cfg = config.glow(32, ny=2, ew=10.0, gap=20.0, lapl_rtol=1e-10, vl=-400.0 / config.PH0)
+    mesh = cfg.mesh()
+    k = api.constants(cfg, oracle.load(), "or_")
+    st = grid.blob_state(mesh, k, noise=0.0, seed=1, vl=cfg.vl)
+    o = oracle.OracleDischarge(cfg, mesh, st)
+    rel = []
+    for chunk in range(6):
+        o.run(10000)
+        s = o.stats()
+        rel.append(abs(s["ida"] - s["idc"]) / abs(s["idc"]))
+    assert rel[0] > 0.5, rel            # early: space charge building up
+    assert rel[-1] < 1e-2, rel          # late: continuity
+    assert rel[-1] < rel[0] / 50, rel
