@@ -36,6 +36,8 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# before anything creates the CUDA context (see fluidsim_gb300/__init__.py)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "steps/s, 1024² glow: plain FP64 vs mixed+learned-PC at 1e-8 Poisson resid"
 UNIT = "steps/s"
