@@ -591,7 +591,10 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     dim3 b(32, 8);
     for (int l = 0; l < lb; l++) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
-        if (c->mg_fused && l > 0) {
+        // fused (temporally blocked) levels only where launches dominate: the
+        // FP64 levels above 256^2 are FP64-issue-bound, and the fused kernel's
+        // redundant halo sweeps cost more there than the launches they save
+        if (c->mg_fused && l > 0 && c->mg[l].nx <= 256 && c->mg[l].ny <= 256) {
             LvT<double> F = lvt(c->mg[l]), C = lvt(c->mg[l + 1]);
             fs_prof_begin(c, PROF_SMOOTH);
             k_mg_down<double, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_down_smem<double>(2), c->stream>>>(F, C);
@@ -614,7 +617,8 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
             fs_prof_end(c);
         }
         fs_prof_begin(c, PROF_TRANSFER);
-        k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+        if (l == 0) k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+        else k_restrict_t<double><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
     }
     BottomArgs<double> ba;
@@ -629,7 +633,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     fs_prof_end(c);
     for (int l = lb - 1; l >= 0; l--) {
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
-        if (c->mg_fused && l > 0) {
+        if (c->mg_fused && l > 0 && c->mg[l].nx <= 256 && c->mg[l].ny <= 256) {
             LvT<double> F = lvt(c->mg[l]), C = lvt(c->mg[l + 1]);
             fs_prof_begin(c, PROF_SMOOTH);
             k_mg_up<double, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_up_smem<double>(2), c->stream>>>(F, C);

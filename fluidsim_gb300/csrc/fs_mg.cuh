@@ -253,6 +253,15 @@ __device__ __forceinline__ T restrict_at(const LevelT<T> &f, const LevelT<T> &c,
     return s;
 }
 
+// coarse right-hand sides by restrict_at (the unfused FP64 levels below the
+// finest: the transpose of the prolongation, as the fused levels restrict)
+template <typename T>
+__global__ void k_restrict_t(const LevelT<T> f, const LevelT<T> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > c.nx || J > c.ny) return;
+    c.rhs[(size_t)J * c.P + I] = restrict_at(f, c, I, J);
+}
+
 template <typename T, int NU>
 __global__ void __launch_bounds__(256) k_mg_down(const LvT<T> f, const LvT<T> c) {
     constexpr bool FW = RestrictFW<T>::value;
