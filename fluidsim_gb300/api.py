@@ -147,11 +147,24 @@ class Handle:
         self.check(self._f("upload_state")(self.ctx, *[abi.dptr(a) for a in arrs],
                                            self.nx + 2, nlev))
 
-    def download(self, nlev=1):
+    def download(self, nlev=1, out=None):
+        """The module arrays (ni, ne, nt[, nm], ph) in the reference's layout;
+        into the caller's arrays when `out` holds them (Fortran-ordered float64
+        of the right shapes, e.g. views of pinned memory), else new ones."""
         shp = (self.nx + 2, self.ny + 2) + ((3,) if nlev == 3 else ())
-        out = {k: np.zeros(shp, order="F") for k in ("ni", "ne", "nt")}
-        out["nm"] = np.zeros(shp, order="F") if self.cfg.nspecies == 4 else None
-        out["ph"] = np.zeros((self.nx + 2, self.ny + 2), order="F")
+        if out is None:
+            out = {k: np.zeros(shp, order="F") for k in ("ni", "ne", "nt")}
+            out["nm"] = np.zeros(shp, order="F") if self.cfg.nspecies == 4 else None
+            out["ph"] = np.zeros((self.nx + 2, self.ny + 2), order="F")
+        else:
+            out = dict(out)
+            out.setdefault("nm", None)
+            for k, want in (("ni", shp), ("ne", shp), ("nt", shp), ("ph", (self.nx + 2, self.ny + 2))):
+                a = out[k]
+                if a.shape != want or a.dtype != np.float64 or not a.flags.f_contiguous:
+                    raise ValueError("download: %s must be a Fortran-ordered float64 array of shape %s" % (k, want))
+            if self.cfg.nspecies == 4 and out["nm"] is None:
+                out["nm"] = np.zeros(shp, order="F")
         self.check(self._f("download_state")(
             self.ctx, abi.dptr(out["ni"]), abi.dptr(out["ne"]), abi.dptr(out["nt"]),
             abi.dptr(out["nm"]), abi.dptr(out["ph"]), self.nx + 2, nlev))
