@@ -179,6 +179,7 @@ struct fs_ctx {
     int mg_nlev;
     int mg_fused;                // coarse launched levels use the fused kernels
     int mg_lb, mg_dl;            // first level of the one-CTA bottom solver; its dense level
+    int strip_kl, strip_kr;      // electrode strips of the finest level: columns 1..kl and kr..nx
     double *d_ainv64;            // dense inverse of level mg_dl (FP64 solver)
     float *d_ainv32;             // dense inverse of level mg_dl (mixed solver)
     double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D
@@ -258,6 +259,7 @@ int fs_sig_copy(fs_ctx *c, int dst, int src);   // slot dst <- slot src, on the 
 void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
+void fs_mg_strips(fs_ctx *c);   // electrode strips of the finest level (strip_kl, strip_kr)
 void fs_lapl_free(fs_ctx *c);
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
 // mixed-precision Poisson (fs_lapl_mixed.cu)

@@ -21,9 +21,11 @@
 //   * phi += d and ph_mi = phi (lapl_lib.F90:112-119).
 // All reductions are two-level and fixed-order: per-CTA partials, then the
 // last CTA to finish sums them in index order.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
@@ -419,13 +421,13 @@ __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
 
 // Last half sweep of the fine level (red, after the black one) fused with
 // rz = r.z over all nodes and beta = rz/rz_old (0 on the first iteration).
-__global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a) {
+__global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a, double om) {
     double v = 0.0;
     CG_NODES(a, {
         const int J = (int)j_ + 1, I = (int)(q_ - j_ * (unsigned)a.nx) + 1;
         double z = L.x[o];
         if (((I + J) & 1) == 0) {
-            z = gs_node(L, o);
+            z = relax(z, gs_node(L, o), om);
             L.x[o] = z;
         }
         v += L.rhs[o] * z;   // black nodes are final after the previous half sweep
@@ -498,6 +500,7 @@ LvT<double> lvt(const MGLevel &m) {
     LvT<double> L;
     L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
     L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
+    L.om = FS_MG_OMEGA_POST;
     return L;
 }
 
@@ -511,7 +514,30 @@ static int alloc_zero(fs_ctx *c, double **p, size_t n) {
     return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "cudaMemset");
 }
 
+// Electrode strips of the finest level (k_rb_strip): the leading and trailing
+// columns whose x faces conduct more than twice as well as their y faces, by
+// the mesh spacings of the middle row; none when either is wider than
+// FS_STRIP_MAX columns.
+void fs_mg_strips(fs_ctx *c) {
+    const int nx = c->nx, j = c->ny / 2 + 1;
+    const std::vector<double> &x = c->h_x, &y = c->h_y;
+    const double dy = y[j + 1] - y[j], dly = 0.5 * (y[j + 1] - y[j - 1]);
+    auto stretched = [&](int i) {
+        double cx = 0.0;
+        if (i > 1) cx = fmax(cx, dly / (x[i] - x[i - 1]));
+        if (i < nx) cx = fmax(cx, dly / (x[i + 1] - x[i]));
+        return cx > 2.0 * (0.5 * (x[i + 1] - x[i - 1]) / dy);
+    };
+    int kl = 0, kr = nx + 1;
+    while (kl < nx / 2 && stretched(kl + 1)) kl++;
+    while (kr - 1 > nx / 2 + 1 && stretched(kr - 1)) kr--;
+    if (kl > FS_STRIP_MAX || nx + 1 - kr > FS_STRIP_MAX) { kl = 0; kr = nx + 1; }
+    c->strip_kl = kl;
+    c->strip_kr = kr;
+}
+
 int fs_lapl_alloc(fs_ctx *c) {
+    fs_mg_strips(c);
     int nx = c->nx, ny = c->ny, nl = 0;
     for (;;) {
         MGLevel &m = c->mg[nl];
@@ -628,6 +654,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     ba.nu = nu;
     ba.dl = c->mg_dl;
     ba.ainv = c->d_ainv64;
+    ba.om = FS_MG_OMEGA_POST;
     fs_prof_begin(c, PROF_BOTTOM);
     k_bottom_smem<double><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
@@ -646,14 +673,28 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<<<gh, b, 0, c->stream>>>(f, 1, 0);
+            k_rb<<<gh, b, 0, c->stream>>>(f, 1, 0, FS_MG_OMEGA_POST);
             fs_prof_end(c);
-            fs_prof_begin(c, PROF_SMOOTH);
-            if (l == 0 && it == nu - 1)
-                k_rb_rz<<<ca->grid, 256, 0, c->stream>>>(f, *ca);
-            else
-                k_rb<<<gh, b, 0, c->stream>>>(f, 0, 0);
-            fs_prof_end(c);
+            if (l == 0 && it == nu - 1) {
+                // the strip sweeps go before the last half sweep, which is
+                // fused with r.z: red-black pairs after the black half sweep
+                const int kl = c->strip_kl, kr = c->strip_kr, ns = kl + (c->nx - kr + 1);
+                if (ns > 0) {
+                    const dim3 gs((ns + 31) / 32, (f.ny + 7) / 8);
+                    for (int s = 0; s < 2 * FS_STRIP_PAIRS; s++) {
+                        fs_prof_begin(c, PROF_SMOOTH);
+                        k_rb_strip<double><<<gs, b, 0, c->stream>>>(f, s & 1, kl, kr, FS_MG_OMEGA_POST);
+                        fs_prof_end(c);
+                    }
+                }
+                fs_prof_begin(c, PROF_SMOOTH);
+                k_rb_rz<<<ca->grid, 256, 0, c->stream>>>(f, *ca, FS_MG_OMEGA_POST);
+                fs_prof_end(c);
+            } else {
+                fs_prof_begin(c, PROF_SMOOTH);
+                k_rb<<<gh, b, 0, c->stream>>>(f, 0, 0, FS_MG_OMEGA_POST);
+                fs_prof_end(c);
+            }
         }
     }
     if (lb == 0) {   // the whole V-cycle ran in the bottom kernel: r.z separately

@@ -780,6 +780,7 @@ LvT<float> lvt_f(const MGLevelF &m) {
     LvT<float> L;
     L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
     L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
+    L.om = (float)FS_MG_OMEGA_POST;
     return L;
 }
 
@@ -897,6 +898,7 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     ba.nu = nu;
     ba.dl = c->mg_dl;
     ba.ainv = c->d_ainv32;
+    ba.om = (float)FS_MG_OMEGA_POST;
     fs_prof_begin(c, PROF_BOTTOM);
     k_bottom_smem<float><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
@@ -915,10 +917,20 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
         fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<float><<<gh, b, 0, c->stream>>>(f, 1, 0);
+            k_rb<float><<<gh, b, 0, c->stream>>>(f, 1, 0, (float)FS_MG_OMEGA_POST);
             fs_prof_end(c);
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<float><<<gh, b, 0, c->stream>>>(f, 0, 0);
+            k_rb<float><<<gh, b, 0, c->stream>>>(f, 0, 0, (float)FS_MG_OMEGA_POST);
+            fs_prof_end(c);
+        }
+    }
+    const int kl = c->strip_kl, kr = c->strip_kr, ns = kl + (c->nx - kr + 1);
+    if (ns > 0 && lb > 0) {
+        LevelT<float> f0 = level_f(c->mgf[0]);
+        const dim3 gs((ns + 31) / 32, (f0.ny + 7) / 8);
+        for (int s = 0; s < 2 * FS_STRIP_PAIRS; s++) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_rb_strip<float><<<gs, b, 0, c->stream>>>(f0, (s & 1) ? 0 : 1, kl, kr, (float)FS_MG_OMEGA_POST);
             fs_prof_end(c);
         }
     }
