@@ -501,14 +501,28 @@ __global__ void __launch_bounds__(1024) k_dense_inv(const LevelT<T> L, T *ainv) 
     }
     for (int q = t; q < DENSE_N * DENSE_N; q += 1024) ainv[q] = A[q];
 }
+// Every level of the bottom solver has at most BOTTOM_N x BOTTOM_N = 32 x 32
+// nodes, so each phase gives one node per thread: thread t owns node
+// (t mod w + 1, t / w + 1) of the level it works on, w = nx rounded up to a
+// power of two (a shift, not a division; rows packed into full warps, which
+// matters to the FP64 levels, whose pipe is paid per warp instruction).
 template <typename T>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs<T> a) {
+    static_assert(BOTTOM_THREADS == BOTTOM_N * BOTTOM_N && BOTTOM_N == 32, "one node per thread");
     extern __shared__ __align__(16) unsigned char sm_raw[];
+    __shared__ T scr[DENSE_N];
     const int t = threadIdx.x;
+    int I, J;   // this thread's node of the level set by at()
+    auto at = [&](const LevelT<T> &L) {
+        const int sh = 32 - __clz(L.nx - 1);
+        I = (t & ((1 << sh) - 1)) + 1;
+        J = (t >> sh) + 1;
+        return I <= L.nx && J <= L.ny;
+    };
     const int tot = bottom_smem_elems(a);
     T *base = (T *)sm_raw;
     const int nd = a.L[a.dl].nx * a.L[a.dl].ny;
-    T *sinv = base + 6 * tot;   // DENSE_N x DENSE_N
+    T *sinv = base + 6 * tot;   // DENSE_N x DENSE_N, transposed: sinv[j * DENSE_N + i] = ainv[i][j]
     T *sres = sinv + DENSE_N * DENSE_N;   // fine residuals of the level being restricted
     LevelT<T> S[FS_MG_MAX_LEVELS];
     {
@@ -530,13 +544,13 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
             }
             off += n;
         }
-        for (int q = t; q < DENSE_N * DENSE_N; q += BOTTOM_THREADS) sinv[q] = a.ainv[q];
+        for (int q = t; q < DENSE_N * DENSE_N; q += BOTTOM_THREADS)
+            sinv[(q & (DENSE_N - 1)) * DENSE_N + (q >> 6)] = a.ainv[q];
     }
     __syncthreads();
     auto sweep = [&](const LevelT<T> &L, int color, int zero, T om) {
-        for (int q = t; q < L.nx * L.ny; q += BOTTOM_THREADS) {
-            int I = q % L.nx + 1, J = q / L.nx + 1;
-            int o = J * L.P + I;
+        if (at(L)) {
+            const int o = J * L.P + I;
             if (((I + J) & 1) == color)
                 L.x[o] = zero ? L.rhs[o] * L.inv_mc[o] : relax(L.x[o], gs_node(L, (size_t)o), om);
             else if (zero) L.x[o] = T(0);
@@ -549,13 +563,12 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
         sweep(f, 1, 0, T(1));
         for (int it = 1; it < a.nu; it++) { sweep(f, 0, 0, T(1)); sweep(f, 1, 0, T(1)); }
         if (RestrictFW<T>::value) {   // each fine residual once, then the transpose weights
-            for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
-                const int I = q % f.nx + 1, J = q / f.nx + 1, o = J * f.P + I;
+            if (at(f)) {
+                const int o = J * f.P + I;
                 sres[o] = ((I + J) & 1) == 0 ? resid(f, (size_t)o) : T(0);
             }
             __syncthreads();
-            for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
-                const int I = q % c.nx + 1, J = q / c.nx + 1;
+            if (at(c)) {
                 T s = T(0);
                 for (int fy = max(2 * J - 2, 1); fy <= min(2 * J + 1, f.ny); fy++) {
                     const T wy = prolong_w<T>(fy, J, c.ny);
@@ -565,36 +578,29 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
                 c.rhs[J * c.P + I] = s;
             }
         } else {
-            for (int q = t; q < c.nx * c.ny; q += BOTTOM_THREADS) {
-                int I = q % c.nx + 1, J = q / c.nx + 1;
-                c.rhs[J * c.P + I] = restrict_at(f, c, I, J);
-            }
+            if (at(c)) c.rhs[J * c.P + I] = restrict_at(f, c, I, J);
         }
         __syncthreads();
     }
     {   // level dl: x = A^-1 rhs with the precomputed dense inverse
         const LevelT<T> c = S[a.dl];
+        if (t < nd) scr[t] = c.rhs[(t / c.nx + 1) * c.P + t % c.nx + 1];
+        __syncthreads();
         if (t < nd) {
             T acc = T(0);
-            for (int j = 0; j < nd; j++) acc += sinv[t * DENSE_N + j] * c.rhs[(j / c.nx + 1) * c.P + j % c.nx + 1];
+            for (int j = 0; j < nd; j++) acc += sinv[j * DENSE_N + t] * scr[j];
             c.x[(t / c.nx + 1) * c.P + t % c.nx + 1] = acc;
         }
         __syncthreads();
     }
     for (int l = a.dl - 1; l >= a.lb; l--) {
         const LevelT<T> f = S[l], c = S[l + 1];
-        for (int q = t; q < f.nx * f.ny; q += BOTTOM_THREADS) {
-            int I = q % f.nx + 1, J = q / f.nx + 1;
-            f.x[J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
-        }
+        if (at(f)) f.x[J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
         __syncthreads();
         for (int it = 0; it < a.nu; it++) { sweep(f, 1, 0, a.om); sweep(f, 0, 0, a.om); }
     }
     const LevelT<T> G = a.L[a.lb], L = S[a.lb];
-    for (int q = t; q < G.nx * G.ny; q += BOTTOM_THREADS) {
-        int I = q % G.nx + 1, J = q / G.nx + 1;
-        G.x[(size_t)J * G.P + I] = L.x[J * L.P + I];
-    }
+    if (at(L)) G.x[(size_t)J * G.P + I] = L.x[J * L.P + I];
 }
 
 // grid-stride loop over the interior nodes; o is the node's field offset
