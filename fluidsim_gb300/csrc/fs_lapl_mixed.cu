@@ -339,8 +339,8 @@ __global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *
 // true residual in FP64 and restarts the inner loop from it.  The FP32
 // recurrence drifts from the true residual (rounding of the FP32 vectors and
 // operator products); the refinement removes the drift, so the converged
-// residual is the true FP64 one.  Dot products: FP32 products summed per thread, then FP64 across
-// threads and CTAs in a fixed order.
+// residual is the true FP64 one.  Dot products of the inner loop: FP32 sums in
+// a fixed order (grid_sumf); the refinement's norms: FP64 (grid_sum2).
 struct CgmArgs {
     int nx, ny, P, nblk;
     dim3 grid;
@@ -380,13 +380,8 @@ __device__ bool grid_sum2(double v, double w, double *part, unsigned int *counte
     if (!s_last) return false;
     __threadfence();
     __shared__ double s_r[256], s_w[256];
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < nblk; k += 256) {
-        a += ((volatile double *)part)[k];
-        b += ((volatile double *)part)[nblk + k];
-    }
-    s_r[threadIdx.x] = a;
-    s_w[threadIdx.x] = b;
+    s_r[threadIdx.x] = strided_sum<256>(part, nblk, threadIdx.x);
+    s_w[threadIdx.x] = strided_sum<256>(part + nblk, nblk, threadIdx.x);
     __syncthreads();
     for (int k = 128; k > 0; k >>= 1) {
         if (threadIdx.x < k) { s_r[threadIdx.x] += s_r[threadIdx.x + k]; s_w[threadIdx.x] += s_w[threadIdx.x + k]; }
@@ -398,45 +393,59 @@ __device__ bool grid_sum2(double v, double w, double *part, unsigned int *counte
     return true;
 }
 
-// Fixed-order sums of three per-thread values; part needs 3 * nblk entries.
-__device__ bool grid_sum3(double v0, double v1, double v2, double *part, unsigned int *counter, int nblk,
-                          double out[3]) {
-    __shared__ double s_p[3][8];
+// Fixed-order FP32 sums of N per-thread values over the grid (warp shuffles,
+// then the eight warps, then the CTAs' partials by the last CTA); true in the
+// last CTA, whose thread 0 holds the sums in out.  part needs N * nblk floats.
+// The inner iteration's dot products are sums of FP32 products and feed FP32
+// updates, so FP32 sums (relative error ~1e-6 over 10^6 terms) lose nothing
+// that matters; FP64 sums would cost more than the kernel's streaming: a
+// warp-wide FP64 add occupies an SM's FP64 pipe for ~16 cycles on this GPU.
+template <int N>
+__device__ bool grid_sumf(float (&v)[N], float *part, unsigned int *counter, int nblk, double (&out)[N]) {
+    __shared__ float s_p[N][8];
     __shared__ bool s_last;
-    double v[3] = {v0, v1, v2};
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-        for (int k = 0; k < 3; k++) s_p[k][wid] = v[k];
-    __syncthreads();
+    auto block_sum = [&]() {   // v (per thread) -> s_p[k][0..7] -> v[k] in thread 0
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        if (lane == 0)
+            for (int k = 0; k < N; k++) s_p[k][wid] = v[k];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int k = 0; k < N; k++) {
+                float r = 0.0f;
+                for (int wv = 0; wv < 8; wv++) r += s_p[k][wv];
+                v[k] = r;
+            }
+    };
+    block_sum();
     if (threadIdx.x == 0) {
-        for (int k = 0; k < 3; k++) {
-            double r = 0.0;
-            for (int wv = 0; wv < 8; wv++) r += s_p[k][wv];
-            part[(size_t)k * nblk + blockIdx.x] = r;
-        }
+        for (int k = 0; k < N; k++) part[(size_t)k * nblk + blockIdx.x] = v[k];
         __threadfence();
         s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
     }
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
-    __shared__ double s_r[3][256];
-    for (int k = 0; k < 3; k++) {
-        double a = 0.0;
-        for (int b = threadIdx.x; b < nblk; b += 256) a += ((volatile double *)part)[(size_t)k * nblk + b];
-        s_r[k][threadIdx.x] = a;
+    // all N partials of a stride issued together (one L2 round trip per
+    // stride), each value's sum in stride order; loads bypass L1 (the
+    // writers' __threadfence and the counter make them visible in L2)
+#pragma unroll
+    for (int k = 0; k < N; k++) v[k] = 0.0f;
+    for (int b = threadIdx.x; b < nblk; b += 256) {
+        float t[N];
+#pragma unroll
+        for (int k = 0; k < N; k++) t[k] = __ldcg(part + (size_t)k * nblk + b);
+#pragma unroll
+        for (int k = 0; k < N; k++) v[k] += t[k];
     }
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w)
-            for (int k = 0; k < 3; k++) s_r[k][threadIdx.x] += s_r[k][threadIdx.x + w];
-        __syncthreads();
+    __syncthreads();   // every thread is past its reads of s_p above
+    block_sum();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < N; k++) out[k] = (double)v[k];
+        *counter = 0u;
     }
-    for (int k = 0; k < 3; k++) out[k] = s_r[k][0];
-    if (threadIdx.x == 0) *counter = 0u;
     return true;
 }
 
@@ -515,11 +524,17 @@ __device__ __forceinline__ float mz_ff(float z, float ze, float zw, float zn, fl
 // FCG(1): -z.(M p_old) / p_old.(M p_old)), and p.q of the new directions
 // p = z + beta p_old, q = w + beta q_old follows from the same sums:
 // p.q = z.w + 2 beta z.q + beta^2 (p_old.q_old), with p_old.(M z) = q_old.z
-// for the symmetric M.  alpha = rz / p.q.
+// for the symmetric M.  alpha = rz / p.q.  The same reduction carries r.r,
+// r.w, r.q, w.w, w.q and q.q, from which the norm of the updated residual
+// r - alpha q_new follows without a second reduction:
+// |r|^2 - 2 alpha (r.w + beta r.q) + alpha^2 (w.w + 2 beta w.q + beta^2 q.q),
+// each sum taken fresh from the vectors (no recurrence to drift), so that
+// k_cgm_upd is a plain pointwise update; the refinement and stall decisions
+// are taken here from that norm.
 __global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
     if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
     const int P = a.P;
-    float v = 0.0f, u = 0.0f, t = 0.0f;
+    float v = 0.0f, u = 0.0f, t = 0.0f, rr = 0.0f, rw = 0.0f, rq = 0.0f, ww = 0.0f, wq = 0.0f, qq = 0.0f;
     CG_VEC4(a, {
         const float4 z = ld4(a.z, o), zn = ld4(a.z, o + P), zs = ld4(a.z, o - P);
         const float zw = a.z[o - 1], ze = a.z[o + 4];
@@ -531,34 +546,56 @@ __global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
         mz.z = mz_ff(z.z, z.w, z.y, zn.z, zs.z, ce.z, ce.y, cn.z, cs.z, ex.z);
         mz.w = mz_ff(z.w, ze, z.z, zn.w, zs.w, ce.w, ce.z, cn.w, cs.w, ex.w);
         st4(a.w, o, mz);
-        v += dot4(ld4(a.r32, o), z);
-        u += dot4(z, ld4(a.q, o));
+        const float4 r = ld4(a.r32, o), q = ld4(a.q, o);
+        v += dot4(r, z);
+        u += dot4(z, q);
         t += dot4(z, mz);
+        rr += dot4(r, r);
+        rw += dot4(r, mz);
+        rq += dot4(r, q);
+        ww += dot4(mz, mz);
+        wq += dot4(mz, q);
+        qq += dot4(q, q);
     })
-    double s[3];
-    if (grid_sum3((double)v, (double)u, (double)t, a.part, &a.ctrl->counter[1], a.nblk, s) && threadIdx.x == 0) {
+    float in[9] = {v, u, t, rr, rw, rq, ww, wq, qq};
+    double s[9];
+    if (grid_sumf<9>(in, reinterpret_cast<float *>(a.part), &a.ctrl->counter[1], a.nblk, s) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
         c->rz_old = c->rz;
         c->rz = s[0];
-        const double be = c->inner_it == 0 ? 0.0 : -c->alpha * s[1] / c->rz_old;
+        const bool first = c->inner_it == 0;   // q_old = 0 after a (re)start
+        const double be = first ? 0.0 : -c->alpha * s[1] / c->rz_old;
         c->beta = be;
-        const double pq = c->inner_it == 0 ? s[2] : s[2] + 2.0 * be * s[1] + be * be * c->pq;
+        const double pq = first ? s[2] : s[2] + 2.0 * be * s[1] + be * be * c->pq;
         c->pq = pq;
-        c->alpha = pq > 0.0 ? c->rz / pq : 0.0;
+        const double al = pq > 0.0 ? c->rz / pq : 0.0;
+        c->alpha = al;
+        const double rqn = s[4] + be * s[5], qqn = s[6] + 2.0 * be * s[7] + be * be * s[8];
+        const double out = fmax(s[3] - 2.0 * al * rqn + al * al * qqn, 0.0);
+        // the learned correction stalls the iteration: plain MG-PCG for the rest of the solve
+        if (a.lpc && c->inner_it > 0 && out > 0.25 * c->rr_prev) c->lpc_off = 1;
+        c->rr_prev = out;
+        c->cg_iters += 1;
+        c->inner_it += 1;
+        c->rnorm2 = out;   // inner recurrence residual (diagnostic)
+        // this cycle's target: inner_tol, or just enough to reach rtol overall
+        const double need = 0.3 * a.rtol / fmax(c->relres, 1e-300);
+        const double tgt2 = fmax(a.inner_tol2, need * need);
+        if (!(pq > 0.0) || out <= tgt2 * c->r0in2 || c->inner_it >= a.inner_max || c->cg_iters >= a.maxit ||
+            isnan(s[3] + s[6]))
+            c->refine = 1;
     }
 }
 
-// p = z + beta p ; q = w + beta q ; x += alpha p in FP64 ; r32 -= alpha q ;
-// ||r32|| decides when the next refinement runs.  x is accumulated in FP64:
-// an FP32 correction would carry a rounding of ~eps |d| that M amplifies by
-// its condition number (~5e-4 relative residual at 1024^2), the floor no
-// inner iteration can get below.
+// p = z + beta p ; q = w + beta q ; x += alpha p in FP64 ; r32 -= alpha q.
+// x is accumulated in FP64: an FP32 correction would carry a rounding of
+// ~eps |d| that M amplifies by its condition number (~5e-4 relative residual
+// at 1024^2), the floor no inner iteration can get below.
 __global__ void __launch_bounds__(256) k_cgm_upd(const CgmArgs a) {
     if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
     const float be = (float)a.ctrl->beta;
     const double ald = a.ctrl->alpha;
     const float al = (float)ald;
-    float v = 0.0f;
     CG_VEC4(a, {
         const float4 z = ld4(a.z, o), w = ld4(a.w, o), p0 = ld4(a.p, o), q0 = ld4(a.q, o);
         const float4 p = make_float4(z.x + be * p0.x, z.y + be * p0.y, z.z + be * p0.z, z.w + be * p0.w);
@@ -574,24 +611,7 @@ __global__ void __launch_bounds__(256) k_cgm_upd(const CgmArgs a) {
         float4 r = ld4(a.r32, o);
         r.x -= al * q.x; r.y -= al * q.y; r.z -= al * q.z; r.w -= al * q.w;
         st4(a.r32, o, r);
-        v += dot4(r, r);
     })
-    double out;
-    if (grid_sum<256>((double)v, a.part, &a.ctrl->counter[3], a.nblk, &out) && threadIdx.x == 0) {
-        Ctrl *c = a.ctrl;
-        // the learned correction stalls the iteration: plain MG-PCG for the rest of the solve
-        if (a.lpc && c->inner_it > 0 && out > 0.25 * c->rr_prev) c->lpc_off = 1;
-        c->rr_prev = out;
-        c->cg_iters += 1;
-        c->inner_it += 1;
-        c->rnorm2 = out;   // inner recurrence residual (diagnostic)
-        // this cycle's target: inner_tol, or just enough to reach rtol overall
-        const double need = 0.3 * a.rtol / fmax(c->relres, 1e-300);
-        const double tgt2 = fmax(a.inner_tol2, need * need);
-        if (!(c->pq > 0.0) || out <= tgt2 * c->r0in2 || c->inner_it >= a.inner_max ||
-            c->cg_iters >= a.maxit || isnan(out))
-            c->refine = 1;
-    }
 }
 
 // refinement: r = D b - M x in FP64, r32 = r; convergence on the FP64 residual
@@ -817,8 +837,8 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         if (e == cudaSuccess) e = cudaMemset(*v, 0, c->field_elems * sizeof(float));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 CG vectors)");
     }
-    {   // three partials per CTA of the CG reductions (<= 4 CTAs per SM)
-        const int need = 3 * 4 * c->nsm;
+    {   // nine partials per CTA of the CG reductions (<= 4 CTAs per SM)
+        const int need = 9 * 4 * c->nsm;
         if (c->cg_nblk < need) {
             cudaFree(c->d_cg_part);
             cudaError_t e = cudaMalloc(&c->d_cg_part, sizeof(double) * need);

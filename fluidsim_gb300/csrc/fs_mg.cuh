@@ -29,6 +29,25 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// part[tid] + part[tid + NTH] + part[tid + 2 NTH] + ... (< nblk), summed in
+// that order, the loads issued four at a time: the partials were just written
+// by other CTAs, so each load is an L2 round trip, and a chain of dependent
+// ones is what the last CTA of a grid reduction would otherwise wait on.  The
+// loads bypass L1 (ld.global.cg): the writers' __threadfence and the counter
+// make their values visible in L2.
+template <int NTH>
+__device__ __forceinline__ double strided_sum(const double *part, int nblk, int tid) {
+    double s = 0.0;
+    for (int b = tid; b < nblk; b += 4 * NTH) {
+        double v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = b + k * NTH < nblk ? __ldcg(part + b + k * NTH) : 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) s += v[k];
+    }
+    return s;
+}
+
 // Block sum of v, then deterministic grid sum by the last CTA.  Returns true
 // in the last CTA (all threads), with *out written.
 template <int NTH>
@@ -52,9 +71,7 @@ __device__ bool grid_sum(double v, double *part, unsigned int *counter, int nblk
     if (!s_last) return false;
     __threadfence();
     __shared__ double s_r[NTH];
-    double s = 0.0;
-    for (int b = tid; b < nblk; b += NTH) s += ((volatile double *)part)[b];
-    s_r[tid] = s;
+    s_r[tid] = strided_sum<NTH>(part, nblk, tid);
     __syncthreads();
     for (int w = NTH / 2; w > 0; w >>= 1) {
         if (tid < w) s_r[tid] += s_r[tid + w];
