@@ -211,6 +211,7 @@ struct fs_ctx {
     float *d_tab32;
     MGLevelF mgf[FS_MG_MAX_LEVELS];
     float *p32, *q32, *w32;      // FP32 inner CG vectors (w = M z)
+    float *xh32, *xl32, *dinv32; // the mixed CG's iterate as a float-float pair; 1/D in FP32
     // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
     struct LpcState *lpc;
     int lpc_on, lpc_level;

@@ -324,19 +324,23 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
 }
 
 // 1/D of the row scaling D = dlx dly r (a property of the mesh)
-__global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *dinv) {
+__global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *dinv, float *dinv32) {
     const int gi = blockIdx.x * blockDim.x + threadIdx.x + 1, gj = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (gi > nx || gj > ny) return;
-    dinv[(size_t)gj * P + gi] = 1.0 / (m.dlx[gi - 1] * m.dly[gj - 1] * (cyl ? m.r[gj] : 1.0));
+    const double d = 1.0 / (m.dlx[gi - 1] * m.dly[gj - 1] * (cyl ? m.r[gj] : 1.0));
+    dinv[(size_t)gj * P + gi] = d;
+    dinv32[(size_t)gj * P + gi] = (float)d;
 }
 
 // --------------------------------------------- FP32 CG under FP64 refinement
-// Outer loop (FP64): r = D b - M x, ||r|| / ||b|| checked against lapl_rtol.
-// Inner loop: flexible PCG with FP32 vectors and the FP32 V-cycle on the
-// current residual, the iterate accumulated in FP64, run until its FP32
+// Outer loop: r = D b - M x to FP64 accuracy, ||r|| / ||b|| checked against
+// lapl_rtol.  Inner loop: flexible PCG with FP32 vectors and the FP32 V-cycle
+// on the current residual, the iterate accumulated as a float-float pair
+// (~48-bit significand; FP32 arithmetic, which this GPU issues ~60 times
+// faster than FP64), run until its FP32
 // recurrence residual has fallen by inner_tol (or just enough to reach
 // lapl_rtol, or inner_max iterations); then the refinement recomputes the
-// true residual in FP64 and restarts the inner loop from it.  The FP32
+// true residual in float-float and restarts the inner loop from it.  The FP32
 // recurrence drifts from the true residual (rounding of the FP32 vectors and
 // operator products); the refinement removes the drift, so the converged
 // residual is the true FP64 one.  Dot products of the inner loop: FP32 sums in
@@ -344,7 +348,9 @@ __global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *
 struct CgmArgs {
     int nx, ny, P, nblk;
     dim3 grid;
-    double *x, *r, *rhs, *dinv, *part;   // FP64: iterate, true residual, D b, 1/D
+    double *rhs, *dinv, *part;           // FP64: D b, 1/D; reduction partials
+    float *xh, *xl;                      // the iterate as a float-float pair xh + xl
+    const float *dinv32;                 // 1/D rounded to FP32 (the refinement's norm)
     float *z, *r32, *p, *q, *w;          // FP32 inner vectors (z, r32 are level 0 of the V-cycle; w = M z)
     const float *ce, *cn, *extra;
     Ctrl *ctrl;
@@ -455,8 +461,8 @@ __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
     CG_NODES(a, {
         const double b = a.rhs[o];
         const float b32 = (float)b;
-        a.x[o] = 0.0;
-        a.r[o] = b;
+        a.xh[o] = 0.0f;
+        a.xl[o] = 0.0f;
         a.r32[o] = b32;
         a.p[o] = 0.0f;
         a.q[o] = 0.0f;
@@ -490,6 +496,32 @@ __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a
 // The inner-loop kernels stream whole rows 1..ny in float4 steps: every
 // inner vector and coefficient is zero on the ghost ring and the row padding,
 // so those lanes add nothing to the dot products and stay zero.
+
+// Float-float values hi + lo (|lo| <= ulp(hi) / 2) by error-free
+// transformations: Knuth's two-sum, Dekker's fast two-sum and the FMA
+// two-product; the _rn intrinsics keep the compiler from contracting them.
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF ff_fast2(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_sum(FF a, FF b) {
+    const float s = __fadd_rn(a.h, b.h), bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return ff_fast2(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ FF ff_mulf(FF a, float c) {   // (a.h + a.l) c
+    const float p = __fmul_rn(a.h, c);
+    return ff_fast2(p, __fmaf_rn(a.l, c, __fmaf_rn(a.h, c, -p)));
+}
+// a double split into a float-float pair (three FP64-pipe instructions)
+__device__ __forceinline__ FF ff_from(double d) {
+    const float h = __double2float_rn(d);
+    return {h, __double2float_rn(d - (double)h)};
+}
 
 // M z at one node in float-float arithmetic: each face term c (z_i - z_j) is
 // formed exactly (the difference of neighbouring, similar values is exact,
@@ -587,63 +619,94 @@ __global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
     }
 }
 
-// p = z + beta p ; q = w + beta q ; x += alpha p in FP64 ; r32 -= alpha q.
-// x is accumulated in FP64: an FP32 correction would carry a rounding of
+// p = z + beta p ; q = w + beta q ; x += alpha p in float-float ; r32 -= alpha q.
+// x is accumulated beyond FP32: an FP32 correction would carry a rounding of
 // ~eps |d| that M amplifies by its condition number (~5e-4 relative residual
 // at 1024^2), the floor no inner iteration can get below.
 __global__ void __launch_bounds__(256) k_cgm_upd(const CgmArgs a) {
     if (a.ctrl->cg_done || a.ctrl->cg_fail) return;
     const float be = (float)a.ctrl->beta;
-    const double ald = a.ctrl->alpha;
-    const float al = (float)ald;
+    const FF alf = ff_from(a.ctrl->alpha);
+    const float al = alf.h;
     CG_VEC4(a, {
         const float4 z = ld4(a.z, o), w = ld4(a.w, o), p0 = ld4(a.p, o), q0 = ld4(a.q, o);
         const float4 p = make_float4(z.x + be * p0.x, z.y + be * p0.y, z.z + be * p0.z, z.w + be * p0.w);
         const float4 q = make_float4(w.x + be * q0.x, w.y + be * q0.y, w.z + be * q0.z, w.w + be * q0.w);
         st4(a.p, o, p);
         st4(a.q, o, q);
-        double2 *x2 = reinterpret_cast<double2 *>(a.x + o);
-        double2 x01 = x2[0], x23 = x2[1];
-        x01.x += ald * (double)p.x; x01.y += ald * (double)p.y;
-        x23.x += ald * (double)p.z; x23.y += ald * (double)p.w;
-        x2[0] = x01;
-        x2[1] = x23;
+        float4 xh = ld4(a.xh, o), xl = ld4(a.xl, o);
+        FF t;
+        t = ff_sum({xh.x, xl.x}, ff_mulf(alf, p.x)); xh.x = t.h; xl.x = t.l;
+        t = ff_sum({xh.y, xl.y}, ff_mulf(alf, p.y)); xh.y = t.h; xl.y = t.l;
+        t = ff_sum({xh.z, xl.z}, ff_mulf(alf, p.z)); xh.z = t.h; xl.z = t.l;
+        t = ff_sum({xh.w, xl.w}, ff_mulf(alf, p.w)); xh.w = t.h; xl.w = t.l;
+        st4(a.xh, o, xh);
+        st4(a.xl, o, xl);
         float4 r = ld4(a.r32, o);
         r.x -= al * q.x; r.y -= al * q.y; r.z -= al * q.z; r.w -= al * q.w;
         st4(a.r32, o, r);
     })
 }
 
-// refinement: r = D b - M x in FP64, r32 = r; convergence on the FP64 residual
+// refinement: r = D b - M x in float-float (each face term c (x_i - x_j) and
+// the sum carried to ~48 bits: the terms are up to ~1e3 times larger than
+// their sum, which must be right to well below lapl_rtol), r32 = r rounded;
+// convergence on |D^-1 r| / |D^-1 D b|.  The norms are FP32 sums of values
+// scaled by sc, a power of two near 1 / |D^-1 D b| (so that the summands stay
+// far inside the FP32 range for relative residuals from 1e3 down to 1e-15).
 __global__ void __launch_bounds__(256) k_cgm_refine(const CgmArgs a) {
     if (!a.ctrl->refine || a.ctrl->cg_done || a.ctrl->cg_fail) return;
-    double v = 0.0, w = 0.0;
+    const double bn2 = a.ctrl->bnorm2;
+    // sc = 2^-floor(e/2), e the binary exponent of |b|^2: integer arithmetic only
+    const int e2 = (int)((__double_as_longlong(bn2) >> 52) & 0x7ff) - 1023;
+    const int esc = min(max(-(e2 >> 1), -120), 120);
+    const float sc = __int_as_float((127 + esc) << 23);
+    float v = 0.0f, w = 0.0f;
     CG_NODES(a, {
-        const double xc = a.x[o];
-        const double mx = (double)a.ce[o] * (xc - a.x[o + 1]) + (double)a.ce[o - 1] * (xc - a.x[o - 1])
-                        + (double)a.cn[o] * (xc - a.x[o + a.P]) + (double)a.cn[o - a.P] * (xc - a.x[o - a.P])
-                        + (double)a.extra[o] * xc;
-        const double rr = a.rhs[o] - mx;
-        a.r[o] = rr;
-        const float r32 = (float)rr;
+        const FF xc = {a.xh[o], a.xl[o]};
+        auto face = [&](float c, size_t on) {   // c (x_o - x_on)
+            return ff_mulf(ff_sum(xc, ff_neg({a.xh[on], a.xl[on]})), c);
+        };
+        FF mx = face(a.ce[o], o + 1);
+        mx = ff_sum(mx, face(a.ce[o - 1], o - 1));
+        mx = ff_sum(mx, face(a.cn[o], o + a.P));
+        mx = ff_sum(mx, face(a.cn[o - a.P], o - a.P));
+        mx = ff_sum(mx, ff_mulf(xc, a.extra[o]));
+        const FF rr = ff_sum(ff_from(a.rhs[o]), ff_neg(mx));
+        const float r32 = __fadd_rn(rr.h, rr.l);
         a.r32[o] = r32;
-        const double u = rr * a.dinv[o];
+        const float u = r32 * a.dinv32[o] * sc;
         v += u * u;
-        w += (double)(r32 * r32);
+        w += r32 * r32;
     })
-    double sv, sw;
-    if (grid_sum2(v, w, a.part, &a.ctrl->counter[4], a.nblk, sv, sw) && threadIdx.x == 0) {
+    float in[2] = {v, w};
+    double sums[2];
+    if (grid_sumf<2>(in, reinterpret_cast<float *>(a.part), &a.ctrl->counter[4], a.nblk, sums) && threadIdx.x == 0) {
         Ctrl *c = a.ctrl;
-        const double prev = c->relres;
-        c->rnorm2 = sv;
-        c->r0in2 = sw;
-        c->relres = c->bnorm2 > 0.0 ? sqrt(sv / c->bnorm2) : 0.0;
+        const double prev = c->relres, s2 = (double)sc * (double)sc;
+        c->rnorm2 = sums[0] / s2;
+        c->r0in2 = sums[1];
+        c->relres = bn2 > 0.0 ? sqrt(sums[0] / (bn2 * s2)) : 0.0;
         c->inner_it = 0;
         c->refine = 0;
-        c->rr_prev = sw;
+        c->rr_prev = sums[1];
         if (c->relres <= a.rtol) c->cg_done = 1;
-        else if (isnan(sv) || c->cg_iters >= a.maxit || !(c->relres < prev)) c->cg_fail = 1;
+        else if (isnan(sums[0]) || c->cg_iters >= a.maxit || !(c->relres < prev)) c->cg_fail = 1;
         if (a.use_cond && (c->cg_done || c->cg_fail)) cudaGraphSetConditional(a.cond, 0u);
+    }
+}
+
+// phi(interior) += xh + xl ; ph_mi = phi (lapl_lib.F90:112-119), after convergence
+__global__ void k_phi_update_ff(double *ph, double *phm, const float *xh, const float *xl, int nx, int ny, int P,
+                                const Ctrl *ctrl) {
+    if (!ctrl->cg_done || ctrl->cg_fail) return;
+    size_t n = (size_t)(ny + 2) * P;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
+        int gi = (int)(o % P), gj = (int)(o / P);
+        double v = ph[o];
+        if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) v = v + ((double)xh[o] + (double)xl[o]);
+        ph[o] = v;
+        phm[o] = v;
     }
 }
 
@@ -664,7 +727,7 @@ struct LpcArgs {
     const float *y;
     double *rhs64;                       // harvest: fine r - M z in FP64 (or null)
     float *tgt;                          // harvest: target slot
-    const double *e;                     // harvest: solution of M e = r - M z
+    const float *eh, *el;                // harvest: solution of M e = r - M z (float-float)
 };
 
 __global__ void __launch_bounds__(256) k_lpc_opfeat(const LpcArgs l, const CgmArgs a) {
@@ -782,7 +845,11 @@ __global__ void k_lpc_target(const LpcArgs l, const CgmArgs a) {
         double acc = 0.0;
         int cnt = 0;
         for (int j = (J - 1) * s + 1; j <= min(J * s, a.ny); j++)
-            for (int i = (I - 1) * s + 1; i <= min(I * s, a.nx); i++) { acc += l.e[(size_t)j * a.P + i]; cnt++; }
+            for (int i = (I - 1) * s + 1; i <= min(I * s, a.nx); i++) {
+                const size_t o = (size_t)j * a.P + i;
+                acc += (double)l.eh[o] + (double)l.el[o];
+                cnt++;
+            }
         const double sc = a.ctrl->lpc_s > 0.0 ? a.ctrl->lpc_mcm / a.ctrl->lpc_s : 0.0;
         v = (float)(acc / cnt * sc);
     }
@@ -831,7 +898,7 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         }
         m.res = nullptr;
     }
-    float **vecs[] = {&c->p32, &c->q32, &c->w32};
+    float **vecs[] = {&c->p32, &c->q32, &c->w32, &c->xh32, &c->xl32, &c->dinv32};
     for (float **v : vecs) {
         cudaError_t e = cudaMalloc(v, c->field_elems * sizeof(float));
         if (e == cudaSuccess) e = cudaMemset(*v, 0, c->field_elems * sizeof(float));
@@ -863,7 +930,7 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
     }
     c->launches++;
     k_dinv<<<grid2(c->nx, c->ny, dim3(32, 8)), dim3(32, 8), 0, c->stream>>>(c->mesh, c->nx, c->ny, c->pitch,
-                                                                           c->cfg.cyl, c->dinv);
+                                                                           c->cfg.cyl, c->dinv, c->dinv32);
     return fs_cuda_check(c, cudaGetLastError(), "row scaling");
 }
 
@@ -878,6 +945,9 @@ void fs_lapl_free_mixed(fs_ctx *c) {
     cudaFree(c->p32);
     cudaFree(c->q32);
     cudaFree(c->w32);
+    cudaFree(c->xh32);
+    cudaFree(c->xl32);
+    cudaFree(c->dinv32);
     cudaFree(c->d_ainv32);
 }
 
@@ -1028,7 +1098,8 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     if (e == cudaSuccess)
         e = cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        k_phi_update<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
+        k_phi_update_ff<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xh32, c->xl32, c->nx, c->ny, c->pitch,
+                                                         c->d_ctrl);
         e = cudaStreamEndCapture(c->stream, &g);
     }
     c->launches = l0;
@@ -1085,7 +1156,7 @@ static CgmArgs cgm_args(fs_ctx *c) {
         ca.nblk = (int)(nb < cap ? nb : cap);
         ca.grid = dim3(ca.nblk);
     }
-    ca.x = c->xs; ca.r = c->r;
+    ca.xh = c->xh32; ca.xl = c->xl32; ca.dinv32 = c->dinv32;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
     ca.z = m0.x; ca.r32 = m0.rhs; ca.p = c->p32; ca.q = c->q32; ca.w = c->w32;
     ca.ce = m0.ce; ca.cn = m0.cn; ca.extra = m0.extra;
@@ -1202,7 +1273,8 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     *lerr = 0;
     c->faces_valid = 0;
     c->launches++;
-    k_phi_update<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xs, c->nx, c->ny, c->pitch, c->d_ctrl);
+    k_phi_update_ff<<<4 * c->nsm, 256, 0, c->stream>>>(c->ph, c->ph_mi, c->xh32, c->xl32, c->nx, c->ny, c->pitch,
+                                                         c->d_ctrl);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fs_cuda_check(c, e, "Poisson kernels (mixed)");
     return FS_OK;
@@ -1316,7 +1388,8 @@ int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added) {
         (void)s;
         (void)mcm;
         lh.tgt = L->dtgt + slot * px;
-        lh.e = c->xs;
+        lh.eh = c->xh32;
+        lh.el = c->xl32;
         k_lpc_target<<<(int)((px + 255) / 256), 256, 0, c->stream>>>(lh, ca);
         L->nsamp++;
         (*added)++;
