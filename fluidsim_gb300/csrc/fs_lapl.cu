@@ -788,20 +788,25 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_prof_begin(c, PROF_ASSEMBLE);
     k_assemble<<<g, LNT, 0, c->stream>>>(a);
     fs_prof_end(c);
-    // coarse operators
-    dim3 b2(16, 16);
-    for (int l = 0; l + 1 < c->mg_nlev; l++) {
-        LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+    // coarse operators: one launch per large level, then one CTA for the
+    // small levels and the dense inverse
+    {
+        CoarsenTail<double> ct;
+        for (int l = 0; l < c->mg_nlev; l++) ct.L[l] = level_dev(c->mg[l]);
+        ct.nl = c->mg_nlev;
+        ct.l0 = coarsen_tail_level(ct.L, ct.nl);
+        ct.dl = c->mg_dl;
+        ct.ainv = c->d_ainv64;
+        dim3 b2(16, 16);
+        for (int l = 1; l < ct.l0; l++) {
+            fs_prof_begin(c, PROF_COARSEN);
+            k_coarsen<<<grid2(ct.L[l].nx, ct.L[l].ny, b2), b2, 0, c->stream>>>(ct.L[l - 1], ct.L[l]);
+            fs_prof_end(c);
+        }
         fs_prof_begin(c, PROF_COARSEN);
-        k_coarsen<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(f, cc);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_COARSEN);
-        k_coarsen_diag<<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
+        k_coarsen_tail<double><<<1, 1024, 0, c->stream>>>(ct);
         fs_prof_end(c);
     }
-    fs_prof_begin(c, PROF_COARSEN);
-    k_dense_inv<double><<<1, 1024, 0, c->stream>>>(level_dev(c->mg[c->mg_dl]), c->d_ainv64);
-    fs_prof_end(c);
     // CG on M d = D b
     CgArgs ca;
     ca.nx = c->nx; ca.ny = c->ny; ca.P = c->pitch;

@@ -1200,19 +1200,24 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_prof_begin(c, PROF_ASSEMBLE);
     k_assemble_mix<<<grid2(c->nx, c->ny, dim3(ABX, ABY)), ANT, 0, c->stream>>>(a);
     fs_prof_end(c);
-    dim3 b2(16, 16);
-    for (int l = 0; l + 1 < c->mg_nlev; l++) {
-        LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+    {   // coarse operators: one launch per large level, then one CTA for the
+        // small levels and the dense inverse
+        CoarsenTail<float> ct;
+        for (int l = 0; l < c->mg_nlev; l++) ct.L[l] = level_f(c->mgf[l]);
+        ct.nl = c->mg_nlev;
+        ct.l0 = coarsen_tail_level(ct.L, ct.nl);
+        ct.dl = c->mg_dl;
+        ct.ainv = c->d_ainv32;
+        dim3 b2(16, 16);
+        for (int l = 1; l < ct.l0; l++) {
+            fs_prof_begin(c, PROF_COARSEN);
+            k_coarsen<float><<<grid2(ct.L[l].nx, ct.L[l].ny, b2), b2, 0, c->stream>>>(ct.L[l - 1], ct.L[l]);
+            fs_prof_end(c);
+        }
         fs_prof_begin(c, PROF_COARSEN);
-        k_coarsen<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(f, cc);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_COARSEN);
-        k_coarsen_diag<float><<<grid2(cc.nx, cc.ny, b2), b2, 0, c->stream>>>(cc);
+        k_coarsen_tail<float><<<1, 1024, 0, c->stream>>>(ct);
         fs_prof_end(c);
     }
-    fs_prof_begin(c, PROF_COARSEN);
-    k_dense_inv<float><<<1, 1024, 0, c->stream>>>(level_f(c->mgf[c->mg_dl]), c->d_ainv32);
-    fs_prof_end(c);
     CgmArgs ca = cgm_args(c);
     if (ca.lpc) {   // the network's operator features, only for a solve that runs it
         LpcArgs l = lpc_args(c);

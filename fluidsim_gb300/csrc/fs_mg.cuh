@@ -93,67 +93,79 @@ struct LevelT {
 };
 using LevelDev = LevelT<double>;
 
+// Coarse operators of the 2x2 aggregation: an aggregate's x face conducts as
+// the fine x faces across it in parallel, each in series with half of the
+// fine faces inside the two aggregates it joins (y alike), and the boundary
+// remainder of a fine cell, in series with half of its aggregate's inner
+// face, adds up.  The arithmetic is FP32 on every level, also under the FP64
+// solver: the coarse operators only shape its preconditioner (a fixed linear
+// map either way), and the FP64 divisions cost ~20 us a level on this GPU.
 template <typename T>
-__device__ __forceinline__ T inv_or_big(T c) {
-    const T tiny = sizeof(T) == 8 ? T(1e-300) : T(1e-37), big = sizeof(T) == 8 ? T(1e300) : T(1e37);
-    return c > tiny ? T(1) / c : big;
+__device__ __forceinline__ float inv_or_big(T c) {
+    const float cf = (float)c;
+    return cf > 1e-37f ? 1.0f / cf : 1e37f;
 }
-
-// coarse operator of one aggregate level (series along, parallel across faces)
+// x face between aggregates (I, J) and (I + 1, J); 0 at the grid's edges
 template <typename T>
-__device__ void coarsen_cell(const LevelT<T> &f, const LevelT<T> &c, int I, int J) {
+__device__ float coarse_ce(const LevelT<T> &f, int cnx, int I, int J) {
+    if (I < 1 || I >= cnx) return 0.0f;
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
-    const size_t oc = (size_t)J * c.P + I;
-    T ce = T(0), cn = T(0), ex = T(0);
-    if (I < c.nx) {
-        const int gx0 = fx1 + 1, gx1 = min(fx1 + 2, f.nx);
-        for (int fy = fy0; fy <= fy1; fy++) {
-            T R = inv_or_big(f.ce[(size_t)fy * f.P + fx1]);
-            if (fx1 > fx0) R += T(0.5) * inv_or_big(f.ce[(size_t)fy * f.P + fx0]);
-            if (gx1 > gx0) R += T(0.5) * inv_or_big(f.ce[(size_t)fy * f.P + gx0]);
-            ce += T(1) / R;
-        }
+    const int gx0 = fx1 + 1, gx1 = min(fx1 + 2, f.nx);
+    float ce = 0.0f;
+    for (int fy = fy0; fy <= fy1; fy++) {
+        float R = inv_or_big(f.ce[(size_t)fy * f.P + fx1]);
+        if (fx1 > fx0) R += 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + fx0]);
+        if (gx1 > gx0) R += 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + gx0]);
+        ce += 1.0f / R;
     }
-    if (J < c.ny) {
-        const int gy0 = fy1 + 1, gy1 = min(fy1 + 2, f.ny);
-        for (int fx = fx0; fx <= fx1; fx++) {
-            T R = inv_or_big(f.cn[(size_t)fy1 * f.P + fx]);
-            if (fy1 > fy0) R += T(0.5) * inv_or_big(f.cn[(size_t)fy0 * f.P + fx]);
-            if (gy1 > gy0) R += T(0.5) * inv_or_big(f.cn[(size_t)gy0 * f.P + fx]);
-            cn += T(1) / R;
-        }
+    return ce;
+}
+// y face between aggregates (I, J) and (I, J + 1)
+template <typename T>
+__device__ float coarse_cn(const LevelT<T> &f, int cny, int I, int J) {
+    if (J < 1 || J >= cny) return 0.0f;
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    const int gy0 = fy1 + 1, gy1 = min(fy1 + 2, f.ny);
+    float cn = 0.0f;
+    for (int fx = fx0; fx <= fx1; fx++) {
+        float R = inv_or_big(f.cn[(size_t)fy1 * f.P + fx]);
+        if (fy1 > fy0) R += 0.5f * inv_or_big(f.cn[(size_t)fy0 * f.P + fx]);
+        if (gy1 > gy0) R += 0.5f * inv_or_big(f.cn[(size_t)gy0 * f.P + fx]);
+        cn += 1.0f / R;
     }
+    return cn;
+}
+template <typename T>
+__device__ float coarse_extra(const LevelT<T> &f, int I, int J) {
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    float ex = 0.0f;
     for (int fy = fy0; fy <= fy1; fy++)
         for (int fx = fx0; fx <= fx1; fx++) {
-            T e = f.extra[(size_t)fy * f.P + fx];
-            if (e > T(0) && fx1 > fx0) {
-                T ci = f.ce[(size_t)fy * f.P + fx0];
-                e = T(1) / (T(1) / e + T(0.5) * inv_or_big(ci));
-            }
+            float e = (float)f.extra[(size_t)fy * f.P + fx];
+            if (e > 0.0f && fx1 > fx0) e = 1.0f / (1.0f / e + 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + fx0]));
             ex += e;
         }
-    c.ce[oc] = ce;
-    c.cn[oc] = cn;
-    c.extra[oc] = ex;
+    return ex;
 }
-
+// the whole coarse row of aggregate (I, J): its faces, remainder, diagonal
+// and inverse diagonal (the west and south faces recomputed, not read back,
+// so one pass builds a level)
 template <typename T>
-__device__ void coarsen_diag(const LevelT<T> &c, int I, int J) {
+__device__ void coarsen_cell(const LevelT<T> &f, const LevelT<T> &c, int I, int J) {
     const size_t oc = (size_t)J * c.P + I;
-    T mc = c.ce[oc] + c.ce[oc - 1] + c.cn[oc] + c.cn[oc - c.P] + c.extra[oc];
-    c.mc[oc] = mc;
-    c.inv_mc[oc] = mc > T(0) ? T(1) / mc : T(0);
+    const float ce = coarse_ce(f, c.nx, I, J), cn = coarse_cn(f, c.ny, I, J), ex = coarse_extra(f, I, J);
+    const float mc = ce + coarse_ce(f, c.nx, I - 1, J) + cn + coarse_cn(f, c.ny, I, J - 1) + ex;
+    c.ce[oc] = (T)ce;
+    c.cn[oc] = (T)cn;
+    c.extra[oc] = (T)ex;
+    c.mc[oc] = (T)mc;
+    c.inv_mc[oc] = mc > 0.0f ? (T)(1.0f / mc) : T(0);
 }
 
 template <typename T>
 __global__ void k_coarsen(const LevelT<T> f, const LevelT<T> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (I <= c.nx && J <= c.ny) coarsen_cell(f, c, I, J);
-}
-template <typename T>
-__global__ void k_coarsen_diag(const LevelT<T> c) {
-    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (I <= c.nx && J <= c.ny) coarsen_diag(c, I, J);
 }
 
 // Gauss-Seidel update of one node
@@ -442,7 +454,7 @@ struct BottomArgs {
 };
 // The V-cycle over levels [lb, dl] with every level held in shared memory
 // (operators, right-hand sides, iterates), and level dl -- the first with at
-// most 64 unknowns -- solved exactly with its dense inverse (k_dense_inv, once
+// most 64 unknowns -- solved exactly with its dense inverse (dense_inverse, once
 // per solve) instead of recursing further: ~20 dependent phases instead of
 // ~50.  Only the top level's right-hand side is read from, and its iterate
 // written to, global memory.
@@ -466,63 +478,93 @@ inline int bottom_dense_level(const BottomArgs<T> &a) {
     return l;
 }
 
-// Exact inverse of the level operator (at most 64 unknowns), once per solve:
-// in-place Gauss-Jordan without pivoting (the operator is symmetric positive
-// definite), one CTA, on a 64 x 64 matrix (identity beyond the n unknowns) so
-// that every index is a shift.  A node without a positive pivot gets x = 0.
-// ainv is 64 x 64, row-major over the compact index (J-1)*nx + I-1.
+// Inverse of the operator of level L (at most 64 unknowns), once per solve,
+// by Gauss-Jordan elimination without pivoting (the operator is symmetric
+// positive definite) on a 64 x 64 matrix (identity beyond the n unknowns),
+// in FP32 on every level type: it is the preconditioner's exact coarsest
+// solve, to FP32 accuracy.  The 1024 threads of the CTA hold the matrix in
+// registers, thread t the four entries (t / 16, 4 (t % 16) .. + 3); pivot k
+// reads row k and column k from shared buffers that the previous pivot's
+// owners wrote (double-buffered: one barrier per pivot).  A node without a
+// positive pivot gets x = 0.  ainv is row-major over the compact index
+// (J-1)*nx + I-1.
 #define DENSE_N 64
 template <typename T>
-__global__ void __launch_bounds__(1024) k_dense_inv(const LevelT<T> L, T *ainv) {
-    __shared__ T A[DENSE_N * DENSE_N];
-    __shared__ T col[DENSE_N];
+__device__ void dense_inverse(const LevelT<T> &L, T *ainv) {
+    __shared__ float rowb[2][DENSE_N], colb[2][DENSE_N];
     const int nx = L.nx, n = L.nx * L.ny, t = threadIdx.x;
-    for (int q = t; q < DENSE_N * DENSE_N; q += 1024) {
-        const int r = q >> 6, cidx = q & (DENSE_N - 1);
-        T v = T(0);
-        if (r >= n || cidx >= n) {
-            v = r == cidx ? T(1) : T(0);
+    const int i = t >> 4, j0 = (t & 15) * 4;
+    float a[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int cidx = j0 + m;
+        float v = 0.0f;
+        if (i >= n || cidx >= n) {
+            v = i == cidx ? 1.0f : 0.0f;
         } else {
-            const int I = r % nx + 1, J = r / nx + 1;
+            const int I = i % nx + 1, J = i / nx + 1;
             const size_t o = (size_t)J * L.P + I;
-            if (cidx == r) v = L.mc[o];
-            else if (cidx == r + 1 && I < nx) v = -L.ce[o];
-            else if (cidx == r - 1 && I > 1) v = -L.ce[o - 1];
-            else if (cidx == r + nx) v = -L.cn[o];
-            else if (cidx == r - nx) v = -L.cn[o - L.P];
+            if (cidx == i) v = (float)L.mc[o];
+            else if (cidx == i + 1 && I < nx) v = -(float)L.ce[o];
+            else if (cidx == i - 1 && I > 1) v = -(float)L.ce[o - 1];
+            else if (cidx == i + nx) v = -(float)L.cn[o];
+            else if (cidx == i - nx) v = -(float)L.cn[o - L.P];
         }
-        A[q] = v;
+        a[m] = v;
     }
+    auto publish = [&](int k, int b) {   // row k and column k as they stand
+        if (i == k)
+            for (int m = 0; m < 4; m++) rowb[b][j0 + m] = a[m];
+        if (k >= j0 && k < j0 + 4) colb[b][i] = a[k - j0];
+    };
+    publish(0, 0);
     __syncthreads();
-    const int j = t & (DENSE_N - 1), i0 = t >> 6;   // this thread's column, first row
     for (int k = 0; k < n; k++) {
-        // column k and the pivot as they stand
-        if (t < DENSE_N) col[t] = A[(t << 6) + k];
-        __syncthreads();
-        const T piv = col[k];
-        const bool ok = piv > T(0);
-        // row k: A[k][j] /= piv, with A[k][k] = 1/piv (64 threads)
-        if (t < DENSE_N) {
-            const int jj = t;
-            A[(k << 6) + jj] = ok ? (jj == k ? T(1) : A[(k << 6) + jj]) / piv : T(0);
+        const int b = k & 1;
+        const float piv = colb[b][k], ip = piv > 0.0f ? 1.0f / piv : 0.0f;
+        const float cip = colb[b][i] * ip;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int j = j0 + m;
+            const float rkj = rowb[b][j];
+            if (i == k) a[m] = j == k ? ip : rkj * ip;
+            else a[m] = j == k ? -cip : a[m] - cip * rkj;
         }
-        __syncthreads();
-        // other rows: A[i][j] -= col_i A[k][j] (j != k), A[i][k] = -col_i A[k][k]
-        const T akj = A[(k << 6) + j];
-        for (int i = i0; i < DENSE_N; i += 1024 / DENSE_N) {
-            if (i == k) continue;
-            const int q = (i << 6) + j;
-            A[q] = j == k ? -col[i] * akj : A[q] - col[i] * akj;
-        }
+        if (k + 1 < n) publish(k + 1, b ^ 1);
         __syncthreads();
     }
-    for (int q = t; q < DENSE_N * DENSE_N; q += 1024) ainv[q] = A[q];
+#pragma unroll
+    for (int m = 0; m < 4; m++) ainv[i * DENSE_N + j0 + m] = (T)a[m];
 }
-// Every level of the bottom solver has at most BOTTOM_N x BOTTOM_N = 32 x 32
-// nodes, so each phase gives one node per thread: thread t owns node
-// (t mod w + 1, t / w + 1) of the level it works on, w = nx rounded up to a
-// power of two (a shift, not a division; rows packed into full warps, which
-// matters to the FP64 levels, whose pipe is paid per warp instruction).
+// The coarse levels of at most COARSEN_TAIL_CELLS aggregates, built one after
+// another by a single CTA (a barrier between levels instead of a launch per
+// level), then the dense inverse of level dl.
+#define COARSEN_TAIL_CELLS 4096
+template <typename T>
+struct CoarsenTail {
+    LevelT<T> L[FS_MG_MAX_LEVELS];
+    int l0, nl;   // build levels l0 .. nl-1 (each from the one above)
+    int dl;       // then invert level dl into ainv
+    T *ainv;
+};
+template <typename T>
+__global__ void __launch_bounds__(1024) k_coarsen_tail(const CoarsenTail<T> a) {
+    for (int l = a.l0; l < a.nl; l++) {
+        const LevelT<T> &f = a.L[l - 1], &c = a.L[l];
+        for (int q = threadIdx.x; q < c.nx * c.ny; q += 1024) coarsen_cell(f, c, q % c.nx + 1, q / c.nx + 1);
+        __syncthreads();   // the CTA's global writes of level l are visible to it
+    }
+    dense_inverse(a.L[a.dl], a.ainv);
+}
+// first level built by k_coarsen_tail: the finest with at most
+// COARSEN_TAIL_CELLS aggregates, never level 0 (assembled, not coarsened)
+template <typename T>
+inline int coarsen_tail_level(const LevelT<T> *L, int nl) {
+    int l = 1;
+    while (l < nl && L[l].nx * L[l].ny > COARSEN_TAIL_CELLS) l++;
+    return l;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs<T> a) {
     static_assert(BOTTOM_THREADS == BOTTOM_N * BOTTOM_N && BOTTOM_N == 32, "one node per thread");
