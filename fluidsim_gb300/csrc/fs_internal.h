@@ -180,6 +180,11 @@ struct fs_ctx {
     int mg_fused;                // coarse launched levels use the fused kernels
     int mg_lb, mg_dl;            // first level of the one-CTA bottom solver; its dense level
     int strip_kl, strip_kr;      // electrode strips of the finest level: columns 1..kl and kr..nx
+    // FP64 solver: levels mg_lf.. of its preconditioner run in FP32 (mg_lf =
+    // mg_nlev: none), on these arrays, with the FP32 dense inverse d_ainvc
+    int mg_lf;
+    MGLevelF mgc[FS_MG_MAX_LEVELS];
+    float *d_ainvc;
     double *d_ainv64;            // dense inverse of level mg_dl (FP64 solver)
     float *d_ainv32;             // dense inverse of level mg_dl (mixed solver)
     double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D

@@ -21,6 +21,7 @@
 //   * phi += d and ph_mi = phi (lapl_lib.F90:112-119).
 // All reductions are two-level and fixed-order: per-CTA partials, then the
 // last CTA to finish sums them in index order.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -580,6 +581,39 @@ int fs_lapl_alloc(fs_ctx *c) {
         if ((e = cudaMalloc(&c->d_ainv64, 64 * 64 * sizeof(double))) != cudaSuccess)
             return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
     }
+    // FP32 levels 1.. of the preconditioner (see vcycle): with the fused
+    // smoother and at least two levels above the bottom solver
+    c->mg_lf = nl;
+    if (!c->mixed && c->mg_fused && c->mg_lb >= 2) {
+        c->mg_lf = 1;
+        for (int l = c->mg_lf; l < nl; l++) {
+            MGLevelF &m = c->mgc[l];
+            m.nx = c->mg[l].nx;
+            m.ny = c->mg[l].ny;
+            m.pitch = c->mg[l].pitch;
+            m.res = nullptr;
+            const size_t n = (size_t)(m.ny + 2) * m.pitch;
+            float **fields[] = {&m.mc, &m.ce, &m.cn, &m.extra, &m.inv_mc, &m.rhs, &m.x, &m.xd};
+            for (float **f : fields) {
+                cudaError_t e = cudaMalloc(f, n * sizeof(float));
+                if (e == cudaSuccess) e = cudaMemset(*f, 0, n * sizeof(float));
+                if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (FP32 coarse levels)");
+            }
+        }
+        cudaError_t e = cudaMalloc(&c->d_ainvc, 64 * 64 * sizeof(float));
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
+        cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)mg_down_smem<float>(2));
+        cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
+        BottomArgs<float> bf;
+        bf.nl = nl;
+        bf.lb = c->mg_lb;
+        bf.dl = c->mg_dl;
+        for (int l = 0; l < nl; l++) { bf.L[l].nx = c->mg[l].nx; bf.L[l].ny = c->mg[l].ny; }
+        e = cudaFuncSetAttribute(k_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bottom_smem_bytes(bf));
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
+    }
     size_t n0 = (size_t)(c->ny + 2) * c->pitch;
     double **vecs[] = {&c->p, &c->q, &c->z, &c->r, &c->xs, &c->bs, &c->dinv};
     for (double **v : vecs) {
@@ -607,15 +641,37 @@ void fs_lapl_free(fs_ctx *c) {
     }
     double *vs[] = {c->p, c->q, c->z, c->r, c->xs, c->bs, c->dinv, c->d_cg_part, c->d_ainv64};
     for (double *v : vs) cudaFree(v);
+    for (int l = c->mg_lf; l < c->mg_nlev; l++) {
+        MGLevelF &m = c->mgc[l];
+        float *fs[] = {m.mc, m.ce, m.cn, m.extra, m.inv_mc, m.rhs, m.x, m.xd};
+        for (float *f : fs) cudaFree(f);
+        memset(&m, 0, sizeof(m));
+    }
+    cudaFree(c->d_ainvc);
+    c->d_ainvc = nullptr;
     c->mg_nlev = 0;
 }
 
+// The V-cycle of the FP64 solver's preconditioner.  Levels mg_lf.. (level 1
+// and coarser on grids with at least two levels above the bottom solver) run
+// in FP32 with the mixed solver's fused level kernels and bottom solver: they
+// are latency- and FP64-issue-bound on this GPU (the FP64 fused levels and
+// bottom solve took ~2.5x their FP32 time) and only shape the preconditioner
+// of the FP64 CG, whose iterate, residual and convergence test stay FP64.
+// Level 0 restricts into and prolongs from the FP32 level 1 in FP64.
 static void vcycle(fs_ctx *c, const CgArgs *ca) {
-    const int nl = c->mg_nlev, nu = c->cfg.mg_smooth;
+    const int nl = c->mg_nlev, nu = c->cfg.mg_smooth, lf = c->mg_lf;
     int lb = 0;
     while (lb < nl && (c->mg[lb].nx > BOTTOM_N || c->mg[lb].ny > BOTTOM_N)) lb++;
     dim3 b(32, 8);
     for (int l = 0; l < lb; l++) {
+        if (l >= lf) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_down<float, 2><<<grid2(c->mgc[l].nx, c->mgc[l].ny, dim3(MTX, MTY)), 256, mg_down_smem<float>(2),
+                                  c->stream>>>(lvt_f(c->mgc[l]), lvt_f(c->mgc[l + 1]));
+            fs_prof_end(c);
+            continue;
+        }
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
         // fused (temporally blocked) levels only where launches dominate: the
         // FP64 levels above 256^2 are FP64-issue-bound, and the fused kernel's
@@ -643,22 +699,44 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
             fs_prof_end(c);
         }
         fs_prof_begin(c, PROF_TRANSFER);
-        if (l == 0) k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+        if (l + 1 == lf) k_restrict<double, float><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, level_f(c->mgc[lf]));
+        else if (l == 0) k_restrict<<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
         else k_restrict_t<double><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
     }
-    BottomArgs<double> ba;
-    for (int l = 0; l < nl; l++) ba.L[l] = level_dev(c->mg[l]);
-    ba.lb = lb;
-    ba.nl = nl;
-    ba.nu = nu;
-    ba.dl = c->mg_dl;
-    ba.ainv = c->d_ainv64;
-    ba.om = FS_MG_OMEGA_POST;
-    fs_prof_begin(c, PROF_BOTTOM);
-    k_bottom_smem<double><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
-    fs_prof_end(c);
+    if (lf < nl) {
+        BottomArgs<float> ba;
+        for (int l = 0; l < nl; l++) ba.L[l] = level_f(c->mgc[l]);
+        ba.lb = lb;
+        ba.nl = nl;
+        ba.nu = nu;
+        ba.dl = c->mg_dl;
+        ba.ainv = c->d_ainvc;
+        ba.om = (float)FS_MG_OMEGA_POST;
+        fs_prof_begin(c, PROF_BOTTOM);
+        k_bottom_smem<float><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
+        fs_prof_end(c);
+    } else {
+        BottomArgs<double> ba;
+        for (int l = 0; l < nl; l++) ba.L[l] = level_dev(c->mg[l]);
+        ba.lb = lb;
+        ba.nl = nl;
+        ba.nu = nu;
+        ba.dl = c->mg_dl;
+        ba.ainv = c->d_ainv64;
+        ba.om = FS_MG_OMEGA_POST;
+        fs_prof_begin(c, PROF_BOTTOM);
+        k_bottom_smem<double><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
+        fs_prof_end(c);
+    }
     for (int l = lb - 1; l >= 0; l--) {
+        if (l >= lf) {
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_mg_up<float, 2><<<grid2(c->mgc[l].nx, c->mgc[l].ny, dim3(MTX, MTY)), 256, mg_up_smem<float>(2),
+                                c->stream>>>(lvt_f(c->mgc[l]), lvt_f(c->mgc[l + 1]));
+            fs_prof_end(c);
+            continue;
+        }
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
         if (c->mg_fused && l > 0 && c->mg[l].nx <= 256 && c->mg[l].ny <= 256) {
             LvT<double> F = lvt(c->mg[l]), C = lvt(c->mg[l + 1]);
@@ -669,7 +747,8 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         }
         dim3 g = grid2(f.nx, f.ny, b), gh = grid2((f.nx + 1) / 2, f.ny, b);
         fs_prof_begin(c, PROF_TRANSFER);
-        k_prolong<<<g, b, 0, c->stream>>>(f, cc);
+        if (l + 1 == lf) k_prolong<double, float><<<g, b, 0, c->stream>>>(f, level_f(c->mgc[lf]));
+        else k_prolong<<<g, b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
             fs_prof_begin(c, PROF_SMOOTH);
@@ -790,7 +869,32 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_prof_end(c);
     // coarse operators: one launch per large level, then one CTA for the
     // small levels and the dense inverse
-    {
+    if (c->mg_lf < c->mg_nlev) {   // FP32 levels lf.. (lf = 1): level 1 from the FP64 level 0
+        const int lf = c->mg_lf;
+        CoarsenTail<float> ct;
+        for (int l = 0; l < c->mg_nlev; l++) {
+            ct.L[l] = level_f(c->mgc[l]);
+            ct.L[l].nx = c->mg[l].nx;
+            ct.L[l].ny = c->mg[l].ny;
+        }
+        ct.nl = c->mg_nlev;
+        ct.l0 = std::max(coarsen_tail_level(ct.L, ct.nl), lf + 1);
+        ct.dl = c->mg_dl;
+        ct.ainv = c->d_ainvc;
+        dim3 b2(16, 16);
+        fs_prof_begin(c, PROF_COARSEN);
+        k_coarsen<double, float><<<grid2(ct.L[lf].nx, ct.L[lf].ny, b2), b2, 0, c->stream>>>(
+            level_dev(c->mg[lf - 1]), ct.L[lf]);
+        fs_prof_end(c);
+        for (int l = lf + 1; l < ct.l0; l++) {
+            fs_prof_begin(c, PROF_COARSEN);
+            k_coarsen<float><<<grid2(ct.L[l].nx, ct.L[l].ny, b2), b2, 0, c->stream>>>(ct.L[l - 1], ct.L[l]);
+            fs_prof_end(c);
+        }
+        fs_prof_begin(c, PROF_COARSEN);
+        k_coarsen_tail<float><<<1, 1024, 0, c->stream>>>(ct);
+        fs_prof_end(c);
+    } else {
         CoarsenTail<double> ct;
         for (int l = 0; l < c->mg_nlev; l++) ct.L[l] = level_dev(c->mg[l]);
         ct.nl = c->mg_nlev;

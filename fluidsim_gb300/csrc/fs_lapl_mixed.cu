@@ -856,20 +856,6 @@ __global__ void k_lpc_target(const LpcArgs l, const CgmArgs a) {
     l.tgt[p] = v;
 }
 
-LevelT<float> level_f(const MGLevelF &m) {
-    LevelT<float> L;
-    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
-    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.extra = m.extra; L.inv_mc = m.inv_mc;
-    L.rhs = m.rhs; L.x = m.x; L.res = nullptr;
-    return L;
-}
-LvT<float> lvt_f(const MGLevelF &m) {
-    LvT<float> L;
-    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
-    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
-    L.om = (float)FS_MG_OMEGA_POST;
-    return L;
-}
 
 }  // namespace
 

@@ -150,20 +150,20 @@ __device__ float coarse_extra(const LevelT<T> &f, int I, int J) {
 // the whole coarse row of aggregate (I, J): its faces, remainder, diagonal
 // and inverse diagonal (the west and south faces recomputed, not read back,
 // so one pass builds a level)
-template <typename T>
-__device__ void coarsen_cell(const LevelT<T> &f, const LevelT<T> &c, int I, int J) {
+template <typename T, typename TC>
+__device__ void coarsen_cell(const LevelT<T> &f, const LevelT<TC> &c, int I, int J) {
     const size_t oc = (size_t)J * c.P + I;
     const float ce = coarse_ce(f, c.nx, I, J), cn = coarse_cn(f, c.ny, I, J), ex = coarse_extra(f, I, J);
     const float mc = ce + coarse_ce(f, c.nx, I - 1, J) + cn + coarse_cn(f, c.ny, I, J - 1) + ex;
-    c.ce[oc] = (T)ce;
-    c.cn[oc] = (T)cn;
-    c.extra[oc] = (T)ex;
-    c.mc[oc] = (T)mc;
-    c.inv_mc[oc] = mc > 0.0f ? (T)(1.0f / mc) : T(0);
+    c.ce[oc] = (TC)ce;
+    c.cn[oc] = (TC)cn;
+    c.extra[oc] = (TC)ex;
+    c.mc[oc] = (TC)mc;
+    c.inv_mc[oc] = mc > 0.0f ? (TC)(1.0f / mc) : TC(0);
 }
 
-template <typename T>
-__global__ void k_coarsen(const LevelT<T> f, const LevelT<T> c) {
+template <typename T, typename TC = T>
+__global__ void k_coarsen(const LevelT<T> f, const LevelT<TC> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (I <= c.nx && J <= c.ny) coarsen_cell(f, c, I, J);
 }
@@ -226,8 +226,10 @@ __device__ __forceinline__ T resid(const LevelT<T> &L, size_t o) {
     return L.rhs[o] - (L.mc[o] * L.x[o] - L.ce[o] * L.x[o + 1] - L.ce[o - 1] * L.x[o - 1]
                        - L.cn[o] * L.x[o + L.P] - L.cn[o - L.P] * L.x[o - L.P]);
 }
-template <typename T>
-__global__ void k_restrict(const LevelT<T> f, const LevelT<T> c) {
+// (the coarse level may be FP32 under an FP64 fine level: the sum is formed
+// in the fine level's type and rounded once)
+template <typename T, typename TC = T>
+__global__ void k_restrict(const LevelT<T> f, const LevelT<TC> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (I > c.nx || J > c.ny) return;
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
@@ -235,7 +237,7 @@ __global__ void k_restrict(const LevelT<T> f, const LevelT<T> c) {
     for (int fy = fy0; fy <= fy1; fy++)
         for (int fx = fx0; fx <= fx1; fx++)
             if (((fx + fy) & 1) == 0) s += resid(f, (size_t)fy * f.P + fx);
-    c.rhs[(size_t)J * c.P + I] = s;
+    c.rhs[(size_t)J * c.P + I] = (TC)s;
 }
 // Coarse-grid correction at fine node (gi, gj): cell-centred bilinear
 // interpolation of the coarse iterate -- weights 9/16, 3/16, 3/16, 1/16 from
@@ -265,11 +267,11 @@ __device__ __forceinline__ T prolong_w(int fi, int I, int cn) {
     return (I == Ic ? T(0.75) : T(0)) + (I == In ? T(0.25) : T(0));
 }
 
-template <typename T>
-__global__ void k_prolong(const LevelT<T> f, const LevelT<T> c) {
+template <typename T, typename TC = T>
+__global__ void k_prolong(const LevelT<T> f, const LevelT<TC> c) {
     int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (I > f.nx || J > f.ny) return;
-    f.x[(size_t)J * f.P + I] += prolong_at(c.x, c.P, c.nx, c.ny, I, J);
+    f.x[(size_t)J * f.P + I] += (T)prolong_at(c.x, c.P, c.nx, c.ny, I, J);
 }
 
 // ---------------------------------------------- fused (temporally blocked) levels
@@ -697,6 +699,22 @@ __global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, i
 }
 
 inline dim3 grid2(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+// device views of an FP32 level
+inline LevelT<float> level_f(const MGLevelF &m) {
+    LevelT<float> L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.extra = m.extra; L.inv_mc = m.inv_mc;
+    L.rhs = m.rhs; L.x = m.x; L.res = nullptr;
+    return L;
+}
+inline LvT<float> lvt_f(const MGLevelF &m) {
+    LvT<float> L;
+    L.nx = m.nx; L.ny = m.ny; L.P = m.pitch;
+    L.mc = m.mc; L.ce = m.ce; L.cn = m.cn; L.inv_mc = m.inv_mc; L.rhs = m.rhs; L.x = m.x; L.xd = m.xd;
+    L.om = (float)FS_MG_OMEGA_POST;
+    return L;
+}
 
 template <typename T>
 size_t mg_down_smem(int nu) {

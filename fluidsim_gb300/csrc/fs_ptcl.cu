@@ -71,33 +71,6 @@ __device__ __forceinline__ double tab_val(const double *tab, int k, double w, in
     return __ldg(t + row) + w * __ldg(t + 8 + row);
 }
 
-// get_Flux for q = +1 (ions: mui and Di are constants, so on a face the flux
-// is linear in the two densities, flux = cl*n_left - cr*n_right, with
-// coefficients fixed for the whole step while phi is frozen)
-__device__ __forceinline__ void ion_coef(const PhysParams &pp, double E, double dh, double inv_dh,
-                                         double &cl, double &cr) {
-    const double tol = 9.9999999600419720025e-13;   // REAL(4) 1e-12
-    double v = pp.mui * E;
-    double arg = v * dh / pp.Di;
-    if (fabs(E) < tol) {
-        cl = cr = pp.Di * inv_dh;
-    } else if (fabs(arg) < 1e-2) {   // Bernoulli form near a = 0, where 1 - exp(-a) cancels
-        double a2 = arg * arg, c2 = a2 * (1.0 / 12.0 - a2 / 720.0), d = pp.Di * inv_dh;
-        cl = d * (1.0 + 0.5 * arg + c2);
-        cr = d * (1.0 - 0.5 * arg + c2);
-    } else if (arg > 0) {
-        double ex = exp(fmax(-arg, -100.0));
-        double inv = 1.0 / (1.0 - ex);
-        cl = v * inv;
-        cr = v * ex * inv;
-    } else {
-        double ex = exp(fmax(arg, -100.0));
-        double inv = 1.0 / (1.0 - ex);
-        cl = -(v * ex * inv);
-        cr = -(v * inv);
-    }
-}
-
 // get_Flux for q = -1 with (mue, De) and (5/3 mue, 5/3 De): one exponential
 __device__ __forceinline__ void sg_elec(double E, double dh, double inv_dh, double mue, double De,
                                         double nel, double ner, double ntl, double ntr,
@@ -461,26 +434,59 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
     }
 }
 
-// dFdPh for ions (lapl_lib.F90:611-636) at field E is linear in the two
-// densities, dF/dv = dl*n1 + dr*n2, with the same small-|a| series as the oracle.
-__device__ __forceinline__ void ion_dcoef(const PhysParams &pp, double E, double dh, double &dl,
-                                          double &dr) {
-    double v = pp.mui * E;
-    double a = v * dh / pp.Di;
+// Ion face coefficients while phi is frozen.  get_Flux for q = +1
+// (ptcl_props.F90:142-165): mui and Di are constants, so on a face the flux is
+// linear in the two densities, flux = cl n_left - cr n_right, with the
+// Bernoulli form near a = 0 where 1 - exp(-a) cancels and the exponent clamped
+// at -100 as get_Flux clamps it.  dFdPh for ions (lapl_lib.F90:611-636) is
+// linear too, dF/dv = dl n1 + dr n2, with its own small-|a| series.  The two
+// share the Bernoulli argument, so the exponential and 1 / (1 - exp(-|a|))
+// are formed once.
+__device__ __forceinline__ void ion_face(const PhysParams &pp, double E, double dh, double inv_dh, double &cl,
+                                         double &cr, double &dl, double &dr) {
+    const double tol = 9.9999999600419720025e-13;   // REAL(4) 1e-12
+    const double v = pp.mui * E;
+    const double a = v * dh / pp.Di, aa = fabs(a);
+    double ex = 0.0, inv = 0.0;
+    if (aa >= 1e-2) {
+        ex = exp(-aa);
+        inv = 1.0 / (1.0 - ex);
+    }
+    if (fabs(E) < tol) {
+        cl = cr = pp.Di * inv_dh;
+    } else if (aa < 1e-2) {
+        double a2 = a * a, c2 = a2 * (1.0 / 12.0 - a2 / 720.0), d = pp.Di * inv_dh;
+        cl = d * (1.0 + 0.5 * a + c2);
+        cr = d * (1.0 - 0.5 * a + c2);
+    } else {
+        double exc = ex, ic = inv;
+        if (aa > 100.0) {
+            exc = exp(-100.0);
+            ic = 1.0 / (1.0 - exc);
+        }
+        if (a > 0) {
+            cl = v * ic;
+            cr = v * exc * ic;
+        } else {
+            cl = -(v * exc * ic);
+            cr = -(v * ic);
+        }
+    }
     if (fabs(v) < 1e-12) {
         dl = dr = 0.0;
-    } else if (fabs(a) < 0.05) {
+    } else if (aa < 0.05) {
         double a2 = a * a, sres = a * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
         dl = 0.5 + sres;
         dr = 0.5 - sres;
-    } else if (a > 0) {
-        double ex = exp(-a), i1 = 1.0 / (1.0 - ex), t = a * ex * i1 * i1;
-        dl = i1 - t;
-        dr = -(ex * i1) + t;
     } else {
-        double ex = exp(a), i1 = 1.0 / (1.0 - ex), t = a * ex * i1 * i1;
-        dl = -(ex * i1) - t;
-        dr = i1 + t;
+        const double t = a * ex * inv * inv;
+        if (a > 0) {
+            dl = inv - t;
+            dr = -(ex * inv) + t;
+        } else {
+            dl = -(ex * inv) - t;
+            dr = inv + t;
+        }
     }
 }
 
@@ -499,15 +505,13 @@ __global__ void k_faces(const PhysParams pp, const MeshDev m, const double *ph, 
     if (gj >= 1) {
         double E = -(ph[o + 1] - ph[o]) / m.dx[gi];
         double cl, cr, dl, dr;
-        ion_coef(pp, E, m.dx[gi], m.inv_dx[gi], cl, cr);
-        ion_dcoef(pp, E, m.dx[gi], dl, dr);
+        ion_face(pp, E, m.dx[gi], m.inv_dx[gi], cl, cr, dl, dr);
         f.fx_e[o] = E; f.fx_cl[o] = cl; f.fx_cr[o] = cr; f.fx_dl[o] = dl; f.fx_dr[o] = dr;
     }
     if (gi >= 1) {
         double E = -(ph[o + P] - ph[o]) / m.dy[gj];
         double cl, cr, dl, dr;
-        ion_coef(pp, E, m.dy[gj], m.inv_dy[gj], cl, cr);
-        ion_dcoef(pp, E, m.dy[gj], dl, dr);
+        ion_face(pp, E, m.dy[gj], m.inv_dy[gj], cl, cr, dl, dr);
         f.fy_e[o] = E; f.fy_cl[o] = cl; f.fy_cr[o] = cr; f.fy_dl[o] = dl; f.fy_dr[o] = dr;
     }
 }
