@@ -105,46 +105,81 @@ __device__ __forceinline__ float inv_or_big(T c) {
     const float cf = (float)c;
     return cf > 1e-37f ? 1.0f / cf : 1e37f;
 }
+// The face functions issue all their loads before any arithmetic, so that a
+// thread's loads overlap (otherwise each waits for the division before it).
 // x face between aggregates (I, J) and (I + 1, J); 0 at the grid's edges
 template <typename T>
-__device__ float coarse_ce(const LevelT<T> &f, int cnx, int I, int J) {
+__device__ __forceinline__ float coarse_ce(const LevelT<T> &f, int cnx, int I, int J) {
     if (I < 1 || I >= cnx) return 0.0f;
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
     const int gx0 = fx1 + 1, gx1 = min(fx1 + 2, f.nx);
+    float cross[2], own[2], next[2];   // ce at fx1 (the face), fx0 and gx0 of rows fy0, fy1
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const size_t o = (size_t)(r ? fy1 : fy0) * f.P;
+        cross[r] = (float)f.ce[o + fx1];
+        own[r] = (float)f.ce[o + fx0];
+        next[r] = (float)f.ce[o + gx0];
+    }
     float ce = 0.0f;
-    for (int fy = fy0; fy <= fy1; fy++) {
-        float R = inv_or_big(f.ce[(size_t)fy * f.P + fx1]);
-        if (fx1 > fx0) R += 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + fx0]);
-        if (gx1 > gx0) R += 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + gx0]);
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        if (r && fy1 == fy0) break;
+        float R = inv_or_big(cross[r]);
+        if (fx1 > fx0) R += 0.5f * inv_or_big(own[r]);
+        if (gx1 > gx0) R += 0.5f * inv_or_big(next[r]);
         ce += 1.0f / R;
     }
     return ce;
 }
 // y face between aggregates (I, J) and (I, J + 1)
 template <typename T>
-__device__ float coarse_cn(const LevelT<T> &f, int cny, int I, int J) {
+__device__ __forceinline__ float coarse_cn(const LevelT<T> &f, int cny, int I, int J) {
     if (J < 1 || J >= cny) return 0.0f;
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
     const int gy0 = fy1 + 1, gy1 = min(fy1 + 2, f.ny);
+    float cross[2], own[2], next[2];   // cn at rows fy1 (the face), fy0 and gy0 of columns fx0, fx1
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int fx = k ? fx1 : fx0;
+        cross[k] = (float)f.cn[(size_t)fy1 * f.P + fx];
+        own[k] = (float)f.cn[(size_t)fy0 * f.P + fx];
+        next[k] = (float)f.cn[(size_t)gy0 * f.P + fx];
+    }
     float cn = 0.0f;
-    for (int fx = fx0; fx <= fx1; fx++) {
-        float R = inv_or_big(f.cn[(size_t)fy1 * f.P + fx]);
-        if (fy1 > fy0) R += 0.5f * inv_or_big(f.cn[(size_t)fy0 * f.P + fx]);
-        if (gy1 > gy0) R += 0.5f * inv_or_big(f.cn[(size_t)gy0 * f.P + fx]);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        if (k && fx1 == fx0) break;
+        float R = inv_or_big(cross[k]);
+        if (fy1 > fy0) R += 0.5f * inv_or_big(own[k]);
+        if (gy1 > gy0) R += 0.5f * inv_or_big(next[k]);
         cn += 1.0f / R;
     }
     return cn;
 }
 template <typename T>
-__device__ float coarse_extra(const LevelT<T> &f, int I, int J) {
+__device__ __forceinline__ float coarse_extra(const LevelT<T> &f, int I, int J) {
     const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy0 = 2 * J - 1, fy1 = min(2 * J, f.ny);
+    float e[2][2], ci[2];   // extra of the aggregate's cells; ce at fx0 of its rows
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const size_t o = (size_t)(r ? fy1 : fy0) * f.P;
+        e[r][0] = (float)f.extra[o + fx0];
+        e[r][1] = (float)f.extra[o + fx1];
+        ci[r] = (float)f.ce[o + fx0];
+    }
     float ex = 0.0f;
-    for (int fy = fy0; fy <= fy1; fy++)
-        for (int fx = fx0; fx <= fx1; fx++) {
-            float e = (float)f.extra[(size_t)fy * f.P + fx];
-            if (e > 0.0f && fx1 > fx0) e = 1.0f / (1.0f / e + 0.5f * inv_or_big(f.ce[(size_t)fy * f.P + fx0]));
-            ex += e;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        if (r && fy1 == fy0) break;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            if (k && fx1 == fx0) break;
+            float v = e[r][k];
+            if (v > 0.0f && fx1 > fx0) v = 1.0f / (1.0f / v + 0.5f * inv_or_big(ci[r]));
+            ex += v;
         }
+    }
     return ex;
 }
 // the whole coarse row of aggregate (I, J): its faces, remainder, diagonal
