@@ -180,6 +180,9 @@ struct fs_ctx {
     int mg_fused;                // coarse launched levels use the fused kernels
     int mg_lb, mg_dl;            // first level of the one-CTA bottom solver; its dense level
     int strip_kl, strip_kr;      // electrode strips of the finest level: columns 1..kl and kr..nx
+    int strip_w;                 // their snapshot's row width (StripSnap)
+    double *strip_snap64;        // the snapshot, FP64 solver
+    float *strip_snap32;         // the snapshot, mixed solver
     // FP64 solver: levels mg_lf.. of its preconditioner run in FP32 (mg_lf =
     // mg_nlev: none), on these arrays, with the FP32 dense inverse d_ainvc
     int mg_lf;
@@ -265,7 +268,7 @@ int fs_sig_copy(fs_ctx *c, int dst, int src);   // slot dst <- slot src, on the 
 void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
-void fs_mg_strips(fs_ctx *c);   // electrode strips of the finest level (strip_kl, strip_kr)
+int fs_mg_strips(fs_ctx *c);    // electrode strips of the finest level (strip_kl, strip_kr) and their snapshot
 void fs_lapl_free(fs_ctx *c);
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
 // mixed-precision Poisson (fs_lapl_mixed.cu)

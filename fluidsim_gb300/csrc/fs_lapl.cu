@@ -515,11 +515,11 @@ static int alloc_zero(fs_ctx *c, double **p, size_t n) {
     return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "cudaMemset");
 }
 
-// Electrode strips of the finest level (k_rb_strip): the leading and trailing
+// Electrode strips of the finest level (k_rb_strips): the leading and trailing
 // columns whose x faces conduct more than twice as well as their y faces, by
 // the mesh spacings of the middle row; none when either is wider than
-// FS_STRIP_MAX columns.
-void fs_mg_strips(fs_ctx *c) {
+// FS_STRIP_MAX columns.  Allocates their snapshot in the solver's type.
+int fs_mg_strips(fs_ctx *c) {
     const int nx = c->nx, j = c->ny / 2 + 1;
     const std::vector<double> &x = c->h_x, &y = c->h_y;
     const double dy = y[j + 1] - y[j], dly = 0.5 * (y[j + 1] - y[j - 1]);
@@ -535,10 +535,28 @@ void fs_mg_strips(fs_ctx *c) {
     if (kl > FS_STRIP_MAX || nx + 1 - kr > FS_STRIP_MAX) { kl = 0; kr = nx + 1; }
     c->strip_kl = kl;
     c->strip_kr = kr;
+    c->strip_w = std::max(kl + 2, nx - kr + 3);
+    if (!has_strips(c)) return FS_OK;
+    const size_t n = (size_t)2 * (c->ny + 2) * c->strip_w;
+    cudaError_t e;
+    if (c->mixed) {
+        e = cudaMalloc(&c->strip_snap32, n * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(c->strip_snap32, 0, n * sizeof(float));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_rb_strips<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)strip_smem<float>(c->strip_w));
+    } else {
+        e = cudaMalloc(&c->strip_snap64, n * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemset(c->strip_snap64, 0, n * sizeof(double));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_rb_strips<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)strip_smem<double>(c->strip_w));
+    }
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "strip snapshot");
 }
 
 int fs_lapl_alloc(fs_ctx *c) {
-    fs_mg_strips(c);
+    if (int rs = fs_mg_strips(c)) return rs;
     int nx = c->nx, ny = c->ny, nl = 0;
     for (;;) {
         MGLevel &m = c->mg[nl];
@@ -649,6 +667,10 @@ void fs_lapl_free(fs_ctx *c) {
     }
     cudaFree(c->d_ainvc);
     c->d_ainvc = nullptr;
+    cudaFree(c->strip_snap64);
+    cudaFree(c->strip_snap32);
+    c->strip_snap64 = nullptr;
+    c->strip_snap32 = nullptr;
     c->mg_nlev = 0;
 }
 
@@ -751,20 +773,20 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         else k_prolong<<<g, b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
         for (int it = 0; it < nu; it++) {
+            // the strip sweeps go before the last half sweep, which is fused
+            // with r.z: red-black pairs after the black half sweep, which
+            // fills their snapshot
+            const bool strips = l == 0 && it == nu - 1 && has_strips(c);
+            const StripSnap<double> sn = strips ? strip_snap(c, c->strip_snap64) : StripSnap<double>{};
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<<<gh, b, 0, c->stream>>>(f, 1, 0, FS_MG_OMEGA_POST);
+            k_rb<<<gh, b, 0, c->stream>>>(f, 1, 0, FS_MG_OMEGA_POST, sn);
             fs_prof_end(c);
             if (l == 0 && it == nu - 1) {
-                // the strip sweeps go before the last half sweep, which is
-                // fused with r.z: red-black pairs after the black half sweep
-                const int kl = c->strip_kl, kr = c->strip_kr, ns = kl + (c->nx - kr + 1);
-                if (ns > 0) {
-                    const dim3 gs((ns + 31) / 32, (f.ny + 7) / 8);
-                    for (int s = 0; s < 2 * FS_STRIP_PAIRS; s++) {
-                        fs_prof_begin(c, PROF_SMOOTH);
-                        k_rb_strip<double><<<gs, b, 0, c->stream>>>(f, s & 1, kl, kr, FS_MG_OMEGA_POST);
-                        fs_prof_end(c);
-                    }
+                if (strips) {
+                    fs_prof_begin(c, PROF_SMOOTH);
+                    k_rb_strips<double><<<dim3((f.ny + STRIP_ROWS - 1) / STRIP_ROWS, 2), 256,
+                                          strip_smem<double>(c->strip_w), c->stream>>>(f, sn, 0, FS_MG_OMEGA_POST);
+                    fs_prof_end(c);
                 }
                 fs_prof_begin(c, PROF_SMOOTH);
                 k_rb_rz<<<ca->grid, 256, 0, c->stream>>>(f, *ca, FS_MG_OMEGA_POST);

@@ -978,12 +978,17 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     fs_prof_begin(c, PROF_BOTTOM);
     k_bottom_smem<float><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
+    // the finest level's last post-smoothing launch fills the strip snapshot
+    const bool strips = lb > 0 && has_strips(c);
+    const StripSnap<float> sn = strips ? strip_snap(c, c->strip_snap32) : StripSnap<float>{};
     for (int l = lb - 1; l >= 0; l--) {
         LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
         if (fused) {
+            LvT<float> F = lvt_f(c->mgf[l]);
+            if (l == 0) F.sn = sn;
             fs_prof_begin(c, PROF_SMOOTH);
             const dim3 g = grid2(f.nx, f.ny, dim3(MTX, MTY));
-            k_mg_up<float, 2><<<g, 256, mg_up_smem<float>(2), c->stream>>>(lvt_f(c->mgf[l]), lvt_f(c->mgf[l + 1]));
+            k_mg_up<float, 2><<<g, 256, mg_up_smem<float>(2), c->stream>>>(F, lvt_f(c->mgf[l + 1]));
             fs_prof_end(c);
             continue;
         }
@@ -996,19 +1001,16 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
             k_rb<float><<<gh, b, 0, c->stream>>>(f, 1, 0, (float)FS_MG_OMEGA_POST);
             fs_prof_end(c);
             fs_prof_begin(c, PROF_SMOOTH);
-            k_rb<float><<<gh, b, 0, c->stream>>>(f, 0, 0, (float)FS_MG_OMEGA_POST);
+            k_rb<float><<<gh, b, 0, c->stream>>>(f, 0, 0, (float)FS_MG_OMEGA_POST,
+                                                  l == 0 && it == nu - 1 ? sn : StripSnap<float>{});
             fs_prof_end(c);
         }
     }
-    const int kl = c->strip_kl, kr = c->strip_kr, ns = kl + (c->nx - kr + 1);
-    if (ns > 0 && lb > 0) {
-        LevelT<float> f0 = level_f(c->mgf[0]);
-        const dim3 gs((ns + 31) / 32, (f0.ny + 7) / 8);
-        for (int s = 0; s < 2 * FS_STRIP_PAIRS; s++) {
-            fs_prof_begin(c, PROF_SMOOTH);
-            k_rb_strip<float><<<gs, b, 0, c->stream>>>(f0, (s & 1) ? 0 : 1, kl, kr, (float)FS_MG_OMEGA_POST);
-            fs_prof_end(c);
-        }
+    if (strips) {   // black-red pairs after the red half sweep
+        fs_prof_begin(c, PROF_SMOOTH);
+        k_rb_strips<float><<<dim3((c->ny + STRIP_ROWS - 1) / STRIP_ROWS, 2), 256, strip_smem<float>(c->strip_w),
+                             c->stream>>>(level_f(c->mgf[0]), sn, 1, (float)FS_MG_OMEGA_POST);
+        fs_prof_end(c);
     }
 }
 

@@ -13,7 +13,7 @@
 
 // Post-smoothing of both solvers' V-cycles: every half sweep after the
 // coarse-grid correction is over-relaxed by FS_MG_OMEGA_POST, and the finest
-// level's electrode strips (k_rb_strip) get FS_STRIP_PAIRS more red-black
+// level's electrode strips (k_rb_strips) get FS_STRIP_PAIRS more red-black
 // sweep pairs; strips wider than FS_STRIP_MAX columns (a mesh stretched
 // everywhere) get none.  The pre-smoothing stays plain Gauss-Seidel, so the
 // black residuals the down sweeps leave are still zero.  On the 1024^2 glow
@@ -217,22 +217,6 @@ __device__ __forceinline__ T relax(T x, T g, T om) {
     return om == T(1) ? g : x + om * (g - x);
 }
 
-// one red (color 0) or black (color 1) half sweep; zero_init: x starts at 0;
-// om: relaxation factor (1 before the coarse-grid correction)
-// Each thread owns the column pair (2t+1, 2t+2) of a row and updates the
-// node of the swept colour in it, so every lane does useful FP64 work.
-template <typename T>
-__global__ void k_rb(const LevelT<T> L, int color, int zero_init, T om = T(1)) {
-    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int c0 = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + 1;
-    if (J > L.ny || c0 > L.nx) return;
-    const int I = ((c0 + J) & 1) == color ? c0 : c0 + 1, Io = I == c0 ? c0 + 1 : c0;
-    if (zero_init && Io <= L.nx) L.x[(size_t)J * L.P + Io] = T(0);
-    if (I > L.nx) return;
-    const size_t o = (size_t)J * L.P + I;
-    L.x[o] = zero_init ? L.rhs[o] * L.inv_mc[o] : relax(L.x[o], gs_node(L, o), om);
-}
-
 // Electrode strips.  Where the mesh is stretched along x next to the
 // electrodes (x faces conducting several times better than y faces), point
 // Gauss-Seidel barely damps error that is smooth in x and oscillates in y, and
@@ -240,17 +224,99 @@ __global__ void k_rb(const LevelT<T> L, int color, int zero_init, T om = T(1)) {
 // the 1024^2 glow mesh (spacing 1/4 of the bulk's over ~28 cells at each
 // electrode) these strips alone raise the CG iterations from 7 to 10.  Two
 // more over-relaxed sweep pairs confined to the strip columns of the finest
-// level, in its post-smoothing, bring them back.  One launch is one half
-// sweep over columns 1..kl and kr..nx (every row), in place: a half sweep
-// reads only the other colour.
+// level (1..kl and kr..nx), in its post-smoothing, bring them back.
+//
+// They run as one launch (k_rb_strips) on row tiles with a halo of one row per
+// half sweep.  So that no tile reads a value another tile of the launch
+// writes, the kernel before it copies the strips, with their inner neighbour
+// column, into a snapshot as it writes them, and k_rb_strips reads only the
+// snapshot.  Strip s (0: columns 0..kl+1, 1: columns kr-1..nx+1), row gj
+// (0..ny+1), column gi is at v[(s (ny + 2) + gj) w + gi - c0], c0 = 0 or
+// kr - 1; the ghost entries stay zero.
 template <typename T>
-__global__ void k_rb_strip(const LevelT<T> L, int color, int kl, int kr, T om) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (q >= kl + (L.nx - kr + 1) || J > L.ny) return;
-    const int I = q < kl ? q + 1 : kr + (q - kl);
-    if (((I + J) & 1) != color) return;
+struct StripSnap {
+    T *v = nullptr;   // no snapshot
+    int kl = 0, kr = 0, w = 0;
+    __device__ __forceinline__ bool holds(int gi) const {
+        return (kl > 0 && gi <= kl + 1) || (kr > 0 && gi >= kr - 1);
+    }
+    __device__ __forceinline__ void put(int gi, int gj, int ny, T val) const {
+        if (kl > 0 && gi <= kl + 1) v[(size_t)gj * w + gi] = val;
+        if (kr > 0 && gi >= kr - 1) v[((size_t)(ny + 2) + gj) * w + (gi - kr + 1)] = val;
+    }
+};
+
+// one red (color 0) or black (color 1) half sweep; zero_init: x starts at 0;
+// om: relaxation factor (1 before the coarse-grid correction); sn: the strip
+// snapshot to fill, before k_rb_strips
+// Each thread owns the column pair (2t+1, 2t+2) of a row and updates the
+// node of the swept colour in it, so every lane does useful FP64 work.
+template <typename T>
+__global__ void k_rb(const LevelT<T> L, int color, int zero_init, T om = T(1), StripSnap<T> sn = {}) {
+    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int c0 = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + 1;
+    if (J > L.ny || c0 > L.nx) return;
+    const int I = ((c0 + J) & 1) == color ? c0 : c0 + 1, Io = I == c0 ? c0 + 1 : c0;
+    if (zero_init && Io <= L.nx) L.x[(size_t)J * L.P + Io] = T(0);
+    if (I > L.nx) return;
     const size_t o = (size_t)J * L.P + I;
-    L.x[o] = relax(L.x[o], gs_node(L, o), om);
+    const T v = zero_init ? L.rhs[o] * L.inv_mc[o] : relax(L.x[o], gs_node(L, o), om);
+    L.x[o] = v;
+    if (sn.v && (sn.holds(c0) || sn.holds(c0 + 1))) {
+        sn.put(I, J, L.ny, v);
+        if (Io <= L.nx) sn.put(Io, J, L.ny, L.x[(size_t)J * L.P + Io]);
+    }
+}
+
+// The 2 FS_STRIP_PAIRS half sweeps (colours color0, 1 - color0, ...) over both
+// strips of level L, from the snapshot sn, into L.x.  Grid (row tiles of
+// STRIP_ROWS, 2 strips), 256 threads, strip_smem() bytes of shared memory.
+#define STRIP_ROWS 32
+template <typename T>
+inline size_t strip_smem(int w) {
+    return (size_t)5 * w * (STRIP_ROWS + 4 * FS_STRIP_PAIRS) * sizeof(T);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_rb_strips(const LevelT<T> L, const StripSnap<T> sn, int color0, T om) {
+    constexpr int H = 2 * FS_STRIP_PAIRS, WY = STRIP_ROWS + 2 * H;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int s = blockIdx.y;
+    if ((s == 0 && sn.kl == 0) || (s == 1 && sn.kr == 0)) return;
+    const int c0 = s == 0 ? 0 : sn.kr - 1;                    // first column held
+    const int nc = s == 0 ? sn.kl + 2 : L.nx - sn.kr + 3;     // the strip, its inner neighbour, the ghost
+    const int nu = nc - 2;                                    // columns updated: local 1..nu
+    const int W = nc * WY;
+    T *sx = (T *)sm_raw, *srhs = sx + W, *simc = srhs + W, *sce = simc + W, *scn = sce + W;
+    const int gy0 = blockIdx.x * STRIP_ROWS + 1;
+    const T *snap = sn.v + (size_t)s * (L.ny + 2) * sn.w;
+    for (int q = threadIdx.x; q < W; q += blockDim.x) {
+        const int k = q % nc, ly = q / nc, gi = c0 + k, gj = gy0 - H + ly;
+        const bool row = gj >= 0 && gj <= L.ny + 1;
+        const bool in = gj >= 1 && gj <= L.ny && gi >= 1 && gi <= L.nx;
+        const size_t o = (size_t)gj * L.P + gi;
+        sx[q] = in ? snap[(size_t)gj * sn.w + k] : T(0);
+        srhs[q] = in ? L.rhs[o] : T(0);
+        simc[q] = in ? L.inv_mc[o] : T(0);
+        sce[q] = row ? L.ce[o] : T(0);
+        scn[q] = row ? L.cn[o] : T(0);
+    }
+    __syncthreads();
+    for (int st = 0; st < 2 * FS_STRIP_PAIRS; st++) {
+        const int color = color0 ^ (st & 1), lo = st + 1, n = (WY - 2 - 2 * st) * nu;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int k = 1 + q % nu, ly = lo + q / nu, gi = c0 + k, gj = gy0 - H + ly;
+            if (gj < 1 || gj > L.ny || ((gi + gj) & 1) != color) continue;
+            const int i = ly * nc + k;
+            const T g = (srhs[i] + sce[i] * sx[i + 1] + sce[i - 1] * sx[i - 1] + scn[i] * sx[i + nc]
+                         + scn[i - nc] * sx[i - nc]) * simc[i];
+            sx[i] = relax(sx[i], g, om);
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < STRIP_ROWS * nu; q += blockDim.x) {
+        const int k = 1 + q % nu, ty = q / nu, gj = gy0 + ty;
+        if (gj <= L.ny) L.x[(size_t)gj * L.P + c0 + k] = sx[(H + ty) * nc + k];
+    }
 }
 
 // coarse rhs = sum over the aggregate of the fine residual rhs - M x.  The
@@ -328,7 +394,8 @@ struct LvT {
     int nx, ny, P;
     const T *mc, *ce, *cn, *inv_mc;
     T *rhs, *x, *xd;
-    T om;   // relaxation factor of the up (post-smoothing) sweeps
+    T om;             // relaxation factor of the up (post-smoothing) sweeps
+    StripSnap<T> sn;  // the up kernel fills it (the finest level, before k_rb_strips)
 };
 
 // Restriction.  The FP64 levels, under the plain (non-flexible) PCG that
@@ -476,7 +543,11 @@ __global__ void __launch_bounds__(256) k_mg_up(const LvT<T> f, const LvT<T> c) {
     }
     for (int q = threadIdx.x; q < MTX * MTY; q += blockDim.x) {
         const int tx = q % MTX, ty = q / MTX, gi = gx0 + tx, gj = gy0 + ty;
-        if (gi <= f.nx && gj <= f.ny) f.x[(size_t)gj * f.P + gi] = sx[(H + ty) * WX + H + tx];
+        if (gi <= f.nx && gj <= f.ny) {
+            const T v = sx[(H + ty) * WX + H + tx];
+            f.x[(size_t)gj * f.P + gi] = v;
+            if (f.sn.v) f.sn.put(gi, gj, f.ny, v);
+        }
     }
 }
 
@@ -750,6 +821,18 @@ inline LvT<float> lvt_f(const MGLevelF &m) {
     L.om = (float)FS_MG_OMEGA_POST;
     return L;
 }
+
+// the strip snapshot of a context (kl, kr = 0 for a side without a strip)
+template <typename T>
+inline StripSnap<T> strip_snap(const fs_ctx *c, T *v) {
+    StripSnap<T> s;
+    s.v = v;
+    s.kl = c->strip_kl;
+    s.kr = c->strip_kr <= c->nx ? c->strip_kr : 0;
+    s.w = c->strip_w;
+    return s;
+}
+inline bool has_strips(const fs_ctx *c) { return c->strip_kl > 0 || c->strip_kr <= c->nx; }
 
 template <typename T>
 size_t mg_down_smem(int nu) {
