@@ -407,23 +407,32 @@ __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
     }
 }
 
-// rz = r.z; beta = rz/rz_old (0 on the first iteration)
+// rz = r.z and zq = z.q (q = M p_old) of the preconditioned residual, then the
+// flexible beta = -zq / p_old.q (Notay's FCG(1); 0 on the first iteration).
+// Plain CG's rz / rz_old assumes a symmetric preconditioner, and the V-cycle
+// is not one: its post-smoothing is over-relaxed and its pre-smoothing not,
+// the electrode strips get sweeps after the post-smoothing only, and the
+// finest level pre-smooths with fewer sweeps than it post-smooths.
+__device__ __forceinline__ void cg_beta(Ctrl *c, double rz, double zq) {
+    c->rz_old = c->rz;
+    c->rz = rz;
+    c->beta = c->cg_iters == 0 ? 0.0 : -zq / c->pq;
+}
+
 __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
-    double v = 0.0;
-    CG_NODES(a, { v += a.r[o] * a.z[o]; })
-    double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
-        Ctrl *c = a.ctrl;
-        c->rz_old = c->rz;
-        c->rz = out;
-        c->beta = c->cg_iters == 0 ? 0.0 : out / c->rz_old;
-    }
+    double v = 0.0, u = 0.0;
+    CG_NODES(a, {
+        v += a.r[o] * a.z[o];
+        u += a.z[o] * a.q[o];
+    })
+    double sv, su;
+    if (grid_sum2(v, u, a.part, &a.ctrl->counter[1], a.nblk, sv, su) && threadIdx.x == 0) cg_beta(a.ctrl, sv, su);
 }
 
 // Last half sweep of the fine level (red, after the black one) fused with
-// rz = r.z over all nodes and beta = rz/rz_old (0 on the first iteration).
+// rz = r.z and zq = z.q over all nodes and the flexible beta (cg_beta).
 __global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a, double om) {
-    double v = 0.0;
+    double v = 0.0, u = 0.0;
     CG_NODES(a, {
         const int J = (int)j_ + 1, I = (int)(q_ - j_ * (unsigned)a.nx) + 1;
         double z = L.x[o];
@@ -432,14 +441,10 @@ __global__ void __launch_bounds__(256) k_rb_rz(const LevelDev L, const CgArgs a,
             L.x[o] = z;
         }
         v += L.rhs[o] * z;   // black nodes are final after the previous half sweep
+        u += a.q[o] * z;
     })
-    double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[1], a.nblk, &out) && threadIdx.x == 0) {
-        Ctrl *c = a.ctrl;
-        c->rz_old = c->rz;
-        c->rz = out;
-        c->beta = c->cg_iters == 0 ? 0.0 : out / c->rz_old;
-    }
+    double sv, su;
+    if (grid_sum2(v, u, a.part, &a.ctrl->counter[1], a.nblk, sv, su) && threadIdx.x == 0) cg_beta(a.ctrl, sv, su);
 }
 
 // p = z + beta p ; q = M z + beta q (= M p, since q held M p_old) ; pq = p.q ;
@@ -641,7 +646,8 @@ int fs_lapl_alloc(fs_ctx *c) {
     c->mg[0].rhs = c->r;
     c->mg[0].x = c->z;
     dim3 g = grid2(c->nx, c->ny, dim3(32, 8));
-    c->cg_nblk = g.x * g.y;
+    // partials of the CG reductions: two per CTA of the (<= 4 per SM) CG grids
+    c->cg_nblk = std::max((int)(g.x * g.y), 2 * 4 * c->nsm);
     return alloc_zero(c, &c->d_cg_part, (size_t)c->cg_nblk);
 }
 
@@ -712,7 +718,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         fs_prof_begin(c, PROF_SMOOTH);
         k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
         fs_prof_end(c);
-        for (int it = 1; it < nu; it++) {
+        for (int it = 1; it < (l == 0 ? fs_mg_pre0(nu) : nu); it++) {
             fs_prof_begin(c, PROF_SMOOTH);
             k_rb<<<g, b, 0, c->stream>>>(f, 0, 0);
             fs_prof_end(c);

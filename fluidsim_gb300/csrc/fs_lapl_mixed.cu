@@ -361,43 +361,6 @@ struct CgmArgs {
     cudaGraphConditionalHandle cond;
 };
 
-// Fixed-order sum of two per-thread values over the grid; true in the last
-// CTA (thread 0 holds the sums).  part needs 2 * nblk entries.
-__device__ bool grid_sum2(double v, double w, double *part, unsigned int *counter, int nblk, double &sv,
-                          double &sw) {
-    __shared__ double s_a[8], s_b[8];
-    __shared__ bool s_last;
-    for (int o = 16; o > 0; o >>= 1) {
-        v += __shfl_down_sync(0xffffffffu, v, o);
-        w += __shfl_down_sync(0xffffffffu, w, o);
-    }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { s_a[wid] = v; s_b[wid] = w; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ra = 0.0, rb = 0.0;
-        for (int k = 0; k < 8; k++) { ra += s_a[k]; rb += s_b[k]; }
-        part[blockIdx.x] = ra;
-        part[nblk + blockIdx.x] = rb;
-        __threadfence();
-        s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    __shared__ double s_r[256], s_w[256];
-    s_r[threadIdx.x] = strided_sum<256>(part, nblk, threadIdx.x);
-    s_w[threadIdx.x] = strided_sum<256>(part + nblk, nblk, threadIdx.x);
-    __syncthreads();
-    for (int k = 128; k > 0; k >>= 1) {
-        if (threadIdx.x < k) { s_r[threadIdx.x] += s_r[threadIdx.x + k]; s_w[threadIdx.x] += s_w[threadIdx.x + k]; }
-        __syncthreads();
-    }
-    sv = s_r[0];
-    sw = s_w[0];
-    if (threadIdx.x == 0) *counter = 0u;
-    return true;
-}
 
 // Fixed-order FP32 sums of N per-thread values over the grid (warp shuffles,
 // then the eight warps, then the CTAs' partials by the last CTA); true in the

@@ -20,6 +20,13 @@
 // Jacobians this takes the CG from 11-12 iterations to 8.
 #define FS_MG_OMEGA_POST 1.3
 #define FS_STRIP_PAIRS 2
+// The FP64 solver's finest level pre-smooths with one sweep pair fewer than
+// the others (at least one): its FP64 sweeps are the costliest of the cycle,
+// and with the strip sweeps after its post-smoothing the CG needs no more
+// iterations for it (8 at 1024^2 with 1 or 2 pre-sweeps there; 9 with 1
+// post-sweep, 10 with 1 + 1).  The mixed solver keeps both: its FP32 inner
+// iteration, restarted at each refinement, went from 8 to 9.2 iterations.
+inline int fs_mg_pre0(int nu) { return nu > 1 ? nu - 1 : 1; }
 #define FS_STRIP_MAX 64
 
 namespace {
@@ -82,6 +89,44 @@ __device__ bool grid_sum(double v, double *part, unsigned int *counter, int nblk
         *counter = 0u;
     }
     __syncthreads();
+    return true;
+}
+
+// Fixed-order sum of two per-thread values over the grid (256-thread CTAs);
+// true in the last CTA (thread 0 holds the sums).  part needs 2 * nblk entries.
+__device__ bool grid_sum2(double v, double w, double *part, unsigned int *counter, int nblk, double &sv,
+                          double &sw) {
+    __shared__ double s_a[8], s_b[8];
+    __shared__ bool s_last;
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+        w += __shfl_down_sync(0xffffffffu, w, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { s_a[wid] = v; s_b[wid] = w; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ra = 0.0, rb = 0.0;
+        for (int k = 0; k < 8; k++) { ra += s_a[k]; rb += s_b[k]; }
+        part[blockIdx.x] = ra;
+        part[nblk + blockIdx.x] = rb;
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    __shared__ double s_r[256], s_w[256];
+    s_r[threadIdx.x] = strided_sum<256>(part, nblk, threadIdx.x);
+    s_w[threadIdx.x] = strided_sum<256>(part + nblk, nblk, threadIdx.x);
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) { s_r[threadIdx.x] += s_r[threadIdx.x + k]; s_w[threadIdx.x] += s_w[threadIdx.x + k]; }
+        __syncthreads();
+    }
+    sv = s_r[0];
+    sw = s_w[0];
+    if (threadIdx.x == 0) *counter = 0u;
     return true;
 }
 
