@@ -443,12 +443,13 @@ struct LvT {
     StripSnap<T> sn;  // the up kernel fills it (the finest level, before k_rb_strips)
 };
 
-// Restriction.  The FP64 levels, under the plain (non-flexible) PCG that
-// wants a symmetric preconditioner, restrict with the transpose of the
-// bilinear prolongation (11 instead of 13 CG iterations at 1024^2); the FP32
-// levels under the flexible CG sum the aggregate's residuals, which costs less
-// and needs the same iterations there.  With the transpose the down kernel
-// keeps one more halo ring than the sweeps need, so that the residuals of the
+// Restriction.  FP64 levels below the finest (the FP64 solver's coarse levels
+// on grids too small for FP32 ones) restrict with the transpose of the
+// bilinear prolongation (it took the FP64 solver from 13 to 11 CG iterations
+// at 1024^2 when that solver was plain CG and its coarse levels FP64); FP32
+// levels sum the aggregate's residuals, which costs less and needs the same
+// iterations under the flexible CG.  With the transpose the down kernel keeps
+// one more halo ring than the sweeps need, so that the residuals of the
 // tile's first ring, which the transpose reaches, are exact too.
 template <typename T>
 struct RestrictFW { static constexpr bool value = sizeof(T) == 8; };
