@@ -713,10 +713,7 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         }
         dim3 g = grid2((f.nx + 1) / 2, f.ny, b);
         fs_prof_begin(c, PROF_SMOOTH);
-        k_rb<<<g, b, 0, c->stream>>>(f, 0, 1);
-        fs_prof_end(c);
-        fs_prof_begin(c, PROF_SMOOTH);
-        k_rb<<<g, b, 0, c->stream>>>(f, 1, 0);
+        k_rb_pair0<<<g, b, 0, c->stream>>>(f);   // the first red-black pair, from x = 0
         fs_prof_end(c);
         for (int it = 1; it < (l == 0 ? fs_mg_pre0(nu) : nu); it++) {
             fs_prof_begin(c, PROF_SMOOTH);

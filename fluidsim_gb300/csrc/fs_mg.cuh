@@ -313,6 +313,34 @@ __global__ void k_rb(const LevelT<T> L, int color, int zero_init, T om = T(1), S
     }
 }
 
+// One red-black sweep pair from x = 0 in one pass: the red half sweep gives
+// x = rhs / mc on the red nodes, and the black half sweep after it reads only
+// those, so each black node forms its red neighbours' values from their rhs
+// and 1/mc itself (the same products as the two launches, bit for bit; the
+// ghost ring counts as zero, as x is there).  Threads own column pairs as in
+// k_rb.
+template <typename T>
+__global__ void k_rb_pair0(const LevelT<T> L) {
+    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int c0 = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + 1;
+    if (J > L.ny || c0 > L.nx) return;
+    auto xr = [&](int i, int j) -> T {
+        if (i < 1 || i > L.nx || j < 1 || j > L.ny) return T(0);
+        const size_t o = (size_t)j * L.P + i;
+        return L.rhs[o] * L.inv_mc[o];
+    };
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+        const int I = c0 + d;
+        if (I > L.nx) break;
+        const size_t o = (size_t)J * L.P + I;
+        L.x[o] = ((I + J) & 1) == 0
+                     ? xr(I, J)
+                     : (L.rhs[o] + L.ce[o] * xr(I + 1, J) + L.ce[o - 1] * xr(I - 1, J) + L.cn[o] * xr(I, J + 1)
+                        + L.cn[o - L.P] * xr(I, J - 1)) * L.inv_mc[o];
+    }
+}
+
 // The 2 FS_STRIP_PAIRS half sweeps (colours color0, 1 - color0, ...) over both
 // strips of level L, from the snapshot sn, into L.x.  Grid (row tiles of
 // STRIP_ROWS, 2 strips), 256 threads, strip_smem() bytes of shared memory.
