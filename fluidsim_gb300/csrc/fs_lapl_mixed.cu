@@ -663,9 +663,9 @@ __global__ void __launch_bounds__(256) k_cgm_refine(const CgmArgs a) {
 __global__ void k_phi_update_ff(double *ph, double *phm, const float *xh, const float *xl, int nx, int ny, int P,
                                 const Ctrl *ctrl) {
     if (!ctrl->cg_done || ctrl->cg_fail) return;
-    size_t n = (size_t)(ny + 2) * P;
-    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
-        int gi = (int)(o % P), gj = (int)(o / P);
+    const unsigned n = (unsigned)(ny + 2) * (unsigned)P;   // 32-bit indices, as in k_phi_update
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < n; o += gridDim.x * blockDim.x) {
+        const int gj = (int)(o / (unsigned)P), gi = (int)(o - (unsigned)gj * (unsigned)P);
         double v = ph[o];
         if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) v = v + ((double)xh[o] + (double)xl[o]);
         ph[o] = v;

@@ -868,9 +868,11 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_smem(const BottomArgs
 __global__ void k_phi_update(double *ph, double *phm, const double *x, int nx, int ny, int P,
                              const Ctrl *ctrl) {
     if (!ctrl->cg_done || ctrl->cg_fail) return;
-    size_t n = (size_t)(ny + 2) * P;
-    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
-        int gi = (int)(o % P), gj = (int)(o / P);
+    // 32-bit index arithmetic (grids are limited to 2^28 nodes): a 64-bit
+    // division per element costs more than the update
+    const unsigned n = (unsigned)(ny + 2) * (unsigned)P;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < n; o += gridDim.x * blockDim.x) {
+        const int gj = (int)(o / (unsigned)P), gi = (int)(o - (unsigned)gj * (unsigned)P);
         double v = ph[o];
         if (gi >= 1 && gi <= nx && gj >= 1 && gj <= ny) v = v + x[o];
         ph[o] = v;
