@@ -84,7 +84,9 @@ typedef struct fs_config {
     int32_t precision;      /* FS_PREC_*                                              */
     int32_t lapl_maxit;     /* Krylov iteration cap                                   */
     int32_t table_n;        /* table points (FS_COEF_TABLE)                           */
-    int32_t mg_smooth;      /* red-black GS iterations per V-cycle leg (default 2)    */
+    int32_t mg_smooth;      /* red-black GS sweep pairs per V-cycle leg (default 2;   */
+                            /* the FP64 solver's finest level pre-smooths with one */
+                            /* pair fewer, at least one)                           */
     double  table_emin_ev;  /* table range in mean energy [eV]                        */
     double  table_emax_ev;
     double  kir_arrh_a;     /* Arrhenius ionisation prefactor [m^3/s] (table mode)    */
@@ -302,7 +304,8 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
  * parameters, two-level U-Net, tensor cores with FP32 accumulation) on the
  * grid of multigrid level `level` predicts the error the V-cycle leaves; its
  * interpolated prediction is added to each V-cycle's result inside the
- * flexible CG.  The FP64 refinement of the mixed solver judges convergence,
+ * flexible CG.  The refinement of the mixed solver (the true residual, to
+ * FP64 accuracy) judges convergence,
  * so every solve reaches lapl_rtol exactly as without the network, and if an
  * iteration stalls (inner residual falling by less than 2x) the network is
  * switched off for the rest of that solve.  In mode 1 the
