@@ -15,14 +15,17 @@ from fluidsim_gb300.api import FluidsimError, Handle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
+# the same source built for speed (-O3, contraction allowed): the timed CPU
+# baseline; parity tests use LIB
+LIB_TIMED = os.path.join(HERE, "liboracle_timed.so")
 SOLVER_DIRECT = 0
 SOLVER_BICGSTAB = 1
-_lib = None
+_libs = {}
 
 
 def build(quiet=True):
-    """Compile liboracle.so with the Makefile beside this file."""
-    out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
+    """Compile liboracle.so and liboracle_timed.so with the Makefile beside this file."""
+    out = subprocess.run(["make", "-C", HERE, "all"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:
@@ -30,13 +33,14 @@ def build(quiet=True):
     return LIB
 
 
-def load():
-    global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(LIB):
+def load(timed=False):
+    """The parity build, or with timed=True the build the CPU baseline times."""
+    if timed in _libs:
+        return _libs[timed]
+    path = LIB_TIMED if timed else LIB
+    if not os.path.exists(path):
         build()
-    lib = C.CDLL(LIB)
+    lib = C.CDLL(path)
     abi.declare_api(lib, "or_")
     P = C.POINTER
     dp = P(C.c_double)
@@ -54,12 +58,12 @@ def load():
     lib.or_dfdph.restype = C.c_double
     lib.or_coef.argtypes = [C.c_void_p, C.c_int32, C.c_double]
     lib.or_coef.restype = C.c_double
-    _lib = lib
+    _libs[timed] = lib
     return lib
 
 
-def set_threads(n):
-    return load().or_set_threads(int(n))
+def set_threads(n, timed=False):
+    return load(timed).or_set_threads(int(n))
 
 
 def get_flux(E, dh, q, mu, D, nl, nr):
@@ -73,8 +77,8 @@ def dfdph(E_pl, E_mi, q, mu, D, dx, n1, n2):
 class OracleDischarge(Handle):
     prefix = "or_"
 
-    def __init__(self, cfg, mesh=None, state=None, solver=SOLVER_DIRECT):
-        lib = load()
+    def __init__(self, cfg, mesh=None, state=None, solver=SOLVER_DIRECT, timed=False):
+        lib = load(timed)
         mesh = mesh or cfg.mesh()
         self._c_cfg = cfg.c_struct()
         self._c_mesh = mesh.c_struct()
