@@ -46,15 +46,32 @@ UNIT = "steps/s"
 # (stage 1 reads n2, n3, phi and writes k1, n2'; ...; stage 5 reads n2, n3,
 # k1, k3, k4, phi and writes n1), i.e. 640 B per node per attempt, 128 B per stage.
 STAGE_BYTES_PER_NODE = (25 * 3 + 5) * 8 / 5.0
-# measured DRAM traffic of one FP64 stage launch at 1024^2: 113.0 MB read + 27.8 MB written
-STAGE_TRAFFIC_1024 = 140.7e6
-# learned preconditioner variant: training pairs harvested over this many
-# steps (4 per step), then this many Adam steps of batch 16
+# One FP64 stage launch on the 1024^2 workload, averaged over the five stages
+# of an attempt, from one ncu capture (profiles/k_stage_glow1024.md):
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch,
+STAGE_TRAFFIC_1024 = 167.2e6
+# FP64 work per interior node, flops = dadd + dmul + 2 dfma
+# (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum / nodes),
+STAGE_FP64_FLOPS_PER_NODE = 297.2
+# and FP64-pipe thread instructions per node (sm__inst_executed_pipe_fp64.sum
+# x 32 / nodes: the DFMA/DADD/DMUL above plus conversions and comparisons),
+# the resource the kernel's time is bound by
+STAGE_FP64_PIPE_INST_PER_NODE = 245.0
+# algorithmic HBM bytes per node of one step's parts (FP64, 3 species): an RK
+# attempt (640), the Poisson assembly (reads n_e, n_i, n_t, phi; writes b and
+# three operator fields: 64) and one multigrid-PCG iteration (~57 fields: 456)
+STEP_ATTEMPT_BYTES = 640
+STEP_ASSEMBLY_BYTES = 64
+STEP_CG_BYTES = 456
+# learned preconditioner variant: training pairs harvested over LPC_HARVEST
+# steps (4 per step: full 1024^2 grids), then LPC_ITERS Adam steps (lr 1e-3)
+# on batches of LPC_BATCH random 128 x 128 crops
 # the device control block the host reads once per RK attempt and twice per
 # Poisson solve (sizeof(Ctrl) in fluidsim_gb300/csrc/fs_internal.h)
 CTRL_BYTES = 312
 LPC_HARVEST = 12
-LPC_ITERS = 400
+LPC_ITERS = 2000
+LPC_BATCH = 64
 
 
 def measured_peaks():
@@ -143,8 +160,8 @@ def cpu_threads():
 def time_oracle(cfg, mesh, state, t, dt, ts, max_seconds, max_steps, threads):
     """Run the oracle from a given state; returns (steps, seconds)."""
     from oracle import oracle
-    oracle.set_threads(threads)
-    o = oracle.OracleDischarge(cfg, mesh, state, solver=oracle.SOLVER_BICGSTAB)
+    oracle.set_threads(threads, timed=True)
+    o = oracle.OracleDischarge(cfg, mesh, state, solver=oracle.SOLVER_BICGSTAB, timed=True)
     o.set_time(t, dt)
     o.ts = ts
     steps = 0
@@ -169,11 +186,11 @@ def run_reference(args):
     oracle.build()
     cfg = workload(args.n, args.dt)
     mesh = cfg.mesh()
-    k = api.constants(cfg, oracle.load(), "or_")
+    k = api.constants(cfg, oracle.load(timed=True), "or_")
     st = initial_state(cfg, mesh, k)
     threads = cpu_threads()
-    oracle.set_threads(threads)
-    o = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_BICGSTAB)
+    oracle.set_threads(threads, timed=True)
+    o = oracle.OracleDischarge(cfg, mesh, st, solver=oracle.SOLVER_BICGSTAB, timed=True)
     # start-up iterations (Poisson only) and the requested warm-up steps,
     # untimed; the warm-up stops early only past 30 s (a step takes ~1.7 s
     # at 1024^2 on 16 cores), and the line reports the count run
@@ -200,7 +217,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded Gaussian blob + 1% noise",
         "config": {"workload": "2D Ar DC glow %dx%d, %s dt, Poisson rtol 1e-8" % (args.n, args.n, args.dt),
-                   "solver": "BiCGStab + block-Jacobi ILU(0), one block per thread"},
+                   "solver": "BiCGStab + block-Jacobi ILU(0), one block per thread",
+                   "build": "C++ oracle, g++ -O3 -fopenmp -ffp-contract=fast"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d main-loop steps of the same workload after start-up" % steps},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -209,7 +227,7 @@ def run_reference(args):
     return 0
 
 
-def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
+def measure_variant(cfg, mesh, st0, args, barrier, target_ts, learned=False):
     """Device-resident and end-to-end steps/s of one solver variant on the
     same workload (fresh context, same warm-up), for the comparison keys.
     learned: first harvest training pairs from the plain multigrid-PCG over
@@ -219,24 +237,26 @@ def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
     from fluidsim_gb300 import api
     d = api.Discharge(cfg, mesh, st0)
     stream = torch.cuda.ExternalStream(d.stream_handle())
-    d.run(2 + args.warmup)
+    d.run(target_ts)               # the plain run's checkpoint step
     train = None
     if learned:
         t0 = time.perf_counter()
-        d.lpc_init(level=3, max_batch=16, max_samples=1024, seed=1)
+        d.lpc_init(crop=128, max_batch=LPC_BATCH, max_samples=4 * LPC_HARVEST, seed=1)
         for _ in range(LPC_HARVEST):
             d.step()
             d.lpc_harvest(per_solve=4)
-        hist = d.lpc_train(iters=LPC_ITERS, batch=16, lr=1e-3, seed=2)
+        hist = d.lpc_train(iters=LPC_ITERS, batch=LPC_BATCH, lr=1e-3, seed=2)
         d.lpc_use(True)
         torch.cuda.synchronize()
-        train = {"pairs": d.lpc_info()["samples"], "adam_steps": LPC_ITERS, "batch": 16,
+        train = {"pairs": d.lpc_info()["samples"], "adam_steps": LPC_ITERS, "batch": LPC_BATCH,
+                 "crop": 128, "crops_seen": LPC_ITERS * LPC_BATCH,
                  "loss_first20": float(hist[:20].mean()), "loss_last20": float(hist[-20:].mean()),
                  "seconds": time.perf_counter() - t0, "nn_grid": [d.lpc_info()["h"], d.lpc_info()["w"]],
                  "params": d.lpc_info()["nparam"]}
     warm_state = d.download(nlev=3)
     warm_t, warm_dt, warm_ts = d.t, d.dt, d.ts
     w = d.stats()
+    li0 = d.lpc_info() if learned else None
     l0 = d.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
@@ -247,6 +267,12 @@ def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = d.launch_count() - l0
+    nn = None
+    if learned:
+        li1 = d.lpc_info()
+        ns = li1["solves"] - li0["solves"]
+        nn = {"timed_solves": ns, "with_network": li1["nn_solves"] - li0["nn_solves"],
+              "fraction": (li1["nn_solves"] - li0["nn_solves"]) / max(ns, 1)}
     pinned = {}
     for key in ("ni", "ne", "nt", "ph"):
         t = torch.empty(warm_state[key].shape[::-1], dtype=torch.float64, pin_memory=True)
@@ -279,7 +305,7 @@ def measure_variant(cfg, mesh, st0, args, barrier, learned=False):
             "h2d_bytes_per_step": (sum(a.nbytes for a in pinned.values()) + 8 * args.steps) / args.steps,
             "d2h_bytes_per_step": (sum(a.nbytes for a in out.values())
                                    + CTRL_BYTES * (e2e_attempts + 2 * args.steps)) / args.steps,
-            "training": train, "network_switched_off_in_last_solve": off}
+            "training": train, "network_use": nn, "network_switched_off_in_last_solve": off}
 
 
 def run_accuracy(args):
@@ -386,6 +412,40 @@ def run_sweep(args):
     return 0
 
 
+def timed_steps(d, steps, stream, barrier, ws):
+    """Device-resident main-loop steps timed with CUDA events on the context's
+    stream, max over ranks.  Returns (ms, stats after, launches)."""
+    import torch
+    l0 = d.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s = d.run(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, s, d.launch_count() - l0
+
+
+def fp64_peak_tflops(device):
+    """FP64 roof of this GPU, measured now: 2 x the DFMA rate of the library's
+    own microbenchmark (fs_fp64_rate; CUDA events, no clock changes)."""
+    import ctypes as C
+    from fluidsim_gb300 import api
+    v = C.c_double()
+    rc = api.load_library().fs_fp64_rate(int(device), C.byref(v))
+    if rc != 0:
+        raise RuntimeError("fs_fp64_rate failed (%d)" % rc)
+    return 2.0 * v.value / 1e12
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -408,56 +468,54 @@ def run_gpu(args):
     d = api.Discharge(cfg, mesh, st0)
     stream = torch.cuda.ExternalStream(d.stream_handle())
 
-    # start-up (two Poisson-only iterations) and warm-up steps
-    d.run(2 + args.warmup)
-    warm_state = d.download(nlev=3)
-    warm_t, warm_dt, warm_ts = d.t, d.dt, d.ts
-    warm_stats = d.stats()
-
     def barrier():
         if ws > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- timed region: device-resident steps --------------------------------
+    # ---- start-up figure: right after the two Poisson-only iterations -------
+    d.run(2 + args.warmup)
+    w0 = d.stats()
+    ms0, s0, _ = timed_steps(d, args.steps, stream, barrier, ws)
+    startup = {"value": ws * args.steps / (ms0 * 1e-3), "ms_per_step": ms0 / args.steps,
+               "from_step": w0["steps"], "rk_attempts": s0["attempts"] - w0["attempts"],
+               "rk_rejects": s0["rk_rejects"] - w0["rk_rejects"],
+               "cg_iters_per_step": (s0["lapl_iters"] - w0["lapl_iters"]) / args.steps}
+
+    # ---- developed state: checkpoint after >= args.develop adaptive steps ----
+    more = max(0, args.develop - d.ts)
+    if more:
+        d.run(more)
+    d.run(args.warmup)
+    ck = d.checkpoint()
+    warm_stats = d.stats()
+
+    # ---- timed region: device-resident steps from the checkpoint ------------
     sampler = ClockSampler(local)
     sampler.start()
     d.profile(["stage"])          # CUDA events around the RK stage launches only
-    n_launch0 = d.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    s = d.run(args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
+    ms, s, launches = timed_steps(d, args.steps, stream, barrier, ws)
     clocks = sampler.stop()
-    launches = d.launch_count() - n_launch0
     prof = d.profile_read()
     d.profile([])
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     attempts = s["attempts"] - warm_stats["attempts"]
+    rejects = s["rk_rejects"] - warm_stats["rk_rejects"]
     iters = s["lapl_iters"] - warm_stats["lapl_iters"]
 
     # ---- end to end through the C ABI with host buffers ---------------------
     pinned = {}
     for key in ("ni", "ne", "nt", "ph"):
-        a = warm_state[key]
+        a = ck["state"][key]
         t = torch.empty(a.shape[::-1], dtype=torch.float64, pin_memory=True)
         v = t.numpy().T          # Fortran-ordered view of pinned memory
         v[...] = a
         pinned[key] = v
-    d.set_time(warm_t, warm_dt)
-    d.ts = warm_ts
     out = {key: torch.empty(pinned[key].shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
            for key in ("ni", "ne", "nt", "ph")}
     state_bytes = sum(a.nbytes for a in pinned.values())
+    d.restore(ck)               # time, dt, controller, circuit (untimed)
+    d.ts = ck["controller"]["ts"]
+    a0 = d.stats()["attempts"]
     barrier()
     torch.cuda.synchronize()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -470,6 +528,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     barrier()
     ms_e2e = e2.elapsed_time(e3)
+    e2e_attempts = d.stats()["attempts"] - a0
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([ms_e2e], device="cuda")
@@ -477,43 +536,50 @@ def run_gpu(args):
         ms_e2e = float(t.item())
 
     # ---- per-class kernel time on a separate pass (Krylov loop host-driven) --
-    d.upload(pinned)
-    d.set_time(warm_t, warm_dt)
-    d.ts = warm_ts
+    d.restore(ck)
+    d.ts = ck["controller"]["ts"]
     d.profile(None)
     d.run(args.steps)
     breakdown = d.profile_read()
     d.profile([])
 
-    # ---- roofline of the dominant kernel (RK stage) -------------------------
-    peak, peak_kind = measured_peaks()
+    # ---- roofline of the dominant kernel (RK stage, FP64-issue-bound) -------
+    hbm_peak, peak_kind = measured_peaks()
+    fp64_peak = fp64_peak_tflops(local)
     st_ms, st_n = prof["stage"]
     nodes = cfg.nx * cfg.ny
     stage_ms = st_ms / max(st_n, 1)
-    achieved = STAGE_BYTES_PER_NODE * nodes / (stage_ms * 1e-3) / 1e9
+    fp64_achieved = STAGE_FP64_FLOPS_PER_NODE * nodes / (stage_ms * 1e-3) / 1e12
+    pipe_achieved = STAGE_FP64_PIPE_INST_PER_NODE * nodes / (stage_ms * 1e-3) / 1e9
+    hbm_achieved = STAGE_BYTES_PER_NODE * nodes / (stage_ms * 1e-3) / 1e9
     # DRAM bytes of one stage launch (dram__bytes_read.sum + dram__bytes_write.sum)
     # from one ncu capture of the 1024^2 workload; scaled by nodes elsewhere
     traffic = STAGE_TRAFFIC_1024 * nodes / (1024.0 * 1024.0)
+    # the whole step against HBM: algorithmic bytes of the RK attempts, the
+    # assembly and the CG iterations actually run
+    step_bytes = (STEP_ATTEMPT_BYTES * attempts + STEP_ASSEMBLY_BYTES * args.steps
+                  + STEP_CG_BYTES * iters) * nodes / args.steps
+    step_gbs = step_bytes / (ms / args.steps * 1e-3) / 1e9
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample ---------
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = cpu_threads()
-        steps_c, el_c = time_oracle(cfg, mesh, warm_state, warm_t, warm_dt, warm_ts,
+        steps_c, el_c = time_oracle(cfg, mesh, ck["state"], ck["t"], ck["dt"], ck["controller"]["ts"],
                                     max_seconds=args.cpu_seconds, max_steps=args.steps, threads=threads)
         cpu = {"value": steps_c / el_c, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d main-loop steps of the %dx%d workload from the warmed-up state "
-                         "(C++ oracle, OpenMP, BiCGStab+ILU(0))" % (steps_c, args.n, args.n)}
+               "sample": "%d main-loop steps of the %dx%d workload from the same checkpoint "
+                         "(C++ oracle built -O3 with OpenMP, BiCGStab+ILU(0))" % (steps_c, args.n, args.n)}
 
     # ---- the mixed-precision solver on the same workload ---------------------
     variants = {}
     if args.precision == "fp64" and not args.no_variants:
         cfgm = workload(args.n, args.dt, precision="mixed")
-        vm = measure_variant(cfgm, mesh, st0, args, barrier)
+        vm = measure_variant(cfgm, mesh, st0, args, barrier, ck["controller"]["ts"])
         vm["speedup_vs_plain"] = vm["value"] / (args.steps / (ms * 1e-3))
         vm["e2e_speedup_vs_plain"] = vm["e2e"] / (args.steps / (ms_e2e * 1e-3))
         variants["mixed"] = vm
-        vl = measure_variant(cfgm, mesh, st0, args, barrier, learned=True)
+        vl = measure_variant(cfgm, mesh, st0, args, barrier, ck["controller"]["ts"], learned=True)
         vl["speedup_vs_plain"] = vl["value"] / (args.steps / (ms * 1e-3))
         vl["e2e_speedup_vs_plain"] = vl["e2e"] / (args.steps / (ms_e2e * 1e-3))
         variants["mixed+learned-PC"] = vl
@@ -527,16 +593,28 @@ def run_gpu(args):
             "data": "synthetic: seeded Gaussian blob (1e14 m^-3, sigma 1 mm) + 1% noise",
             "config": {"workload": "2D Ar DC glow %dx%d, plain FP64 path" % (args.n, args.n),
                        "dt": args.dt, "poisson_rtol": 1e-8, "species": 3,
-                       "rk_attempts": attempts, "cg_iters_per_step": iters / args.steps,
+                       "timed_from_step": ck["controller"]["ts"],
+                       "rk_attempts": attempts, "rk_rejects": rejects,
+                       "cg_iters_per_step": iters / args.steps,
                        "l2": "working set per step > 129 MB L2 (no flush needed)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "startup": startup,
             "e2e": {"value": ws * args.steps / (ms_e2e * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": (state_bytes + 8 * args.steps) / args.steps,
-                    "d2h_bytes_per_step": (state_bytes + CTRL_BYTES * (attempts + 2 * args.steps)) / args.steps},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_stage (RK-Merson stage, FP64)", "peak_kind": peak_kind,
-                         "stage_ms": stage_ms},
+                    "d2h_bytes_per_step": (state_bytes + CTRL_BYTES * (e2e_attempts + 2 * args.steps)) / args.steps},
+            "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": fp64_achieved / fp64_peak, "traffic": traffic,
+                         "kernel": "k_stage (RK-Merson stage, FP64)",
+                         "peak_kind": "measured in this run (fs_fp64_rate: 2 x DFMA/s)",
+                         "flops_per_node": STAGE_FP64_FLOPS_PER_NODE, "stage_ms": stage_ms,
+                         "fp64_pipe": {"achieved": pipe_achieved, "peak": fp64_peak / 2 * 1e3,
+                                       "unit": "G inst/s", "frac": pipe_achieved / (fp64_peak / 2 * 1e3),
+                                       "inst_per_node": STAGE_FP64_PIPE_INST_PER_NODE},
+                         "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                                 "frac": hbm_achieved / hbm_peak, "peak_kind": peak_kind,
+                                 "bytes_per_node": STAGE_BYTES_PER_NODE},
+                         "step_hbm": {"achieved": step_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                      "frac": step_gbs / hbm_peak, "bytes_per_step": step_bytes}},
             "kernel_ms_per_step": {kk: v / args.steps for kk, v in total_ms.items()},
             "cpu_baseline": cpu,
             "variants": variants,
@@ -561,6 +639,8 @@ def main():
     ap.add_argument("--dt", default="adaptive", choices=("adaptive", "fixed"))
     ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    ap.add_argument("--develop", type=int, default=500,
+                    help="main-loop steps run before the checkpoint the timed steps start from")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the mixed-precision comparison run")

@@ -53,6 +53,13 @@ def load_library():
     lib.fs_profile_read.restype = C.c_int
     lib.fs_launch_count.argtypes = [C.c_void_p]
     lib.fs_launch_count.restype = C.c_int64
+    lib.fs_fp64_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]
+    lib.fs_fp64_rate.restype = C.c_int
+    lib.fs_math_eval.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64]
+    lib.fs_math_eval.restype = C.c_int
+    lib.fs_conv3x3_tc.argtypes = [C.c_int32] * 6 + [C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                                                    C.POINTER(C.c_float), C.c_int32, C.c_void_p]
+    lib.fs_conv3x3_tc.restype = C.c_int
     fp, i32, vp = C.POINTER(C.c_float), C.c_int32, C.c_void_p
     for name, args in (("fs_lpc_init", [vp, i32, i32, i32, C.c_uint64]),
                        ("fs_lpc_harvest", [vp, i32, C.POINTER(i32)]),
@@ -61,7 +68,8 @@ def load_library():
                        ("fs_lpc_weights", [vp, fp, C.c_int64, i32]),
                        ("fs_lpc_grad", [vp, fp, fp, fp, i32, fp, fp, fp]),
                        ("fs_lpc_info", [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
-                                        C.POINTER(C.c_int64), C.POINTER(i32)])):
+                                        C.POINTER(C.c_int64), C.POINTER(i32), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)])):
         getattr(lib, name).argtypes = args
         getattr(lib, name).restype = C.c_int
     lib.fs_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_double, C.c_int32,
@@ -366,15 +374,19 @@ class Discharge(Handle):
         self.check(self._lib.fs_output_wait(self.ctx))
 
     # -- learned Poisson preconditioner (mixed contexts) -----------------------
-    def lpc_init(self, level=3, max_batch=16, max_samples=512, seed=0):
-        self.check(self._lib.fs_lpc_init(self.ctx, level, max_batch, max_samples, seed))
+    def lpc_init(self, crop=0, max_batch=16, max_samples=64, seed=0):
+        """Network on the fine grid; training on crops of crop x crop cells
+        (a multiple of 8; 0: 128, at most the grid), batches up to max_batch,
+        up to max_samples stored training pairs (full grids)."""
+        self.check(self._lib.fs_lpc_init(self.ctx, crop, max_batch, max_samples, seed))
 
     def lpc_info(self):
         h, w, n, off = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
-        npar = C.c_int64()
+        npar, sol, nns = C.c_int64(), C.c_int64(), C.c_int64()
         self.check(self._lib.fs_lpc_info(self.ctx, C.byref(h), C.byref(w), C.byref(n), C.byref(npar),
-                                         C.byref(off)))
-        return dict(h=h.value, w=w.value, samples=n.value, nparam=npar.value, off=off.value)
+                                         C.byref(off), C.byref(sol), C.byref(nns)))
+        return dict(h=h.value, w=w.value, samples=n.value, nparam=npar.value, off=off.value,
+                    solves=sol.value, nn_solves=nns.value)
 
     def lpc_harvest(self, per_solve=4):
         a = C.c_int32()

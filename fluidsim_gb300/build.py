@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 OUT = os.path.join(HERE, "libfluidsim_gb300.so")
-SOURCES = ["fs_api.cu", "fs_ptcl.cu", "fs_lapl.cu", "fs_mixed.cu", "fs_lapl_mixed.cu", "fs_lpc.cu", "fs_host.cpp", "fs_batch.cpp", "fs_output.cpp"]
+SOURCES = ["fs_api.cu", "fs_ptcl.cu", "fs_lapl.cu", "fs_mixed.cu", "fs_lapl_mixed.cu", "fs_lpc.cu", "fs_conv_tc.cu", "fs_probe.cu", "fs_host.cpp", "fs_batch.cpp", "fs_output.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -748,9 +748,9 @@ extern "C" int fs_max_ne_noalloc(fs_ctx *c, double *out) {
 // ------------------------------------------------ learned Poisson preconditioner
 #include "fs_lpc.cuh"
 
-int fs_lpc_init(fs_ctx *c, int32_t level, int32_t max_batch, int32_t max_samples, uint64_t seed) {
+int fs_lpc_init(fs_ctx *c, int32_t crop, int32_t max_batch, int32_t max_samples, uint64_t seed) {
     if (!c) return FS_ERR_INVALID;
-    return fs_lpc_init_impl(c, level, max_batch, max_samples, seed);
+    return fs_lpc_init_impl(c, crop, max_batch, max_samples, seed);
 }
 
 int fs_lpc_harvest(fs_ctx *c, int32_t per_solve, int32_t *added) {
@@ -778,6 +778,7 @@ int fs_lpc_use(fs_ctx *c, int32_t on) {
     c->lpc_since_probe = 0;
     c->lpc_probe_every = 25;
     c->lpc_probe_pending = 0;
+    c->lpc_solves = c->lpc_nn_solves = 0;
     return FS_OK;
 }
 
@@ -806,7 +807,8 @@ int fs_lpc_grad(fs_ctx *c, const float *feat, const float *tgt, const float *mas
     return fs_lpc_grad_impl(c, feat, tgt, mask, batch, grad, loss, pred);
 }
 
-int fs_lpc_info(fs_ctx *c, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off) {
+int fs_lpc_info(fs_ctx *c, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off,
+                int64_t *solves, int64_t *nn_solves) {
     if (!c) return FS_ERR_INVALID;
     if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
     if (h) *h = c->lpc->Hn;
@@ -814,5 +816,7 @@ int fs_lpc_info(fs_ctx *c, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *n
     if (nsamples) *nsamples = c->lpc->nsamp < c->lpc->Nmax ? c->lpc->nsamp : c->lpc->Nmax;
     if (nparam) *nparam = (int64_t)c->lpc->net.nparam;
     if (off) *off = c->h_ctrl->lpc_off;
+    if (solves) *solves = c->lpc_solves;
+    if (nn_solves) *nn_solves = c->lpc_nn_solves;
     return FS_OK;
 }

@@ -1,0 +1,478 @@
+// fs_conv_tc.cu -- 3x3 convolutions of the learned preconditioner on the
+// Blackwell tensor cores (tcgen05), fed by the tensor memory accelerator.
+//
+// Implicit GEMM, one CTA per tile of 128 output pixels (TW x TH pixels of one
+// image, TW = min(128, W) rounded up to a power of two): D[128 px][cout] =
+// sum over the 9 taps and the input channels of A[px][cin] W[cin][cout].
+//   * A: for each tap (dy, dx) and each source tensor (the decoder's
+//     concatenation has two), the tile's input pixels shifted by (dy, dx) --
+//     one TMA load of a TW x TH x kc box of the NHWC BF16 activations, with
+//     the 128-byte / 64-byte / 32-byte swizzle the MMA descriptor names; the
+//     zero padding at the grid edge is TMA's out-of-bounds fill;
+//   * B: the layer's weights, stored once per refresh as the exact shared-
+//     memory image the MMA reads (K-major, swizzled, one block per tap and
+//     source), copied in by one bulk copy;
+//   * one thread issues the TMA loads into a ring of A stages, one thread
+//     issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128, N = cout)
+//     with the accumulator in tensor memory, and tcgen05.commit frees each
+//     A stage when its MMAs are done;
+//   * the four warps then read the accumulator (tcgen05.ld, one pixel per
+//     thread) and apply bias, ReLU (or the ReLU mask of the backward pass)
+//     and the BF16 store.
+// Every wait on an mbarrier is bounded: a wait that runs out sets *err and
+// the CTA skips the rest of its work (after a bounded wait for its own
+// copies and MMAs in flight) and frees its tensor memory.
+#include <cuda.h>   // CUtensorMap and its enums; the encoder is fetched through the runtime
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fs_conv_tc.cuh"
+
+namespace {
+
+constexpr int kStages = 4;                 // A ring depth
+constexpr int kStageBytes = 128 * 64 * 2;  // largest A tile: 128 px x 64 ch BF16
+constexpr long kSpinLimit = 1L << 20;      // bounded waits (each try_wait may sleep ~us)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+                 : "memory");
+}
+
+// true once the phase with this parity has completed; false if the wait ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+    const uint32_t a = smem_u32(b);
+    for (long i = 0; i < kSpinLimit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c, int x, int y, int b,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(b), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading byte
+// offset (unused by the swizzled K-major layouts: 1), stride byte offset
+// (one 8-row swizzle atom), descriptor version 1, swizzle mode in bits 61-63.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo, uint32_t mode) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)mode << 61;
+    return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// swizzle mode field and atom size of a K chunk of kc BF16 channels
+__device__ __host__ __forceinline__ uint32_t swz_mode(int kc) { return kc == 64 ? 2u : kc == 32 ? 4u : 6u; }
+__device__ __host__ __forceinline__ uint32_t swz_atom(int kc) { return 8u * 2u * (uint32_t)kc; }
+
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tm0,
+                                                    const __grid_constant__ CUtensorMap tm1, const TcConvArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t *sw = smem;                               // weight image
+    uint8_t *sa = smem + a.wbytes;                    // A stages (wbytes is a multiple of 1024)
+    uint64_t *full = reinterpret_cast<uint64_t *>(sa + kStages * kStageBytes);
+    uint64_t *empty = full + kStages;
+    uint64_t *wbar = empty + kStages;
+    uint64_t *done = wbar + 1;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x;
+    tile /= a.tiles_x;
+    const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
+    const int x0 = tx * a.TW, y0 = ty * a.TH;
+    const int nper = a.nchunk[0] + a.nchunk[1];       // K chunks per tap
+    const int nk = 9 * nper;
+
+    if (threadIdx.x == 0) {
+        // a CTA of this launch whose wait ran out voids the result: skip the work
+        s_fail = *reinterpret_cast<volatile int *>(a.err) ? 2 : 0;
+        for (int s = 0; s < kStages; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
+        mbar_init(wbar, 1);
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (s_fail == 2) return;   // uniform over the CTA
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"((uint32_t)a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0 && lane == 0) {
+        // producer: the weight image, then the A chunks tap by tap
+        mbar_expect_tx(wbar, (uint32_t)a.wbytes);
+        bulk_copy(sw, a.wimg, (uint32_t)a.wbytes, wbar);
+        for (int kc = 0; kc < nk; ++kc) {
+            const int s = kc % kStages, n = kc / kStages;
+            if (n > 0 && !mbar_wait(empty + s, (uint32_t)((n - 1) & 1))) { atomicExch(&s_fail, 1); break; }
+            const int t = kc / nper, q = kc - t * nper;
+            const int src = q < a.nchunk[0] ? 0 : 1, j = src ? q - a.nchunk[0] : q;
+            const int kcw = a.kc[src];
+            mbar_expect_tx(full + s, (uint32_t)(128 * kcw * 2));
+            tma_load_4d(sa + s * kStageBytes, src ? &tm1 : &tm0, j * kcw, x0 + t % 3 - 1, y0 + t / 3 - 1, b,
+                        full + s);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.cout >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
+        bool ok = mbar_wait(wbar, 0);
+        for (int kc = 0; ok && kc < nk; ++kc) {
+            const int s = kc % kStages, n = kc / kStages;
+            if (!mbar_wait(full + s, (uint32_t)(n & 1))) { ok = false; break; }
+            tc_fence_after();
+            const int t = kc / nper, q = kc - t * nper;
+            const int src = q < a.nchunk[0] ? 0 : 1;
+            const int kcw = a.kc[src];
+            const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
+            const uint32_t abase = smem_u32(sa + s * kStageBytes);
+            const uint32_t bbase = smem_u32(sw + a.boff[t * nper + q]);
+            for (int k = 0; k < kcw / 16; ++k)
+                mma_bf16(tmem, smem_desc(abase + 32 * k, atom, mode), smem_desc(bbase + 32 * k, atom, mode), idesc,
+                         (kc > 0 || k > 0) ? 1u : 0u);
+            mma_commit(empty + s);
+        }
+        if (ok) mma_commit(done);
+        else atomicExch(&s_fail, 1);
+    }
+    __syncwarp();
+
+    // epilogue: thread = one pixel of the tile (its TMEM lane)
+    bool ok = mbar_wait(done, 0);
+    ok = __all_sync(0xffffffffu, ok);   // warp-uniform (tcgen05.ld is warp-collective)
+    if (!ok) atomicExch(&s_fail, 1);
+    tc_fence_after();
+    const int p = warp * 32 + lane;
+    const int px = x0 + p % a.TW, py = y0 + p / a.TW;
+    const bool in = px < a.W && py < a.H;
+    const long pix = ((long)b * a.H + py) * a.W + px;
+    if (ok) {
+        for (int c0 = 0; c0 < a.cout; c0 += 16) {
+            float v[16];
+            __syncwarp();
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (!in) continue;
+            if (a.out32) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + a.bias[c0 + i];
+                continue;
+            }
+            // BF16 output, split over up to two tensors (the backward pass's
+            // concatenated inputs): channels [0, split) to out, the rest to out2
+            __nv_bfloat16 *dst;
+            int cc, cs;
+            const __nv_bfloat16 *msk;
+            if (c0 < a.split) { dst = a.out; cc = c0; cs = a.split; msk = a.mask; }
+            else { dst = a.out2; cc = c0 - a.split; cs = a.cout - a.split; msk = a.mask2; }
+            uint32_t pk[8];
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                float u0 = v[i] + (a.bias ? a.bias[c0 + i] : 0.0f), u1 = v[i + 1] + (a.bias ? a.bias[c0 + i + 1] : 0.0f);
+                if (a.relu) { u0 = fmaxf(u0, 0.0f); u1 = fmaxf(u1, 0.0f); }
+                if (msk) {
+                    const __nv_bfloat16 *m = msk + pix * cs + cc + i;
+                    if (!(__bfloat162float(m[0]) > 0.0f)) u0 = 0.0f;
+                    if (!(__bfloat162float(m[1]) > 0.0f)) u1 = 0.0f;
+                }
+                const __nv_bfloat162 h = __floats2bfloat162_rn(u0, u1);
+                pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+            }
+            uint4 *o = reinterpret_cast<uint4 *>(dst + pix * cs + cc);
+            o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (s_fail && threadIdx.x == 0) {
+        atomicExch(a.err, 1);
+        // a bounded wait for the copies and MMAs this CTA may still have in flight
+        mbar_wait(done, 0);
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)a.tmem_cols)
+                     : "memory");
+}
+
+// The weight image of one layer from FP32 weights w[9][cout][c1 + c2]: per
+// (tap, K chunk) block, row co holds the chunk's kc input channels in BF16,
+// rows of 2 kc bytes with the 16-byte pieces of row r permuted as the
+// swizzle mode permutes them (128 B: piece ^ (r & 7); 64 B: ^ ((r >> 1) & 3);
+// 32 B: ^ ((r >> 2) & 1)) -- the layout the MMA descriptor reads.
+// transposed = 1: the image of the data-gradient convolution of a layer
+// w[9][cin][cout] (input channels = that layer's cout = c1 here, outputs its
+// cin = cout here): entry (t, co, ci) = w[8 - t][ci][co], the flipped taps.
+__global__ void k_tc_weights(const float *w, int c1, int c2, int cout, TcConvArgs lay, uint8_t *img, int transposed) {
+    const int cin = c1 + c2, nper = lay.nchunk[0] + lay.nchunk[1];
+    const int n = 9 * cout * cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int t = i / (cout * cin), rem = i - t * cout * cin, co = rem / cin, ci = rem - co * cin;
+        const float wv = transposed ? w[((size_t)(8 - t) * cin + ci) * cout + co] : w[i];
+        const int src = ci < c1 ? 0 : 1, cl = src ? ci - c1 : ci, kc = lay.kc[src];
+        const int j = cl / kc, e = cl - j * kc;
+        const int q = src ? lay.nchunk[0] + j : j;
+        const int piece = e >> 3, f = kc == 64 ? (co & 7) : kc == 32 ? ((co >> 1) & 3) : ((co >> 2) & 1);
+        const size_t off = (size_t)lay.boff[t * nper + q] + (size_t)co * (2 * kc) + (size_t)(piece ^ f) * 16 +
+                           (size_t)(e & 7) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(img + off) = __float2bfloat16_rn(wv);
+    }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------- host
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn g_encode = nullptr;
+
+int load_encoder() {
+    if (g_encode) return 0;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return -1;
+    g_encode = reinterpret_cast<EncodeTiledFn>(fn);
+    return 0;
+}
+}  // namespace
+
+int tc_tmem_cols(int n) {
+    int c = 32;
+    while (c < n) c *= 2;
+    return c;
+}
+
+void tc_tile_shape(int W, int &TW, int &TH) {
+    TW = 16;
+    while (TW < 128 && TW < W) TW *= 2;
+    TH = 128 / TW;
+}
+
+int tc_make_map(CUtensorMap *m, const void *base, int B, int H, int W, int C, int kc) {
+    if (load_encoder()) return -1;
+    if (!(kc == 16 || kc == 32 || kc == 64) || C % kc || (reinterpret_cast<uintptr_t>(base) & 15)) return -2;
+    int TW, TH;
+    tc_tile_shape(W, TW, TH);
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)kc, (cuuint32_t)TW, (cuuint32_t)TH, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle sw = kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                  : kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                             : CU_TENSOR_MAP_SWIZZLE_32B;
+    const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims, strides, box,
+                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : -3;
+}
+
+int tc_weight_layout(int c1, int c2, int cout, int *boff, int *kc, int *nchunk) {
+    kc[0] = c1 >= 64 ? 64 : c1;
+    kc[1] = c2 >= 64 ? 64 : c2;
+    nchunk[0] = c1 / (kc[0] ? kc[0] : 1);
+    nchunk[1] = c2 ? c2 / kc[1] : 0;
+    const int nper = nchunk[0] + nchunk[1];
+    int off = 0;
+    for (int t = 0; t < 9; ++t)
+        for (int q = 0; q < nper; ++q) {
+            const int src = q < nchunk[0] ? 0 : 1;
+            boff[t * nper + q] = off;
+            const int bytes = cout * kc[src] * 2;
+            off += (bytes + 1023) / 1024 * 1024;
+        }
+    return off;
+}
+
+static void build_image(const float *w, int c1, int c2, int cout, void *img, int transposed, cudaStream_t st) {
+    TcConvArgs lay = {};
+    const int bytes = tc_weight_layout(c1, c2, cout, lay.boff, lay.kc, lay.nchunk);
+    cudaMemsetAsync(img, 0, (size_t)bytes, st);
+    const int n = 9 * cout * (c1 + c2);
+    k_tc_weights<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, st>>>(
+        w, c1, c2, cout, lay, reinterpret_cast<uint8_t *>(img), transposed);
+}
+
+void tc_build_weights(const float *w, int c1, int c2, int cout, void *img, cudaStream_t st) {
+    build_image(w, c1, c2, cout, img, 0, st);
+}
+
+void tc_build_weights_bwd(const float *w, int cin, int cout, void *img, cudaStream_t st) {
+    build_image(w, cout, 0, cin, img, 1, st);
+}
+
+size_t tc_smem_bytes(int wbytes) {
+    return 1024 + (size_t)wbytes + (size_t)kStages * kStageBytes + 8 * (2 * kStages + 2) + 16;
+}
+
+namespace {
+// the dynamic shared memory a launch may take: the device's opt-in limit
+// per block less the kernel's static shared memory
+size_t g_smem_max = 0;
+}  // namespace
+
+int tc_init() {
+    if (g_smem_max) return 0;
+    if (load_encoder()) return -1;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_conv_tc) != cudaSuccess)
+        return -2;
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) return -2;
+    g_smem_max = (size_t)dyn;
+    return 0;
+}
+
+size_t tc_smem_limit() { return g_smem_max; }
+
+int tc_conv(const CUtensorMap *m0, const CUtensorMap *m1, const TcConvArgs &a, cudaStream_t st) {
+    const size_t smem = tc_smem_bytes(a.wbytes);
+    if (!g_smem_max || smem > g_smem_max) return -2;
+    const int grid = a.tiles_x * a.tiles_y * a.B;
+    k_conv_tc<<<grid, 128, smem, st>>>(*m0, m1 ? *m1 : *m0, a);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : -100 - (int)e;
+}
+
+// One 3x3 convolution through the tcgen05 path on host arrays (tests): in1
+// [B][H][W][c1] and in2 [B][H][W][c2] (may be null) as BF16 bit patterns,
+// w [9][cout][c1 + c2] and bias [cout] in FP32; mode 0 writes FP32
+// out[B][H][W][cout] (bias, no ReLU), mode 1 BF16 bit patterns (bias, ReLU).
+extern "C" int fs_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t c1, int32_t c2, int32_t cout,
+                             const uint16_t *in1, const uint16_t *in2, const float *w, const float *bias,
+                             int32_t mode, void *out) {
+    if (B < 1 || H < 1 || W < 1 || cout < 16 || cout > 128 || cout % 16 || !in1 || !w || !out ||
+        (c2 > 0 && !in2) || c1 < 16 || c1 % 16 || c2 < 0 || c2 % 16 || (c1 > 64 && c1 % 64) ||
+        (c2 > 64 && c2 % 64) || (mode != 0 && mode != 1))
+        return -1;
+    const size_t P = (size_t)B * H * W, cin = (size_t)c1 + c2;
+    TcConvArgs a = {};
+    a.wbytes = tc_weight_layout(c1, c2, cout, a.boff, a.kc, a.nchunk);
+    if (9 * (a.nchunk[0] + a.nchunk[1]) > TC_MAX_CHUNKS) return -1;
+    uint8_t *d = nullptr;
+    const size_t o_in1 = 0, o_in2 = o_in1 + (P * c1 * 2 + 1023) / 1024 * 1024,
+                 o_w = o_in2 + (P * c2 * 2 + 1023) / 1024 * 1024, o_b = o_w + 9 * cin * cout * 4,
+                 o_img = (o_b + cout * 4 + 1023) / 1024 * 1024, o_out = o_img + (size_t)a.wbytes,
+                 o_err = o_out + P * cout * 4, total = o_err + 16;
+    if (tc_init()) return -3;
+    if (cudaMalloc(&d, total) != cudaSuccess) return -2;
+    int rc = 0;
+    cudaStream_t st = 0;
+    cudaMemcpy(d + o_in1, in1, P * c1 * 2, cudaMemcpyHostToDevice);
+    if (c2) cudaMemcpy(d + o_in2, in2, P * c2 * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + o_w, w, 9 * cin * cout * 4, cudaMemcpyHostToDevice);
+    if (bias) cudaMemcpy(d + o_b, bias, cout * 4, cudaMemcpyHostToDevice);
+    else cudaMemset(d + o_b, 0, cout * 4);
+    cudaMemset(d + o_err, 0, 16);
+    tc_build_weights(reinterpret_cast<float *>(d + o_w), c1, c2, cout, d + o_img, st);
+    CUtensorMap m0, m1;
+    if (tc_make_map(&m0, d + o_in1, B, H, W, c1, a.kc[0]) ||
+        (c2 && tc_make_map(&m1, d + o_in2, B, H, W, c2, a.kc[1])))
+        rc = -3;
+    if (!rc) {
+        a.cout = cout;
+        a.tmem_cols = tc_tmem_cols(cout);
+        a.B = B; a.H = H; a.W = W;
+        tc_tile_shape(W, a.TW, a.TH);
+        a.tiles_x = (W + a.TW - 1) / a.TW;
+        a.tiles_y = (H + a.TH - 1) / a.TH;
+        a.wimg = d + o_img;
+        a.bias = reinterpret_cast<float *>(d + o_b);
+        a.relu = mode == 1;
+        a.split = cout;
+        if (mode == 0) { a.out32 = reinterpret_cast<float *>(d + o_out); a.out32_ch = cout; }
+        else a.out = reinterpret_cast<__nv_bfloat16 *>(d + o_out);
+        a.err = reinterpret_cast<int *>(d + o_err);
+        const cudaError_t pre = cudaGetLastError();   // anything the set-up left
+        rc = pre != cudaSuccess ? -100 - (int)pre : tc_conv(&m0, c2 ? &m1 : nullptr, a, st);
+    }
+    int err = 0;
+    if (!rc) {
+        const cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) rc = -100 - (int)e;
+    }
+    if (!rc) cudaMemcpy(&err, d + o_err, 4, cudaMemcpyDeviceToHost);
+    if (!rc && err) rc = -6;
+    if (!rc) cudaMemcpy(out, d + o_out, P * cout * (mode == 0 ? 4 : 2), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return rc;
+}

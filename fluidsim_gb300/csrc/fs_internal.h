@@ -80,15 +80,16 @@ struct Ctrl {
     unsigned int status;  // FS_ST_* bits
     int rejected;         // last attempt rejected by the error norm
     int min_dt;           // dt fell to dt_min
-    int pad;
+    int lpc_stalls;       // mixed solver: stalled iterations with the learned correction
     // Krylov scalars
     double rz, rz_old, pq, alpha, beta, rnorm2, bnorm2, relres;
     int cg_done, cg_iters, cg_fail, pad2;
     double r0in2;              // mixed solver: inner residual norm^2 at the last refinement
     int inner_it, refine;      // mixed solver: inner iterations since it, refinement due
     double rr_prev;            // mixed solver: previous inner residual norm^2
-    double lpc_s, lpc_mcm;     // learned correction: residual scale, mean level diagonal
-    int lpc_off, pad3;         // learned correction switched off for this solve (stall)
+    double spare[2];
+    int lpc_off;               // learned correction switched off for this solve (stall)
+    int cgm_restarted;         // mixed solver: the last refinement restarted the search direction
     double vd_pl, vd_mi;       // electrode voltage of the RC circuit (AC source, circ_lib.F90:158-174)
     double kv[6];              // its Merson slopes kv(1..5)
     unsigned int counter[8];   // last-block-done counters of grid reductions
@@ -220,16 +221,14 @@ struct fs_ctx {
     MGLevelF mgf[FS_MG_MAX_LEVELS];
     float *p32, *q32, *w32;      // FP32 inner CG vectors (w = M z)
     float *xh32, *xl32, *dinv32; // the mixed CG's iterate as a float-float pair; 1/D in FP32
-    // learned preconditioner (fs_lpc.cu): network on the grid of MG level lpc_level
+    // learned preconditioner (fs_lpc.cu): network on the fine grid
     struct LpcState *lpc;
-    int lpc_on, lpc_level;
+    int lpc_on, pad_lpc;
     // choice between the two solvers, judged on measured solve time
     double lpc_t_nn, lpc_t_plain;   // moving averages of the solve time (ms), < 0: none yet
     int lpc_use_next, lpc_since_probe;
+    int64_t lpc_solves, lpc_nn_solves;   // solves since fs_lpc_use turned it on, and those that ran the network
     int lpc_probe_every, lpc_probe_pending;   // probe interval of the other choice, last solve was a probe
-    float *lpc_op;               // [Hn][Wn][3] operator features of the level (per solve)
-    float *lpc_rr;               // [Hn][Wn] restricted residual
-    double *lpc_rhs64;           // fine right-hand side of a harvest solve
     float *lpc_snap;             // harvested residual snapshots (fine FP32 fields)
     int lpc_snap_max;
     cudaGraph_t cgm_graph[2];    // [0] plain MG-PCG, [1] with the learned correction
@@ -275,7 +274,7 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);
 int fs_lapl_alloc_mixed(fs_ctx *c);
 void fs_lapl_free_mixed(fs_ctx *c);
 // learned preconditioner (fs_lapl_mixed.cu, network in fs_lpc.cu)
-int fs_lpc_init_impl(fs_ctx *c, int level, int max_batch, int max_samples, uint64_t seed);
+int fs_lpc_init_impl(fs_ctx *c, int crop, int max_batch, int max_samples, uint64_t seed);
 void fs_lpc_free_impl(fs_ctx *c);
 int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added);
 int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, float *loss_hist);

@@ -29,6 +29,7 @@
 #include <vector>
 #include <cuda_runtime.h>
 
+#include "fs_fastmath.cuh"
 #include "fs_internal.h"
 
 #include "fs_mg.cuh"
@@ -54,7 +55,7 @@ struct AsmArgs {
 };
 
 __device__ __forceinline__ void tab_index(const PhysParams &pp, double T, int &k, double &w) {
-    double x = log(T * pp.ph0);
+    double x = fs_log(T * pp.ph0);
     double u = (x - pp.lemin) * pp.inv_h;
     if (!(u >= 0.0)) u = 0.0;
     if (u > (double)(pp.ntab - 1)) u = (double)(pp.ntab - 1);
@@ -78,7 +79,7 @@ __device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double
     const double tolf = 9.9999999600419720025e-13;   // REAL(4) 1e-12 of get_Flux
     double v = (double)q * mu * E;
     double arg = v * dh / D;
-    double exa = exp(-fabs(arg));
+    double exa = fs_exp(-fabs(arg));
     if (fabs((double)q * E) < tolf) {
         flux = D * (nl - nr) / dh;
     } else if (fabs(arg) < 1e-2) {   // Bernoulli form near a = 0
@@ -99,7 +100,7 @@ __device__ __forceinline__ void sg_and_dfdph(int q, double E, double Emi, double
         double dn = nl - nr, a2 = am * am;
         df = 0.5 * (nl + nr) + dn * am * (1.0 / 6.0 - a2 * (1.0 / 180.0 - a2 / 5040.0));
     } else {
-        double ex = (Emi == E) ? exa : exp(-fabs(am));
+        double ex = (Emi == E) ? exa : fs_exp(-fabs(am));
         double one = 1.0 - ex;
         if (am > 0) df = (nl - nr * ex) / one + vm * ex * (nr - nl) / (one * one) * dh / D;
         else df = (nr - nl * ex) / one + vm * ex * (nr - nl) / (one * one) * dh / D;
@@ -116,7 +117,7 @@ __device__ __forceinline__ void elec_face(double E, double dh, double idh, doubl
     double v = -mue * E;
     double arg = v * dh / De;
     double aa = fabs(arg);
-    double ex = aa >= 1e-2 ? exp(-aa) : 0.0;
+    double ex = aa >= 1e-2 ? fs_exp(-aa) : 0.0;
     if (fabs(E) < tolf) {
         flux = De * (nl - nr) * idh;
     } else if (aa < 1e-2) {

@@ -340,11 +340,12 @@ __global__ void k_dinv(const MeshDev m, int nx, int ny, int P, int cyl, double *
 // faster than FP64), run until its FP32
 // recurrence residual has fallen by inner_tol (or just enough to reach
 // lapl_rtol, or inner_max iterations); then the refinement recomputes the
-// true residual in float-float and restarts the inner loop from it.  The FP32
+// true residual in float-float, and the inner loop goes on from it with its
+// search direction kept (CG with reliable updates).  The FP32
 // recurrence drifts from the true residual (rounding of the FP32 vectors and
 // operator products); the refinement removes the drift, so the converged
-// residual is the true FP64 one.  Dot products of the inner loop: FP32 sums in
-// a fixed order (grid_sumf); the refinement's norms: FP64 (grid_sum2).
+// residual is the true FP64 one.  Dot products: FP32 sums in a fixed order
+// (grid_sumf), the refinement's of power-of-two scaled values.
 struct CgmArgs {
     int nx, ny, P, nblk;
     dim3 grid;
@@ -449,6 +450,8 @@ __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
         c->alpha = 0.0;
         c->rr_prev = sw;
         c->lpc_off = 0;
+        c->lpc_stalls = 0;
+        c->cgm_restarted = 1;
     }
 }
 
@@ -558,7 +561,11 @@ __global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
         Ctrl *c = a.ctrl;
         c->rz_old = c->rz;
         c->rz = s[0];
-        const bool first = c->inner_it == 0;   // q_old = 0 after a (re)start
+        // the search direction carries over a refinement (the true residual
+        // replaces the recurrence one, the Krylov recurrence goes on, as in
+        // CG with reliable updates); it restarts only at the solve's start
+        // and after a breakdown (alpha = 0 there, so beta = 0)
+        const bool first = c->cg_iters == 0;   // q_old = 0
         const double be = first ? 0.0 : -c->alpha * s[1] / c->rz_old;
         c->beta = be;
         const double pq = first ? s[2] : s[2] + 2.0 * be * s[1] + be * be * c->pq;
@@ -568,7 +575,10 @@ __global__ void __launch_bounds__(256) k_cgm_rzw(const CgmArgs a) {
         const double rqn = s[4] + be * s[5], qqn = s[6] + 2.0 * be * s[7] + be * be * s[8];
         const double out = fmax(s[3] - 2.0 * al * rqn + al * al * qqn, 0.0);
         // the learned correction stalls the iteration: plain MG-PCG for the rest of the solve
-        if (a.lpc && c->inner_it > 0 && out > 0.25 * c->rr_prev) c->lpc_off = 1;
+        // an iteration with the network whose residual falls by less than 4x
+        // stalls (plain MG-PCG takes about 10x per iteration on these
+        // systems); after 3 stalls the solve goes on with plain MG-PCG
+        if (a.lpc && c->inner_it > 0 && out > 0.0625 * c->rr_prev && ++c->lpc_stalls >= 3) c->lpc_off = 1;
         c->rr_prev = out;
         c->cg_iters += 1;
         c->inner_it += 1;
@@ -653,8 +663,14 @@ __global__ void __launch_bounds__(256) k_cgm_refine(const CgmArgs a) {
         c->inner_it = 0;
         c->refine = 0;
         c->rr_prev = sums[1];
+        // the search direction is kept across the refinement unless the
+        // cycle broke down (pq <= 0) or the true residual did not fall over
+        // it; a cycle that fails to reduce it after a restart fails the solve
+        const bool fell = c->relres < prev;
         if (c->relres <= a.rtol) c->cg_done = 1;
-        else if (isnan(sums[0]) || c->cg_iters >= a.maxit || !(c->relres < prev)) c->cg_fail = 1;
+        else if (isnan(sums[0]) || c->cg_iters >= a.maxit || (!fell && c->cgm_restarted)) c->cg_fail = 1;
+        c->cgm_restarted = !(c->pq > 0.0) || !fell;
+        if (c->cgm_restarted) c->alpha = 0.0;   // restart from z (beta = 0)
         if (a.use_cond && (c->cg_done || c->cg_fail)) cudaGraphSetConditional(a.cond, 0u);
     }
 }
@@ -674,151 +690,83 @@ __global__ void k_phi_update_ff(double *ph, double *phm, const float *xh, const 
 }
 
 // ------------------------------------------- learned correction (inference)
-// The network works on the grid of MG level lev (aggregates of 2^lev x 2^lev
-// fine nodes; NN cell (I, J), 1-based, covers fine i in (I-1) 2^lev + 1 ..
-// I 2^lev).  Inputs per cell: the aggregated residual R (r - M z) after the
-// V-cycle, scaled by its RMS s, and the level operator's ce/mc, cn/mc,
-// extra/mc.  Output y: the aggregate mean of the remaining error
-// M^-1 (r - M z), scaled by mcm/s (mcm the mean level diagonal); it is
-// interpolated bilinearly (cell centred) to the fine grid and added to z.
+// The network works on the fine grid (NN cell (J, I), 0-based, is node
+// (I + 1, J + 1); the NN grid is padded to multiples of 8 with zero cells).
+// Inputs per cell, x0 [Hn][Wn][16] BF16 (channels 4..15 stay zero):
+//   f0 = s / sigma: the residual the V-cycle leaves, s = r - M z, over the
+//        current residual's RMS sigma = |r| / sqrt(nx ny);
+//   f1, f2 = c_e / m_c, c_n / m_c: the shares of the east and north face
+//        conductances in the diagonal -- the grid-spacing map (the
+//        permittivity is eps0 everywhere in this model);
+//   f3 = asinh(n_i - n_e): the net charge density.
+// Output y: the correction a second V-cycle adds for s, scaled by m_c / sigma;
+// the preconditioner is z = V(r) + sigma y / m_c, about two V-cycles for the
+// price of one plus the network.
 struct LpcArgs {
-    int lev, nxl, nyl, Hn, Wn;
-    const float *mc, *ce, *cn, *extra;   // level operator
-    int Pl;                              // level pitch
-    float *op, *rr;
-    __nv_bfloat16 *x0;
-    const float *y;
-    double *rhs64;                       // harvest: fine r - M z in FP64 (or null)
-    float *tgt;                          // harvest: target slot
-    const float *eh, *el;                // harvest: solution of M e = r - M z (float-float)
+    int Hn, Wn;
+    const float *mc;          // level-0 diagonal (FP32)
+    const double *ni, *ne;    // the current densities, for the charge feature
+    __nv_bfloat16 *x0;        // network input
+    const float *y;           // network output (channel 0)
+    __nv_bfloat16 *feat;      // harvest: feature slot [Hn][Wn][LPC_NFEAT], or null
+    float *tgt;               // harvest: target slot [Hn][Wn]
+    int s_to_r;               // harvest: write s over r32 (the next V-cycle's input)
 };
 
-__global__ void __launch_bounds__(256) k_lpc_opfeat(const LpcArgs l, const CgmArgs a) {
-    double v = 0.0;
-    const int n = l.nxl * l.nyl;
-    for (int q = blockIdx.x * 256 + threadIdx.x; q < n; q += gridDim.x * 256) {
-        const int J = q / l.nxl + 1, I = q - (J - 1) * l.nxl + 1;
-        const size_t o = (size_t)J * l.Pl + I;
+__device__ __forceinline__ float lpc_sigma(const CgmArgs &a) {
+    const double n = (double)a.nx * (double)a.ny, r2 = a.ctrl->rr_prev;
+    return r2 > 0.0 ? (float)sqrt(r2 / n) : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_lpc_feat(const LpcArgs l, const CgmArgs a) {
+    const float sg = lpc_sigma(a), is = sg > 0.0f ? 1.0f / sg : 0.0f;
+    CG_NODES(a, {
+        const int jj = (int)j_, ii = (int)(q_ - j_ * (unsigned)a.nx);
+        const float s = a.r32[o] - mz_ff(a.z[o], a.z[o + 1], a.z[o - 1], a.z[o + a.P], a.z[o - a.P], a.ce[o],
+                                         a.ce[o - 1], a.cn[o], a.cn[o - a.P], a.extra[o]);
         const float mc = l.mc[o], im = mc > 0.0f ? 1.0f / mc : 0.0f;
-        float *f = l.op + ((size_t)(J - 1) * l.Wn + (I - 1)) * 3;
-        f[0] = l.ce[o] * im;
-        f[1] = l.cn[o] * im;
-        f[2] = l.extra[o] * im;
-        v += (double)mc;
-    }
-    double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[5], a.nblk, &out) && threadIdx.x == 0)
-        a.ctrl->lpc_mcm = out / (double)n;
+        const __nv_bfloat162 f01 = __floats2bfloat162_rn(s * is, a.ce[o] * im);
+        const __nv_bfloat162 f23 = __floats2bfloat162_rn(a.cn[o] * im, asinhf((float)(l.ni[o] - l.ne[o])));
+        const size_t p = (size_t)jj * l.Wn + ii;
+        uint2 v;
+        v.x = *reinterpret_cast<const uint32_t *>(&f01);
+        v.y = *reinterpret_cast<const uint32_t *>(&f23);
+        *reinterpret_cast<uint2 *>(l.x0 + p * LPC_CIN0) = v;
+        if (l.feat) *reinterpret_cast<uint2 *>(l.feat + p * LPC_NFEAT) = v;
+        if (l.s_to_r) a.r32[o] = s;
+    })
 }
 
-// R (r32 - M z) per NN cell (aggregates of s x s fine nodes, s = 2, 4 or 8);
-// for a harvest also r - M z in FP64.  A CTA takes a 32 x 8 tile of fine
-// nodes (whole cells, since s divides both), one node per thread; the cell
-// sums are formed in shared memory in a fixed order.
-__global__ void __launch_bounds__(256) k_lpc_resid(const LpcArgs l, const CgmArgs a) {
-    __shared__ float v[8][32];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
-    float r1 = 0.0f;
-    if (i <= a.nx && j <= a.ny) {
-        const size_t o = (size_t)j * a.P + i;
-        r1 = a.r32[o] - mz_ff(a.z[o], a.z[o + 1], a.z[o - 1], a.z[o + a.P], a.z[o - a.P], a.ce[o], a.ce[o - 1],
-                              a.cn[o], a.cn[o - a.P], a.extra[o]);
-        if (l.rhs64) l.rhs64[o] = (double)r1;
-    }
-    v[ty][tx] = r1;
-    __syncthreads();
-    const int s = 1 << l.lev;
-    if ((tx % s) == 0 && (ty % s) == 0) {
-        const int I = (i - 1) / s, J = (j - 1) / s;   // 0-based cell
-        if (I < l.nxl && J < l.nyl) {
-            float acc = 0.0f;
-            for (int dy = 0; dy < s && ty + dy < 8; dy++)
-                for (int dx = 0; dx < s; dx++) acc += v[ty + dy][tx + dx];
-            l.rr[(size_t)J * l.Wn + I] = acc;
-        }
-    }
-}
-
-// network input [Hn][Wn][16] BF16 (channels 4..15 stay zero), the residual
-// channel scaled by its RMS s over the level's cells.  One CTA, fixed order.
-__global__ void __launch_bounds__(1024) k_lpc_x0(const LpcArgs l, Ctrl *ctrl) {
-    __shared__ double red[1024];
-    const int n = l.nxl * l.nyl;
-    double acc = 0.0;
-    for (int q = threadIdx.x; q < n; q += 1024) {
-        const int J = q / l.nxl, I = q - J * l.nxl;
-        const double r = l.rr[(size_t)J * l.Wn + I];
-        acc += r * r;
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int k = 512; k > 0; k >>= 1) {
-        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-        __syncthreads();
-    }
-    const double s = sqrt(red[0] / (double)n);
-    if (threadIdx.x == 0) ctrl->lpc_s = s;
-    const float is = s > 0.0 ? (float)(1.0 / s) : 0.0f;
-    for (int p = threadIdx.x; p < l.Hn * l.Wn; p += 1024) {
-        const int J = p / l.Wn, I = p - J * l.Wn;
-        const bool ok = J < l.nyl && I < l.nxl;
-        __nv_bfloat16 *x = l.x0 + (size_t)p * LPC_CIN0;
-        x[0] = __float2bfloat16_rn(ok ? l.rr[p] * is : 0.0f);
-        x[1] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 0] : 0.0f);
-        x[2] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 1] : 0.0f);
-        x[3] = __float2bfloat16_rn(ok ? l.op[(size_t)p * 3 + 2] : 0.0f);
-    }
-}
-
-// bilinear, cell-centred interpolation of the NN grid value to fine node (i, j)
-__device__ __forceinline__ float lpc_interp(const LpcArgs &l, const float *y, int stride, int i, int j) {
-    const float h = (float)(1 << l.lev);
-    float u = ((float)i - 0.5f) / h - 0.5f, w = ((float)j - 0.5f) / h - 0.5f;
-    u = fminf(fmaxf(u, 0.0f), (float)(l.nxl - 1));
-    w = fminf(fmaxf(w, 0.0f), (float)(l.nyl - 1));
-    const int i0 = min((int)u, l.nxl - 1), j0 = min((int)w, l.nyl - 1);
-    const int i1 = min(i0 + 1, l.nxl - 1), j1 = min(j0 + 1, l.nyl - 1);
-    const float fu = u - (float)i0, fw = w - (float)j0;
-    const float y00 = y[((size_t)j0 * l.Wn + i0) * stride], y01 = y[((size_t)j0 * l.Wn + i1) * stride];
-    const float y10 = y[((size_t)j1 * l.Wn + i0) * stride], y11 = y[((size_t)j1 * l.Wn + i1) * stride];
-    return (1.0f - fw) * ((1.0f - fu) * y00 + fu * y01) + fw * ((1.0f - fu) * y10 + fu * y11);
-}
-
-// z += interp(y) * s / mcm, unless the correction is switched off
-__global__ void __launch_bounds__(256) k_lpc_prolong(const LpcArgs l, const CgmArgs a) {
+// z += sigma y / m_c, unless the correction is switched off for this solve
+__global__ void __launch_bounds__(256) k_lpc_add(const LpcArgs l, const CgmArgs a) {
     Ctrl *c = a.ctrl;
     if (c->lpc_off || c->cg_done || c->cg_fail) return;
-    const float sc = c->lpc_mcm > 0.0 ? (float)(c->lpc_s / c->lpc_mcm) : 0.0f;
+    const float sg = lpc_sigma(a);
     CG_NODES(a, {
-        const int j = (int)j_ + 1, i = (int)(q_ - j_ * (unsigned)a.nx) + 1;
-        const float v = lpc_interp(l, l.y, LPC_COUT_LAST, i, j) * sc;
+        const size_t p = (size_t)j_ * l.Wn + (q_ - j_ * (unsigned)a.nx);
+        const float mc = l.mc[o];
+        const float v = mc > 0.0f ? sg * l.y[p] / mc : 0.0f;
         if (isfinite(v)) a.z[o] += v;
         else c->lpc_off = 1;
     })
 }
 
-// harvest target: aggregate mean of e, times mcm / s
-__global__ void k_lpc_target(const LpcArgs l, const CgmArgs a) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= l.Hn * l.Wn) return;
-    const int J = p / l.Wn + 1, I = p - (J - 1) * l.Wn + 1, s = 1 << l.lev;
-    float v = 0.0f;
-    if (J <= l.nyl && I <= l.nxl) {
-        double acc = 0.0;
-        int cnt = 0;
-        for (int j = (J - 1) * s + 1; j <= min(J * s, a.ny); j++)
-            for (int i = (I - 1) * s + 1; i <= min(I * s, a.nx); i++) {
-                const size_t o = (size_t)j * a.P + i;
-                acc += (double)l.eh[o] + (double)l.el[o];
-                cnt++;
-            }
-        const double sc = a.ctrl->lpc_s > 0.0 ? a.ctrl->lpc_mcm / a.ctrl->lpc_s : 0.0;
-        v = (float)(acc / cnt * sc);
-    }
-    l.tgt[p] = v;
+// harvest: rr_prev = |r32|^2 (the feature scale of the residual in r32)
+__global__ void __launch_bounds__(256) k_lpc_norm(const CgmArgs a) {
+    double v = 0.0;
+    CG_NODES(a, { v += (double)a.r32[o] * (double)a.r32[o]; })
+    double out;
+    if (grid_sum<256>(v, a.part, &a.ctrl->counter[5], a.nblk, &out) && threadIdx.x == 0) a.ctrl->rr_prev = out;
 }
 
+// harvest target: the second V-cycle's correction z = V(s), times m_c / sigma
+__global__ void __launch_bounds__(256) k_lpc_target(const LpcArgs l, const CgmArgs a) {
+    const float sg = lpc_sigma(a), is = sg > 0.0f ? 1.0f / sg : 0.0f;
+    CG_NODES(a, {
+        const size_t p = (size_t)j_ * l.Wn + (q_ - j_ * (unsigned)a.nx);
+        l.tgt[p] = a.z[o] * l.mc[o] * is;
+    })
+}
 
 }  // namespace
 
@@ -979,30 +927,31 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
 
 static LpcArgs lpc_args(fs_ctx *c) {
     LpcArgs l = {};
-    const MGLevelF &m = c->mgf[c->lpc_level];
-    l.lev = c->lpc_level; l.nxl = m.nx; l.nyl = m.ny; l.Hn = c->lpc->Hn; l.Wn = c->lpc->Wn;
-    l.mc = m.mc; l.ce = m.ce; l.cn = m.cn; l.extra = m.extra; l.Pl = m.pitch;
-    l.op = c->lpc_op; l.rr = c->lpc_rr; l.x0 = c->lpc->x0; l.y = c->lpc->y;
+    l.Hn = c->lpc->Hn; l.Wn = c->lpc->Wn;
+    l.mc = c->mgf[0].mc;
+    l.ni = c->sp[0].buf[c->lev[0]];
+    l.ne = c->sp[1].buf[c->lev[0]];
+    l.x0 = c->lpc->x0; l.y = c->lpc->y;
     return l;
 }
 
-// z += learned correction of the V-cycle's remaining error
+// z += the network's correction for the residual the V-cycle leaves
 static void lpc_apply(fs_ctx *c, const CgmArgs &ca) {
     LpcArgs l = lpc_args(c);
     fs_prof_begin(c, PROF_OTHER);
-    k_lpc_resid<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(l, ca);
-    k_lpc_x0<<<1, 1024, 0, c->stream>>>(l, c->d_ctrl);
-    lpc_forward(c->lpc, 1, c->stream);
-    k_lpc_prolong<<<ca.grid, 256, 0, c->stream>>>(l, ca);
-    // one black-red Gauss-Seidel pass removes the cell-scale error the
-    // interpolated correction brings in (as post-smoothing does after a
-    // coarse-grid correction)
+    k_lpc_feat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
+    lpc_forward(c->lpc, 1, c->lpc->Hn, c->lpc->Wn, c->stream);
+    k_lpc_add<<<ca.grid, 256, 0, c->stream>>>(l, ca);
+    // one black-red Gauss-Seidel pass on the fine level removes the
+    // cell-scale error the network's correction brings in (M amplifies it
+    // most), as post-smoothing does after a coarse-grid correction
     LevelT<float> f0 = level_f(c->mgf[0]);
     dim3 b(32, 8), gh = grid2((f0.nx + 1) / 2, f0.ny, b);
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 1, 0);
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 0, 0);
     fs_prof_end(c);
-    c->launches += 3 + 13 + 2 - 1;   // feature, input, prolongation, network, sweep (one counted above)
+    // features, correction, 12 convolutions, 3 pools, 3 upsamplings, 2 half sweeps
+    c->launches += 2 + LPC_NLAYER + 6 + 2 - 1;
 }
 
 static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
@@ -1073,6 +1022,8 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
 // (up to 400) after each probe that did not.
 static void lpc_account(fs_ctx *c, const CgmArgs &ca, double ms) {
     if (!c->lpc_on) return;
+    c->lpc_solves++;
+    if (ca.lpc) c->lpc_nn_solves++;
     const double a = 0.3;
     if (ca.lpc) {
         const double t = c->h_ctrl->lpc_off ? 2.0 * ms : ms;
@@ -1170,11 +1121,6 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         fs_prof_end(c);
     }
     CgmArgs ca = cgm_args(c);
-    if (ca.lpc) {   // the network's operator features, only for a solve that runs it
-        LpcArgs l = lpc_args(c);
-        c->launches++;
-        k_lpc_opfeat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
-    }
     fs_prof_begin(c, PROF_CG);
     k_cgm_init<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
@@ -1237,36 +1183,29 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
 }
 
 // ---------------------------------------------------- learned preconditioner
-static int round4(int v) { return (v + 3) / 4 * 4; }
+static int round8(int v) { return (v + 7) / 8 * 8; }
 
-int fs_lpc_init_impl(fs_ctx *c, int level, int max_batch, int max_samples, uint64_t seed) {
+// crop: edge of the training crops in cells (a multiple of 8; 0: 128), at most the grid's
+int fs_lpc_init_impl(fs_ctx *c, int crop, int max_batch, int max_samples, uint64_t seed) {
     if (!c->mixed) return fs_set_error(c, FS_ERR_UNSUPPORTED, "the learned preconditioner needs the mixed solver");
-    if (level < 1 || level > 3 || level >= c->mg_nlev)
-        return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner level %d outside 1..%d", level,
-                            c->mg_nlev - 1 < 3 ? c->mg_nlev - 1 : 3);
     if (max_batch < 1 || max_samples < 1) return fs_set_error(c, FS_ERR_INVALID, "batch and sample counts must be positive");
+    if (crop < 0 || crop % 8) return fs_set_error(c, FS_ERR_INVALID, "crop %d is not a multiple of 8", crop);
     fs_lpc_free_impl(c);
-    const MGLevelF &m = c->mgf[level];
-    const int Hn = round4(m.ny), Wn = round4(m.nx);
+    const int Hn = round8(c->ny), Wn = round8(c->nx);
+    const int cr = crop ? crop : 128, Hc = std::min(cr, Hn), Wc = std::min(cr, Wn);
     LpcState *L = nullptr;
-    int e = lpc_alloc(&L, Hn, Wn, max_batch, max_samples, seed, c->stream);
+    int e = lpc_alloc(&L, Hn, Wn, Hc, Wc, max_batch, max_samples, seed, c->stream);
+    if (e == (int)cudaErrorNotSupported)
+        return fs_set_error(c, FS_ERR_UNSUPPORTED, "tensor-core convolutions unavailable (no TMA descriptor encoder)");
     if (e) return fs_cuda_check(c, (cudaError_t)e, "learned preconditioner buffers");
-    L->level = level;
     c->lpc = L;
-    c->lpc_level = level;
     c->lpc_snap_max = 8;
-    cudaError_t ce = cudaMalloc(&c->lpc_op, (size_t)Hn * Wn * 3 * sizeof(float));
-    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_op, 0, (size_t)Hn * Wn * 3 * sizeof(float));
-    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_rr, (size_t)Hn * Wn * sizeof(float));
-    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_rr, 0, (size_t)Hn * Wn * sizeof(float));
-    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_rhs64, c->field_elems * sizeof(double));
-    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_rhs64, 0, c->field_elems * sizeof(double));
-    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_snap, (size_t)c->lpc_snap_max * c->field_elems * sizeof(float));
+    cudaError_t ce = cudaMalloc(&c->lpc_snap, (size_t)c->lpc_snap_max * c->field_elems * sizeof(float));
     if (ce != cudaSuccess) { fs_lpc_free_impl(c); return fs_cuda_check(c, ce, "learned preconditioner buffers"); }
-    // valid cells of the padded NN grid
+    // interior cells of the padded NN grid
     std::vector<float> mk((size_t)Hn * Wn, 0.0f);
-    for (int j = 0; j < m.ny; j++)
-        for (int i = 0; i < m.nx; i++) mk[(size_t)j * Wn + i] = 1.0f;
+    for (int j = 0; j < c->ny; j++)
+        for (int i = 0; i < c->nx; i++) mk[(size_t)j * Wn + i] = 1.0f;
     ce = cudaMemcpyAsync(L->mask, mk.data(), mk.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
     return fs_cuda_check(c, ce, "learned preconditioner init");
@@ -1277,8 +1216,8 @@ void fs_lpc_free_impl(fs_ctx *c) {
     lpc_free(c->lpc);
     c->lpc = nullptr;
     c->lpc_on = 0;
-    cudaFree(c->lpc_op); cudaFree(c->lpc_rr); cudaFree(c->lpc_rhs64); cudaFree(c->lpc_snap);
-    c->lpc_op = c->lpc_rr = nullptr; c->lpc_rhs64 = nullptr; c->lpc_snap = nullptr;
+    cudaFree(c->lpc_snap);
+    c->lpc_snap = nullptr;
 }
 
 // Host-driven solve of the current (assembled) system with the plain mixed
@@ -1310,13 +1249,16 @@ static int solve_plain(fs_ctx *c, CgmArgs ca, std::vector<int> *snap_iters) {
     return c->h_ctrl->cg_iters;
 }
 
+// Training pairs from the plain solver: the step's assembled system is
+// re-solved with the plain multigrid-PCG, and for up to per_solve of its
+// residuals r: z = V(r), s = r - M z (the residual the first V-cycle leaves,
+// its features stored), then the target: the second V-cycle's correction
+// V(s), scaled as the network's output.
 int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added) {
     if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
     LpcState *L = c->lpc;
     *added = 0;
     CgmArgs ca = cgm_args(c);
-    LpcArgs l = lpc_args(c);
-    k_lpc_opfeat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
     std::vector<int> its;
     int rc = solve_plain(c, ca, &its);
     if (rc < 0) return rc;
@@ -1324,35 +1266,25 @@ int fs_lpc_harvest_impl(fs_ctx *c, int per_solve, int *added) {
     const int n = std::min((int)its.size(), std::min(per_solve, c->lpc_snap_max));
     for (int k = 0; k < n; k++) {
         const int slot = L->nsamp % L->Nmax;
-        // r: a residual of the plain solve; z = V(r); features of R (r - M z)
         cudaMemcpyAsync(ca.r32, c->lpc_snap + (size_t)k * c->field_elems, c->field_elems * sizeof(float),
                         cudaMemcpyDeviceToDevice, c->stream);
+        k_lpc_norm<<<ca.grid, 256, 0, c->stream>>>(ca);
         vcycle_mixed(c, ca);
-        LpcArgs lh = l;
-        lh.rhs64 = c->lpc_rhs64;
-        k_lpc_resid<<<grid2(c->nx, c->ny, dim3(32, 8)), 256, 0, c->stream>>>(lh, ca);
-        k_lpc_x0<<<1, 1024, 0, c->stream>>>(lh, c->d_ctrl);
-        cudaMemcpyAsync(L->dfeat + slot * px * LPC_CIN0, L->x0, px * LPC_CIN0 * sizeof(__nv_bfloat16),
-                        cudaMemcpyDeviceToDevice, c->stream);
-        if ((rc = fs_sync_ctrl(c))) return rc;
-        const double s = c->h_ctrl->lpc_s, mcm = c->h_ctrl->lpc_mcm;
-        // the correction multigrid-PCG gives for that remaining residual
-        CgmArgs ch = ca;
-        ch.rhs = c->lpc_rhs64;
-        rc = solve_plain(c, ch, nullptr);
-        if (rc < 0) return rc;
-        (void)s;
-        (void)mcm;
-        lh.tgt = L->dtgt + slot * px;
-        lh.eh = c->xh32;
-        lh.el = c->xl32;
-        k_lpc_target<<<(int)((px + 255) / 256), 256, 0, c->stream>>>(lh, ca);
+        LpcArgs l = lpc_args(c);
+        l.feat = L->dfeat + slot * px * LPC_NFEAT;
+        l.s_to_r = 1;
+        k_lpc_feat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
+        vcycle_mixed(c, ca);   // z = V(s)
+        l.tgt = L->dtgt + slot * px;
+        k_lpc_target<<<ca.grid, 256, 0, c->stream>>>(l, ca);
         L->nsamp++;
         (*added)++;
     }
     return fs_cuda_check(c, cudaStreamSynchronize(c->stream), "harvest");
 }
 
+// iters Adam steps on batches of random Hc x Wc crops (origins on the
+// 8-cell pooling grid) of the stored pairs
 int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, float *loss_hist) {
     if (!c->lpc) return fs_set_error(c, FS_ERR_INVALID, "learned preconditioner not initialised");
     LpcState *L = c->lpc;
@@ -1360,20 +1292,26 @@ int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, 
     if (n < 1) return fs_set_error(c, FS_ERR_INVALID, "no harvested samples");
     if (batch < 1 || batch > L->Bmax) return fs_set_error(c, FS_ERR_INVALID, "batch %d outside 1..%d", batch, L->Bmax);
     uint64_t st = seed * 0x9E3779B97F4A7C15ull + 7;
-    std::vector<int> idx(batch);
+    auto draw = [&](uint64_t m) {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return (int)((z ^ (z >> 31)) % m);
+    };
+    const int ny8 = (L->Hn - L->Hc) / 8 + 1, nx8 = (L->Wn - L->Wc) / 8 + 1;
+    std::vector<int> idx(batch), y0(batch), x0(batch);
     float *h_loss = nullptr;
-    cudaMallocHost(&h_loss, sizeof(float) * (size_t)iters);
+    cudaMallocHost(&h_loss, sizeof(float) * (size_t)std::max(iters, 1));
     for (int it = 0; it < iters; it++) {
         for (int b = 0; b < batch; b++) {
-            st += 0x9E3779B97F4A7C15ull;
-            uint64_t z = st;
-            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-            idx[b] = (int)((z ^ (z >> 31)) % (uint64_t)n);
+            idx[b] = draw((uint64_t)n);
+            y0[b] = 8 * draw((uint64_t)ny8);
+            x0[b] = 8 * draw((uint64_t)nx8);
         }
-        lpc_gather(L, idx.data(), batch, c->stream);
-        lpc_forward(L, batch, c->stream);
-        int e = lpc_loss_backward(L, batch, c->stream);
+        lpc_gather(L, idx.data(), y0.data(), x0.data(), batch, c->stream);
+        int e = lpc_forward(L, batch, L->Hc, L->Wc, c->stream);
+        if (!e) e = lpc_loss_backward(L, batch, L->Hc, L->Wc, c->stream);
         if (e) { cudaFreeHost(h_loss); return fs_cuda_check(c, (cudaError_t)e, "training step"); }
         cudaMemcpyAsync(h_loss + it, L->d_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
         lpc_adam(L, lr, c->stream);
@@ -1381,6 +1319,8 @@ int fs_lpc_train_impl(fs_ctx *c, int iters, int batch, float lr, uint64_t seed, 
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess && loss_hist) memcpy(loss_hist, h_loss, sizeof(float) * (size_t)iters);
     cudaFreeHost(h_loss);
+    if (e == cudaSuccess && lpc_tc_error(L, c->stream))
+        return fs_set_error(c, FS_ERR_CUDA, "tensor-core convolution failed (a bounded wait ran out)");
     return fs_cuda_check(c, e, "training");
 }
 
@@ -1400,18 +1340,16 @@ int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float
     if (e == cudaSuccess) e = cudaMemcpyAsync(L->btgt, tgt, P * sizeof(float), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(L->bmask, bm.data(), P * sizeof(float), cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "gradient inputs");
-    lpc_forward(L, batch, c->stream);
-    int r = lpc_loss_backward(L, batch, c->stream);
+    if ((long)batch * L->Hn * L->Wn > L->cap0)
+        return fs_set_error(c, FS_ERR_INVALID, "batch %d of full grids exceeds the activation buffers", batch);
+    int r = lpc_forward(L, batch, L->Hn, L->Wn, c->stream);
+    if (!r) r = lpc_loss_backward(L, batch, L->Hn, L->Wn, c->stream);
     if (r) return fs_cuda_check(c, (cudaError_t)r, "gradient");
     if (grad) e = cudaMemcpyAsync(grad, L->g, L->net.nparam * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, L->d_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
-    std::vector<float> y;
-    if (e == cudaSuccess && pred) {
-        y.resize(P * LPC_COUT_LAST);
-        e = cudaMemcpyAsync(y.data(), L->y, y.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
-    }
+    if (e == cudaSuccess && pred) e = cudaMemcpyAsync(pred, L->y, P * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e == cudaSuccess && pred)
-        for (size_t p = 0; p < P; p++) pred[p] = y[p * LPC_COUT_LAST];
+    if (e == cudaSuccess && lpc_tc_error(L, c->stream))
+        return fs_set_error(c, FS_ERR_CUDA, "tensor-core convolution failed (a bounded wait ran out)");
     return fs_cuda_check(c, e, "gradient outputs");
 }

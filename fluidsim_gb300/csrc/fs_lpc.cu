@@ -1,33 +1,33 @@
-// fs_lpc.cu -- kernels of the learned Poisson preconditioner (see fs_lpc.cuh).
+// fs_lpc.cu -- the learned Poisson preconditioner's network (see fs_lpc.cuh).
 //
-// Network (a two-level U-Net, ~250k parameters, 3x3 convolutions, ReLU):
-//   e1a 16->32, e1b 32->32                    (full NN grid; e1b output = skip s1)
-//   pool, e2a 32->64, e2b 64->64              (1/2; e2b output = skip s2)
-//   pool, b1 64->64, b2 64->64                (1/4)
-//   up, d2 [up(b2), s2] 128->64               (1/2)
-//   up, d1 [up(d2), s1] 96->32                (full)
-//   out 32->8 (channel 0 is the prediction, no ReLU)
-// Activations are NHWC BF16 tensors [B][H][W][C]; every convolution is an
-// implicit GEMM on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
-// accumulation) with zero padding at the grid edge.  Backward: data gradients
-// by the transposed implicit GEMM, weight gradients by a split-K GEMM over
-// pixels with a fixed-order reduction; Adam on FP32 master weights, from
-// which the two BF16 copies (forward [tap][cout][cin], backward
-// [tap][cin][cout]) are refreshed.
+// A four-level U-Net, 3x3 convolutions, ReLU, 2x2 average pooling, nearest
+// upsampling, 258,528 parameters:
+//   enc0 16->16->16 (skip s0)  | pool | enc1 16->32->32 (skip s1) | pool |
+//   enc2 32->64->64 (skip s2)  | pool | bottleneck 64->64->64 | up |
+//   dec2 [up, s2] 128->64 | up | dec1 [up, s1] 96->32 | up |
+//   dec0 [up, s0] 48->16 | out 16->16 (channel 0 is the prediction, no ReLU)
+// Activations are NHWC BF16 tensors [B][H][W][C].  Every convolution runs on
+// the tcgen05 tensor cores (fs_conv_tc.cu: TMA-staged BF16 operands, FP32
+// accumulators in tensor memory): the forward pass, and the data gradient as
+// the convolution of the output gradient with the flipped, transposed
+// weights (ReLU masks applied in its epilogue).  Weight gradients: a split-K
+// GEMM over pixels on mma.sync with a fixed-order reduction.  Adam on FP32
+// master weights, from which the BF16 weight images are rebuilt.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
+#include "fluidsim_gpu.h"
 #include "fs_lpc.cuh"
 
 typedef __nv_bfloat16 bf16;
 
 namespace {
 
-__device__ __forceinline__ uint32_t ld_b32(const bf16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
 __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
@@ -71,141 +71,6 @@ struct ConvArgs {
     int relu;
     int B, H, W;
 };
-
-// Forward 3x3 convolution.  A warp computes 16 output pixels x 8*NT output
-// channels; the warps of a CTA split the output channels of one 16-pixel tile
-// (wpt = cout / (8 NT) warps per tile, 4 / wpt tiles per CTA), which keeps
-// enough warps in flight on the small grids of the coarse levels.
-template <int NT>
-__global__ void __launch_bounds__(128) k_conv_fwd(const ConvArgs a) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    const int wpt = a.cout / (8 * NT), tpc = 4 / wpt;
-    const int co_base = (warp % wpt) * 8 * NT;
-    const long P = (long)a.B * a.H * a.W;
-    const long p0 = ((long)blockIdx.x * tpc + warp / wpt) * 16 + g, p1 = p0 + 8;
-    const Pix q0 = pix_of(p0, a.H, a.W, P), q1 = pix_of(p1, a.H, a.W, P);
-    const int cin = a.c1 + a.c2;
-    float acc[NT][4];
-#pragma unroll
-    for (int j = 0; j < NT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    for (int t = 0; t < 9; t++) {
-        const long n0 = nbr(q0, t, a.H, a.W), n1 = nbr(q1, t, a.H, a.W);
-        for (int ci0 = 0; ci0 < cin; ci0 += 16) {
-            const bf16 *src;
-            int cs, cc;
-            if (ci0 < a.c1) { src = a.in1; cs = a.c1; cc = ci0; }
-            else { src = a.in2; cs = a.c2; cc = ci0 - a.c1; }
-            uint32_t af[4];
-            const int ca = cc + tq * 2;
-            af[0] = n0 >= 0 ? ld_b32(src + n0 * cs + ca) : 0u;
-            af[1] = n1 >= 0 ? ld_b32(src + n1 * cs + ca) : 0u;
-            af[2] = n0 >= 0 ? ld_b32(src + n0 * cs + ca + 8) : 0u;
-            af[3] = n1 >= 0 ? ld_b32(src + n1 * cs + ca + 8) : 0u;
-#pragma unroll
-            for (int j = 0; j < NT; j++) {
-                const bf16 *wr = a.w + ((size_t)t * a.cout + co_base + j * 8 + g) * cin + ci0 + tq * 2;
-                uint32_t bfr[2] = {ld_b32(wr), ld_b32(wr + 8)};
-                mma_bf16(acc[j], af, bfr);
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < NT; j++) {
-        const int co = co_base + j * 8 + tq * 2;
-        float v[4] = {acc[j][0] + a.bias[co], acc[j][1] + a.bias[co + 1], acc[j][2] + a.bias[co],
-                      acc[j][3] + a.bias[co + 1]};
-        if (a.relu)
-            for (int k = 0; k < 4; k++) v[k] = fmaxf(v[k], 0.0f);
-        if (a.out32) {
-            if (q0.ok) { a.out32[p0 * a.cout + co] = v[0]; a.out32[p0 * a.cout + co + 1] = v[1]; }
-            if (q1.ok) { a.out32[p1 * a.cout + co] = v[2]; a.out32[p1 * a.cout + co + 1] = v[3]; }
-        } else {
-            if (q0.ok) *reinterpret_cast<uint32_t *>(a.out + p0 * a.cout + co) =
-                pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
-            if (q1.ok) *reinterpret_cast<uint32_t *>(a.out + p1 * a.cout + co) =
-                pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
-        }
-    }
-}
-
-// Backward data: dIn[q][ci] = sum_t sum_co dOut[q - off_t][co] W[t][co][ci],
-// with the ReLU mask of the input tensor applied in the epilogue.
-// A CTA computes 16 pixels; its 4 warps take 8*NT input channels each
-// (NT = cin / 32).  cout a multiple of 16.
-template <int NT>
-__global__ void __launch_bounds__(128) k_conv_bwd_data(const ConvArgs a, const bf16 *dout) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    const int ci_base = warp * 8 * NT;
-    const long P = (long)a.B * a.H * a.W;
-    const long p0 = (long)blockIdx.x * 16 + g, p1 = p0 + 8;
-    const Pix q0 = pix_of(p0, a.H, a.W, P), q1 = pix_of(p1, a.H, a.W, P);
-    const int cin = a.c1 + a.c2, cout = a.cout;
-    float acc[NT][4];
-#pragma unroll
-    for (int j = 0; j < NT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    for (int t = 0; t < 9; t++) {
-        const long n0 = nbr(q0, 8 - t, a.H, a.W), n1 = nbr(q1, 8 - t, a.H, a.W);
-        for (int co0 = 0; co0 < cout; co0 += 16) {
-            uint32_t af[4];
-            const int ca = co0 + tq * 2;
-            af[0] = n0 >= 0 ? ld_b32(dout + n0 * cout + ca) : 0u;
-            af[1] = n1 >= 0 ? ld_b32(dout + n1 * cout + ca) : 0u;
-            af[2] = n0 >= 0 ? ld_b32(dout + n0 * cout + ca + 8) : 0u;
-            af[3] = n1 >= 0 ? ld_b32(dout + n1 * cout + ca + 8) : 0u;
-#pragma unroll
-            for (int j = 0; j < NT; j++) {
-                const bf16 *wr = a.w + ((size_t)t * cin + ci_base + j * 8 + g) * cout + ca;
-                uint32_t bfr[2] = {ld_b32(wr), ld_b32(wr + 8)};
-                mma_bf16(acc[j], af, bfr);
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < NT; j++) {
-        const int ci = ci_base + j * 8 + tq * 2;
-        bf16 *dst;
-        const bf16 *msk;
-        int cs, cc;
-        if (ci < a.c1) { dst = a.out; msk = a.mask1; cs = a.c1; cc = ci; }
-        else { dst = a.dout2; msk = a.mask2; cs = a.c2; cc = ci - a.c1; }
-        float v[4] = {acc[j][0], acc[j][1], acc[j][2], acc[j][3]};
-        if (msk) {
-            if (q0.ok) {
-                if (!(__bfloat162float(msk[p0 * cs + cc]) > 0.0f)) v[0] = 0.0f;
-                if (!(__bfloat162float(msk[p0 * cs + cc + 1]) > 0.0f)) v[1] = 0.0f;
-            }
-            if (q1.ok) {
-                if (!(__bfloat162float(msk[p1 * cs + cc]) > 0.0f)) v[2] = 0.0f;
-                if (!(__bfloat162float(msk[p1 * cs + cc + 1]) > 0.0f)) v[3] = 0.0f;
-            }
-        }
-        if (q0.ok) *reinterpret_cast<uint32_t *>(dst + p0 * cs + cc) =
-            pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
-        if (q1.ok) *reinterpret_cast<uint32_t *>(dst + p1 * cs + cc) =
-            pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
-    }
-}
-
-// Backward data of the last layer (one live output channel): CUDA cores.
-// dIn[q][ci] = sum_t dy[q - off_t] W[t][0][ci], masked by the input's ReLU.
-__global__ void k_out_bwd_data(const bf16 *dy, int cy, const float *w32, int cin, const bf16 *mask, bf16 *din,
-                               int B, int H, int W) {
-    const long P = (long)B * H * W;
-    const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= P) return;
-    const Pix qq = pix_of(q, H, W, P);
-    float d[9];
-    for (int t = 0; t < 9; t++) {
-        const long n = nbr(qq, 8 - t, H, W);
-        d[t] = n >= 0 ? __bfloat162float(dy[n * cy]) : 0.0f;
-    }
-    for (int ci = 0; ci < cin; ci++) {
-        float s = 0.0f;
-        for (int t = 0; t < 9; t++) s += d[t] * __bfloat162float(__float2bfloat16_rn(w32[(size_t)t * LPC_COUT_LAST * cin + ci]));
-        if (!(__bfloat162float(mask[q * cin + ci]) > 0.0f)) s = 0.0f;
-        din[q * cin + ci] = __float2bfloat16_rn(s);
-    }
-}
 
 // Weight gradient, split over pixel chunks: part[chunk][t][ci][co] =
 // sum_{p in chunk} In[p + off_t][ci] dOut[p][co].  One CTA per (tap, chunk);
@@ -345,7 +210,7 @@ __global__ void k_loss(const float *y, const float *tgt, const float *msk, long 
     __shared__ float s_l[1024], s_m[1024];
     float l = 0.0f, m = 0.0f;
     for (long p = threadIdx.x; p < P; p += 1024) {
-        const float d = y[p * LPC_COUT_LAST] - tgt[p];
+        const float d = y[p] - tgt[p];
         l += msk[p] * d * d;
         m += msk[p];
     }
@@ -359,9 +224,30 @@ __global__ void k_loss(const float *y, const float *tgt, const float *msk, long 
     const float inv = s_m[0] > 0.0f ? 1.0f / s_m[0] : 0.0f;
     if (threadIdx.x == 0) *loss = s_l[0] * inv;
     for (long p = threadIdx.x; p < P; p += 1024) {
-        const float d = y[p * LPC_COUT_LAST] - tgt[p];
-        dy[p * LPC_COUT_LAST] = __float2bfloat16_rn(2.0f * msk[p] * d * inv);
-        for (int c = 1; c < LPC_COUT_LAST; c++) dy[p * LPC_COUT_LAST + c] = __float2bfloat16_rn(0.0f);
+        const float d = y[p] - tgt[p];
+        uint4 *o = reinterpret_cast<uint4 *>(dy + p * LPC_COUT_LAST);
+        const uint32_t v0 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(2.0f * msk[p] * d * inv));
+        o[0] = make_uint4(v0, 0u, 0u, 0u);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// B crops of Hc x Wc cells from the training pairs: crop b of pair idx[b] at
+// (y0[b], x0[b]) -> x0 [b][y][x][16] (the LPC_NFEAT features, zeros after),
+// batch target and mask (interior cells of the padded grid)
+__global__ void k_gather(const bf16 *feat, const float *tgt, const float *mask, int Hn, int Wn, const int *crops,
+                         int B, int Hc, int Wc, bf16 *x0, float *btgt, float *bmask) {
+    const long n = (long)B * Hc * Wc;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(q / ((long)Hc * Wc)), r = (int)(q - (long)b * Hc * Wc), y = r / Wc, x = r - y * Wc;
+        const int i = crops[3 * b], yy = crops[3 * b + 1] + y, xx = crops[3 * b + 2] + x;
+        const size_t src = ((size_t)i * Hn + yy) * Wn + xx, cell = (size_t)yy * Wn + xx;
+        const uint2 f = *reinterpret_cast<const uint2 *>(feat + src * LPC_NFEAT);
+        uint4 *o = reinterpret_cast<uint4 *>(x0 + q * LPC_CIN0);
+        o[0] = make_uint4(f.x, f.y, 0u, 0u);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
+        btgt[q] = tgt[src];
+        bmask[q] = mask[cell];
     }
 }
 
@@ -378,39 +264,29 @@ __global__ void k_adam(float *w, const float *gr, float *m, float *v, size_t n, 
     }
 }
 
-// BF16 copies of the weights: wf[l][t][co][ci] and wb[l][t][ci][co]
-__global__ void k_refresh(const LpcNet net, const float *w, bf16 *wf, bf16 *wb) {
-    for (int l = 0; l < LPC_NLAYER; l++) {
-        const LpcLayer &L = net.L[l];
-        const int cin = L.c1 + L.c2, n = 9 * cin * L.cout;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-            const int t = i / (L.cout * cin), rem = i - t * L.cout * cin, co = rem / cin, ci = rem - co * cin;
-            const bf16 v = __float2bfloat16_rn(w[L.w_off + i]);
-            wf[L.wf_off + i] = v;
-            wb[L.wb_off + ((size_t)t * cin + ci) * L.cout + co] = v;
-        }
-    }
-}
-
 }  // namespace
 
 // ------------------------------------------------------------------ host side
 void lpc_describe(LpcNet &net) {
     // c1, c2, cout, resolution level
-    const int spec[LPC_NLAYER][4] = {{LPC_CIN0, 0, 32, 0}, {32, 0, 32, 0}, {32, 0, 64, 1}, {64, 0, 64, 1},
-                                     {64, 0, 64, 2},       {64, 0, 64, 2}, {64, 64, 64, 1}, {64, 32, 32, 0},
-                                     {32, 0, LPC_COUT_LAST, 0}};
-    size_t wp = 0, w16 = 0;
+    const int spec[LPC_NLAYER][4] = {{LPC_CIN0, 0, 16, 0}, {16, 0, 16, 0},  {16, 0, 32, 1},  {32, 0, 32, 1},
+                                     {32, 0, 64, 2},       {64, 0, 64, 2},  {64, 0, 64, 3},  {64, 0, 64, 3},
+                                     {64, 64, 64, 2},      {64, 32, 32, 1}, {32, 16, 16, 0}, {16, 0, LPC_COUT_LAST, 0}};
+    size_t wp = 0, img = 0;
     for (int l = 0; l < LPC_NLAYER; l++) {
         LpcLayer &L = net.L[l];
         L.c1 = spec[l][0]; L.c2 = spec[l][1]; L.cout = spec[l][2]; L.res = spec[l][3];
         const size_t nw = (size_t)9 * (L.c1 + L.c2) * L.cout;
         L.w_off = wp; wp += nw;
         L.b_off = wp; wp += L.cout;
-        L.wf_off = w16; L.wb_off = w16; w16 += nw;
+        TcConvArgs t = {};
+        L.bytes_f = tc_weight_layout(L.c1, L.c2, L.cout, t.boff, t.kc, t.nchunk);
+        L.bytes_b = l > 0 ? tc_weight_layout(L.cout, 0, L.c1 + L.c2, t.boff, t.kc, t.nchunk) : 0;
+        L.img_f = img; img += (size_t)L.bytes_f;
+        L.img_b = img; img += (size_t)L.bytes_b;
     }
     net.nparam = wp;
-    net.nw16 = w16;
+    net.img_bytes = img;
 }
 
 namespace {
@@ -432,36 +308,40 @@ double unif(uint64_t &s) { return ((sm64(s) >> 11) + 0.5) * (1.0 / 9007199254740
 
 inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 
-void conv_fwd(const LpcState *L, int l, const bf16 *in1, const bf16 *in2, bf16 *out, float *out32, int B, int H,
-              int W, cudaStream_t st) {
+// One tensor-core convolution over B images of H x W cells.  Forward (bwd = 0):
+// inputs in1 (c1 channels), in2 (c2), output out (BF16, bias, ReLU) or y
+// (FP32 channel 0, bias).  Data gradient (bwd = 1): input in1 = the output
+// gradient (cout channels), outputs out (c1 channels, ReLU mask m1) and out2
+// (c2 channels, mask m2).
+int tc_layer(LpcState *L, int l, int bwd, int B, int H, int W, const bf16 *in1, const bf16 *in2, bf16 *out,
+             bf16 *out2, const bf16 *m1, const bf16 *m2, float *y, cudaStream_t st) {
     const LpcLayer &Y = L->net.L[l];
-    ConvArgs a = {};
-    a.in1 = in1; a.in2 = in2; a.c1 = Y.c1; a.c2 = Y.c2; a.cout = Y.cout;
-    a.w = L->wf + Y.wf_off; a.bias = L->w + Y.b_off;
-    a.out = out; a.out32 = out32; a.relu = out32 ? 0 : 1;
+    TcConvArgs a = {};
+    int ci1, ci2, co;
+    if (!bwd) { ci1 = Y.c1; ci2 = Y.c2; co = Y.cout; }
+    else { ci1 = Y.cout; ci2 = 0; co = Y.c1 + Y.c2; }
+    a.wbytes = tc_weight_layout(ci1, ci2, co, a.boff, a.kc, a.nchunk);
+    CUtensorMap m[2];
+    if (tc_make_map(&m[0], in1, B, H, W, ci1, a.kc[0]) || (ci2 && tc_make_map(&m[1], in2, B, H, W, ci2, a.kc[1])))
+        return -1;
+    a.cout = co;
+    a.tmem_cols = tc_tmem_cols(co);
     a.B = B; a.H = H; a.W = W;
-    const long P = (long)B * H * W;
-    // warps per 16-pixel tile: cout / 16 for cout >= 16 (two 8-channel tiles a warp), 1 for the last layer
-    if (Y.cout == LPC_COUT_LAST) k_conv_fwd<1><<<nblk(P, 64), 128, 0, st>>>(a);
-    else if (Y.cout == 32) k_conv_fwd<2><<<nblk(P, 32), 128, 0, st>>>(a);
-    else k_conv_fwd<2><<<nblk(P, 16), 128, 0, st>>>(a);   // cout 64
-}
-
-void conv_bwd_data(const LpcState *L, int l, const bf16 *dout, bf16 *din1, bf16 *din2, const bf16 *m1, const bf16 *m2,
-                   int B, int H, int W, cudaStream_t st) {
-    const LpcLayer &Y = L->net.L[l];
-    ConvArgs a = {};
-    a.c1 = Y.c1; a.c2 = Y.c2; a.cout = Y.cout;
-    a.w = L->wb + Y.wb_off;
-    a.out = din1; a.dout2 = din2; a.mask1 = m1; a.mask2 = m2;
-    a.B = B; a.H = H; a.W = W;
-    const int g = nblk((long)B * H * W, 16);
-    switch ((Y.c1 + Y.c2) / 32) {
-        case 1: k_conv_bwd_data<1><<<g, 128, 0, st>>>(a, dout); break;
-        case 2: k_conv_bwd_data<2><<<g, 128, 0, st>>>(a, dout); break;
-        case 3: k_conv_bwd_data<3><<<g, 128, 0, st>>>(a, dout); break;
-        case 4: k_conv_bwd_data<4><<<g, 128, 0, st>>>(a, dout); break;
+    tc_tile_shape(W, a.TW, a.TH);
+    a.tiles_x = (W + a.TW - 1) / a.TW;
+    a.tiles_y = (H + a.TH - 1) / a.TH;
+    a.wimg = L->img + (bwd ? Y.img_b : Y.img_f);
+    a.err = L->d_tc_err;
+    if (!bwd) {
+        a.bias = L->w + Y.b_off;
+        if (y) { a.out32 = y; a.out32_ch = 1; }
+        else { a.out = out; a.relu = 1; }
+        a.split = co;
+    } else {
+        a.out = out; a.out2 = out2; a.split = Y.c1;
+        a.mask = m1; a.mask2 = m2;
     }
+    return tc_conv(&m[0], ci2 ? &m[1] : nullptr, a, st);
 }
 
 void conv_bwd_w(LpcState *L, int l, const bf16 *in1, const bf16 *in2, const bf16 *dout, int B, int H, int W,
@@ -476,7 +356,7 @@ void conv_bwd_w(LpcState *L, int l, const bf16 *in1, const bf16 *in2, const bf16
     const int nch = (int)((P + chunk - 1) / chunk);
     dim3 g(9, nch);
     switch (Y.cout / 8) {
-        case 1: k_conv_bwd_w<1><<<g, 128, 0, st>>>(a, dout, L->part, chunk); break;
+        case 2: k_conv_bwd_w<2><<<g, 128, 0, st>>>(a, dout, L->part, chunk); break;
         case 4: k_conv_bwd_w<4><<<g, 128, 0, st>>>(a, dout, L->part, chunk); break;
         case 8: k_conv_bwd_w<8><<<g, 128, 0, st>>>(a, dout, L->part, chunk); break;
     }
@@ -487,26 +367,32 @@ void conv_bwd_w(LpcState *L, int l, const bf16 *in1, const bf16 *in2, const bf16
 
 }  // namespace
 
-int lpc_alloc(LpcState **out, int Hn, int Wn, int Bmax, int Nmax, uint64_t seed, cudaStream_t st) {
+int lpc_alloc(LpcState **out, int Hn, int Wn, int Hc, int Wc, int Bmax, int Nmax, uint64_t seed, cudaStream_t st) {
+    if (Hn % 8 || Wn % 8 || Hc % 8 || Wc % 8 || Hc > Hn || Wc > Wn || Bmax < 1 || Nmax < 1) return (int)cudaErrorInvalidValue;
+    if (tc_init()) return (int)cudaErrorNotSupported;
     LpcState *L = new LpcState();
     lpc_describe(L->net);
-    L->Hn = Hn; L->Wn = Wn; L->Bmax = Bmax; L->Nmax = Nmax; L->nsamp = 0; L->adam_t = 0;
-    const long P0 = (long)Bmax * Hn * Wn, P1 = P0 / 4, P2 = P0 / 16;
-    const size_t np = L->net.nparam, nw = L->net.nw16;
+    L->Hn = Hn; L->Wn = Wn; L->Hc = Hc; L->Wc = Wc; L->Bmax = Bmax; L->Nmax = Nmax; L->nsamp = 0; L->adam_t = 0;
+    const long c0 = std::max((long)Bmax * Hc * Wc, (long)Hn * Wn), c1 = c0 / 4, c2 = c0 / 16, c3 = c0 / 64;
+    L->cap0 = c0;
+    const size_t np = L->net.nparam;
     L->nchunk_max = 64;
     L->part_n = (size_t)L->nchunk_max * 9 * 128 * 64;
     cudaError_t e = cudaSuccess;
 #define A(ptr, n) if (e == cudaSuccess) e = dalloc(&(ptr), (size_t)(n))
-    A(L->w, np); A(L->g, np); A(L->m, np); A(L->v, np); A(L->wf, nw); A(L->wb, nw);
-    A(L->x0, P0 * LPC_CIN0); A(L->a1, P0 * 32); A(L->s1, P0 * 32); A(L->p1, P1 * 32); A(L->a2, P1 * 64);
-    A(L->s2, P1 * 64); A(L->p2, P2 * 64); A(L->a3, P2 * 64); A(L->a4, P2 * 64); A(L->u2, P1 * 64);
-    A(L->a5, P1 * 64); A(L->u1, P0 * 64); A(L->a6, P0 * 32); A(L->y, P0 * LPC_COUT_LAST);
-    A(L->dy, P0 * LPC_COUT_LAST); A(L->da6, P0 * 32); A(L->du1, P0 * 64); A(L->ds1b, P0 * 32); A(L->da5, P1 * 64);
-    A(L->du2, P1 * 64); A(L->ds2b, P1 * 64); A(L->da4, P2 * 64); A(L->da3, P2 * 64); A(L->dp2, P2 * 64);
-    A(L->ds2, P1 * 64); A(L->da2, P1 * 64); A(L->dp1, P1 * 32); A(L->ds1, P0 * 32); A(L->da1, P0 * 32);
+    A(L->w, np); A(L->g, np); A(L->m, np); A(L->v, np); A(L->img, L->net.img_bytes);
+    A(L->x0, c0 * LPC_CIN0); A(L->a0, c0 * 16); A(L->s0, c0 * 16); A(L->p0, c1 * 16); A(L->a1, c1 * 32);
+    A(L->s1, c1 * 32); A(L->p1, c2 * 32); A(L->a2, c2 * 64); A(L->s2, c2 * 64); A(L->p2, c3 * 64);
+    A(L->a3, c3 * 64); A(L->b3, c3 * 64); A(L->u2, c2 * 64); A(L->d2, c2 * 64); A(L->u1, c1 * 64);
+    A(L->d1, c1 * 32); A(L->u0, c0 * 32); A(L->d0, c0 * 16); A(L->y, c0);
+    A(L->dy, c0 * LPC_COUT_LAST); A(L->dd0, c0 * 16); A(L->du0, c0 * 32); A(L->ds0b, c0 * 16); A(L->dd1, c1 * 32);
+    A(L->du1, c1 * 64); A(L->ds1b, c1 * 32); A(L->dd2, c2 * 64); A(L->du2, c2 * 64); A(L->ds2b, c2 * 64);
+    A(L->db3, c3 * 64); A(L->da3, c3 * 64); A(L->dp2, c3 * 64); A(L->ds2, c2 * 64); A(L->da2, c2 * 64);
+    A(L->dp1, c2 * 32); A(L->ds1, c1 * 32); A(L->da1, c1 * 32); A(L->dp0, c1 * 16); A(L->ds0, c0 * 16);
+    A(L->da0, c0 * 16);
     A(L->part, L->part_n);
-    A(L->dfeat, (size_t)Nmax * Hn * Wn * LPC_CIN0); A(L->dtgt, (size_t)Nmax * Hn * Wn);
-    A(L->mask, (size_t)Hn * Wn); A(L->btgt, P0); A(L->bmask, P0); A(L->d_loss, 4);
+    A(L->dfeat, (size_t)Nmax * Hn * Wn * LPC_NFEAT); A(L->dtgt, (size_t)Nmax * Hn * Wn);
+    A(L->mask, (size_t)Hn * Wn); A(L->btgt, c0); A(L->bmask, c0); A(L->d_loss, 4); A(L->d_tc_err, 4);
 #undef A
     if (e != cudaSuccess) { lpc_free(L); return (int)e; }
     // He-normal weights from a seeded generator, zero biases; the last layer
@@ -535,62 +421,94 @@ int lpc_alloc(LpcState **out, int Hn, int Wn, int Bmax, int Nmax, uint64_t seed,
 
 void lpc_free(LpcState *L) {
     if (!L) return;
-    void *ps[] = {L->w, L->g, L->m, L->v, L->wf, L->wb, L->x0, L->a1, L->s1, L->p1, L->a2, L->s2, L->p2, L->a3,
-                  L->a4, L->u2, L->a5, L->u1, L->a6, L->y, L->dy, L->da6, L->du1, L->ds1b, L->da5, L->du2,
-                  L->ds2b, L->da4, L->da3, L->dp2, L->ds2, L->da2, L->dp1, L->ds1, L->da1, L->part, L->dfeat,
-                  L->dtgt, L->mask, L->btgt, L->bmask, L->d_loss};
+    void *ps[] = {L->w,   L->g,    L->m,    L->v,    L->img,  L->x0,  L->a0,  L->s0,    L->p0,    L->a1,   L->s1,
+                  L->p1,  L->a2,   L->s2,   L->p2,   L->a3,   L->b3,  L->u2,  L->d2,    L->u1,    L->d1,   L->u0,
+                  L->d0,  L->y,    L->dy,   L->dd0,  L->du0,  L->ds0b, L->dd1, L->du1,  L->ds1b,  L->dd2,  L->du2,
+                  L->ds2b, L->db3, L->da3,  L->dp2,  L->ds2,  L->da2, L->dp1, L->ds1,   L->da1,   L->dp0,  L->ds0,
+                  L->da0, L->part, L->dfeat, L->dtgt, L->mask, L->btgt, L->bmask, L->d_loss, L->d_tc_err};
     for (void *p : ps) cudaFree(p);
     delete L;
 }
 
-void lpc_refresh(LpcState *L, cudaStream_t st) { k_refresh<<<256, 256, 0, st>>>(L->net, L->w, L->wf, L->wb); }
-
-void lpc_forward(LpcState *L, int B, cudaStream_t st) {
-    const int H0 = L->Hn, W0 = L->Wn, H1 = H0 / 2, W1 = W0 / 2, H2 = H1 / 2, W2 = W1 / 2;
-    const int ew = 1024;
-    conv_fwd(L, 0, L->x0, nullptr, L->a1, nullptr, B, H0, W0, st);
-    conv_fwd(L, 1, L->a1, nullptr, L->s1, nullptr, B, H0, W0, st);
-    k_pool<<<ew, 256, 0, st>>>(L->s1, L->p1, B, H0, W0, 32);
-    conv_fwd(L, 2, L->p1, nullptr, L->a2, nullptr, B, H1, W1, st);
-    conv_fwd(L, 3, L->a2, nullptr, L->s2, nullptr, B, H1, W1, st);
-    k_pool<<<ew, 256, 0, st>>>(L->s2, L->p2, B, H1, W1, 64);
-    conv_fwd(L, 4, L->p2, nullptr, L->a3, nullptr, B, H2, W2, st);
-    conv_fwd(L, 5, L->a3, nullptr, L->a4, nullptr, B, H2, W2, st);
-    k_up<<<ew, 256, 0, st>>>(L->a4, L->u2, B, H2, W2, 64);
-    conv_fwd(L, 6, L->u2, L->s2, L->a5, nullptr, B, H1, W1, st);
-    k_up<<<ew, 256, 0, st>>>(L->a5, L->u1, B, H1, W1, 64);
-    conv_fwd(L, 7, L->u1, L->s1, L->a6, nullptr, B, H0, W0, st);
-    conv_fwd(L, 8, L->a6, nullptr, nullptr, L->y, B, H0, W0, st);
+void lpc_refresh(LpcState *L, cudaStream_t st) {
+    for (int l = 0; l < LPC_NLAYER; l++) {
+        const LpcLayer &Y = L->net.L[l];
+        tc_build_weights(L->w + Y.w_off, Y.c1, Y.c2, Y.cout, L->img + Y.img_f, st);
+        if (l > 0) tc_build_weights_bwd(L->w + Y.w_off, Y.c1 + Y.c2, Y.cout, L->img + Y.img_b, st);
+    }
 }
 
-int lpc_loss_backward(LpcState *L, int B, cudaStream_t st) {
-    const int H0 = L->Hn, W0 = L->Wn, H1 = H0 / 2, W1 = W0 / 2, H2 = H1 / 2, W2 = W1 / 2;
-    const long P0 = (long)B * H0 * W0;
+int lpc_forward(LpcState *L, int B, int H, int W, cudaStream_t st) {
+    if ((long)B * H * W > L->cap0 || H % 8 || W % 8) return (int)cudaErrorInvalidValue;
+    const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
     const int ew = 1024;
+    int r = 0;
+    r |= tc_layer(L, 0, 0, B, H, W, L->x0, nullptr, L->a0, nullptr, nullptr, nullptr, nullptr, st);
+    r |= tc_layer(L, 1, 0, B, H, W, L->a0, nullptr, L->s0, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool<<<ew, 256, 0, st>>>(L->s0, L->p0, B, H, W, 16);
+    r |= tc_layer(L, 2, 0, B, H1, W1, L->p0, nullptr, L->a1, nullptr, nullptr, nullptr, nullptr, st);
+    r |= tc_layer(L, 3, 0, B, H1, W1, L->a1, nullptr, L->s1, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool<<<ew, 256, 0, st>>>(L->s1, L->p1, B, H1, W1, 32);
+    r |= tc_layer(L, 4, 0, B, H2, W2, L->p1, nullptr, L->a2, nullptr, nullptr, nullptr, nullptr, st);
+    r |= tc_layer(L, 5, 0, B, H2, W2, L->a2, nullptr, L->s2, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool<<<ew, 256, 0, st>>>(L->s2, L->p2, B, H2, W2, 64);
+    r |= tc_layer(L, 6, 0, B, H3, W3, L->p2, nullptr, L->a3, nullptr, nullptr, nullptr, nullptr, st);
+    r |= tc_layer(L, 7, 0, B, H3, W3, L->a3, nullptr, L->b3, nullptr, nullptr, nullptr, nullptr, st);
+    k_up<<<ew, 256, 0, st>>>(L->b3, L->u2, B, H3, W3, 64);
+    r |= tc_layer(L, 8, 0, B, H2, W2, L->u2, L->s2, L->d2, nullptr, nullptr, nullptr, nullptr, st);
+    k_up<<<ew, 256, 0, st>>>(L->d2, L->u1, B, H2, W2, 64);
+    r |= tc_layer(L, 9, 0, B, H1, W1, L->u1, L->s1, L->d1, nullptr, nullptr, nullptr, nullptr, st);
+    k_up<<<ew, 256, 0, st>>>(L->d1, L->u0, B, H1, W1, 32);
+    r |= tc_layer(L, 10, 0, B, H, W, L->u0, L->s0, L->d0, nullptr, nullptr, nullptr, nullptr, st);
+    r |= tc_layer(L, 11, 0, B, H, W, L->d0, nullptr, nullptr, nullptr, nullptr, nullptr, L->y, st);
+    if (r) L->tc_bad = 1;
+    return r ? (int)cudaErrorLaunchFailure : 0;
+}
+
+int lpc_loss_backward(LpcState *L, int B, int H, int W, cudaStream_t st) {
+    const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
+    const long P0 = (long)B * H * W;
+    const int ew = 1024;
+    int r = 0;
     k_loss<<<1, 1024, 0, st>>>(L->y, L->btgt, L->bmask, P0, L->dy, L->d_loss);
-    const LpcLayer &Lo = L->net.L[8];
-    conv_bwd_w(L, 8, L->a6, nullptr, L->dy, B, H0, W0, st);
-    k_out_bwd_data<<<nblk(P0, 256), 256, 0, st>>>(L->dy, LPC_COUT_LAST, L->w + Lo.w_off, Lo.c1, L->a6, L->da6, B,
-                                                   H0, W0);
-    conv_bwd_w(L, 7, L->u1, L->s1, L->da6, B, H0, W0, st);
-    conv_bwd_data(L, 7, L->da6, L->du1, L->ds1b, nullptr, nullptr, B, H0, W0, st);
-    k_up_bwd<<<ew, 256, 0, st>>>(L->du1, L->a5, L->da5, B, H1, W1, 64);
-    conv_bwd_w(L, 6, L->u2, L->s2, L->da5, B, H1, W1, st);
-    conv_bwd_data(L, 6, L->da5, L->du2, L->ds2b, nullptr, nullptr, B, H1, W1, st);
-    k_up_bwd<<<ew, 256, 0, st>>>(L->du2, L->a4, L->da4, B, H2, W2, 64);
-    conv_bwd_w(L, 5, L->a3, nullptr, L->da4, B, H2, W2, st);
-    conv_bwd_data(L, 5, L->da4, L->da3, nullptr, L->a3, nullptr, B, H2, W2, st);
-    conv_bwd_w(L, 4, L->p2, nullptr, L->da3, B, H2, W2, st);
-    conv_bwd_data(L, 4, L->da3, L->dp2, nullptr, nullptr, nullptr, B, H2, W2, st);
-    k_pool_bwd<<<ew, 256, 0, st>>>(L->dp2, L->ds2b, L->s2, L->ds2, B, H1, W1, 64);
-    conv_bwd_w(L, 3, L->a2, nullptr, L->ds2, B, H1, W1, st);
-    conv_bwd_data(L, 3, L->ds2, L->da2, nullptr, L->a2, nullptr, B, H1, W1, st);
-    conv_bwd_w(L, 2, L->p1, nullptr, L->da2, B, H1, W1, st);
-    conv_bwd_data(L, 2, L->da2, L->dp1, nullptr, nullptr, nullptr, B, H1, W1, st);
-    k_pool_bwd<<<ew, 256, 0, st>>>(L->dp1, L->ds1b, L->s1, L->ds1, B, H0, W0, 32);
-    conv_bwd_w(L, 1, L->a1, nullptr, L->ds1, B, H0, W0, st);
-    conv_bwd_data(L, 1, L->ds1, L->da1, nullptr, L->a1, nullptr, B, H0, W0, st);
-    conv_bwd_w(L, 0, L->x0, nullptr, L->da1, B, H0, W0, st);
+    // output layer
+    conv_bwd_w(L, 11, L->d0, nullptr, L->dy, B, H, W, st);
+    r |= tc_layer(L, 11, 1, B, H, W, L->dy, nullptr, L->dd0, nullptr, L->d0, nullptr, nullptr, st);
+    // dec0 [u0, s0] -> d0
+    conv_bwd_w(L, 10, L->u0, L->s0, L->dd0, B, H, W, st);
+    r |= tc_layer(L, 10, 1, B, H, W, L->dd0, nullptr, L->du0, L->ds0b, nullptr, nullptr, nullptr, st);
+    k_up_bwd<<<ew, 256, 0, st>>>(L->du0, L->d1, L->dd1, B, H1, W1, 32);
+    // dec1 [u1, s1] -> d1
+    conv_bwd_w(L, 9, L->u1, L->s1, L->dd1, B, H1, W1, st);
+    r |= tc_layer(L, 9, 1, B, H1, W1, L->dd1, nullptr, L->du1, L->ds1b, nullptr, nullptr, nullptr, st);
+    k_up_bwd<<<ew, 256, 0, st>>>(L->du1, L->d2, L->dd2, B, H2, W2, 64);
+    // dec2 [u2, s2] -> d2
+    conv_bwd_w(L, 8, L->u2, L->s2, L->dd2, B, H2, W2, st);
+    r |= tc_layer(L, 8, 1, B, H2, W2, L->dd2, nullptr, L->du2, L->ds2b, nullptr, nullptr, nullptr, st);
+    k_up_bwd<<<ew, 256, 0, st>>>(L->du2, L->b3, L->db3, B, H3, W3, 64);
+    // bottleneck
+    conv_bwd_w(L, 7, L->a3, nullptr, L->db3, B, H3, W3, st);
+    r |= tc_layer(L, 7, 1, B, H3, W3, L->db3, nullptr, L->da3, nullptr, L->a3, nullptr, nullptr, st);
+    conv_bwd_w(L, 6, L->p2, nullptr, L->da3, B, H3, W3, st);
+    r |= tc_layer(L, 6, 1, B, H3, W3, L->da3, nullptr, L->dp2, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool_bwd<<<ew, 256, 0, st>>>(L->dp2, L->ds2b, L->s2, L->ds2, B, H2, W2, 64);
+    // enc2
+    conv_bwd_w(L, 5, L->a2, nullptr, L->ds2, B, H2, W2, st);
+    r |= tc_layer(L, 5, 1, B, H2, W2, L->ds2, nullptr, L->da2, nullptr, L->a2, nullptr, nullptr, st);
+    conv_bwd_w(L, 4, L->p1, nullptr, L->da2, B, H2, W2, st);
+    r |= tc_layer(L, 4, 1, B, H2, W2, L->da2, nullptr, L->dp1, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool_bwd<<<ew, 256, 0, st>>>(L->dp1, L->ds1b, L->s1, L->ds1, B, H1, W1, 32);
+    // enc1
+    conv_bwd_w(L, 3, L->a1, nullptr, L->ds1, B, H1, W1, st);
+    r |= tc_layer(L, 3, 1, B, H1, W1, L->ds1, nullptr, L->da1, nullptr, L->a1, nullptr, nullptr, st);
+    conv_bwd_w(L, 2, L->p0, nullptr, L->da1, B, H1, W1, st);
+    r |= tc_layer(L, 2, 1, B, H1, W1, L->da1, nullptr, L->dp0, nullptr, nullptr, nullptr, nullptr, st);
+    k_pool_bwd<<<ew, 256, 0, st>>>(L->dp0, L->ds0b, L->s0, L->ds0, B, H, W, 16);
+    // enc0
+    conv_bwd_w(L, 1, L->a0, nullptr, L->ds0, B, H, W, st);
+    r |= tc_layer(L, 1, 1, B, H, W, L->ds0, nullptr, L->da0, nullptr, L->a0, nullptr, nullptr, st);
+    conv_bwd_w(L, 0, L->x0, nullptr, L->da0, B, H, W, st);
+    if (r) { L->tc_bad = 1; return (int)cudaErrorLaunchFailure; }
     return (int)cudaGetLastError();
 }
 
@@ -602,13 +520,23 @@ void lpc_adam(LpcState *L, float lr, cudaStream_t st) {
     lpc_refresh(L, st);
 }
 
-void lpc_gather(LpcState *L, const int *h_idx, int B, cudaStream_t st) {
-    const size_t px = (size_t)L->Hn * L->Wn;
-    for (int b = 0; b < B; b++) {
-        const size_t i = (size_t)h_idx[b];
-        cudaMemcpyAsync(L->x0 + b * px * LPC_CIN0, L->dfeat + i * px * LPC_CIN0, px * LPC_CIN0 * sizeof(bf16),
-                        cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(L->btgt + b * px, L->dtgt + i * px, px * sizeof(float), cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(L->bmask + b * px, L->mask, px * sizeof(float), cudaMemcpyDeviceToDevice, st);
-    }
+void lpc_gather(LpcState *L, const int *h_idx, const int *h_y0, const int *h_x0, int B, cudaStream_t st) {
+    // crop table through a small pinned-free staging: B <= Bmax triples in the loss slot's neighbour
+    std::vector<int> cr(3 * (size_t)B);
+    for (int b = 0; b < B; b++) { cr[3 * b] = h_idx[b]; cr[3 * b + 1] = h_y0[b]; cr[3 * b + 2] = h_x0[b]; }
+    int *d_cr = reinterpret_cast<int *>(L->part);   // the weight-gradient partials are free here
+    cudaMemcpyAsync(d_cr, cr.data(), cr.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    const long n = (long)B * L->Hc * L->Wc;
+    k_gather<<<nblk(n, 256) < 4096 ? nblk(n, 256) : 4096, 256, 0, st>>>(L->dfeat, L->dtgt, L->mask, L->Hn, L->Wn, d_cr,
+                                                                       B, L->Hc, L->Wc, L->x0, L->btgt, L->bmask);
+    cudaStreamSynchronize(st);   // the host table must outlive the copy
+}
+
+int lpc_tc_error(LpcState *L, cudaStream_t st) {
+    int err = 0;
+    if (cudaMemcpyAsync(&err, L->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return FS_ERR_CUDA;
+    if (err || L->tc_bad) { L->tc_bad = 1; return FS_ERR_CUDA; }
+    return 0;
 }

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cuda_runtime.h>
 
+#include "fs_fastmath.cuh"
 #include "fs_internal.h"
 #include "fs_sg.cuh"
 
@@ -56,7 +57,7 @@ struct StageArgs {
 };
 
 __device__ __forceinline__ void tab_index(const PhysParams &pp, double T, int &k, double &w) {
-    double x = log(T * pp.ph0);
+    double x = fs_log(T * pp.ph0);
     double u = (x - pp.lemin) * pp.inv_h;
     if (!(u >= 0.0)) u = 0.0;
     if (u > (double)(pp.ntab - 1)) u = (double)(pp.ntab - 1);
@@ -93,12 +94,12 @@ __device__ __forceinline__ void sg_elec(double E, double dh, double inv_dh, doub
     }
     double ex;
     if (arg > 0) {
-        ex = exp(fmax(-arg, -100.0));
+        ex = fs_exp(fmax(-arg, -100.0));
         double inv = 1.0 / (1.0 - ex);
         fe = ve * (nel - ner * ex) * inv;
         ft = vt * (ntl - ntr * ex) * inv;
     } else {
-        ex = exp(fmax(arg, -100.0));
+        ex = fs_exp(fmax(arg, -100.0));
         double inv = 1.0 / (1.0 - ex);
         fe = ve * (ner - nel * ex) * inv;
         ft = vt * (ntr - ntl * ex) * inv;
@@ -158,8 +159,10 @@ __device__ __noinline__ double wall_face(const StageArgs &a, int gi, double te, 
     return E;
 }
 
+// One RK stage on the tile (bx, by) of the grid (BX x BY nodes); blk is the
+// tile's index among the grid's tiles (its slot in the error partials).
 template <int NS>
-__global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
+__device__ __forceinline__ void stage_tile(const StageArgs &a, int bx, int by, int blk) {
     __shared__ double s_n[NS][HY][HX];
     __shared__ double s_ph[HY][HX];
     __shared__ double s_te[HY][HX];
@@ -177,7 +180,7 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
     const PhysParams &pp = a.pp;
     const int nx = pp.nx, ny = pp.ny, P = pp.pitch;
     const int tid = threadIdx.x;
-    const int gx0 = blockIdx.x * BX + 1, gy0 = blockIdx.y * BY + 1;
+    const int gx0 = bx * BX + 1, gy0 = by * BY + 1;
     unsigned int st = 0;
 
     // phase 1: tile + halo of the stage state and phi
@@ -423,7 +426,7 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
         if (tid < NS) {
             double v = 0.0;
             for (int wv = 0; wv < NT / 32; wv++) v += s_red[tid][wv];
-            a.part[(size_t)tid * a.nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+            a.part[(size_t)tid * a.nblk + blk] = v;
         }
         if (tid == 0) {
             double m = s_tm[0];
@@ -432,6 +435,11 @@ __global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
                 atomicMin((unsigned long long *)&a.ctrl->t_m, (unsigned long long)__double_as_longlong(m));
         }
     }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
+    stage_tile<NS>(a, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Ion face coefficients while phi is frozen.  get_Flux for q = +1
@@ -449,7 +457,7 @@ __device__ __forceinline__ void ion_face(const PhysParams &pp, double E, double 
     const double a = v * dh / pp.Di, aa = fabs(a);
     double ex = 0.0, inv = 0.0;
     if (aa >= 1e-2) {
-        ex = exp(-aa);
+        ex = fs_exp(-aa);
         inv = 1.0 / (1.0 - ex);
     }
     if (fabs(E) < tol) {

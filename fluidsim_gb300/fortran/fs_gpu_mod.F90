@@ -80,12 +80,19 @@ module fs_gpu_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: v
     end function
+    ! fs_max_ne with its scratch in a fixed device array of the library, for
+    ! callers that may not allocate device memory once set up
+    integer(c_int) function fs_max_ne_noalloc(ctx, v) bind(C, name="fs_max_ne_noalloc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: v
+    end function
     ! learned Poisson preconditioner of the mixed solver (no reference counterpart)
-    integer(c_int) function fs_lpc_init(ctx, level, max_batch, max_samples, seed) &
+    integer(c_int) function fs_lpc_init(ctx, crop, max_batch, max_samples, seed) &
         bind(C, name="fs_lpc_init")
       import :: c_ptr, c_int, c_int32_t, c_int64_t
       type(c_ptr), value :: ctx
-      integer(c_int32_t), value :: level, max_batch, max_samples
+      integer(c_int32_t), value :: crop, max_batch, max_samples
       integer(c_int64_t), value :: seed
     end function
     integer(c_int) function fs_lpc_harvest(ctx, per_solve, added) bind(C, name="fs_lpc_harvest")

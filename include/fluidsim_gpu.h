@@ -235,7 +235,9 @@ int fs_run(fs_ctx *ctx, int32_t nsteps, fs_stats *stats_out);
 int fs_get_stats(fs_ctx *ctx, fs_stats *out);
 
 /* maxval(ne) over the whole module array -- every level, ghosts included
- * (main.F90:131). */
+ * (main.F90:131).  NaN entries are skipped (the maximum of the other values
+ * is returned; an all-NaN array gives -inf): the ptcl_step and lapl_solve
+ * entry points report NaN densities themselves (FS_ERR_NAN). */
 int fs_max_ne(fs_ctx *ctx, double *out);
 
 /* ---- diagnostics with no counterpart in the reference ------------------- */
@@ -257,6 +259,35 @@ int fs_profile_read(fs_ctx *ctx, double *ms_out, int64_t *launches_out, int32_t 
 
 /* Number of kernels ctx has launched since fs_create. */
 int64_t fs_launch_count(fs_ctx *ctx);
+
+/* FP64 issue rate of device `device`: fused multiply-adds per second of a
+ * DFMA microbenchmark (4 to 16 CTAs per SM, 8 or 16 independent chains per
+ * thread, the best of all shapes and of 5 timed launches each, CUDA
+ * events).  The roof of the FP64-issue-bound kernels (RK stage, Poisson
+ * assembly); FP64 FLOP/s = 2 x this.  Needs no context; changes no device
+ * setting. */
+int fs_fp64_rate(int32_t device, double *dfma_per_s);
+
+/* The FP64 kernels' elementary functions on n host values, for accuracy
+ * tests: fn 0 the table-driven logarithm and 1 the table-driven exponential
+ * the FP64 kernels use, 2 and 3 CUDA's log and exp.  Runs on the current
+ * device; allocates and frees its own device buffers. */
+int fs_math_eval(int32_t fn, const double *x, double *y, int64_t n);
+
+/* One 3x3 convolution (zero padding) of the learned preconditioner's network
+ * through its tcgen05 tensor-core path, on host arrays, for tests: in1
+ * [B][H][W][c1] and in2 [B][H][W][c2] (the decoder's concatenation; NULL
+ * when c2 = 0) as BF16 bit patterns, w [9][cout][c1 + c2] (tap = 3 (dy+1) +
+ * (dx+1)) and bias [cout] in FP32.  mode 0: out is FP32 [B][H][W][cout],
+ * bias added; mode 1: out is BF16 bit patterns, bias and ReLU applied.
+ * Channels: c1, c2 multiples of 16 (of 64 above 64), cout a multiple of 16
+ * up to 128.
+ * Returns 0, or a negative code (-1 bad arguments, -2 no device memory or
+ * shared memory over the limit, -3 TMA descriptor, -6 a bounded wait ran
+ * out, -100 - e for the CUDA error e). */
+int fs_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t c1, int32_t c2, int32_t cout,
+                  const uint16_t *in1, const uint16_t *in2, const float *w, const float *bias,
+                  int32_t mode, void *out);
 
 /* fs_max_ne for callers that may not allocate device memory after set-up
  * (this entry point has no counterpart in the reference): same result as
@@ -300,49 +331,57 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
 
 /* ---- Learned Poisson preconditioner (FS_PREC_MIXED contexts only).  No
  * counterpart in the reference, which hands the system to PETSc
- * (lapl_lib.F90:83-104).  A small BF16 convolutional network (~250k
- * parameters, two-level U-Net, tensor cores with FP32 accumulation) on the
- * grid of multigrid level `level` predicts the error the V-cycle leaves; its
- * interpolated prediction is added to each V-cycle's result inside the
- * flexible CG.  The refinement of the mixed solver (the true residual, to
- * FP64 accuracy) judges convergence,
- * so every solve reaches lapl_rtol exactly as without the network, and if an
- * iteration stalls (inner residual falling by less than 2x) the network is
- * switched off for the rest of that solve.  In mode 1 the
- * library times every solve and runs each next one with whichever of the
- * two -- with or without the network -- has been faster on average (a
- * stalled solve counts double), trying the other one every 25 solves.
+ * (lapl_lib.F90:83-104).  A BF16 convolutional network (a four-level U-Net,
+ * 16 to 64 channels, 258,528 parameters, on the tcgen05 tensor cores with
+ * FP32 accumulation) on the fine grid.  In a CG iteration that runs it, the
+ * preconditioner is z = V(r) + N(s): V the multigrid V-cycle, s = r - M V(r)
+ * the residual it leaves, N the network's estimate of the correction a second
+ * V-cycle would add for s (inputs: s, the two face-coupling shares of the
+ * diagonal -- the grid-spacing map -- and the net charge density).  The
+ * flexible CG tolerates the nonlinear preconditioner; the refinement of the
+ * mixed solver (the true residual, to FP64 accuracy) judges convergence, so
+ * every solve reaches lapl_rtol exactly as without the network, and after 3
+ * stalled iterations (inner residual falling by less than 4x) the network is
+ * switched off for the rest of that solve.  One black-red Gauss-Seidel pass
+ * follows the correction.  In mode 1 the library times
+ * every solve and runs each next one with whichever of the two -- with or
+ * without the network -- has been faster on average (a stalled solve counts
+ * double), trying the other one every 25 solves.
  *
  * fs_lpc_init      allocate the network (seeded He init), its training state
- *                  and a ring of up to max_samples training pairs; batches up
- *                  to max_batch.
+ *                  and up to max_samples stored training pairs (full grids);
+ *                  training batches of up to max_batch crops of crop x crop
+ *                  cells (a multiple of 8; 0: 128; at most the grid).
  * fs_lpc_harvest   after fs_lapl_solve: re-solve the step's assembled system
  *                  with the plain multigrid-PCG, take up to per_solve of its
- *                  residuals r, and store for each the pair (features of the
- *                  residual left by one V-cycle, aggregate means of the
- *                  correction multigrid-PCG computes for it).  phi is not
- *                  changed.
- * fs_lpc_train     iters Adam steps (lr) on random batches of the stored
- *                  pairs (seeded); loss_hist (may be NULL) gets each step's
- *                  training loss.
+ *                  residuals r, and store for each the pair (features of
+ *                  s = r - M V(r), the second V-cycle's correction V(s)).
+ *                  phi is not changed.
+ * fs_lpc_train     iters Adam steps (lr) on batches of random crops of the
+ *                  stored pairs (seeded); loss_hist (may be NULL) gets each
+ *                  step's training loss.
  * fs_lpc_use       0: plain multigrid-PCG; 1: the network where it pays off
- *                  (see below); 2: the network in every solve.
+ *                  (see above); 2: the network in every solve.
  * fs_lpc_weights   copy the FP32 parameters out (to_device = 0) or in
  *                  (to_device = 1, Adam state reset); n must equal nparam.
- * fs_lpc_grad      loss and parameter gradient for given inputs: feat
- *                  [batch][h][w][4], tgt [batch][h][w], mask [h][w]; pred
- *                  (may be NULL) gets the predictions [batch][h][w].
- * fs_lpc_info      NN grid size (h, w, padded to multiples of 4), stored
- *                  pairs, parameter count; off = 1 if the last solve switched
- *                  the network off. */
-int fs_lpc_init(fs_ctx *ctx, int32_t level, int32_t max_batch, int32_t max_samples, uint64_t seed);
+ * fs_lpc_grad      loss and parameter gradient for given inputs on batch
+ *                  full grids: feat [batch][h][w][4], tgt [batch][h][w], mask
+ *                  [h][w]; pred (may be NULL) gets the predictions
+ *                  [batch][h][w].
+ * fs_lpc_info      NN grid size (h, w: the grid padded to multiples of 8),
+ *                  stored pairs, parameter count; off = 1 if the last solve
+ *                  switched the network off; solves since fs_lpc_use turned
+ *                  the network on and how many of them ran it (any output
+ *                  pointer may be NULL). */
+int fs_lpc_init(fs_ctx *ctx, int32_t crop, int32_t max_batch, int32_t max_samples, uint64_t seed);
 int fs_lpc_harvest(fs_ctx *ctx, int32_t per_solve, int32_t *added);
 int fs_lpc_train(fs_ctx *ctx, int32_t iters, int32_t batch, float lr, uint64_t seed, float *loss_hist);
 int fs_lpc_use(fs_ctx *ctx, int32_t on);
 int fs_lpc_weights(fs_ctx *ctx, float *w, int64_t n, int32_t to_device);
 int fs_lpc_grad(fs_ctx *ctx, const float *feat, const float *tgt, const float *mask, int32_t batch, float *grad,
                 float *loss, float *pred);
-int fs_lpc_info(fs_ctx *ctx, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off);
+int fs_lpc_info(fs_ctx *ctx, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *nparam, int32_t *off,
+                int64_t *solves, int64_t *nn_solves);
 
 #ifdef __cplusplus
 }

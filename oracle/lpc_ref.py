@@ -1,7 +1,7 @@
 """CPU oracle of the learned Poisson preconditioner's network (test
 infrastructure only: the product path runs the CUDA kernels).
 
-The same two-level U-Net as the library (layer table, NHWC layout, zero
+The same four-level U-Net as the library (layer table, NHWC layout, zero
 padding, 2x2 average pooling, nearest upsampling, ReLU), in numpy, with the
 library's roundings emulated: BF16 (round to nearest even) for the weights,
 every stored activation and every stored activation gradient; FP32
@@ -15,11 +15,15 @@ then b[cout], tap = 3 (dy + 1) + (dx + 1).
 import numpy as np
 
 CIN0 = 16
-COUT_LAST = 8
+COUT_LAST = 16
 NFEAT = 4
-# c1, c2, cout, resolution level
-LAYERS = [(CIN0, 0, 32, 0), (32, 0, 32, 0), (32, 0, 64, 1), (64, 0, 64, 1), (64, 0, 64, 2),
-          (64, 0, 64, 2), (64, 64, 64, 1), (64, 32, 32, 0), (32, 0, COUT_LAST, 0)]
+# c1, c2, cout, resolution level: a four-level U-Net (16, 32, 64, 64 channels)
+LAYERS = [(CIN0, 0, 16, 0), (16, 0, 16, 0),        # enc0a, enc0b (skip s0)
+          (16, 0, 32, 1), (32, 0, 32, 1),          # enc1a, enc1b (skip s1)
+          (32, 0, 64, 2), (64, 0, 64, 2),          # enc2a, enc2b (skip s2)
+          (64, 0, 64, 3), (64, 0, 64, 3),          # bottleneck
+          (64, 64, 64, 2), (64, 32, 32, 1), (32, 16, 16, 0),   # decoders [up, skip]
+          (16, 0, COUT_LAST, 0)]                   # output (channel 0)
 
 
 def layout():
@@ -96,21 +100,27 @@ class Net:
 
     def forward(self, x0):
         r, relu = self._r, (lambda v: np.maximum(v, 0))
+        cat = lambda a, b: np.concatenate([a, b], axis=3)
         A = {}
         A["x0"] = r(x0)
-        A["a1"] = r(relu(self.conv(0, A["x0"])))
-        A["s1"] = r(relu(self.conv(1, A["a1"])))
+        A["a0"] = r(relu(self.conv(0, A["x0"])))
+        A["s0"] = r(relu(self.conv(1, A["a0"])))
+        A["p0"] = r(self.pool(A["s0"]))
+        A["a1"] = r(relu(self.conv(2, A["p0"])))
+        A["s1"] = r(relu(self.conv(3, A["a1"])))
         A["p1"] = r(self.pool(A["s1"]))
-        A["a2"] = r(relu(self.conv(2, A["p1"])))
-        A["s2"] = r(relu(self.conv(3, A["a2"])))
+        A["a2"] = r(relu(self.conv(4, A["p1"])))
+        A["s2"] = r(relu(self.conv(5, A["a2"])))
         A["p2"] = r(self.pool(A["s2"]))
-        A["a3"] = r(relu(self.conv(4, A["p2"])))
-        A["a4"] = r(relu(self.conv(5, A["a3"])))
-        A["u2"] = self.up(A["a4"])
-        A["a5"] = r(relu(self.conv(6, np.concatenate([A["u2"], A["s2"]], axis=3))))
-        A["u1"] = self.up(A["a5"])
-        A["a6"] = r(relu(self.conv(7, np.concatenate([A["u1"], A["s1"]], axis=3))))
-        A["y"] = self.conv(8, A["a6"]).astype(self.dt)
+        A["a3"] = r(relu(self.conv(6, A["p2"])))
+        A["b3"] = r(relu(self.conv(7, A["a3"])))
+        A["u2"] = self.up(A["b3"])
+        A["d2"] = r(relu(self.conv(8, cat(A["u2"], A["s2"]))))
+        A["u1"] = self.up(A["d2"])
+        A["d1"] = r(relu(self.conv(9, cat(A["u1"], A["s1"]))))
+        A["u0"] = self.up(A["d1"])
+        A["d0"] = r(relu(self.conv(10, cat(A["u0"], A["s0"]))))
+        A["y"] = self.conv(11, A["d0"]).astype(self.dt)
         self.A = A
         return A["y"][..., 0]
 
@@ -119,6 +129,7 @@ class Net:
         r = self._r
         y = self.forward(x0)
         A = self.A
+        cat = lambda a, b: np.concatenate([a, b], axis=3)
         m = np.broadcast_to(mask, y.shape).astype(self.dt)
         d = y - tgt
         msum = m.sum()
@@ -132,28 +143,33 @@ class Net:
             g[wo:bo] = dw.ravel()
             g[bo:bo + LAYERS[l][2]] = db
 
-        mask_of = lambda a: (a > 0).astype(self.dt)
-        da6, dw, db = self.conv_bwd(8, A["a6"], dy); put(8, dw, db)
-        da6 = r(da6 * mask_of(A["a6"]))
-        dcat, dw, db = self.conv_bwd(7, np.concatenate([A["u1"], A["s1"]], axis=3), da6); put(7, dw, db)
+        mk = lambda a: (a > 0).astype(self.dt)
+        dd0, dw, db = self.conv_bwd(11, A["d0"], dy); put(11, dw, db)
+        dd0 = r(dd0 * mk(A["d0"]))
+        dcat, dw, db = self.conv_bwd(10, cat(A["u0"], A["s0"]), dd0); put(10, dw, db)
+        du0, ds0b = r(dcat[..., :32]), r(dcat[..., 32:])
+        dd1 = r(self._upb(du0) * mk(A["d1"]))
+        dcat, dw, db = self.conv_bwd(9, cat(A["u1"], A["s1"]), dd1); put(9, dw, db)
         du1, ds1b = r(dcat[..., :64]), r(dcat[..., 64:])
-        da5 = r(self._upb(du1) * mask_of(A["a5"]))
-        dcat, dw, db = self.conv_bwd(6, np.concatenate([A["u2"], A["s2"]], axis=3), da5); put(6, dw, db)
+        dd2 = r(self._upb(du1) * mk(A["d2"]))
+        dcat, dw, db = self.conv_bwd(8, cat(A["u2"], A["s2"]), dd2); put(8, dw, db)
         du2, ds2b = r(dcat[..., :64]), r(dcat[..., 64:])
-        da4 = r(self._upb(du2) * mask_of(A["a4"]))
-        da3, dw, db = self.conv_bwd(5, A["a3"], da4); put(5, dw, db)
-        da3 = r(da3 * mask_of(A["a3"]))
-        dp2, dw, db = self.conv_bwd(4, A["p2"], da3); put(4, dw, db)
-        dp2 = r(dp2)
-        ds2 = r((0.25 * self.up(dp2) + ds2b) * mask_of(A["s2"]))
-        da2, dw, db = self.conv_bwd(3, A["a2"], ds2); put(3, dw, db)
-        da2 = r(da2 * mask_of(A["a2"]))
-        dp1, dw, db = self.conv_bwd(2, A["p1"], da2); put(2, dw, db)
-        dp1 = r(dp1)
-        ds1 = r((0.25 * self.up(dp1) + ds1b) * mask_of(A["s1"]))
-        da1, dw, db = self.conv_bwd(1, A["a1"], ds1); put(1, dw, db)
-        da1 = r(da1 * mask_of(A["a1"]))
-        _, dw, db = self.conv_bwd(0, A["x0"], da1); put(0, dw, db)
+        db3 = r(self._upb(du2) * mk(A["b3"]))
+        da3, dw, db = self.conv_bwd(7, A["a3"], db3); put(7, dw, db)
+        da3 = r(da3 * mk(A["a3"]))
+        dp2, dw, db = self.conv_bwd(6, A["p2"], da3); put(6, dw, db)
+        ds2 = r((0.25 * self.up(r(dp2)) + ds2b) * mk(A["s2"]))
+        da2, dw, db = self.conv_bwd(5, A["a2"], ds2); put(5, dw, db)
+        da2 = r(da2 * mk(A["a2"]))
+        dp1, dw, db = self.conv_bwd(4, A["p1"], da2); put(4, dw, db)
+        ds1 = r((0.25 * self.up(r(dp1)) + ds1b) * mk(A["s1"]))
+        da1, dw, db = self.conv_bwd(3, A["a1"], ds1); put(3, dw, db)
+        da1 = r(da1 * mk(A["a1"]))
+        dp0, dw, db = self.conv_bwd(2, A["p0"], da1); put(2, dw, db)
+        ds0 = r((0.25 * self.up(r(dp0)) + ds0b) * mk(A["s0"]))
+        da0, dw, db = self.conv_bwd(1, A["a0"], ds0); put(1, dw, db)
+        da0 = r(da0 * mk(A["a0"]))
+        _, dw, db = self.conv_bwd(0, A["x0"], da0); put(0, dw, db)
         return loss, g
 
     @staticmethod

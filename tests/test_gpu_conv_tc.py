@@ -1,0 +1,70 @@
+"""The learned preconditioner's 3x3 convolution on the tcgen05 tensor cores
+(fs_conv3x3_tc: TMA-staged BF16 operands, FP32 accumulation in tensor
+memory) against a float64 numpy convolution of the same BF16-rounded inputs
+and weights (needs a GB300).  Covers every channel shape the network uses
+(one and two sources, 16/32/64-channel chunks, multi-chunk sources), grids
+narrower and wider than the 128-pixel tile, ragged edges and batches."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_bits(x):
+    """Round float32 to BF16 (nearest even); return (bits uint16, values float32)."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return r, (r.astype(np.uint32) << 16).view(np.float32)
+
+
+def _ref(x, w, bias):
+    """x [B][H][W][cin], w [9][cout][cin] -> [B][H][W][cout], zero padding, float64."""
+    B, H, W, cin = x.shape
+    cout = w.shape[1]
+    xp = np.zeros((B, H + 2, W + 2, cin))
+    xp[:, 1:-1, 1:-1] = x
+    out = np.zeros((B, H, W, cout))
+    for t in range(9):
+        dy, dx = t // 3 - 1, t % 3 - 1
+        out += xp[:, 1 + dy:1 + dy + H, 1 + dx:1 + dx + W] @ w[t].T.astype(np.float64)
+    return out + bias
+
+
+def _run(B, H, W, c1, c2, cout, mode, seed=0):
+    from fluidsim_gb300 import api
+    lib = api.load_library()
+    rng = np.random.default_rng(seed)
+    x1b, x1 = _bf16_bits(rng.standard_normal((B, H, W, c1)).astype(np.float32))
+    x2b, x2 = _bf16_bits(rng.standard_normal((B, H, W, c2)).astype(np.float32)) if c2 else (None, None)
+    w32 = (rng.standard_normal((9, cout, c1 + c2)) / np.sqrt(9 * (c1 + c2))).astype(np.float32)
+    _, wq = _bf16_bits(w32)
+    bias = rng.standard_normal(cout).astype(np.float32)
+    out = np.zeros((B, H, W, cout), dtype=np.float32 if mode == 0 else np.uint16)
+    rc = lib.fs_conv3x3_tc(B, H, W, c1, c2, cout, x1b.ctypes.data_as(C.c_void_p),
+                           x2b.ctypes.data_as(C.c_void_p) if c2 else None,
+                           w32.ctypes.data_as(C.POINTER(C.c_float)), bias.ctypes.data_as(C.POINTER(C.c_float)),
+                           mode, out.ctypes.data_as(C.c_void_p))
+    assert rc == 0, rc
+    x = np.concatenate([x1, x2], axis=-1) if c2 else x1
+    ref = _ref(x.astype(np.float64), wq.reshape(9, cout, c1 + c2), bias.astype(np.float64))
+    return out, ref
+
+
+@pytest.mark.parametrize("B,H,W,c1,c2,cout", [
+    (1, 8, 128, 16, 0, 16), (1, 16, 256, 16, 0, 32), (2, 12, 64, 32, 0, 64), (1, 33, 47, 64, 0, 64),
+    (1, 20, 128, 64, 64, 64), (1, 10, 96, 64, 32, 32), (2, 9, 40, 32, 16, 16), (1, 6, 200, 128, 0, 32),
+    (3, 4, 16, 16, 16, 16)])
+def test_conv_fp32_output(built, B, H, W, c1, c2, cout):
+    out, ref = _run(B, H, W, c1, c2, cout, 0)
+    err = np.abs(out - ref) / (np.abs(ref) + 1.0)
+    assert err.max() < 2e-5, err.max()
+
+
+def test_conv_bf16_relu_output(built):
+    out, ref = _run(2, 16, 128, 32, 32, 64, 1, seed=3)
+    got = (out.astype(np.uint32) << 16).view(np.float32)
+    r = np.maximum(ref, 0.0)
+    assert np.all(got >= 0.0)
+    assert np.max(np.abs(got - r) / (np.abs(r) + 1e-2)) < 1e-2   # one BF16 rounding

@@ -1,7 +1,9 @@
 """Learned Poisson preconditioner on the GPU (needs a GB300): the tensor-core
-forward and backward kernels against the CPU oracle (oracle/lpc_ref.py, with
+forward and backward passes against the CPU oracle (oracle/lpc_ref.py, with
 the same BF16 roundings), training on harvested pairs, and the solver with
 the network in the loop."""
+import json
+
 import numpy as np
 import pytest
 
@@ -24,12 +26,12 @@ def _rel(a, b):
 def test_lpc_forward_and_gradient_match_oracle(built):
     from fluidsim_gb300 import api
     from oracle import lpc_ref
-    cfg, mesh, st = _mixed(64)
+    cfg, mesh, st = _mixed(40)
     d = api.Discharge(cfg, mesh, st)
-    d.lpc_init(level=2, max_batch=2, max_samples=4, seed=0)
+    d.lpc_init(crop=0, max_batch=2, max_samples=4, seed=0)
     info = d.lpc_info()
     h, w = info["h"], info["w"]
-    assert (h, w) == (16, 16)
+    assert (h, w) == (40, 40)
     rng = np.random.default_rng(5)
     p = lpc_ref.init_params(3, scale_last=1.0)
     lay, n = lpc_ref.layout()
@@ -62,21 +64,22 @@ def test_lpc_forward_and_gradient_match_oracle(built):
 
 
 def test_lpc_training_and_solver(built):
-    """Harvest pairs from a 256^2 run, train, then solve the following steps
-    with and without the network: every solve converges to lapl_rtol with the
-    residual judged in FP64, and the iteration counts are recorded."""
+    """Harvest pairs from a 256^2 run, train on crops, then solve the following
+    steps with and without the network: every solve converges to lapl_rtol
+    with the residual judged in FP64, the trained network fits the second
+    V-cycle's correction, and the iteration counts are recorded."""
     from fluidsim_gb300 import api
     cfg, mesh, st = _mixed(256)
     d = api.Discharge(cfg, mesh, st)
-    d.lpc_init(level=3, max_batch=8, max_samples=256, seed=1)
-    for s in range(16):
+    d.lpc_init(crop=128, max_batch=8, max_samples=32, seed=1)
+    for s in range(12):
         assert d.step()["lerr"] == 0
         if s >= 2:
             d.lpc_harvest(per_solve=4)
-    assert d.lpc_info()["samples"] >= 40
+    assert d.lpc_info()["samples"] == 32
     hist = d.lpc_train(iters=300, batch=8, lr=1e-3, seed=2)
     assert np.all(np.isfinite(hist))
-    assert hist[-30:].mean() < 0.7 * hist[:30].mean(), (hist[:30].mean(), hist[-30:].mean())
+    assert hist[-30:].mean() < 0.5 * hist[:30].mean(), (hist[:30].mean(), hist[-30:].mean())
     w = d.lpc_weights()
     state = d.download(nlev=3)
     t, dt, ts = d.t, d.dt, d.ts
@@ -86,15 +89,19 @@ def test_lpc_training_and_solver(built):
         e.upload(state)
         e.set_time(t, dt)
         e.ts = ts
-        e.lpc_init(level=3, max_batch=1, max_samples=1, seed=0)
+        e.lpc_init(crop=0, max_batch=1, max_samples=1, seed=0)
         e.lpc_weights(w)
         e.lpc_use(2 if use else 0)
-        its = []
+        its, offs = [], []
         for _ in range(6):
             info = e.step()
             assert info["lerr"] == 0 and info["relres"] <= cfg.lapl_rtol, info
             its.append(info["iters"])
+            offs.append(e.lpc_info()["off"])
         runs[use] = its
+        if use:
+            runs["switched_off"] = offs
         e.close()
-    print("CG iterations without / with the network:", runs[False], runs[True])
-    assert sum(runs[True]) <= sum(runs[False]) + 6
+    print(json.dumps({"loss_first30": float(hist[:30].mean()), "loss_last30": float(hist[-30:].mean()),
+                      "cg_iters_plain": runs[False], "cg_iters_network": runs[True],
+                      "network_switched_off": runs["switched_off"]}))
