@@ -53,6 +53,8 @@ def load_library():
     lib.fs_profile_read.restype = C.c_int
     lib.fs_launch_count.argtypes = [C.c_void_p]
     lib.fs_launch_count.restype = C.c_int64
+    lib.fs_set_stage_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    lib.fs_set_stage_tile.restype = C.c_int
     lib.fs_fp64_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]
     lib.fs_fp64_rate.restype = C.c_int
     lib.fs_math_eval.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64]
@@ -75,6 +77,8 @@ def load_library():
     lib.fs_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                  C.POINTER(abi.FsStats), C.POINTER(C.c_int32)]
     lib.fs_batch_run.restype = C.c_int
+    lib.fs_batch_run_fused.argtypes = lib.fs_batch_run.argtypes
+    lib.fs_batch_run_fused.restype = C.c_int
     lib.fs_write_output.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
     lib.fs_write_output.restype = C.c_int
     lib.fs_output_wait.argtypes = [C.c_void_p]
@@ -356,6 +360,10 @@ class Discharge(Handle):
         self.check(self._lib.fs_profile_read(self.ctx, ms, cnt, n))
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PROF_CLASSES)}
 
+    def set_stage_tile(self, bx, by):
+        """RK stage kernel tile (FP64 path): (32, 8), (32, 4) or (64, 4)."""
+        self.check(self._lib.fs_set_stage_tile(self.ctx, int(bx), int(by)))
+
     def launch_count(self):
         return self._lib.fs_launch_count(self.ctx)
 
@@ -429,17 +437,19 @@ class Discharge(Handle):
         return loss.value, g, pred
 
 
-def batch_run(discharges, steps, t_end=0.0, nthreads=32, check=True):
+def batch_run(discharges, steps, t_end=0.0, nthreads=32, check=True, fused=False):
     """Advance independent discharges concurrently in the library (fs_batch_run):
     `steps` main-loop iterations each, or until t >= t_end (nondimensional,
-    0 = no limit).  Returns (stats dicts, return codes); with check, raises
-    if any instance failed."""
+    0 = no limit).  fused: the RK stages of all discharges as one launch per
+    stage (fs_batch_run_fused; FP64, DC, no dielectric wall).  Returns (stats
+    dicts, return codes); with check, raises if any instance failed."""
     lib = load_library()
     n = len(discharges)
     arr = (C.c_void_p * n)(*[d.ctx for d in discharges])
     st = (abi.FsStats * n)()
     rcs = (C.c_int32 * n)()
-    rc = lib.fs_batch_run(arr, n, int(steps), float(t_end), int(nthreads), st, rcs)
+    fn = lib.fs_batch_run_fused if fused else lib.fs_batch_run
+    rc = fn(arr, n, int(steps), float(t_end), int(nthreads), st, rcs)
     out = [st[i].as_dict() for i in range(n)]
     for d, s in zip(discharges, out):
         d.t, d.dt, d.ts = s["t"], s["dt"], s["steps"]

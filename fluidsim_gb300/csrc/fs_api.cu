@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -37,6 +38,25 @@ int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what) {
     if (e == cudaSuccess) return FS_OK;
     int code = (e == cudaErrorMemoryAllocation) ? FS_ERR_NOMEM : FS_ERR_CUDA;
     return fs_set_error(c, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+cudaError_t fs_smem_limit(const void *kernel, size_t bytes) {
+    static std::mutex m;
+    static std::map<std::pair<const void *, int>, size_t> cur;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(m);
+    size_t &v = cur[{kernel, dev}];
+    if (bytes <= v) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) v = bytes;
+    return e;
+}
+
+std::mutex &fs_graph_mutex() {
+    static std::mutex m;
+    return m;
 }
 
 int fs_sync_ctrl(fs_ctx *c) {
@@ -648,6 +668,11 @@ int fs_get_stats(fs_ctx *c, fs_stats *out) {
 void *fs_stream(fs_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int64_t fs_launch_count(fs_ctx *c) { return c ? c->launches : -1; }
+
+int fs_set_stage_tile(fs_ctx *c, int32_t bx, int32_t by) {
+    if (!c) return FS_ERR_INVALID;
+    return fs_set_stage_tile_impl(c, bx, by);
+}
 
 int fs_profile(fs_ctx *c, int32_t enable) {
     if (!c) return FS_ERR_INVALID;

@@ -60,3 +60,98 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
     for (auto &th : pool) th.join();
     return first_rc.load();
 }
+
+// The same advance with the RK stages of all discharges fused: each round
+// runs one RK-Merson attempt of every unfinished discharge that is past its
+// two Poisson-only start-up iterations as one launch per stage over the tiles
+// of all of them (fs_ptcl_batch_attempt: per-discharge dt, its own accept or
+// reject), then -- host threads in parallel, one discharge each -- the
+// Poisson solve (the CUDA graph of its CG loop) and the accept/reject
+// rotation of every discharge whose attempt was accepted.  A rejected
+// attempt is retried in the next round.  Each discharge takes exactly the
+// steps it takes alone.
+int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
+                       int32_t *rc_out) {
+    if (!ctx || n < 1 || steps < 0 || nthreads < 1) return FS_ERR_INVALID;
+    for (int i = 0; i < n; i++) {
+        fs_ctx *c = ctx[i];
+        if (!c) return FS_ERR_INVALID;
+        if (c->mixed || c->cfg.nspecies != 3 || c->cfg.rf != 0 || c->rwall || c->device != ctx[0]->device)
+            return fs_set_error(c, FS_ERR_UNSUPPORTED,
+                                "fused batches take FP64 contexts with 3 species, a DC source, no dielectric wall "
+                                "and one device");
+    }
+    cudaSetDevice(ctx[0]->device);
+    FsBatchWork *w = nullptr;
+    int rc0 = fs_batch_work_alloc(ctx, n, &w);
+    if (rc0) return rc0;
+    std::vector<int> act(n), fresh(n, 1), rej(n, 0), rc(n, FS_OK), done(n, 0), rk(n), pois(n);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long)ctx[a]->nx * ctx[a]->ny > (long)ctx[b]->nx * ctx[b]->ny;
+    });
+    for (int round = 0;; round++) {
+        int nact = 0, nrk = 0;
+        for (int i = 0; i < n; i++) {
+            fs_ctx *c = ctx[i];
+            act[i] = rc[i] == FS_OK && done[i] < steps && !(t_end > 0.0 && c->t >= t_end);
+            rk[i] = act[i] && c->ts > 1;
+            nact += act[i];
+            nrk += rk[i];
+        }
+        if (!nact) break;
+        if (nrk) {
+            const int e = fs_ptcl_batch_attempt(ctx, n, w, rk.data(), fresh.data(), rej.data(), rc.data());
+            if (e) break;
+        }
+        for (int i = 0; i < n; i++) {
+            pois[i] = act[i] && rc[i] == FS_OK && !(rk[i] && rej[i]);
+            fresh[i] = !(rk[i] && rej[i] && rc[i] == FS_OK);
+        }
+        std::atomic<int> next(0);
+        auto worker = [&]() {
+            cudaSetDevice(ctx[0]->device);
+            for (;;) {
+                const int k = next.fetch_add(1);
+                if (k >= n) return;
+                const int i = order[k];
+                if (!pois[i]) continue;
+                fs_ctx *c = ctx[i];
+                int lerr = 1, iters = 0;
+                double relres = 0;
+                int r = fs_lapl_solve_impl(c, &lerr, &iters, &relres);
+                if (r == FS_OK) {
+                    c->st.lapl_iters += iters;
+                    c->st.last_lapl_iters = iters;
+                    c->st.lapl_relres = relres;
+                    c->st.lerr = lerr;
+                    if (lerr == 0) r = fs_accept(c);
+                    else {
+                        c->st.lapl_rejects++;
+                        r = fs_reject(c);
+                    }
+                }
+                rc[i] = r;
+                done[i]++;
+            }
+        };
+        // the first round builds every discharge's CUDA graphs: one thread
+        const int nt = round == 0 ? 1 : std::min<int>(nthreads, nact);
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; t++) pool.emplace_back(worker);
+        worker();
+        for (auto &th : pool) th.join();
+    }
+    fs_batch_work_free(w);
+    int first = FS_OK;
+    for (int i = 0; i < n; i++) {
+        fs_stats st;
+        memset(&st, 0, sizeof(st));
+        if (rc[i] == FS_OK) rc[i] = fs_get_stats(ctx[i], &st);
+        if (out) out[i] = st;
+        if (rc_out) rc_out[i] = rc[i];
+        if (rc[i] != FS_OK && first == FS_OK) first = rc[i];
+    }
+    return first;
+}

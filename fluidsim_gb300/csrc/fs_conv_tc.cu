@@ -1,9 +1,10 @@
 // fs_conv_tc.cu -- 3x3 convolutions of the learned preconditioner on the
 // Blackwell tensor cores (tcgen05), fed by the tensor memory accelerator.
 //
-// Implicit GEMM, one CTA per tile of 128 output pixels (TW x TH pixels of one
-// image, TW = min(128, W) rounded up to a power of two): D[128 px][cout] =
-// sum over the 9 taps and the input channels of A[px][cin] W[cin][cout].
+// Implicit GEMM over tiles of 128 output pixels (TW x TH pixels of one image,
+// TW = min(128, W) rounded up to a power of two): D[128 px][cout] = sum over
+// the 9 taps and the input channels of A[px][cin] W[cin][cout].  Persistent
+// CTAs (as many as fit on the SMs) take the tiles in turn.
 //   * A: for each tap (dy, dx) and each source tensor (the decoder's
 //     concatenation has two), the tile's input pixels shifted by (dy, dx) --
 //     one TMA load of a TW x TH x kc box of the NHWC BF16 activations, with
@@ -12,13 +13,14 @@
 //   * B: the layer's weights, stored once per refresh as the exact shared-
 //     memory image the MMA reads (K-major, swizzled, one block per tap and
 //     source), copied in by one bulk copy;
-//   * one thread issues the TMA loads into a ring of A stages, one thread
-//     issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128, N = cout)
-//     with the accumulator in tensor memory, and tcgen05.commit frees each
-//     A stage when its MMAs are done;
-//   * the four warps then read the accumulator (tcgen05.ld, one pixel per
+//   * one thread issues the TMA loads into a ring of A stages that runs on
+//     across the CTA's tiles, one thread issues tcgen05.mma (kind::f16,
+//     BF16 x BF16 -> FP32, M = 128, N = cout) into one of two accumulators
+//     in tensor memory, and tcgen05.commit frees each A stage when its MMAs
+//     are done and hands a finished accumulator to the epilogue;
+//   * four warps read the other accumulator (tcgen05.ld, one pixel per
 //     thread) and apply bias, ReLU (or the ReLU mask of the backward pass)
-//     and the BF16 store.
+//     and the BF16 store while the next tile's MMAs run.
 // Every wait on an mbarrier is bounded: a wait that runs out sets *err and
 // the CTA skips the rest of its work (after a bounded wait for its own
 // copies and MMAs in flight) and frees its tensor memory.
@@ -31,8 +33,8 @@
 
 namespace {
 
-constexpr int kStages = 4;                 // A ring depth
-constexpr int kStageBytes = 128 * 64 * 2;  // largest A tile: 128 px x 64 ch BF16
+constexpr int kMaxStages = 32;             // A ring depth at most
+constexpr int kRingBudget = 96 * 1024;     // shared memory the A ring may take
 constexpr long kSpinLimit = 1L << 20;      // bounded waits (each try_wait may sleep ~us)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -125,42 +127,49 @@ __device__ __forceinline__ void tmem_ld16(uint32_t addr, float (&v)[16]) {
 __device__ __host__ __forceinline__ uint32_t swz_mode(int kc) { return kc == 64 ? 2u : kc == 32 ? 4u : 6u; }
 __device__ __host__ __forceinline__ uint32_t swz_atom(int kc) { return 8u * 2u * (uint32_t)kc; }
 
-__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tm0,
+// Persistent: each CTA loops over tiles blockIdx.x, + gridDim.x, ...  Warp 4
+// (one thread) streams the A chunks of its tiles through a ring of nst
+// stages; warp 5 (one thread) issues the MMAs of a tile into one of two
+// accumulators in tensor memory while warps 0-3 drain the other (TMEM lane
+// quarter w to warp w), so loads, MMAs and the epilogue of consecutive tiles
+// overlap.
+__global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUtensorMap tm0,
                                                     const __grid_constant__ CUtensorMap tm1, const TcConvArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int nst = a.nst;
     uint8_t *sw = smem;                               // weight image
-    uint8_t *sa = smem + a.wbytes;                    // A stages (wbytes is a multiple of 1024)
-    uint64_t *full = reinterpret_cast<uint64_t *>(sa + kStages * kStageBytes);
-    uint64_t *empty = full + kStages;
-    uint64_t *wbar = empty + kStages;
-    uint64_t *done = wbar + 1;
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    uint8_t *sa = smem + a.wbytes;                    // A stages (wbytes and stage_bytes are multiples of 1024)
+    uint64_t *full = reinterpret_cast<uint64_t *>(sa + (size_t)nst * a.stage_bytes);
+    uint64_t *empty = full + nst;
+    uint64_t *tfull = empty + nst;                    // accumulator b ready (MMA -> epilogue)
+    uint64_t *tempty = tfull + 2;                     // accumulator b drained (epilogue -> MMA)
+    uint64_t *wbar = tempty + 2;
+    uint64_t *fin = wbar + 1;                         // every MMA of this CTA complete
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
     __shared__ int s_fail;
+    volatile int *vfail = &s_fail;   // raised by any role whose wait ran out
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int tile = blockIdx.x;
-    const int tx = tile % a.tiles_x;
-    tile /= a.tiles_x;
-    const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
-    const int x0 = tx * a.TW, y0 = ty * a.TH;
     const int nper = a.nchunk[0] + a.nchunk[1];       // K chunks per tap
     const int nk = 9 * nper;
+    const int ntile_cta = blockIdx.x < a.ntiles ? (a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     if (threadIdx.x == 0) {
         // a CTA of this launch whose wait ran out voids the result: skip the work
         s_fail = *reinterpret_cast<volatile int *>(a.err) ? 2 : 0;
-        for (int s = 0; s < kStages; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
+        for (int s = 0; s < nst; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
+        for (int s = 0; s < 2; ++s) { mbar_init(tfull + s, 1); mbar_init(tempty + s, 4); }
         mbar_init(wbar, 1);
-        mbar_init(done, 1);
+        mbar_init(fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    if (s_fail == 2) return;   // uniform over the CTA
-    if (warp == 0) {
+    if (s_fail == 2 || ntile_cta == 0) return;   // uniform over the CTA
+    if (warp == 4) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                     "r"((uint32_t)a.tmem_cols)
+                     "r"((uint32_t)(2 * a.tmem_cols))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -169,101 +178,132 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (warp == 0 && lane == 0) {
-        // producer: the weight image, then the A chunks tap by tap
+    if (warp == 4 && lane == 0) {
+        // producer: the weight image, then the A chunks of each tile, tap by tap
         mbar_expect_tx(wbar, (uint32_t)a.wbytes);
         bulk_copy(sw, a.wimg, (uint32_t)a.wbytes, wbar);
-        for (int kc = 0; kc < nk; ++kc) {
-            const int s = kc % kStages, n = kc / kStages;
-            if (n > 0 && !mbar_wait(empty + s, (uint32_t)((n - 1) & 1))) { atomicExch(&s_fail, 1); break; }
-            const int t = kc / nper, q = kc - t * nper;
-            const int src = q < a.nchunk[0] ? 0 : 1, j = src ? q - a.nchunk[0] : q;
-            const int kcw = a.kc[src];
-            mbar_expect_tx(full + s, (uint32_t)(128 * kcw * 2));
-            tma_load_4d(sa + s * kStageBytes, src ? &tm1 : &tm0, j * kcw, x0 + t % 3 - 1, y0 + t / 3 - 1, b,
-                        full + s);
+        long g = 0;   // chunks issued
+        for (int it = 0; it < ntile_cta && !*vfail; ++it) {
+            int tile = blockIdx.x + it * gridDim.x;
+            const int tx = tile % a.tiles_x;
+            tile /= a.tiles_x;
+            const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
+            const int x0 = tx * a.TW, y0 = ty * a.TH;
+            for (int kc = 0; kc < nk; ++kc, ++g) {
+                const int s = (int)(g % nst);
+                const long n = g / nst;
+                if (n > 0 && !mbar_wait(empty + s, (uint32_t)((n - 1) & 1))) { atomicExch(&s_fail, 1); break; }
+                const int t = kc / nper, q = kc - t * nper;
+                const int src = q < a.nchunk[0] ? 0 : 1, j = src ? q - a.nchunk[0] : q;
+                const int kcw = a.kc[src];
+                mbar_expect_tx(full + s, (uint32_t)(128 * kcw * 2));
+                tma_load_4d(sa + (size_t)s * a.stage_bytes, src ? &tm1 : &tm0, j * kcw, x0 + t % 3 - 1,
+                            y0 + t / 3 - 1, b, full + s);
+            }
         }
-    } else if (warp == 1 && lane == 0) {
+        // leave no copy in flight: the last nst chunks issued are complete
+        for (long h = g - nst > 0 ? g - nst : 0; h < g; ++h)
+            mbar_wait(full + (int)(h % nst), (uint32_t)((h / nst) & 1));
+    } else if (warp == 5 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.cout >> 3) << 17) |
                                ((uint32_t)(128 >> 4) << 24);
         bool ok = mbar_wait(wbar, 0);
-        for (int kc = 0; ok && kc < nk; ++kc) {
-            const int s = kc % kStages, n = kc / kStages;
-            if (!mbar_wait(full + s, (uint32_t)(n & 1))) { ok = false; break; }
+        long g = 0;
+        for (int it = 0; ok && it < ntile_cta; ++it) {
+            const int bs = it & 1, u = it >> 1;
+            if (u > 0 && !mbar_wait(tempty + bs, (uint32_t)((u - 1) & 1))) { ok = false; break; }
             tc_fence_after();
-            const int t = kc / nper, q = kc - t * nper;
-            const int src = q < a.nchunk[0] ? 0 : 1;
-            const int kcw = a.kc[src];
-            const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
-            const uint32_t abase = smem_u32(sa + s * kStageBytes);
-            const uint32_t bbase = smem_u32(sw + a.boff[t * nper + q]);
-            for (int k = 0; k < kcw / 16; ++k)
-                mma_bf16(tmem, smem_desc(abase + 32 * k, atom, mode), smem_desc(bbase + 32 * k, atom, mode), idesc,
-                         (kc > 0 || k > 0) ? 1u : 0u);
-            mma_commit(empty + s);
+            const uint32_t acc = tmem + (uint32_t)(bs * a.tmem_cols);
+            for (int kc = 0; kc < nk; ++kc, ++g) {
+                const int s = (int)(g % nst);
+                if (!mbar_wait(full + s, (uint32_t)((g / nst) & 1)) || *vfail) { ok = false; break; }
+                tc_fence_after();
+                const int t = kc / nper, q = kc - t * nper;
+                const int src = q < a.nchunk[0] ? 0 : 1;
+                const int kcw = a.kc[src];
+                const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
+                const uint32_t abase = smem_u32(sa + (size_t)s * a.stage_bytes);
+                const uint32_t bbase = smem_u32(sw + a.boff[t * nper + q]);
+                for (int k = 0; k < kcw / 16; ++k)
+                    mma_bf16(acc, smem_desc(abase + 32 * k, atom, mode), smem_desc(bbase + 32 * k, atom, mode),
+                             idesc, (kc > 0 || k > 0) ? 1u : 0u);
+                mma_commit(empty + s);
+            }
+            if (ok) mma_commit(tfull + bs);
         }
-        if (ok) mma_commit(done);
-        else atomicExch(&s_fail, 1);
-    }
-    __syncwarp();
-
-    // epilogue: thread = one pixel of the tile (its TMEM lane)
-    bool ok = mbar_wait(done, 0);
-    ok = __all_sync(0xffffffffu, ok);   // warp-uniform (tcgen05.ld is warp-collective)
-    if (!ok) atomicExch(&s_fail, 1);
-    tc_fence_after();
-    const int p = warp * 32 + lane;
-    const int px = x0 + p % a.TW, py = y0 + p / a.TW;
-    const bool in = px < a.W && py < a.H;
-    const long pix = ((long)b * a.H + py) * a.W + px;
-    if (ok) {
-        for (int c0 = 0; c0 < a.cout; c0 += 16) {
-            float v[16];
-            __syncwarp();
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (!in) continue;
-            if (a.out32) {
+        if (!ok) atomicExch(&s_fail, 1);
+        // every MMA this thread issued has completed before the memory goes back
+        mma_commit(fin);
+        mbar_wait(fin, 0);
+    } else if (warp < 4) {
+        // epilogue: thread = one pixel of the tile (its TMEM lane)
+        const int p = warp * 32 + lane;
+        for (int it = 0; it < ntile_cta; ++it) {
+            const int bs = it & 1, u = it >> 1;
+            bool ok = mbar_wait(tfull + bs, (uint32_t)(u & 1));
+            ok = __all_sync(0xffffffffu, ok);   // warp-uniform (tcgen05.ld is warp-collective)
+            if (!ok) { atomicExch(&s_fail, 1); break; }
+            tc_fence_after();
+            int tile = blockIdx.x + it * gridDim.x;
+            const int tx = tile % a.tiles_x;
+            tile /= a.tiles_x;
+            const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
+            const int px = tx * a.TW + p % a.TW, py = ty * a.TH + p / a.TW;
+            const bool in = px < a.W && py < a.H;
+            const long pix = ((long)b * a.H + py) * a.W + px;
+            const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(bs * a.tmem_cols);
+            for (int c0 = 0; c0 < a.cout; c0 += 16) {
+                float v[16];
+                __syncwarp();
+                tmem_ld16(acc + (uint32_t)c0, v);
+                if (!in) continue;
+                if (a.out32) {
 #pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + a.bias[c0 + i];
-                continue;
-            }
-            // BF16 output, split over up to two tensors (the backward pass's
-            // concatenated inputs): channels [0, split) to out, the rest to out2
-            __nv_bfloat16 *dst;
-            int cc, cs;
-            const __nv_bfloat16 *msk;
-            if (c0 < a.split) { dst = a.out; cc = c0; cs = a.split; msk = a.mask; }
-            else { dst = a.out2; cc = c0 - a.split; cs = a.cout - a.split; msk = a.mask2; }
-            uint32_t pk[8];
-#pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-                float u0 = v[i] + (a.bias ? a.bias[c0 + i] : 0.0f), u1 = v[i + 1] + (a.bias ? a.bias[c0 + i + 1] : 0.0f);
-                if (a.relu) { u0 = fmaxf(u0, 0.0f); u1 = fmaxf(u1, 0.0f); }
-                if (msk) {
-                    const __nv_bfloat16 *m = msk + pix * cs + cc + i;
-                    if (!(__bfloat162float(m[0]) > 0.0f)) u0 = 0.0f;
-                    if (!(__bfloat162float(m[1]) > 0.0f)) u1 = 0.0f;
+                    for (int i = 0; i < 16; ++i)
+                        if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + a.bias[c0 + i];
+                    continue;
                 }
-                const __nv_bfloat162 h = __floats2bfloat162_rn(u0, u1);
-                pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                // BF16 output, split over up to two tensors (the backward pass's
+                // concatenated inputs): channels [0, split) to out, the rest to out2
+                __nv_bfloat16 *dst;
+                int cc, cs;
+                const __nv_bfloat16 *msk;
+                if (c0 < a.split) { dst = a.out; cc = c0; cs = a.split; msk = a.mask; }
+                else { dst = a.out2; cc = c0 - a.split; cs = a.cout - a.split; msk = a.mask2; }
+                uint32_t pk[8];
+#pragma unroll
+                for (int i = 0; i < 16; i += 2) {
+                    float u0 = v[i] + (a.bias ? a.bias[c0 + i] : 0.0f);
+                    float u1 = v[i + 1] + (a.bias ? a.bias[c0 + i + 1] : 0.0f);
+                    if (a.relu) { u0 = fmaxf(u0, 0.0f); u1 = fmaxf(u1, 0.0f); }
+                    if (msk) {
+                        const __nv_bfloat16 *m = msk + pix * cs + cc + i;
+                        if (!(__bfloat162float(m[0]) > 0.0f)) u0 = 0.0f;
+                        if (!(__bfloat162float(m[1]) > 0.0f)) u1 = 0.0f;
+                    }
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(u0, u1);
+                    pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                }
+                uint4 *o = reinterpret_cast<uint4 *>(dst + pix * cs + cc);
+                o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
             }
-            uint4 *o = reinterpret_cast<uint4 *>(dst + pix * cs + cc);
-            o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-            o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            // this warp's lanes of accumulator bs are read: hand it back
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty + bs))
+                                        : "memory");
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (s_fail && threadIdx.x == 0) {
-        atomicExch(a.err, 1);
-        // a bounded wait for the copies and MMAs this CTA may still have in flight
-        mbar_wait(done, 0);
-    }
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)a.tmem_cols)
+    if (s_fail && threadIdx.x == 0) atomicExch(a.err, 1);
+    tc_fence_after();
+    __syncwarp();
+    if (warp == 4)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"((uint32_t)(2 * a.tmem_cols))
                      : "memory");
 }
 
@@ -377,14 +417,32 @@ void tc_build_weights_bwd(const float *w, int cin, int cout, void *img, cudaStre
     build_image(w, cout, 0, cin, img, 1, st);
 }
 
-size_t tc_smem_bytes(int wbytes) {
-    return 1024 + (size_t)wbytes + (size_t)kStages * kStageBytes + 8 * (2 * kStages + 2) + 16;
+// A ring of a layer: stages of 128 pixels x the larger K chunk, as many as
+// fit the budget and the limit left by the weight image (at least 2, at most
+// the chunks of one tile)
+static void ring_shape(const TcConvArgs &a, size_t limit, int &nst, int &stage_bytes) {
+    const int kcmax = a.kc[0] > a.kc[1] ? a.kc[0] : a.kc[1];
+    stage_bytes = 128 * kcmax * 2;
+    const int nk = 9 * (a.nchunk[0] + a.nchunk[1]);
+    long room = (long)limit - 1024 - a.wbytes - 256;
+    if (room > kRingBudget) room = kRingBudget;
+    nst = (int)(room / stage_bytes);
+    if (nst > kMaxStages) nst = kMaxStages;
+    if (nst > nk) nst = nk;   // one tile ahead: a deeper ring costs CTAs per SM (measured slower)
+    if (nst < 2) nst = 2;
+}
+
+size_t tc_smem_bytes(int wbytes, int nst, int stage_bytes) {
+    return 1024 + (size_t)wbytes + (size_t)nst * stage_bytes + 8 * (2 * (size_t)nst + 6) + 16;
 }
 
 namespace {
 // the dynamic shared memory a launch may take: the device's opt-in limit
-// per block less the kernel's static shared memory
+// per block less the kernel's static shared memory; the SM count
 size_t g_smem_max = 0;
+size_t g_smem_sm = 0;   // shared memory per SM
+int g_nsm = 0;
+int g_regs = 0;         // registers per thread of the kernel
 }  // namespace
 
 int tc_init() {
@@ -398,17 +456,44 @@ int tc_init() {
         return -2;
     const int dyn = optin - (int)fa.sharedSizeBytes;
     if (cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) return -2;
+    // all of the unified L1/shared storage as shared memory, so that several
+    // CTAs fit on an SM (the kernel reads nothing through L1)
+    if (cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        return -2;
+    int smsm = 0;
+    if (cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+        return -2;
+    g_smem_sm = (size_t)smsm;
+    g_regs = fa.numRegs;
     g_smem_max = (size_t)dyn;
     return 0;
 }
 
 size_t tc_smem_limit() { return g_smem_max; }
 
-int tc_conv(const CUtensorMap *m0, const CUtensorMap *m1, const TcConvArgs &a, cudaStream_t st) {
-    const size_t smem = tc_smem_bytes(a.wbytes);
-    if (!g_smem_max || smem > g_smem_max) return -2;
-    const int grid = a.tiles_x * a.tiles_y * a.B;
-    k_conv_tc<<<grid, 128, smem, st>>>(*m0, m1 ? *m1 : *m0, a);
+int tc_conv(const CUtensorMap *m0, const CUtensorMap *m1, const TcConvArgs &a0, cudaStream_t st) {
+    if (!g_smem_max) return -2;
+    TcConvArgs a = a0;
+    ring_shape(a, g_smem_max, a.nst, a.stage_bytes);
+    const size_t smem = tc_smem_bytes(a.wbytes, a.nst, a.stage_bytes);
+    if (smem > g_smem_max) return -2;
+    a.ntiles = a.tiles_x * a.tiles_y * a.B;
+    // CTAs per SM: what shared memory allows, and two accumulators each in
+    // the 512 tensor-memory columns
+    // (counted here from the kernel's registers and the SM's shared memory:
+    // the occupancy query answers 1 for this kernel, while three 47 KB CTAs
+    // are resident at once when launched one tile per CTA)
+    const int by_smem = (int)(g_smem_sm / (smem + 1024));
+    const int regs_cta = ((g_regs + 7) / 8 * 8) * 192;
+    const int by_regs = 65536 / regs_cta;
+    int per_sm = by_smem < by_regs ? by_smem : by_regs;
+    const int tmem_cap = 512 / (2 * a.tmem_cols);
+    if (per_sm > tmem_cap) per_sm = tmem_cap;
+    if (per_sm < 1) return -2;
+    const long grid = (long)g_nsm * per_sm < a.ntiles ? (long)g_nsm * per_sm : a.ntiles;
+    k_conv_tc<<<(int)grid, 192, smem, st>>>(*m0, m1 ? *m1 : *m0, a);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : -100 - (int)e;
 }

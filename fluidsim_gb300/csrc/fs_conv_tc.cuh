@@ -26,6 +26,7 @@ struct TcConvArgs {
     float *out32;              // FP32 output [pix][out32_ch] instead of BF16 (null: BF16)
     int out32_ch;
     int *err;                  // set to 1 if a wait ran out
+    int nst, stage_bytes, ntiles;   // A ring and tile count (set by tc_conv)
 };
 
 // pixel tile of a grid W wide: TW = min(128, W) rounded up to a power of two
@@ -44,12 +45,12 @@ void tc_build_weights(const float *w, int c1, int c2, int cout, void *img, cudaS
 void tc_build_weights_bwd(const float *w, int cin, int cout, void *img, cudaStream_t st);
 // tensor-memory columns of an accumulator of n FP32 columns (a power of two >= 32)
 int tc_tmem_cols(int n);
-// dynamic shared memory of a launch
-size_t tc_smem_bytes(int wbytes);
+// dynamic shared memory of a launch with an A ring of nst stages
+size_t tc_smem_bytes(int wbytes, int nst, int stage_bytes);
 // once per process before the first launch (outside any stream capture):
 // the kernel's shared-memory limit; 0 or a negative error
 int tc_init();
 // the dynamic shared memory a launch may take (0 before tc_init)
 size_t tc_smem_limit();
-// launch over every tile; m1 may be null (one source)
+// launch: persistent CTAs over every tile; m1 may be null (one source)
 int tc_conv(const CUtensorMap *m0, const CUtensorMap *m1, const TcConvArgs &a, cudaStream_t st);

@@ -8,6 +8,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -158,6 +159,7 @@ struct fs_ctx {
     double *ph, *ph_mi;
     double *d_part;              // per-block partial sums (4 species)
     int nblk_stage;              // blocks of one stage launch
+    int stage_bx, stage_by;      // its tile shape (FP64 path)
     double *d_rows;              // per-row current contributions (2*(ny+2))
     // sfc_lib state (dielectric wall, type_y == 3 on the last row): three
     // slots of nx+2 charges (Fortran sig(i) at [i-1]) holding sig_pl, sig_mi,
@@ -265,6 +267,12 @@ inline double *fs_sig(fs_ctx *c, int which) { return c->d_sig + (size_t)c->sig_s
 inline double *fs_sig_ks(fs_ctx *c) { return c->d_sig + (size_t)3 * (c->nx + 2); }
 int fs_sig_copy(fs_ctx *c, int dst, int src);   // slot dst <- slot src, on the stream
 void fs_faces_update(fs_ctx *c);   // recompute the face data if phi changed
+// many discharges, one launch per RK stage (fs_ptcl.cu; DC, FP64, no wall)
+struct FsBatchWork;
+int fs_set_stage_tile_impl(fs_ctx *c, int bx, int by);
+int fs_batch_work_alloc(fs_ctx **cs, int n, FsBatchWork **out);
+void fs_batch_work_free(FsBatchWork *w);
+int fs_ptcl_batch_attempt(fs_ctx **cs, int n, FsBatchWork *w, const int *act, const int *fresh, int *rej, int *rc);
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
 int fs_mg_strips(fs_ctx *c);    // electrode strips of the finest level (strip_kl, strip_kr) and their snapshot
@@ -286,6 +294,16 @@ void fs_output_free(fs_ctx *c);
 int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out);
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);
 int fs_sync_ctrl(fs_ctx *c);
+// Held while a context captures and instantiates its CUDA graphs: captures
+// of several contexts from several host threads at once (the batch drivers'
+// first solves) have failed and left an invalid graph behind.
+std::mutex &fs_graph_mutex();
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The limit belongs to the kernel, not to a context: every
+// context asks for what its grid needs and the largest request stays in
+// force (setting it per context let a later, smaller grid lower it below
+// what an earlier context's launches take).
+cudaError_t fs_smem_limit(const void *kernel, size_t bytes);
 // profiler: bracket one launch; drained at every fs_sync_ctrl
 void fs_prof_begin(fs_ctx *c, int cls);
 void fs_prof_end(fs_ctx *c);

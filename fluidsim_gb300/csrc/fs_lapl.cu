@@ -549,14 +549,12 @@ int fs_mg_strips(fs_ctx *c) {
         e = cudaMalloc(&c->strip_snap32, n * sizeof(float));
         if (e == cudaSuccess) e = cudaMemset(c->strip_snap32, 0, n * sizeof(float));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_rb_strips<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)strip_smem<float>(c->strip_w));
+            e = fs_smem_limit((const void *)k_rb_strips<float>, strip_smem<float>(c->strip_w));
     } else {
         e = cudaMalloc(&c->strip_snap64, n * sizeof(double));
         if (e == cudaSuccess) e = cudaMemset(c->strip_snap64, 0, n * sizeof(double));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_rb_strips<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)strip_smem<double>(c->strip_w));
+            e = fs_smem_limit((const void *)k_rb_strips<double>, strip_smem<double>(c->strip_w));
     }
     return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "strip snapshot");
 }
@@ -599,8 +597,7 @@ int fs_lapl_alloc(fs_ctx *c) {
         ba.dl = bottom_dense_level(ba);
         c->mg_lb = ba.lb;
         c->mg_dl = ba.dl;
-        cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bottom_smem_bytes(ba));
+        cudaError_t e = fs_smem_limit((const void *)k_bottom_smem<double>, bottom_smem_bytes(ba));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
         if ((e = cudaMalloc(&c->d_ainv64, 64 * 64 * sizeof(double))) != cudaSuccess)
             return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
@@ -634,8 +631,7 @@ int fs_lapl_alloc(fs_ctx *c) {
         bf.lb = c->mg_lb;
         bf.dl = c->mg_dl;
         for (int l = 0; l < nl; l++) { bf.L[l].nx = c->mg[l].nx; bf.L[l].ny = c->mg[l].ny; }
-        e = cudaFuncSetAttribute(k_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bottom_smem_bytes(bf));
+        e = fs_smem_limit((const void *)k_bottom_smem<float>, bottom_smem_bytes(bf));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
     }
     size_t n0 = (size_t)(c->ny + 2) * c->pitch;
@@ -823,6 +819,7 @@ static void cg_iteration(fs_ctx *c, const CgArgs &ca, dim3 gb) {
 // Graph: WHILE(cond) { one PCG iteration } -> phi update.  The last CTA of the
 // residual reduction clears cond on convergence, breakdown or the iteration cap.
 static int build_cg_graph(fs_ctx *c, CgArgs ca) {
+    std::lock_guard<std::mutex> lock(fs_graph_mutex());
     cudaGraph_t g = nullptr;
     cudaGraphConditionalHandle h;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -858,7 +855,7 @@ static int build_cg_graph(fs_ctx *c, CgArgs ca) {
     c->prof_on = prof;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cg_exec, g, 0);
     if (e != cudaSuccess) {
-        cudaGraphDestroy(g);
+        if (g) cudaGraphDestroy(g);
         return fs_cuda_check(c, e, "CG graph capture");
     }
     c->cg_graph = g;

@@ -819,8 +819,7 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
         while (ba.lb < ba.nl && (c->mgf[ba.lb].nx > BOTTOM_N || c->mgf[ba.lb].ny > BOTTOM_N)) ba.lb++;
         for (int l = 0; l < ba.nl; l++) { ba.L[l].nx = c->mgf[l].nx; ba.L[l].ny = c->mgf[l].ny; }
         ba.dl = bottom_dense_level(ba);
-        cudaError_t e = cudaFuncSetAttribute(k_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bottom_smem_bytes(ba));
+        cudaError_t e = fs_smem_limit((const void *)k_bottom_smem<float>, bottom_smem_bytes(ba));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "bottom solver shared memory");
         if ((e = cudaMalloc(&c->d_ainv32, 64 * 64 * sizeof(float))) != cudaSuccess)
             return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
@@ -970,6 +969,7 @@ static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
 
 // WHILE(cond) { one iteration } -> phi update, as one graph (see fs_lapl.cu)
 static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
+    std::lock_guard<std::mutex> lock(fs_graph_mutex());
     cudaGraph_t g = nullptr;
     cudaGraphConditionalHandle h;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -1006,7 +1006,7 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     c->prof_on = prof;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cgm_exec[v], g, 0);
     if (e != cudaSuccess) {
-        cudaGraphDestroy(g);
+        if (g) cudaGraphDestroy(g);
         return fs_cuda_check(c, e, "CG graph capture");
     }
     c->cgm_graph[v] = g;
@@ -1035,6 +1035,8 @@ static void lpc_account(fs_ctx *c, const CgmArgs &ca, double ms) {
     if (c->lpc_t_nn < 0.0) pref = 1;
     else if (c->lpc_t_plain < 0.0) pref = 0;
     else pref = c->lpc_t_nn <= c->lpc_t_plain ? 1 : 0;
+    // a network solve more than twice as slow as a plain one: probe rarely
+    if (c->lpc_t_nn > 0.0 && c->lpc_t_plain > 0.0 && c->lpc_t_nn > 2.0 * c->lpc_t_plain) c->lpc_probe_every = 400;
     if (c->lpc_probe_pending) {
         c->lpc_probe_pending = 0;
         if (pref == (ca.lpc ? 1 : 0)) c->lpc_probe_every = 25;

@@ -19,17 +19,17 @@
 // A one-CTA controller kernel then applies the PI step-size control of
 // ptcl_lib.F90:59-95 on the device.
 #include <cstdio>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "fs_fastmath.cuh"
 #include "fs_internal.h"
 #include "fs_sg.cuh"
 
-#define BX 32
-#define BY 8
-#define NT (BX * BY)
-#define HX (BX + 2)
-#define HY (BY + 2)
+// stage tiles: 32 x 8 nodes by default; 32 x 4 and 64 x 4 selectable per
+// context (fs_set_stage_tile); the partial sums are sized for the most tiles
+#define DEF_BX 32
+#define DEF_BY 8
 
 namespace {
 
@@ -161,8 +161,9 @@ __device__ __noinline__ double wall_face(const StageArgs &a, int gi, double te, 
 
 // One RK stage on the tile (bx, by) of the grid (BX x BY nodes); blk is the
 // tile's index among the grid's tiles (its slot in the error partials).
-template <int NS>
+template <int NS, int TBX, int TBY>
 __device__ __forceinline__ void stage_tile(const StageArgs &a, int bx, int by, int blk) {
+    constexpr int BX = TBX, BY = TBY, NT = BX * BY, HX = BX + 2, HY = BY + 2;
     __shared__ double s_n[NS][HY][HX];
     __shared__ double s_ph[HY][HX];
     __shared__ double s_te[HY][HX];
@@ -437,9 +438,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs &a, int bx, int by, i
     }
 }
 
-template <int NS>
-__global__ void __launch_bounds__(NT, 2) k_stage(const StageArgs a) {
-    stage_tile<NS>(a, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
+template <int NS, int TBX, int TBY>
+__global__ void __launch_bounds__(TBX * TBY, 2) k_stage(const StageArgs a) {
+    stage_tile<NS, TBX, TBY>(a, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Ion face coefficients while phi is frozen.  get_Flux for q = +1
@@ -600,9 +601,9 @@ __global__ void __launch_bounds__(256) k_circuit(Ctrl *c, const double *rows, do
 
 // PI controller of ptcl_lib.F90:59-95 plus the current sums of circ_step.
 // All sums are fixed-order: strided per-thread partials, then a fixed tree.
-__global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part, int nblk, int ns,
-                                                    const double *rows, int ny, int adaptive,
-                                                    double dt_min) {
+// One CTA of 256 threads.
+__device__ __forceinline__ void controller_body(Ctrl *c, const double *part, int nblk, int ns, const double *rows,
+                                                int ny, int adaptive, double dt_min) {
     __shared__ double s[FS_MAX_SPECIES + 2][256];
     const int t = threadIdx.x;
     for (int sp = 0; sp < ns; sp++) {
@@ -642,10 +643,82 @@ __global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part,
     else c->rejected = 1;
 }
 
+__global__ void __launch_bounds__(256) k_controller(Ctrl *c, const double *part, int nblk, int ns,
+                                                    const double *rows, int ny, int adaptive, double dt_min) {
+    controller_body(c, part, nblk, ns, rows, ny, adaptive, dt_min);
+}
+
 __global__ void k_reset_step(Ctrl *c, double *rows, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) { c->t_m = 1e9; c->status = 0; c->rejected = 0; c->min_dt = 0; }
     if (i < n) rows[i] = 0.0;
+}
+
+// ---- many discharges in one launch per RK stage (fs_ptcl_batch_attempt)
+// Tile q of the batch: x = discharge, (y, z) = tile coordinates in its grid,
+// w = the tile's index among that grid's tiles.
+template <int NS, int TBX, int TBY>
+__global__ void __launch_bounds__(TBX * TBY, 2) k_stage_batch(const StageArgs *args, const int4 *tiles,
+                                                              const int *act) {
+    const int4 t = tiles[blockIdx.x];
+    if (!act[t.x]) return;   // uniform over the CTA
+    stage_tile<NS, TBX, TBY>(args[t.x], t.y, t.z, t.w);
+}
+
+struct BatchCtl {
+    Ctrl *ctrl;
+    const double *part, *rows;
+    double *rows_w;
+    int nblk, ns, ny, adaptive;
+    double dt_min;
+    // circ_step ghosts (DC)
+    double *ph, *fx_e;
+    const int8_t *tx;
+    const double *r, *dx;
+    int nx, P;
+    double ew, vd;
+};
+
+// start of a step of discharge b (fresh[b]): t_m, status and current rows
+__global__ void __launch_bounds__(256) k_reset_batch(const BatchCtl *bc, const int *act, const int *fresh) {
+    const int b = blockIdx.x;
+    if (!act[b] || !fresh[b]) return;
+    const BatchCtl &q = bc[b];
+    if (threadIdx.x == 0) { q.ctrl->t_m = 1e9; q.ctrl->status = 0; q.ctrl->rejected = 0; q.ctrl->min_dt = 0; }
+    for (int i = threadIdx.x; i < 2 * (q.ny + 2); i += blockDim.x) q.rows_w[i] = 0.0;
+}
+
+__global__ void __launch_bounds__(128) k_circ_ghost_batch(const BatchCtl *bc, const int *act) {
+    const int b = blockIdx.x;
+    if (!act[b]) return;
+    const BatchCtl &q = bc[b];
+    for (int gj = 1 + threadIdx.x; gj <= q.ny; gj += blockDim.x) {
+        const size_t o = (size_t)gj * q.P;
+        if (q.r[gj] <= q.ew) {
+            if (q.tx[(gj - 1) * q.nx + 0] == -2) {
+                q.ph[o + 0] = q.vd / 2.0;
+                q.fx_e[o + 0] = -(q.ph[o + 1] - q.ph[o + 0]) / q.dx[0];
+            }
+            if (q.tx[(gj - 1) * q.nx + q.nx - 1] == 2) {
+                q.ph[o + q.nx + 1] = q.vd / (-2.0);
+                q.fx_e[o + q.nx] = -(q.ph[o + q.nx + 1] - q.ph[o + q.nx]) / q.dx[q.nx];
+            }
+        }
+    }
+}
+
+// the controller of every discharge in the batch (one CTA each), then its
+// control block copied into the batch's gathered array
+__global__ void __launch_bounds__(256) k_controller_batch(const BatchCtl *bc, const int *act, Ctrl *gathered) {
+    const int b = blockIdx.x;
+    if (!act[b]) return;
+    const BatchCtl &q = bc[b];
+    controller_body(q.ctrl, q.part, q.nblk, q.ns, q.rows, q.ny, q.adaptive, q.dt_min);
+    __syncthreads();
+    __threadfence_block();
+    const uint64_t *src = reinterpret_cast<const uint64_t *>(q.ctrl);
+    uint64_t *dst = reinterpret_cast<uint64_t *>(gathered + b);
+    for (int i = threadIdx.x; i < (int)(sizeof(Ctrl) / 8); i += blockDim.x) dst[i] = src[i];
 }
 
 }  // namespace
@@ -666,14 +739,18 @@ int fs_sig_copy(fs_ctx *c, int dst, int src) {
     return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "surface charge copy");
 }
 
+static int stage_tiles(const fs_ctx *c, int bx, int by) { return ((c->nx + bx - 1) / bx) * ((c->ny + by - 1) / by); }
+
 int fs_ptcl_alloc(fs_ctx *c) {
-    dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
-    c->nblk_stage = grid.x * grid.y;
+    c->stage_bx = DEF_BX;
+    c->stage_by = DEF_BY;
+    c->nblk_stage = stage_tiles(c, c->stage_bx, c->stage_by);
+    const int nblk_max = stage_tiles(c, 32, 4);   // the shape with the most tiles
     cudaError_t e = cudaMalloc(&c->d_sig, sizeof(double) * 8 * (c->nx + 2));
     if (e == cudaSuccess) e = cudaMemset(c->d_sig, 0, sizeof(double) * 8 * (c->nx + 2));
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc surface charge");
     for (int q = 0; q < 3; q++) c->sig_slot[q] = q;
-    e = cudaMalloc(&c->d_part, sizeof(double) * FS_MAX_SPECIES * c->nblk_stage);
+    e = cudaMalloc(&c->d_part, sizeof(double) * FS_MAX_SPECIES * nblk_max);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc partials");
     e = cudaMalloc(&c->d_rows, sizeof(double) * 2 * (c->ny + 2));
     if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc rows");
@@ -688,10 +765,30 @@ int fs_ptcl_alloc(fs_ctx *c) {
                                                                                    : FS_ERR_CUDA;
 }
 
+int fs_set_stage_tile_impl(fs_ctx *c, int bx, int by) {
+    if (!((bx == 32 && (by == 8 || by == 4)) || (bx == 64 && by == 4)))
+        return fs_set_error(c, FS_ERR_INVALID, "stage tile %dx%d not one of 32x8, 32x4, 64x4", bx, by);
+    if (bx == 64 && c->cfg.nspecies == 4)   // its shared memory would exceed 48 KB
+        return fs_set_error(c, FS_ERR_UNSUPPORTED, "the 64x4 stage tile takes 3 species");
+    c->stage_bx = bx;
+    c->stage_by = by;
+    c->nblk_stage = stage_tiles(c, bx, by);
+    return FS_OK;
+}
+
+template <int NS>
+static void launch_stage_ns(fs_ctx *c, StageArgs &a) {
+    const dim3 grid((c->nx + c->stage_bx - 1) / c->stage_bx, (c->ny + c->stage_by - 1) / c->stage_by);
+    if constexpr (NS == 3) {
+        if (c->stage_bx == 64) { k_stage<NS, 64, 4><<<grid, 256, 0, c->stream>>>(a); return; }
+    }
+    if (c->stage_by == 4) k_stage<NS, 32, 4><<<grid, 128, 0, c->stream>>>(a);
+    else k_stage<NS, 32, 8><<<grid, 256, 0, c->stream>>>(a);
+}
+
 static void launch_stage(fs_ctx *c, StageArgs &a) {
-    dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
-    if (c->cfg.nspecies == 4) k_stage<4><<<grid, NT, 0, c->stream>>>(a);
-    else k_stage<3><<<grid, NT, 0, c->stream>>>(a);
+    if (c->cfg.nspecies == 4) launch_stage_ns<4>(c, a);
+    else launch_stage_ns<3>(c, a);
 }
 
 // Start of a particle step: t_m, status and the current rows reset on the device.
@@ -801,5 +898,200 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     c->dt = c->h_ctrl->dt;
     c->st.attempts += attempts;
     if (attempts_out) *attempts_out = attempts;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------- batches
+// Work buffers of fs_ptcl_batch_attempt for one set of contexts.
+struct FsBatchWork {
+    int n = 0, ntiles = 0, device = 0, bx = DEF_BX, by = DEF_BY;
+    std::vector<int> nblk;   // tiles of each discharge in the batch's tile shape
+    cudaStream_t st = nullptr;
+    StageArgs *h_args = nullptr, *d_args = nullptr;   // [5][n]
+    BatchCtl *h_ctl = nullptr, *d_ctl = nullptr;
+    int *h_flags = nullptr, *d_flags = nullptr;       // act[n], fresh[n]
+    int4 *d_tiles = nullptr;
+    Ctrl *h_gather = nullptr, *d_gather = nullptr;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> in1, attempts;
+};
+
+void fs_batch_work_free(FsBatchWork *w) {
+    if (!w) return;
+    cudaFreeHost(w->h_args); cudaFree(w->d_args);
+    cudaFreeHost(w->h_ctl); cudaFree(w->d_ctl);
+    cudaFreeHost(w->h_flags); cudaFree(w->d_flags);
+    cudaFree(w->d_tiles);
+    cudaFreeHost(w->h_gather); cudaFree(w->d_gather);
+    for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
+    if (w->st) cudaStreamDestroy(w->st);
+    delete w;
+}
+
+int fs_batch_work_alloc(fs_ctx **cs, int n, FsBatchWork **out) {
+    FsBatchWork *w = new FsBatchWork();
+    w->n = n;
+    w->device = cs[0]->device;
+    w->bx = cs[0]->stage_bx;   // one tile shape for the whole batch: the first discharge's
+    w->by = cs[0]->stage_by;
+    std::vector<int4> tiles;
+    w->nblk.resize(n);
+    for (int b = 0; b < n; b++) {
+        const fs_ctx *c = cs[b];
+        const int gx = (c->nx + w->bx - 1) / w->bx, gy = (c->ny + w->by - 1) / w->by;
+        w->nblk[b] = gx * gy;
+        for (int y = 0; y < gy; y++)
+            for (int x = 0; x < gx; x++) tiles.push_back(make_int4(b, x, y, y * gx + x));
+    }
+    w->ntiles = (int)tiles.size();
+    w->ev.resize(n, nullptr);
+    w->in1.assign(n, 0);
+    w->attempts.assign(n, 0);
+    cudaError_t e = cudaStreamCreateWithFlags(&w->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_args, sizeof(StageArgs) * 5 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_args, sizeof(StageArgs) * 5 * n);
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_ctl, sizeof(BatchCtl) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_ctl, sizeof(BatchCtl) * n);
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_flags, sizeof(int) * 2 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_flags, sizeof(int) * 2 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_tiles, sizeof(int4) * tiles.size());
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_gather, sizeof(Ctrl) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_gather, sizeof(Ctrl) * n);
+    for (int b = 0; b < n && e == cudaSuccess; b++) e = cudaEventCreateWithFlags(&w->ev[b], cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(w->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { fs_batch_work_free(w); return FS_ERR_NOMEM; }
+    *out = w;
+    return FS_OK;
+}
+
+// One RK-Merson attempt (ptcl_step, ptcl_lib.F90:32-97) of every context b
+// with act[b] != 0, the five stages each as one launch over the tiles of all
+// of them, the controllers as one launch: the kernels and the arithmetic of
+// fs_ptcl_step_impl, so every discharge takes the same steps as alone.
+// fresh[b]: the attempt starts a step (else it retries one the controller
+// rejected).  On return rej[b] = 1 for a rejected attempt (its retry is the
+// caller's next call), 0 for an accepted one (levels and dt advanced as
+// fs_ptcl_step_impl leaves them); rc[b] an error of discharge b.  DC source,
+// FP64 path, no dielectric wall.
+int fs_ptcl_batch_attempt(fs_ctx **cs, int n, FsBatchWork *w, const int *act, const int *fresh, int *rej, int *rc) {
+    const int ns = 3;
+    int any = 0;
+    for (int b = 0; b < n; b++) {
+        rej[b] = 0;
+        if (!act[b]) continue;
+        any = 1;
+        fs_ctx *c = cs[b];
+        // order after the discharge's own stream (its last Poisson solve)
+        cudaEventRecord(w->ev[b], c->stream);
+        cudaStreamWaitEvent(w->st, w->ev[b], 0);
+        if (fresh[b]) {
+            c->Vsrc = fs_circ_source(c->cfg, c->k, c->t);
+            if (!c->faces_valid) {   // E and ion face data of the current phi, on the batch stream
+                dim3 bl(32, 8), g((c->nx + 1 + 31) / 32, (c->ny + 1 + 7) / 8);
+                FaceArgs f = {c->fx_e, c->fx_cl, c->fx_cr, c->fx_dl, c->fx_dr,
+                              c->fy_e, c->fy_cl, c->fy_cr, c->fy_dl, c->fy_dr};
+                k_faces<<<g, bl, 0, w->st>>>(c->pp, c->mesh, c->ph, f);
+                c->launches++;
+                c->faces_valid = 1;
+            }
+            w->in1[b] = c->lev[1];
+            w->attempts[b] = 0;
+        }
+        w->attempts[b]++;
+        const int L2 = c->lev[1], L3 = c->lev[2];
+        int freeb[FS_NBUF], nf = 0;
+        for (int q = 0; q < FS_NBUF; q++)
+            if (q != L2 && q != L3) freeb[nf++] = q;
+        const int SA = freeb[0], SB = freeb[1], OUT = freeb[2];
+        const int ins[5] = {w->in1[b], SA, SB, SA, SB};
+        const int outs[5] = {SA, SB, SA, SB, OUT};
+        for (int stg = 1; stg <= 5; stg++) {
+            StageArgs &a = w->h_args[(size_t)(stg - 1) * n + b];
+            memset(&a, 0, sizeof(a));
+            a.pp = c->pp;
+            a.m = c->mesh;
+            a.tab = c->d_tab;
+            a.ph = c->ph;
+            a.fx_e = c->fx_e; a.fx_cl = c->fx_cl; a.fx_cr = c->fx_cr;
+            a.fy_e = c->fy_e; a.fy_cl = c->fy_cl; a.fy_cr = c->fy_cr;
+            a.ctrl = c->d_ctrl;
+            a.part = c->d_part;
+            a.rows = c->d_rows;
+            a.sig_pl = fs_sig(c, 0);
+            a.sig_mi = fs_sig(c, 1);
+            a.sig_or = fs_sig(c, 2);
+            a.ks = fs_sig_ks(c);
+            a.nblk = w->nblk[b];
+            a.stage = stg;
+            for (int sp = 0; sp < ns; sp++) {
+                SpeciesBufs &bf = c->sp[sp];
+                a.nin[sp] = bf.buf[ins[stg - 1]];
+                a.nbase[sp] = bf.buf[L3];
+                a.nout[sp] = bf.buf[outs[stg - 1]];
+                a.k1[sp] = bf.k[0];
+                a.k3[sp] = bf.k[1];
+                a.k4[sp] = bf.k[2];
+                a.kout[sp] = stg == 1 ? bf.k[0] : stg == 3 ? bf.k[1] : stg == 4 ? bf.k[2] : nullptr;
+            }
+        }
+        BatchCtl &q = w->h_ctl[b];
+        q.ctrl = c->d_ctrl; q.part = c->d_part; q.rows = c->d_rows; q.rows_w = c->d_rows;
+        q.nblk = w->nblk[b]; q.ns = ns; q.ny = c->ny; q.adaptive = c->cfg.adaptive; q.dt_min = c->cfg.dt_min;
+        q.ph = c->ph; q.fx_e = c->fx_e; q.tx = c->mesh.tx; q.r = c->mesh.r; q.dx = c->mesh.dx;
+        q.nx = c->nx; q.P = c->pitch; q.ew = c->cfg.ew; q.vd = c->Vsrc;
+        c->launches += 7;   // reset, five stages, ghosts (the controller is counted below)
+    }
+    if (!any) return FS_OK;
+    for (int b = 0; b < n; b++) { w->h_flags[b] = act[b]; w->h_flags[n + b] = fresh[b]; }
+    cudaMemcpyAsync(w->d_args, w->h_args, sizeof(StageArgs) * 5 * n, cudaMemcpyHostToDevice, w->st);
+    cudaMemcpyAsync(w->d_ctl, w->h_ctl, sizeof(BatchCtl) * n, cudaMemcpyHostToDevice, w->st);
+    cudaMemcpyAsync(w->d_flags, w->h_flags, sizeof(int) * 2 * n, cudaMemcpyHostToDevice, w->st);
+    const int *d_act = w->d_flags, *d_fresh = w->d_flags + n;
+    k_reset_batch<<<n, 256, 0, w->st>>>(w->d_ctl, d_act, d_fresh);
+    for (int stg = 1; stg <= 5; stg++) {
+        const StageArgs *sa = w->d_args + (size_t)(stg - 1) * n;
+        if (w->bx == 64) k_stage_batch<3, 64, 4><<<w->ntiles, 256, 0, w->st>>>(sa, w->d_tiles, d_act);
+        else if (w->by == 4) k_stage_batch<3, 32, 4><<<w->ntiles, 128, 0, w->st>>>(sa, w->d_tiles, d_act);
+        else k_stage_batch<3, 32, 8><<<w->ntiles, 256, 0, w->st>>>(sa, w->d_tiles, d_act);
+        if (stg == 1) k_circ_ghost_batch<<<n, 128, 0, w->st>>>(w->d_ctl, d_act);
+    }
+    k_controller_batch<<<n, 256, 0, w->st>>>(w->d_ctl, d_act, w->d_gather);
+    cudaMemcpyAsync(w->h_gather, w->d_gather, sizeof(Ctrl) * n, cudaMemcpyDeviceToHost, w->st);
+    cudaError_t e = cudaStreamSynchronize(w->st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        for (int b = 0; b < n; b++)
+            if (act[b]) rc[b] = fs_cuda_check(cs[b], e, "batched RK attempt");
+        return FS_ERR_CUDA;
+    }
+    for (int b = 0; b < n; b++) {
+        if (!act[b]) continue;
+        fs_ctx *c = cs[b];
+        c->launches++;
+        *c->h_ctrl = w->h_gather[b];
+        const Ctrl &h = *c->h_ctrl;
+        if (h.status & FS_ST_NEG_DENSITY) { rc[b] = fs_set_error(c, FS_ERR_NEG_DENSITY, "negative density in get_Te"); continue; }
+        if (h.status & FS_ST_NAN) { rc[b] = fs_set_error(c, FS_ERR_NAN, "NaN in particle right-hand side"); continue; }
+        if (h.min_dt) { rc[b] = fs_set_error(c, FS_ERR_MIN_DT, "minimum timestep reached"); continue; }
+        c->Vd_pl = c->Vd_mi = c->Vsrc;
+        if (h.rejected) {
+            c->st.rk_rejects++;
+            c->Vd_pl = c->Vd_or;
+            c->Vd_mi = c->Vd_or;
+            w->in1[b] = c->lev[2];   // restart from the base state
+            rej[b] = 1;
+            if (w->attempts[b] > 100000) rc[b] = fs_set_error(c, FS_ERR_MIN_DT, "RK restart limit");
+            continue;
+        }
+        const int L2 = c->lev[1], L3 = c->lev[2];
+        int freeb[FS_NBUF], nf = 0;
+        for (int q = 0; q < FS_NBUF; q++)
+            if (q != L2 && q != L3) freeb[nf++] = q;
+        c->lev[0] = freeb[2];
+        c->lev[1] = freeb[1];
+        c->dt = h.dt;
+        c->st.attempts += w->attempts[b];
+    }
     return FS_OK;
 }

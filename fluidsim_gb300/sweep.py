@@ -46,13 +46,14 @@ def make_discharges(specs, precision=abi.FS_PREC_FP64, schedule=None):
     return out
 
 
-def run(discharges, steps, nthreads, warm=3):
+def run(discharges, steps, nthreads, warm=3, fused=False):
     """Warm up (start-up iterations and `warm` steps, untimed), then time
     `steps` main-loop iterations of every discharge with `nthreads` host
-    threads.  Returns (aggregate steps/s, seconds, stats, return codes)."""
-    api.batch_run(discharges, 2 + warm, nthreads=nthreads, check=False)
+    threads (fused: the RK stages of all discharges as one launch per stage).
+    Returns (aggregate steps/s, seconds, stats, return codes)."""
+    api.batch_run(discharges, 2 + warm, nthreads=nthreads, check=False, fused=fused)
     t0 = time.perf_counter()
-    stats, rcs = api.batch_run(discharges, steps, nthreads=nthreads, check=False)
+    stats, rcs = api.batch_run(discharges, steps, nthreads=nthreads, check=False, fused=fused)
     el = time.perf_counter() - t0
     ok = sum(1 for r in rcs if r == 0)
     return ok * steps / el, el, stats, rcs

@@ -260,6 +260,14 @@ int fs_profile_read(fs_ctx *ctx, double *ms_out, int64_t *launches_out, int32_t 
 /* Number of kernels ctx has launched since fs_create. */
 int64_t fs_launch_count(fs_ctx *ctx);
 
+/* Tile shape of the FP64 RK stage kernel (nodes per CTA): 32 x 8 (the
+ * default), 32 x 4 or 64 x 4.  Results do not depend on it (fixed-order
+ * sums per tile, then over tiles in index order: the sums differ in their
+ * last bits between shapes, not between runs); an autotuner may pick the
+ * fastest per grid size.  A fused batch (fs_batch_run_fused) runs all its
+ * discharges with the first one's shape.  64 x 4 takes 3 species. */
+int fs_set_stage_tile(fs_ctx *ctx, int32_t bx, int32_t by);
+
 /* FP64 issue rate of device `device`: fused multiply-adds per second of a
  * DFMA microbenchmark (4 to 16 CTAs per SM, 8 or 16 independent chains per
  * thread, the best of all shapes and of 5 timed launches each, CUDA
@@ -329,6 +337,19 @@ int fs_output_wait(fs_ctx *ctx);
 int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
                  int32_t *rc_out);
 
+/* fs_batch_run with the RK stages of the discharges fused: every round runs
+ * one RK-Merson attempt of each unfinished discharge (those past the two
+ * Poisson-only start-up iterations) as ONE launch per stage over the tiles of
+ * all of them and one launch of all their step-size controllers, each
+ * discharge with its own dt and its own accept/reject; then, nthreads host
+ * threads in parallel, the Poisson solve (its CUDA graph) and the level
+ * rotation of every discharge whose attempt was accepted; a rejected attempt
+ * is retried in the next round.  Each discharge takes exactly the steps it
+ * takes alone.  FP64 contexts with 3 species, DC source, no dielectric wall,
+ * all on one device (else FS_ERR_UNSUPPORTED). */
+int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
+                       int32_t *rc_out);
+
 /* ---- Learned Poisson preconditioner (FS_PREC_MIXED contexts only).  No
  * counterpart in the reference, which hands the system to PETSc
  * (lapl_lib.F90:83-104).  A BF16 convolutional network (a four-level U-Net,
@@ -346,7 +367,9 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
  * follows the correction.  In mode 1 the library times
  * every solve and runs each next one with whichever of the two -- with or
  * without the network -- has been faster on average (a stalled solve counts
- * double), trying the other one every 25 solves.
+ * double), trying the other one every 25 solves at first (the interval
+ * doubling to 400 while the other keeps losing, and 400 at once while the
+ * network is more than twice as slow).
  *
  * fs_lpc_init      allocate the network (seeded He init), its training state
  *                  and up to max_samples stored training pairs (full grids);
