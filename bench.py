@@ -391,11 +391,15 @@ def run_sweep(args):
         ds = sweep.make_discharges(specs, abi.FS_PREC_FP64, sched)
         try:
             rate, el, stats, rcs = sweep.run(ds, args.sweep_steps, threads, fused=fused)
+            # electron inventory per discharge (after the timed region): a
+            # fingerprint of every instance's state, compared across drivers
+            ne_sum = [float(d.download()["ne"][1:-1, 1:-1].sum()) for d in ds]
         finally:
             sweep.close(ds)
         res[name] = {"steps_per_s": rate, "seconds": el, "failed": [i for i, r in enumerate(rcs) if r != 0],
                      "rk_rejects": sum(s["rk_rejects"] for s in stats),
-                     "idc": [s["idc"] for s in stats], "t_end_s": [s["t"] * 1e-6 for s in stats]}
+                     "idc": [s["idc"] for s in stats], "ida": [s["ida"] for s in stats],
+                     "t_end_s": [s["t"] * 1e-6 for s in stats], "ne_sum": ne_sum}
     line = {
         "metric": "aggregate steps/s, %d-discharge uneven sweep (grids 64-512^2)" % args.sweep_count,
         "value": max(res["batched_autotuned"]["steps_per_s"], res["fused_autotuned"]["steps_per_s"]),
@@ -414,10 +418,13 @@ def run_sweep(args):
         "speedup_fused_vs_sequential": res["fused_autotuned"]["steps_per_s"] / res["sequential_fixed"]["steps_per_s"],
         "speedup_fused_vs_batched": res["fused_autotuned"]["steps_per_s"] / res["batched_autotuned"]["steps_per_s"],
         "fused_idc_equals_batched": res["fused_autotuned"]["idc"] == res["batched_autotuned"]["idc"],
+        "fused_state_equals_batched": (res["fused_autotuned"]["ne_sum"] == res["batched_autotuned"]["ne_sum"]
+                                       and res["fused_autotuned"]["t_end_s"] == res["batched_autotuned"]["t_end_s"]),
         "speedup_autotuned_vs_fixed": res["batched_autotuned"]["steps_per_s"]
                                       / res["batched_fixed"]["steps_per_s"],
-        "autotune": {"mg_smooth_by_size": {str(k): v for k, v in choice.items()},
-                     "steps_per_s_by_size": {str(k): {str(nu): r for nu, r in v.items()} for k, v in table.items()},
+        "autotune": {"mg_smooth_and_stage_tile_by_size": {str(k): [v[0], list(v[1]) if v[1] else None]
+                                                          for k, v in choice.items()},
+                     "steps_per_s_by_size": {str(k): dict(v) for k, v in table.items()},
                      "seconds": t_tune},
     }
     print(json.dumps(line))

@@ -61,53 +61,45 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
     return first_rc.load();
 }
 
-// The same advance with the RK stages of all discharges fused: each round
-// runs one RK-Merson attempt of every unfinished discharge that is past its
-// two Poisson-only start-up iterations as one launch per stage over the tiles
-// of all of them (fs_ptcl_batch_attempt: per-discharge dt, its own accept or
+// One group of the fused advance: rounds of one fused RK-Merson attempt of
+// every unfinished discharge of the group that is past its two Poisson-only
+// start-up iterations (fs_ptcl_batch_attempt: one launch per stage and tile
+// shape over the tiles of all of them, per-discharge dt, its own accept or
 // reject), then -- host threads in parallel, one discharge each -- the
 // Poisson solve (the CUDA graph of its CG loop) and the accept/reject
-// rotation of every discharge whose attempt was accepted.  A rejected
-// attempt is retried in the next round.  Each discharge takes exactly the
-// steps it takes alone.
-int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
-                       int32_t *rc_out) {
-    if (!ctx || n < 1 || steps < 0 || nthreads < 1) return FS_ERR_INVALID;
-    for (int i = 0; i < n; i++) {
-        fs_ctx *c = ctx[i];
-        if (!c) return FS_ERR_INVALID;
-        if (c->mixed || c->cfg.nspecies != 3 || c->cfg.rf != 0 || c->rwall || c->device != ctx[0]->device)
-            return fs_set_error(c, FS_ERR_UNSUPPORTED,
-                                "fused batches take FP64 contexts with 3 species, a DC source, no dielectric wall "
-                                "and one device");
-    }
-    cudaSetDevice(ctx[0]->device);
+// rotation of every discharge whose attempt was accepted.  A rejected attempt
+// is retried in the next round.  rc holds the group's return codes.
+static int fused_group(fs_ctx **ctx, int n, int32_t steps, double t_end, int nthreads, int32_t *rc) {
     FsBatchWork *w = nullptr;
     int rc0 = fs_batch_work_alloc(ctx, n, &w);
-    if (rc0) return rc0;
-    std::vector<int> act(n), fresh(n, 1), rej(n, 0), rc(n, FS_OK), done(n, 0), rk(n), pois(n);
+    if (rc0) {
+        for (int i = 0; i < n; i++) rc[i] = rc0;
+        return rc0;
+    }
+    std::vector<int> act(n), fresh(n, 1), rej(n, 0), done(n, 0), rk(n), pois(n), rci(n, FS_OK);
     std::vector<int> order(n);
     for (int i = 0; i < n; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return (long)ctx[a]->nx * ctx[a]->ny > (long)ctx[b]->nx * ctx[b]->ny;
     });
+    int err = FS_OK;
     for (int round = 0;; round++) {
         int nact = 0, nrk = 0;
         for (int i = 0; i < n; i++) {
             fs_ctx *c = ctx[i];
-            act[i] = rc[i] == FS_OK && done[i] < steps && !(t_end > 0.0 && c->t >= t_end);
+            act[i] = rci[i] == FS_OK && done[i] < steps && !(t_end > 0.0 && c->t >= t_end);
             rk[i] = act[i] && c->ts > 1;
             nact += act[i];
             nrk += rk[i];
         }
         if (!nact) break;
         if (nrk) {
-            const int e = fs_ptcl_batch_attempt(ctx, n, w, rk.data(), fresh.data(), rej.data(), rc.data());
-            if (e) break;
+            err = fs_ptcl_batch_attempt(ctx, n, w, rk.data(), fresh.data(), rej.data(), rci.data());
+            if (err) break;
         }
         for (int i = 0; i < n; i++) {
-            pois[i] = act[i] && rc[i] == FS_OK && !(rk[i] && rej[i]);
-            fresh[i] = !(rk[i] && rej[i] && rc[i] == FS_OK);
+            pois[i] = act[i] && rci[i] == FS_OK && !(rk[i] && rej[i]);
+            fresh[i] = !(rk[i] && rej[i] && rci[i] == FS_OK);
         }
         std::atomic<int> next(0);
         auto worker = [&]() {
@@ -132,11 +124,11 @@ int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int
                         r = fs_reject(c);
                     }
                 }
-                rc[i] = r;
+                rci[i] = r;
                 done[i]++;
             }
         };
-        // the first round builds every discharge's CUDA graphs: one thread
+        // the first round builds the discharges' CUDA graphs: one thread
         const int nt = round == 0 ? 1 : std::min<int>(nthreads, nact);
         std::vector<std::thread> pool;
         for (int t = 1; t < nt; t++) pool.emplace_back(worker);
@@ -144,6 +136,60 @@ int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int
         for (auto &th : pool) th.join();
     }
     fs_batch_work_free(w);
+    for (int i = 0; i < n; i++) rc[i] = err != FS_OK && rci[i] == FS_OK ? err : rci[i];
+    return err;
+}
+
+// The same advance with the RK stages fused across discharges.  The
+// discharges are dealt, largest first, into two groups of about equal node
+// count, each driven by its own host thread (fused_group): while one group's
+// Poisson solves run, the other's fused stages do, so neither phase leaves
+// the GPU idle.  Each discharge takes exactly the steps it takes alone.
+int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
+                       int32_t *rc_out) {
+    if (!ctx || n < 1 || steps < 0 || nthreads < 1) return FS_ERR_INVALID;
+    for (int i = 0; i < n; i++) {
+        fs_ctx *c = ctx[i];
+        if (!c) return FS_ERR_INVALID;
+        if (c->mixed || c->cfg.nspecies != 3 || c->cfg.rf != 0 || c->rwall || c->device != ctx[0]->device)
+            return fs_set_error(c, FS_ERR_UNSUPPORTED,
+                                "fused batches take FP64 contexts with 3 species, a DC source, no dielectric wall "
+                                "and one device");
+    }
+    cudaSetDevice(ctx[0]->device);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long)ctx[a]->nx * ctx[a]->ny > (long)ctx[b]->nx * ctx[b]->ny;
+    });
+    const int ng = n > 1 ? 2 : 1;
+    std::vector<fs_ctx *> gctx[2];
+    std::vector<int> gidx[2];
+    long load[2] = {0, 0};
+    for (int i : order) {
+        const int g = ng == 1 || load[0] <= load[1] ? 0 : 1;
+        gctx[g].push_back(ctx[i]);
+        gidx[g].push_back(i);
+        load[g] += (long)ctx[i]->nx * ctx[i]->ny;
+    }
+    std::vector<int32_t> grc[2];
+    int gerr[2] = {FS_OK, FS_OK};
+    auto run = [&](int g) {
+        cudaSetDevice(ctx[0]->device);
+        grc[g].assign(gctx[g].size(), FS_OK);
+        const int nt = ng == 1 ? nthreads : std::max(1, nthreads / 2);
+        gerr[g] = fused_group(gctx[g].data(), (int)gctx[g].size(), steps, t_end, nt, grc[g].data());
+    };
+    if (ng == 2) {
+        std::thread other(run, 1);
+        run(0);
+        other.join();
+    } else {
+        run(0);
+    }
+    std::vector<int32_t> rc(n, FS_OK);
+    for (int g = 0; g < ng; g++)
+        for (size_t k = 0; k < gidx[g].size(); k++) rc[gidx[g][k]] = grc[g][k];
     int first = FS_OK;
     for (int i = 0; i < n; i++) {
         fs_stats st;
@@ -153,5 +199,6 @@ int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int
         if (rc_out) rc_out[i] = rc[i];
         if (rc[i] != FS_OK && first == FS_OK) first = rc[i];
     }
+    if (first == FS_OK && (gerr[0] || gerr[1])) first = gerr[0] ? gerr[0] : gerr[1];
     return first;
 }

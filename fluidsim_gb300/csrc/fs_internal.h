@@ -88,7 +88,7 @@ struct Ctrl {
     double r0in2;              // mixed solver: inner residual norm^2 at the last refinement
     int inner_it, refine;      // mixed solver: inner iterations since it, refinement due
     double rr_prev;            // mixed solver: previous inner residual norm^2
-    double spare[2];
+    double spare[2];           // [0]: step length of the learned correction
     int lpc_off;               // learned correction switched off for this solve (stall)
     int cgm_restarted;         // mixed solver: the last refinement restarted the search direction
     double vd_pl, vd_mi;       // electrode voltage of the RC circuit (AC source, circ_lib.F90:158-174)
@@ -232,6 +232,7 @@ struct fs_ctx {
     int64_t lpc_solves, lpc_nn_solves;   // solves since fs_lpc_use turned it on, and those that ran the network
     int lpc_probe_every, lpc_probe_pending;   // probe interval of the other choice, last solve was a probe
     float *lpc_snap;             // harvested residual snapshots (fine FP32 fields)
+    float *lpc_s32, *lpc_d32;    // the residual the V-cycle leaves and the network's correction
     int lpc_snap_max;
     cudaGraph_t cgm_graph[2];    // [0] plain MG-PCG, [1] with the learned correction
     cudaGraphExec_t cgm_exec[2];

@@ -699,11 +699,15 @@ __global__ void k_phi_update_ff(double *ph, double *phm, const float *xh, const 
 //        conductances in the diagonal -- the grid-spacing map (the
 //        permittivity is eps0 everywhere in this model);
 //   f3 = asinh(n_i - n_e): the net charge density.
-// Output y: the correction a second V-cycle adds for s, scaled by m_c / sigma;
-// the preconditioner is z = V(r) + sigma y / m_c, about two V-cycles for the
-// price of one plus the network.
+// Output y: the correction a second V-cycle adds for s, scaled by m_c / sigma.
+// The preconditioner is z = V(r) + alpha d with d = sigma y / m_c and alpha
+// the step that minimises |s - alpha M d| (one more grid reduction): the
+// network's correction is taken only as far as it reduces the residual the
+// V-cycle left, so a poor prediction costs little.
 struct LpcArgs {
     int Hn, Wn;
+    float *s;                 // s = r - M V(r), fine FP32 field (kept for the step length)
+    float *d;                 // the network's correction d = sigma y / m_c (fine FP32 field)
     const float *mc;          // level-0 diagonal (FP32)
     const double *ni, *ne;    // the current densities, for the charge feature
     __nv_bfloat16 *x0;        // network input
@@ -728,6 +732,7 @@ __global__ void __launch_bounds__(256) k_lpc_feat(const LpcArgs l, const CgmArgs
         const __nv_bfloat162 f01 = __floats2bfloat162_rn(s * is, a.ce[o] * im);
         const __nv_bfloat162 f23 = __floats2bfloat162_rn(a.cn[o] * im, asinhf((float)(l.ni[o] - l.ne[o])));
         const size_t p = (size_t)jj * l.Wn + ii;
+        if (l.s) l.s[o] = s;
         uint2 v;
         v.x = *reinterpret_cast<const uint32_t *>(&f01);
         v.y = *reinterpret_cast<const uint32_t *>(&f23);
@@ -737,18 +742,46 @@ __global__ void __launch_bounds__(256) k_lpc_feat(const LpcArgs l, const CgmArgs
     })
 }
 
-// z += sigma y / m_c, unless the correction is switched off for this solve
-__global__ void __launch_bounds__(256) k_lpc_add(const LpcArgs l, const CgmArgs a) {
+// d = sigma y / m_c; the step alpha = (s . M d) / (M d . M d) into the control
+// block (0 for a non-finite correction, which also switches the network off)
+__global__ void __launch_bounds__(256) k_lpc_step(const LpcArgs l, const CgmArgs a) {
     Ctrl *c = a.ctrl;
     if (c->lpc_off || c->cg_done || c->cg_fail) return;
     const float sg = lpc_sigma(a);
+    float v[2] = {0.0f, 0.0f};
+    // M d needs the neighbours' d, recomputed from y (no grid-wide barrier);
+    // a non-finite prediction contributes nothing
     CG_NODES(a, {
-        const size_t p = (size_t)j_ * l.Wn + (q_ - j_ * (unsigned)a.nx);
-        const float mc = l.mc[o];
-        const float v = mc > 0.0f ? sg * l.y[p] / mc : 0.0f;
-        if (isfinite(v)) a.z[o] += v;
-        else c->lpc_off = 1;
+        auto dn = [&](size_t on, unsigned jj, unsigned ii) {
+            const float mc = l.mc[on];
+            const float dv = mc > 0.0f ? sg * l.y[(size_t)jj * l.Wn + ii] / mc : 0.0f;
+            return isfinite(dv) ? dv : 0.0f;
+        };
+        const unsigned jj = j_, ii = q_ - j_ * (unsigned)a.nx;
+        const float d0 = dn(o, jj, ii);
+        const float de = ii + 1 < (unsigned)a.nx ? dn(o + 1, jj, ii + 1) : 0.0f;
+        const float dw = ii > 0 ? dn(o - 1, jj, ii - 1) : 0.0f;
+        const float dnn = jj + 1 < (unsigned)a.ny ? dn(o + a.P, jj + 1, ii) : 0.0f;
+        const float ds = jj > 0 ? dn(o - a.P, jj - 1, ii) : 0.0f;
+        l.d[o] = d0;
+        const float md = mz_ff(d0, de, dw, dnn, ds, a.ce[o], a.ce[o - 1], a.cn[o], a.cn[o - a.P], a.extra[o]);
+        v[0] += l.s[o] * md;
+        v[1] += md * md;
     })
+    double sums[2];
+    if (grid_sumf<2>(v, reinterpret_cast<float *>(a.part), &a.ctrl->counter[6], a.nblk, sums) && threadIdx.x == 0) {
+        const double al = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+        c->spare[0] = isfinite(al) ? al : 0.0;
+        if (!isfinite(al)) c->lpc_off = 1;
+    }
+}
+
+// z += alpha d, unless the correction is switched off for this solve
+__global__ void __launch_bounds__(256) k_lpc_add(const LpcArgs l, const CgmArgs a) {
+    Ctrl *c = a.ctrl;
+    if (c->lpc_off || c->cg_done || c->cg_fail) return;
+    const float al = (float)c->spare[0];
+    CG_NODES(a, { a.z[o] += al * l.d[o]; })
 }
 
 // harvest: rr_prev = |r32|^2 (the feature scale of the residual in r32)
@@ -938,8 +971,11 @@ static LpcArgs lpc_args(fs_ctx *c) {
 static void lpc_apply(fs_ctx *c, const CgmArgs &ca) {
     LpcArgs l = lpc_args(c);
     fs_prof_begin(c, PROF_OTHER);
+    l.s = c->lpc_s32;
+    l.d = c->lpc_d32;
     k_lpc_feat<<<ca.grid, 256, 0, c->stream>>>(l, ca);
     lpc_forward(c->lpc, 1, c->lpc->Hn, c->lpc->Wn, c->stream);
+    k_lpc_step<<<ca.grid, 256, 0, c->stream>>>(l, ca);
     k_lpc_add<<<ca.grid, 256, 0, c->stream>>>(l, ca);
     // one black-red Gauss-Seidel pass on the fine level removes the
     // cell-scale error the network's correction brings in (M amplifies it
@@ -949,8 +985,8 @@ static void lpc_apply(fs_ctx *c, const CgmArgs &ca) {
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 1, 0);
     k_rb<float><<<gh, b, 0, c->stream>>>(f0, 0, 0);
     fs_prof_end(c);
-    // features, correction, 12 convolutions, 3 pools, 3 upsamplings, 2 half sweeps
-    c->launches += 2 + LPC_NLAYER + 6 + 2 - 1;
+    // features, step, correction, 12 convolutions, 3 pools, 3 upsamplings, 2 half sweeps
+    c->launches += 3 + LPC_NLAYER + 6 + 2 - 1;
 }
 
 static void cg_iteration_mixed(fs_ctx *c, const CgmArgs &ca) {
@@ -1208,6 +1244,10 @@ int fs_lpc_init_impl(fs_ctx *c, int crop, int max_batch, int max_samples, uint64
     c->lpc = L;
     c->lpc_snap_max = 8;
     cudaError_t ce = cudaMalloc(&c->lpc_snap, (size_t)c->lpc_snap_max * c->field_elems * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_s32, c->field_elems * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_s32, 0, c->field_elems * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->lpc_d32, c->field_elems * sizeof(float));
+    if (ce == cudaSuccess) ce = cudaMemset(c->lpc_d32, 0, c->field_elems * sizeof(float));
     if (ce != cudaSuccess) { fs_lpc_free_impl(c); return fs_cuda_check(c, ce, "learned preconditioner buffers"); }
     // interior cells of the padded NN grid
     std::vector<float> mk((size_t)Hn * Wn, 0.0f);
@@ -1224,7 +1264,10 @@ void fs_lpc_free_impl(fs_ctx *c) {
     c->lpc = nullptr;
     c->lpc_on = 0;
     cudaFree(c->lpc_snap);
+    cudaFree(c->lpc_s32);
+    cudaFree(c->lpc_d32);
     c->lpc_snap = nullptr;
+    c->lpc_s32 = c->lpc_d32 = nullptr;
 }
 
 // Host-driven solve of the current (assembled) system with the plain mixed

@@ -902,15 +902,21 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
 }
 
 // ---------------------------------------------------------------- batches
+// group of a stage tile shape in a batch: 0 = 32x8, 1 = 32x4, 2 = 64x4
+static int shape_group(int bx, int by) { return bx == 64 ? 2 : by == 4 ? 1 : 0; }
+
 // Work buffers of fs_ptcl_batch_attempt for one set of contexts.
 struct FsBatchWork {
-    int n = 0, ntiles = 0, device = 0, bx = DEF_BX, by = DEF_BY;
-    std::vector<int> nblk;   // tiles of each discharge in the batch's tile shape
+    int n = 0, device = 0;
+    // the discharges grouped by stage tile shape: one launch per group and stage
+    static constexpr int kShapes = 3;
+    int ntiles[kShapes] = {0, 0, 0};
+    int4 *d_tiles_g[kShapes] = {nullptr, nullptr, nullptr};
+    std::vector<int> nblk;   // tiles of each discharge (its own tile shape)
     cudaStream_t st = nullptr;
     StageArgs *h_args = nullptr, *d_args = nullptr;   // [5][n]
     BatchCtl *h_ctl = nullptr, *d_ctl = nullptr;
     int *h_flags = nullptr, *d_flags = nullptr;       // act[n], fresh[n]
-    int4 *d_tiles = nullptr;
     Ctrl *h_gather = nullptr, *d_gather = nullptr;
     std::vector<cudaEvent_t> ev;
     std::vector<int> in1, attempts;
@@ -921,7 +927,7 @@ void fs_batch_work_free(FsBatchWork *w) {
     cudaFreeHost(w->h_args); cudaFree(w->d_args);
     cudaFreeHost(w->h_ctl); cudaFree(w->d_ctl);
     cudaFreeHost(w->h_flags); cudaFree(w->d_flags);
-    cudaFree(w->d_tiles);
+    for (int g = 0; g < FsBatchWork::kShapes; g++) cudaFree(w->d_tiles_g[g]);
     cudaFreeHost(w->h_gather); cudaFree(w->d_gather);
     for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
     if (w->st) cudaStreamDestroy(w->st);
@@ -932,18 +938,16 @@ int fs_batch_work_alloc(fs_ctx **cs, int n, FsBatchWork **out) {
     FsBatchWork *w = new FsBatchWork();
     w->n = n;
     w->device = cs[0]->device;
-    w->bx = cs[0]->stage_bx;   // one tile shape for the whole batch: the first discharge's
-    w->by = cs[0]->stage_by;
-    std::vector<int4> tiles;
+    std::vector<int4> tiles[FsBatchWork::kShapes];
     w->nblk.resize(n);
     for (int b = 0; b < n; b++) {
         const fs_ctx *c = cs[b];
-        const int gx = (c->nx + w->bx - 1) / w->bx, gy = (c->ny + w->by - 1) / w->by;
+        const int bx = c->stage_bx, by = c->stage_by, g = shape_group(bx, by);
+        const int gx = (c->nx + bx - 1) / bx, gy = (c->ny + by - 1) / by;
         w->nblk[b] = gx * gy;
         for (int y = 0; y < gy; y++)
-            for (int x = 0; x < gx; x++) tiles.push_back(make_int4(b, x, y, y * gx + x));
+            for (int x = 0; x < gx; x++) tiles[g].push_back(make_int4(b, x, y, y * gx + x));
     }
-    w->ntiles = (int)tiles.size();
     w->ev.resize(n, nullptr);
     w->in1.assign(n, 0);
     w->attempts.assign(n, 0);
@@ -954,12 +958,16 @@ int fs_batch_work_alloc(fs_ctx **cs, int n, FsBatchWork **out) {
     if (e == cudaSuccess) e = cudaMalloc(&w->d_ctl, sizeof(BatchCtl) * n);
     if (e == cudaSuccess) e = cudaMallocHost(&w->h_flags, sizeof(int) * 2 * n);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_flags, sizeof(int) * 2 * n);
-    if (e == cudaSuccess) e = cudaMalloc(&w->d_tiles, sizeof(int4) * tiles.size());
+    for (int g = 0; g < FsBatchWork::kShapes && e == cudaSuccess; g++) {
+        w->ntiles[g] = (int)tiles[g].size();
+        if (tiles[g].empty()) continue;
+        e = cudaMalloc(&w->d_tiles_g[g], sizeof(int4) * tiles[g].size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(w->d_tiles_g[g], tiles[g].data(), sizeof(int4) * tiles[g].size(), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMallocHost(&w->h_gather, sizeof(Ctrl) * n);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_gather, sizeof(Ctrl) * n);
     for (int b = 0; b < n && e == cudaSuccess; b++) e = cudaEventCreateWithFlags(&w->ev[b], cudaEventDisableTiming);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(w->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { fs_batch_work_free(w); return FS_ERR_NOMEM; }
     *out = w;
     return FS_OK;
@@ -1051,9 +1059,9 @@ int fs_ptcl_batch_attempt(fs_ctx **cs, int n, FsBatchWork *w, const int *act, co
     k_reset_batch<<<n, 256, 0, w->st>>>(w->d_ctl, d_act, d_fresh);
     for (int stg = 1; stg <= 5; stg++) {
         const StageArgs *sa = w->d_args + (size_t)(stg - 1) * n;
-        if (w->bx == 64) k_stage_batch<3, 64, 4><<<w->ntiles, 256, 0, w->st>>>(sa, w->d_tiles, d_act);
-        else if (w->by == 4) k_stage_batch<3, 32, 4><<<w->ntiles, 128, 0, w->st>>>(sa, w->d_tiles, d_act);
-        else k_stage_batch<3, 32, 8><<<w->ntiles, 256, 0, w->st>>>(sa, w->d_tiles, d_act);
+        if (w->ntiles[0]) k_stage_batch<3, 32, 8><<<w->ntiles[0], 256, 0, w->st>>>(sa, w->d_tiles_g[0], d_act);
+        if (w->ntiles[1]) k_stage_batch<3, 32, 4><<<w->ntiles[1], 128, 0, w->st>>>(sa, w->d_tiles_g[1], d_act);
+        if (w->ntiles[2]) k_stage_batch<3, 64, 4><<<w->ntiles[2], 256, 0, w->st>>>(sa, w->d_tiles_g[2], d_act);
         if (stg == 1) k_circ_ghost_batch<<<n, 128, 0, w->st>>>(w->d_ctl, d_act);
     }
     k_controller_batch<<<n, 256, 0, w->st>>>(w->d_ctl, d_act, w->d_gather);

@@ -264,8 +264,8 @@ int64_t fs_launch_count(fs_ctx *ctx);
  * default), 32 x 4 or 64 x 4.  Results do not depend on it (fixed-order
  * sums per tile, then over tiles in index order: the sums differ in their
  * last bits between shapes, not between runs); an autotuner may pick the
- * fastest per grid size.  A fused batch (fs_batch_run_fused) runs all its
- * discharges with the first one's shape.  64 x 4 takes 3 species. */
+ * fastest per grid size.  A fused batch (fs_batch_run_fused) launches each
+ * stage once per tile shape present.  64 x 4 takes 3 species. */
 int fs_set_stage_tile(fs_ctx *ctx, int32_t bx, int32_t by);
 
 /* FP64 issue rate of device `device`: fused multiply-adds per second of a
@@ -339,8 +339,9 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
 
 /* fs_batch_run with the RK stages of the discharges fused: every round runs
  * one RK-Merson attempt of each unfinished discharge (those past the two
- * Poisson-only start-up iterations) as ONE launch per stage over the tiles of
- * all of them and one launch of all their step-size controllers, each
+ * Poisson-only start-up iterations) as ONE launch per stage (per stage tile
+ * shape present, see fs_set_stage_tile) over the tiles of all of them and one
+ * launch of all their step-size controllers, each
  * discharge with its own dt and its own accept/reject; then, nthreads host
  * threads in parallel, the Poisson solve (its CUDA graph) and the level
  * rotation of every discharge whose attempt was accepted; a rejected attempt

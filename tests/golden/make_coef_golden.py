@@ -65,7 +65,9 @@ def load(path, names, extra=None, whole=True):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_coef_golden.py <reference checkout>")
+    ref = sys.argv[1]
     ct, ct_coefs = load(os.path.join(ref, "coeftest.py"), ("getDt", "getDe"),
                         extra=("eps0", "e", "x0", "ph0"))
     ac, ac_coefs = load(os.path.join(ref, "wvgAC.py"), ("mu", "nu"), whole=False)

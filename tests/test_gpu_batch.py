@@ -33,7 +33,8 @@ def test_fused_batch_equals_sequential(built):
     """fs_batch_run_fused -- one launch per RK stage over every discharge's
     tiles, per-discharge dt and accept/reject -- ends bit-identical to the
     same discharges advanced one by one, over enough steps that some RK
-    attempts are rejected and retried."""
+    attempts are rejected and retried; discharges with different stage tile
+    shapes share the batch (one launch per shape and stage)."""
     from fluidsim_gb300 import abi, api, sweep
     specs = [dict(n=n, volts=v, p_torr=p, gam=g, seed=i)
              for i, (n, v, p, g) in enumerate([(64, 250.0, 1.0, 0.07), (96, 320.0, 3.0, 0.1),
@@ -41,6 +42,9 @@ def test_fused_batch_equals_sequential(built):
                                                (192, 210.0, 1.5, 0.04), (37, 280.0, 5.0, 0.09)])]
     a = sweep.make_discharges(specs, abi.FS_PREC_FP64)
     b = sweep.make_discharges(specs, abi.FS_PREC_FP64)
+    for i, tile in ((1, (32, 4)), (3, (32, 4)), (4, (64, 4))):
+        a[i].set_stage_tile(*tile)
+        b[i].set_stage_tile(*tile)
     stats, rcs = api.batch_run(a, 20, nthreads=4, fused=True)
     assert rcs == [0] * len(specs)
     for d in b:
