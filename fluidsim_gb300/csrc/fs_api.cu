@@ -189,8 +189,6 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
         return fs_set_error(nullptr, FS_ERR_INVALID, "bad coefficient table range");
     if (cfg->rf < 0 || cfg->rf > 3)
         return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "rf must be 0 (DC), 1 (AC) or 2, 3 (pulses), got %d", cfg->rf);
-    if (cfg->rf != 0 && cfg->precision != FS_PREC_FP64)
-        return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "time-dependent sources run on the FP64 path only");
     if (cfg->rf == 1 && !(cfg->res > 0))
         return fs_set_error(nullptr, FS_ERR_INVALID, "the AC source's RC circuit needs res > 0");
     if (cfg->precision != FS_PREC_FP64 && cfg->precision != FS_PREC_MIXED)
@@ -203,8 +201,6 @@ int validate(const fs_config *cfg, const fs_mesh *m) {
             return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "node type (%d,%d) at %ld not supported", tx, ty, q);
         if (ty == 3 && q / cfg->nx != cfg->ny - 1)   // g_init puts the wall on the last row only
             return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "dielectric wall node off the last row at %ld", q);
-        if (ty == 3 && cfg->precision != FS_PREC_FP64)
-            return fs_set_error(nullptr, FS_ERR_UNSUPPORTED, "the dielectric wall runs on the FP64 path only");
     }
     return FS_OK;
 }

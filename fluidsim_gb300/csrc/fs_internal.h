@@ -253,6 +253,7 @@ void fs_host_table(const fs_config &cfg, const fs_constants &k, std::vector<doub
 double fs_circ_source(const fs_config &cfg, const fs_constants &k, double t);   // Vsrc(t), circ_lib.F90:26-50
 
 // particle kernels (fs_ptcl.cu; the mixed-precision step in fs_mixed.cu)
+void fs_circuit_launch(fs_ctx *c, int stg, float *fx_e32);
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts);
 int fs_ptcl_step_mixed(fs_ctx *c, int *attempts);
 int fs_mixed_alloc(fs_ctx *c, const std::vector<double> &tab_rows);

@@ -26,6 +26,7 @@
 #include "fs_internal.h"
 #include "fs_lpc.cuh"
 #include "fs_mg.cuh"
+#include "fs_wall.cuh"
 
 #define ABX 32
 #define ABY 8
@@ -71,6 +72,8 @@ struct AsmMixArgs {
     const float *f32[10];
     const Ctrl *ctrl;
     Ctrl *ctrl_w;
+    const double *tab64;      // FP64 table (the dielectric wall's row)
+    const double *sig;        // sig_pl of the dielectric wall, nx+2
     float *mc, *ce, *cn, *extra, *inv_mc;
     double *rhs;
 };
@@ -242,6 +245,21 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
             cf = 1.0f / dh + dtf * (dfi - dfe);
         } else if (gj == ny && tb == 1) {
             eu = 0.0;
+        } else if (gj == ny && tb == 3) {
+            // dielectric wall, one row, in FP64 as on the FP64 path: field
+            // -sig (lapl_lib.F90:72-76,263-265), fluxes into an empty wall node
+            // with the node's own coefficients (:322-331), a boundary
+            // conductance of 1/dy without dt terms (:590-600)
+            const size_t on = (size_t)ny * P + gi;
+            const double ni = a.ni[on], ne = a.ne[on], nt = a.nt[on];
+            const double te = (nt >= 0.0) && (ne >= 0.0) ? nt / ne : 1e-8;
+            double mu, de;
+            fs_wall_tab(pp, a.tab64, te, mu, de);
+            const double E = -a.sig[gi], dh64 = a.m.dy[gj];
+            eu = E;
+            fi = (float)fs_sg_flux(1.0, E, dh64, pp.mui, pp.Di, ni, 0.0);
+            fe = (float)fs_sg_flux(-1.0, E, dh64, mu, de, ne, 0.0);
+            cf = idh;
         } else if (gj == ny && tb == 2) {
             const int lc = ly;
             const float te = s_te[lc][lx], ni = s_ni[lc][lx], ne = s_ne[lc][lx], mue = s_mu[lc][lx];
@@ -306,7 +324,7 @@ __global__ void __launch_bounds__(ANT, 3) k_assemble_mix(const AsmMixArgs a) {
         if (gi == 1 && tx == -2) gx += cw;
         if (gi == nx && tx == 2) gx += cee;
         if (gj == 1 && ty == -2) gys += cs;
-        if (gj == ny && ty == 2) gyn += cnn;
+        if (gj == ny && (ty == 2 || ty == 3)) gyn += cnn;
         if (gi == 1 && tx == -1) gx += a.mf.inv_dx[0] - a.mf.inv_dx[1];
         if (gj == 1 && ty == -1) gyn += a.mf.inv_dy[0] - a.mf.inv_dy[1];
         const float sx = fdly * fwr;
@@ -1138,6 +1156,8 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
     for (int k = 0; k < 10; k++) a.f32[k] = c->f32[k];
     a.ctrl = c->d_ctrl;
     a.ctrl_w = c->d_ctrl;
+    a.tab64 = c->d_tab;
+    a.sig = fs_sig(c, 0);
     MGLevelF &m0 = c->mgf[0];
     a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
     a.rhs = c->bs;

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
+#include "fs_wall.cuh"
 
 #define BX 32
 #define BY 8
@@ -180,6 +181,8 @@ struct StageMixArgs {
     Ctrl *ctrl;
     double *part;
     double *rows;
+    WallArgs wall;                  // dielectric wall (FP64): charge, slopes, FP64 table
+    int rows_every_stage;           // the RC circuit needs the electrode current after every stage
     int stage;
     int nblk;
 };
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(NT, 4) k_stage_mix(const StageMixArgs a) {
                 s_l[0][ly][lx + 1], s_n[1][ly][lx], s_n[1][ly][lx + 1], s_l[1][ly][lx], s_l[1][ly][lx + 1],
                 s_n[2][ly][lx], s_n[2][ly][lx + 1], s_l[2][ly][lx], s_l[2][ly][lx + 1], fi, fe, ft);
             if (NS == 4) fm = -pf.Dm * (s_n[3][ly][lx + 1] - s_n[3][ly][lx]) * idh;
-            if (a.stage == 5) {
+            if (a.stage == 5 || a.rows_every_stage) {
                 if (gi == 1 && a.m.dr_a[gj] != 0.0) a.rows[gj] = a.m.dr_a[gj] * (double)(fi - fe);
                 if (gi == nx - 1 && a.m.dr_c[gj] != 0.0) a.rows[(ny + 2) + gj] = a.m.dr_c[gj] * (double)(fi - fe);
             }
@@ -323,6 +326,14 @@ __global__ void __launch_bounds__(NT, 4) k_stage_mix(const StageMixArgs a) {
             // no lower y electrode flux in ptclEqn: zero flux, face field kept
         } else if (gj == ny && tb == 1) {
             eu = 0.0f;
+        } else if (gj == ny && tb == 3) {
+            const int lc = ly;
+            double wfi, wfe, wft, wfm;
+            eu = (float)fs_wall_face<NS>(pp, a.wall, a.m.dy[ny], a.ctrl->dt, a.stage, gi, s_te[lc][lx],
+                                         s_n[0][lc][lx], s_n[1][lc][lx], s_n[2][lc][lx],
+                                         NS == 4 ? s_n[3][lc][lx] : 0.0f, s_mue[lc][lx], s_de[lc][lx], wfi, wfe,
+                                         wft, wfm, st);
+            fi = (float)wfi; fe = (float)wfe; ft = (float)wft; fm = (float)wfm;
         } else if (gj == ny && tb == 2) {
             const int lc = ly;
             const size_t og = (size_t)(ny + 1) * P + gi, oc = (size_t)ny * P + gi;
@@ -593,6 +604,10 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
     const int SA = freeb[0], SB = freeb[1], OUT = freeb[2];
     int in1 = L2;
     int attempts = 0;
+    const bool rc_circuit = c->cfg.rf == 1;
+    // source voltage at the step's time (circ_lib.F90:26-50); without the RC
+    // circuit the electrode voltage is the source's (:176-177)
+    c->Vsrc = fs_circ_source(c->cfg, c->k, c->t);
     fs_ptcl_reset(c);
     fs_faces_update_mixed(c);
     dim3 grid((c->nx + BX - 1) / BX, (c->ny + BY - 1) / BY);
@@ -611,6 +626,8 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
         a.ctrl = c->d_ctrl;
         a.part = c->d_part;
         a.rows = c->d_rows;
+        a.wall = {c->d_tab, fs_sig(c, 2), fs_sig(c, 1), fs_sig(c, 0), fs_sig_ks(c)};
+        a.rows_every_stage = rc_circuit;
         a.nblk = c->nblk_stage;
         const int ins[5] = {in1, SA, SB, SA, SB};
         const int outs[5] = {SA, SB, SA, SB, OUT};
@@ -631,7 +648,9 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
             if (ns == 4) k_stage_mix<4><<<grid, NT, 0, c->stream>>>(a);
             else k_stage_mix<3><<<grid, NT, 0, c->stream>>>(a);
             fs_prof_end(c);
-            if (stg == 1) {
+            if (rc_circuit) {
+                fs_circuit_launch(c, stg, c->f32[0]);
+            } else if (stg == 1) {
                 c->launches++;
                 k_circ_ghost_mix<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
                     c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->f32[0], c->nx, c->ny, c->pitch,
@@ -640,11 +659,18 @@ int fs_ptcl_step_mixed(fs_ctx *c, int *attempts_out) {
         }
         int rc = fs_ptcl_control(c);
         if (rc) return rc;
-        c->Vd_pl = c->Vd_mi = c->Vsrc;
-        if (!c->h_ctrl->rejected) break;
+        const Ctrl &h = *c->h_ctrl;
+        if (rc_circuit) {
+            c->Vd_pl = h.vd_pl;
+            c->Vd_mi = h.vd_mi;
+        } else {
+            c->Vd_pl = c->Vd_mi = c->Vsrc;
+        }
+        if (!h.rejected) break;
         c->st.rk_rejects++;
         c->Vd_pl = c->Vd_or;
         c->Vd_mi = c->Vd_or;
+        if (c->rwall && ((rc = fs_sig_copy(c, 0, 2)) || (rc = fs_sig_copy(c, 1, 2)))) return rc;
         in1 = L3;
         if (attempts > 100000) return fs_set_error(c, FS_ERR_MIN_DT, "RK restart limit");
     }

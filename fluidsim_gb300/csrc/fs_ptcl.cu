@@ -25,6 +25,7 @@
 #include "fs_fastmath.cuh"
 #include "fs_internal.h"
 #include "fs_sg.cuh"
+#include "fs_wall.cuh"
 
 // stage tiles: 32 x 8 nodes by default; 32 x 4 and 64 x 4 selectable per
 // context (fs_set_stage_tile); the partial sums are sized for the most tiles
@@ -111,52 +112,15 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Dielectric wall face of column gi (type_y == 3 on the last row): field
-// -sig_mi(i) (ptcl_lib.F90:292-294), fluxes into an empty wall node with the
-// node's own coefficients and get_mut / get_Dt for the energy (:392-406).
-// The calling thread is the only reader and writer of column gi's charge, so
-// sfc_step (sfc_lib.F90:19-80) runs here too: its slope from the same stage
-// state, then the Merson combination into sig_mi (stages 1-4) or sig_pl
-// (stage 5).  Returns the face field.  Kept out of line: it runs on one row.
+// Dielectric wall face of column gi (type_y == 3 on the last row) and the
+// column's surface-charge step: fs_wall.cuh.
 template <int NS>
-__device__ __noinline__ double wall_face(const StageArgs &a, int gi, double te, double ni, double ne, double nt,
-                                         double nm, double mue, double de, double &fi, double &fe, double &ft,
-                                         double &fm, unsigned int &st) {
-    const PhysParams &pp = a.pp;
-    const int ny = pp.ny;
-    const double E = -a.sig_mi[gi];
-    const double dh = a.m.dy[ny];
-    fi = fs_sg_flux(1.0, E, dh, pp.mui, pp.Di, ni, 0.0);
-    fe = fs_sg_flux(-1.0, E, dh, mue, de, ne, 0.0);
-    ft = fs_sg_flux(-1.0, E, dh, pp.fit.mut(te), pp.fit.Dt(te), nt, 0.0);
-    fm = NS == 4 ? pp.Dm * nm / dh : 0.0;
-    // sfc_step receives (ni, ne, nt) in its (ne, ni, nt) arguments
-    // (ptcl_lib.F90:52): its mean energy is nt/ni, its "ion" flux carries n_e
-    // and its "electron" flux n_i
-    double tes;
-    if ((nt >= 0.0) && (ni >= 0.0)) tes = nt / ni;
-    else { st |= FS_ST_NEG_DENSITY; tes = 1e-8; }
-    double mus, des;
-    if (pp.fits) {
-        mus = pp.fit.mue(tes);
-        des = pp.fit.De(tes);
-    } else {
-        int kq; double wq;
-        tab_index(pp, tes, kq, wq);
-        mus = tab_val(a.tab, kq, wq, 0);
-        des = tab_val(a.tab, kq, wq, 1);
-    }
-    const double ksv = fs_sg_flux(1.0, E, dh, pp.mui, pp.Di, ne, 0.0) - fs_sg_flux(-1.0, E, dh, mus, des, ni, 0.0);
-    const int W = pp.nx + 2, stg = a.stage;
-    a.ks[(size_t)(stg - 1) * W + gi] = ksv;
-    const double dt = a.ctrl->dt, so = a.sig_or[gi];
-    const double k1 = stg > 1 ? a.ks[gi] : ksv;
-    if (stg == 1) a.sig_mi[gi] = so + dt * k1 / 3.0;
-    else if (stg == 2) a.sig_mi[gi] = so + dt * (k1 + ksv) / 6.0;
-    else if (stg == 3) a.sig_mi[gi] = so + dt * (k1 + ksv * 3.0) / 8.0;
-    else if (stg == 4) a.sig_mi[gi] = so + dt * (k1 - a.ks[(size_t)2 * W + gi] * 3.0 + ksv * 4.0) / 2.0;
-    else a.sig_pl[gi] = so + dt * (k1 + a.ks[(size_t)3 * W + gi] * 4.0 + ksv) / 6.0;
-    return E;
+__device__ __forceinline__ double wall_face(const StageArgs &a, int gi, double te, double ni, double ne, double nt,
+                                            double nm, double mue, double de, double &fi, double &fe, double &ft,
+                                            double &fm, unsigned int &st) {
+    const WallArgs w = {a.tab, a.sig_or, a.sig_mi, a.sig_pl, a.ks};
+    return fs_wall_face<NS>(a.pp, w, a.m.dy[a.pp.ny], a.ctrl->dt, a.stage, gi, te, ni, ne, nt, nm, mue, de, fi, fe,
+                            ft, fm, st);
 }
 
 // One RK stage on the tile (bx, by) of the grid (BX x BY nodes); blk is the
@@ -552,7 +516,7 @@ __global__ void k_circ_ghost(double *ph, const int8_t *tx, const double *r, cons
 // Vd_mi at the start of the attempt (a host value); later stages read the
 // device's.
 __global__ void __launch_bounds__(256) k_circuit(Ctrl *c, const double *rows, double *ph, double *fx_e,
-                                                 const int8_t *tx, const double *r, const double *dx, int nx,
+                                                 float *fx_e32, const int8_t *tx, const double *r, const double *dx, int nx,
                                                  int ny, int P, double ew, int stage, double vsrc, double vd_or,
                                                  double vd_mi0, double res, double cap) {
     __shared__ double s[256];
@@ -590,10 +554,12 @@ __global__ void __launch_bounds__(256) k_circuit(Ctrl *c, const double *rows, do
             if (tx[(gj - 1) * nx + 0] == -2) {
                 ph[o + 0] = vd / 2.0;
                 fx_e[o + 0] = -(ph[o + 1] - ph[o + 0]) / dx[0];
+                if (fx_e32) fx_e32[o + 0] = (float)fx_e[o + 0];
             }
             if (tx[(gj - 1) * nx + nx - 1] == 2) {
                 ph[o + nx + 1] = vd / (-2.0);
                 fx_e[o + nx] = -(ph[o + nx + 1] - ph[o + nx]) / dx[nx];
+                if (fx_e32) fx_e32[o + nx] = (float)fx_e[o + nx];
             }
         }
     }
@@ -812,6 +778,15 @@ int fs_ptcl_control(fs_ctx *c) {
     return FS_OK;
 }
 
+// The RC circuit after stage stg (k_circuit); fx_e32, when not null, also
+// receives the electrode faces' fields in FP32 (the mixed path's face field).
+void fs_circuit_launch(fs_ctx *c, int stg, float *fx_e32) {
+    c->launches++;
+    k_circuit<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, c->ph, c->fx_e, fx_e32, c->mesh.tx, c->mesh.r,
+                                        c->mesh.dx, c->nx, c->ny, c->pitch, c->cfg.ew, stg, c->Vsrc, c->Vd_or,
+                                        c->Vd_mi, c->cfg.res, c->k.cap);
+}
+
 // ptcl_step: five stages, restart on rejection (ptcl_lib.F90:32-97).
 int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
     const int ns = c->cfg.nspecies;
@@ -866,10 +841,7 @@ int fs_ptcl_step_impl(fs_ctx *c, int *attempts_out) {
             launch_stage(c, a);
             fs_prof_end(c);
             if (rc_circuit) {
-                c->launches++;
-                k_circuit<<<1, 256, 0, c->stream>>>(c->d_ctrl, c->d_rows, c->ph, c->fx_e, c->mesh.tx, c->mesh.r,
-                                                    c->mesh.dx, c->nx, c->ny, c->pitch, c->cfg.ew, stg, c->Vsrc,
-                                                    c->Vd_or, c->Vd_mi, c->cfg.res, c->k.cap);
+                fs_circuit_launch(c, stg, nullptr);
             } else if (stg == 1 && ++c->launches) {
                 k_circ_ghost<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(
                     c->ph, c->mesh.tx, c->mesh.r, c->mesh.dx, c->fx_e, c->nx, c->ny, c->pitch, c->cfg.ew,

@@ -78,7 +78,7 @@ typedef struct fs_config {
     int32_t coef_mode;      /* FS_COEF_*                                              */
     int32_t cyl;            /* 1: cylindrical r-weighting in y (props.F90:47)          */
     int32_t rf;             /* source (circ_lib.F90:26-50): 0 DC, 1 AC sin(pi t) through
-                               the RC circuit, 2 and 3 the pulse shapes; rf != 0 FP64 only */
+                               the RC circuit, 2 and 3 the pulse shapes              */
     int32_t adaptive;       /* 1: PI dt controller + reject (reference)               */
                             /* 0: dt held fixed, attempts never rejected              */
     int32_t precision;      /* FS_PREC_*                                              */
@@ -345,9 +345,12 @@ int fs_batch_run(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t n
  * discharge with its own dt and its own accept/reject; then, nthreads host
  * threads in parallel, the Poisson solve (its CUDA graph) and the level
  * rotation of every discharge whose attempt was accepted; a rejected attempt
- * is retried in the next round.  Each discharge takes exactly the steps it
- * takes alone.  FP64 contexts with 3 species, DC source, no dielectric wall,
- * all on one device (else FS_ERR_UNSUPPORTED). */
+ * is retried in the next round.  The discharges are split into groups of about
+ * equal node count (8 by default, FS_FUSED_GROUPS=1..16 in the environment),
+ * each with its own rounds on its own host thread and stream, so that one
+ * group's Poisson solves overlap another's stages.  Each discharge takes
+ * exactly the steps it takes alone.  FP64 contexts with 3 species, DC source,
+ * no dielectric wall, all on one device (else FS_ERR_UNSUPPORTED). */
 int fs_batch_run_fused(fs_ctx **ctx, int32_t n, int32_t steps, double t_end, int32_t nthreads, fs_stats *out,
                        int32_t *rc_out);
 

@@ -85,8 +85,8 @@ def test_invalid_config_rejected_before_device(built):
         api.Discharge(cfg, good.mesh())
     assert ei.value.code == abi.FS_ERR_UNSUPPORTED
     for bad, code in ((dict(rf=7), abi.FS_ERR_UNSUPPORTED), (dict(rf=1, res=0.0), abi.FS_ERR_INVALID),
-                      (dict(rf=2, precision=abi.FS_PREC_MIXED), abi.FS_ERR_UNSUPPORTED),
-                      (dict(rwall=True, precision=abi.FS_PREC_MIXED), abi.FS_ERR_UNSUPPORTED)):
+                      (dict(precision=5), abi.FS_ERR_INVALID),
+                      (dict(coef_mode=abi.FS_COEF_FITS, precision=abi.FS_PREC_MIXED), abi.FS_ERR_UNSUPPORTED)):
         cfg = config.glow(8).replace(**bad)
         with pytest.raises(api.FluidsimError) as ei:
             api.Discharge(cfg)
