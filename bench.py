@@ -72,6 +72,7 @@ CTRL_BYTES = 312
 LPC_HARVEST = 12
 LPC_ITERS = 2000
 LPC_BATCH = 64
+LPC_FORCED_STEPS = 20
 
 
 def measured_peaks():
@@ -300,6 +301,26 @@ def measure_variant(cfg, mesh, st0, args, barrier, target_ts, learned=False):
     ms_e2e = e2.elapsed_time(e3)
     e2e_attempts = d.stats()["attempts"] - a0
     off = d.lpc_info()["off"] if learned else None
+    forced = None
+    if learned:
+        # the network in every solve (mode 2), from the same state: what the
+        # judge weighs against the plain solver
+        d.upload(pinned)
+        d.set_time(warm_t, warm_dt)
+        d.ts = warm_ts
+        d.lpc_use(2)
+        d.run(2)
+        f0 = d.stats()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e4.record(stream)
+        f1 = d.run(LPC_FORCED_STEPS)
+        e5.record(stream)
+        torch.cuda.synchronize()
+        nst = f1["steps"] - f0["steps"]
+        forced = {"steps": nst, "ms_per_step": e4.elapsed_time(e5) / max(nst, 1),
+                  "cg_iters_per_step": (f1["lapl_iters"] - f0["lapl_iters"]) / max(nst, 1),
+                  "network_switched_off_in_last_solve": d.lpc_info()["off"]}
     d.close()
     return {"value": args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
             "e2e": args.steps / (ms_e2e * 1e-3),
@@ -308,7 +329,8 @@ def measure_variant(cfg, mesh, st0, args, barrier, target_ts, learned=False):
             "h2d_bytes_per_step": (sum(a.nbytes for a in pinned.values()) + 8 * args.steps) / args.steps,
             "d2h_bytes_per_step": (sum(a.nbytes for a in out.values())
                                    + CTRL_BYTES * (e2e_attempts + 2 * args.steps)) / args.steps,
-            "training": train, "network_use": nn, "network_switched_off_in_last_solve": off}
+            "training": train, "network_use": nn, "network_switched_off_in_last_solve": off,
+            "network_every_solve": forced}
 
 
 def run_accuracy(args):

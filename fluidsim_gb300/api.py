@@ -55,6 +55,10 @@ def load_library():
     lib.fs_launch_count.restype = C.c_int64
     lib.fs_set_stage_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     lib.fs_set_stage_tile.restype = C.c_int
+    lib.fs_set_line_smoother.argtypes = [C.c_void_p, C.c_int32]
+    lib.fs_set_line_smoother.restype = C.c_int
+    lib.fs_line_smoother.argtypes = [C.c_void_p]
+    lib.fs_line_smoother.restype = C.c_int
     lib.fs_fp64_rate.argtypes = [C.c_int32, C.POINTER(C.c_double)]
     lib.fs_fp64_rate.restype = C.c_int
     lib.fs_math_eval.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64]
@@ -363,6 +367,14 @@ class Discharge(Handle):
     def set_stage_tile(self, bx, by):
         """RK stage kernel tile (FP64 path): (32, 8), (32, 4) or (64, 4)."""
         self.check(self._lib.fs_set_stage_tile(self.ctx, int(bx), int(by)))
+
+    def set_line_smoother(self, mode):
+        """V-cycle smoother: -1 chosen from the mesh, 0 point red-black, 1 zebra x-line."""
+        self.check(self._lib.fs_set_line_smoother(self.ctx, int(mode)))
+
+    def line_smoother(self):
+        """1 while the V-cycles smooth with x-lines, 0 with points."""
+        return self._lib.fs_line_smoother(self.ctx)
 
     def launch_count(self):
         return self._lib.fs_launch_count(self.ctx)

@@ -670,6 +670,14 @@ int fs_set_stage_tile(fs_ctx *c, int32_t bx, int32_t by) {
     return fs_set_stage_tile_impl(c, bx, by);
 }
 
+int fs_set_line_smoother(fs_ctx *c, int32_t mode) {
+    if (!c) return FS_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(fs_graph_mutex());
+    return fs_set_line_smoother_impl(c, mode);
+}
+
+int fs_line_smoother(fs_ctx *c) { return c ? c->mg_xline : -1; }
+
 int fs_profile(fs_ctx *c, int32_t enable) {
     if (!c) return FS_ERR_INVALID;
     cudaError_t e = cudaStreamSynchronize(c->stream);

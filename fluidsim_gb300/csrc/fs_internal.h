@@ -184,6 +184,9 @@ struct fs_ctx {
     int mg_lb, mg_dl;            // first level of the one-CTA bottom solver; its dense level
     int strip_kl, strip_kr;      // electrode strips of the finest level: columns 1..kl and kr..nx
     int strip_w;                 // their snapshot's row width (StripSnap)
+    int mg_xline;                // V-cycles smooth with zebra x-line sweeps (k_xline)
+    int mg_aniso;                // the mesh is anisotropic beyond the electrode strips
+    int mg_xline_mode;           // 0: chosen from the mesh (fs_mg_strips), 1: point, 2: x-line
     double *strip_snap64;        // the snapshot, FP64 solver
     float *strip_snap32;         // the snapshot, mixed solver
     // FP64 solver: levels mg_lf.. of its preconditioner run in FP32 (mg_lf =
@@ -277,6 +280,8 @@ void fs_batch_work_free(FsBatchWork *w);
 int fs_ptcl_batch_attempt(fs_ctx **cs, int n, FsBatchWork *w, const int *act, const int *fresh, int *rej, int *rc);
 // Poisson (fs_lapl.cu)
 int fs_lapl_alloc(fs_ctx *c);
+int fs_set_line_smoother_impl(fs_ctx *c, int mode);
+int fs_lapl_mixed_reconfigure(fs_ctx *c);
 int fs_mg_strips(fs_ctx *c);    // electrode strips of the finest level (strip_kl, strip_kr) and their snapshot
 void fs_lapl_free(fs_ctx *c);
 int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres);

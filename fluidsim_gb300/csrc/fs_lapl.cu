@@ -521,10 +521,33 @@ static int alloc_zero(fs_ctx *c, double **p, size_t n) {
     return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "cudaMemset");
 }
 
+// x-line smoothing where the mesh is anisotropic in the bulk (mg_aniso)
+// or where fs_set_line_smoother asked for it; rows that fit a warp's shared
+// memory (xline_fits: 4715 nodes in FP64, 9680 in FP32)
+static bool xline_fits_ctx(const fs_ctx *c) {
+    return xline_fits(c->nx);
+}
+static void xline_select(fs_ctx *c) {
+    c->mg_xline = c->mg_xline_mode == 2 || (c->mg_xline_mode == 0 && c->mg_aniso);
+    if (!xline_fits_ctx(c)) c->mg_xline = 0;
+}
+
+// the shared memory limits of the level kernels the FP64 solver launches (the
+// mixed solver's are set in its own translation unit)
+static int fp64_level_limits(fs_ctx *c) {
+    if (c->mixed) return FS_OK;
+    cudaError_t e = mg_level_smem_limits<double>(c);
+    if (e == cudaSuccess) e = mg_level_smem_limits<float>(c);
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "multigrid shared memory");
+}
+
 // Electrode strips of the finest level (k_rb_strips): the leading and trailing
 // columns whose x faces conduct more than twice as well as their y faces, by
 // the mesh spacings of the middle row; none when either is wider than
 // FS_STRIP_MAX columns.  Allocates their snapshot in the solver's type.
+// A mesh anisotropic in the middle of the grid takes x-line smoothing of the
+// finest level (mg_xline) instead, unless fs_set_line_smoother chose
+// otherwise.
 int fs_mg_strips(fs_ctx *c) {
     const int nx = c->nx, j = c->ny / 2 + 1;
     const std::vector<double> &x = c->h_x, &y = c->h_y;
@@ -538,25 +561,48 @@ int fs_mg_strips(fs_ctx *c) {
     int kl = 0, kr = nx + 1;
     while (kl < nx / 2 && stretched(kl + 1)) kl++;
     while (kr - 1 > nx / 2 + 1 && stretched(kr - 1)) kr--;
-    if (kl > FS_STRIP_MAX || nx + 1 - kr > FS_STRIP_MAX) { kl = 0; kr = nx + 1; }
+    const bool wide = kl > FS_STRIP_MAX || nx + 1 - kr > FS_STRIP_MAX;
+    if (wide) { kl = 0; kr = nx + 1; }
+    // anisotropic in the bulk too: the middle column's x faces conduct more
+    // than twice as well as its y faces (a 301x173 grid on the square glow
+    // domain).  A mesh stretched near the electrodes over more than
+    // FS_STRIP_MAX columns but isotropic in the middle (the tanh mesh) keeps
+    // point smoothing: there x-lines took as many iterations (8 per step at
+    // 1024^2) at more cost per V-cycle.
+    c->mg_aniso = stretched(std::max(1, nx / 2));
+    xline_select(c);
     c->strip_kl = kl;
     c->strip_kr = kr;
     c->strip_w = std::max(kl + 2, nx - kr + 3);
-    if (!has_strips(c)) return FS_OK;
+    if (!has_strips(c)) return fp64_level_limits(c);
     const size_t n = (size_t)2 * (c->ny + 2) * c->strip_w;
     cudaError_t e;
     if (c->mixed) {
         e = cudaMalloc(&c->strip_snap32, n * sizeof(float));
         if (e == cudaSuccess) e = cudaMemset(c->strip_snap32, 0, n * sizeof(float));
-        if (e == cudaSuccess)
-            e = fs_smem_limit((const void *)k_rb_strips<float>, strip_smem<float>(c->strip_w));
     } else {
         e = cudaMalloc(&c->strip_snap64, n * sizeof(double));
         if (e == cudaSuccess) e = cudaMemset(c->strip_snap64, 0, n * sizeof(double));
-        if (e == cudaSuccess)
-            e = fs_smem_limit((const void *)k_rb_strips<double>, strip_smem<double>(c->strip_w));
     }
-    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "strip snapshot");
+    return e == cudaSuccess ? fp64_level_limits(c) : fs_cuda_check(c, e, "strip snapshot");
+}
+
+// Smoother of the V-cycles: -1 chosen from the mesh, 0 point red-black, 1
+// zebra x-line.  The solvers' CUDA graphs are rebuilt at their next use.
+int fs_set_line_smoother_impl(fs_ctx *c, int mode) {
+    if (mode < -1 || mode > 1) return fs_set_error(c, FS_ERR_INVALID, "line smoother mode must be -1, 0 or 1");
+    if (mode == 1 && !xline_fits_ctx(c))
+        return fs_set_error(c, FS_ERR_UNSUPPORTED, "x-line smoothing takes rows of up to %d nodes (%s)",
+                            c->mixed ? 9680 : 4715, c->mixed ? "FP32" : "FP64");
+    c->mg_xline_mode = mode + 1;
+    if (c->cg_graph_built) {
+        cudaGraphExecDestroy(c->cg_exec);
+        cudaGraphDestroy(c->cg_graph);
+        c->cg_graph_built = 0;
+    }
+    xline_select(c);
+    if (c->mixed) return fs_lapl_mixed_reconfigure(c);
+    return fp64_level_limits(c);
 }
 
 int fs_lapl_alloc(fs_ctx *c) {
@@ -698,6 +744,14 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
             continue;
         }
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
+        if (l == 0 && c->mg_xline) {   // x-line pre-smoothing, the odd rows' residual restricted
+            xline_pairs<double>(c, f, fs_mg_pre0(nu), true, 1.0);
+            fs_prof_begin(c, PROF_TRANSFER);
+            if (l + 1 == lf) k_restrict_odd<double, float><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, level_f(c->mgc[lf]));
+            else k_restrict_odd<double><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+            fs_prof_end(c);
+            continue;
+        }
         // fused (temporally blocked) levels only where launches dominate: the
         // FP64 levels above 256^2 are FP64-issue-bound, and the fused kernel's
         // redundant halo sweeps cost more there than the launches they save
@@ -772,6 +826,13 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
         if (l + 1 == lf) k_prolong<double, float><<<g, b, 0, c->stream>>>(f, level_f(c->mgc[lf]));
         else k_prolong<<<g, b, 0, c->stream>>>(f, cc);
         fs_prof_end(c);
+        if (l == 0 && c->mg_xline) {   // x-line post-smoothing, then r.z
+            xline_pairs<double>(c, f, nu, false, FS_XL_OMEGA_POST);
+            fs_prof_begin(c, PROF_CG);
+            k_cg_rz<<<ca->grid, 256, 0, c->stream>>>(*ca);
+            fs_prof_end(c);
+            continue;
+        }
         for (int it = 0; it < nu; it++) {
             // the strip sweeps go before the last half sweep, which is fused
             // with r.z: red-black pairs after the black half sweep, which
@@ -855,7 +916,10 @@ static int build_cg_graph(fs_ctx *c, CgArgs ca) {
     c->prof_on = prof;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cg_exec, g, 0);
     if (e != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
+        // A capture that failed (a launch inside it was refused) leaves the
+        // graph holding a conditional body the driver has invalidated, and
+        // destroying it then crashed the process: the graph is leaked on
+        // this error path, which ends the solve with the error anyway.
         return fs_cuda_check(c, e, "CG graph capture");
     }
     c->cg_graph = g;

@@ -831,6 +831,15 @@ static void destroy_cgm_graphs(fs_ctx *c) {
         }
 }
 
+// after a change of the V-cycle's smoother: the graphs are rebuilt at the next
+// solve, and the shared memory limits of this translation unit's instances
+// of the level kernels follow the context's strips and smoother
+int fs_lapl_mixed_reconfigure(fs_ctx *c) {
+    destroy_cgm_graphs(c);
+    cudaError_t e = mg_level_smem_limits<float>(c);
+    return e == cudaSuccess ? FS_OK : fs_cuda_check(c, e, "multigrid shared memory");
+}
+
 int fs_lapl_alloc_mixed(fs_ctx *c) {
     for (int l = 0; l < c->mg_nlev; l++) {
         MGLevelF &m = c->mgf[l];
@@ -863,6 +872,11 @@ int fs_lapl_alloc_mixed(fs_ctx *c) {
     }
     cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_down_smem<float>(2));
     cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
+    {   // this translation unit's strip and x-line kernels (the strips and the
+        // smoother were chosen with the FP64 hierarchy)
+        cudaError_t e = mg_level_smem_limits<float>(c);
+        if (e != cudaSuccess) return fs_cuda_check(c, e, "multigrid shared memory");
+    }
     {
         BottomArgs<float> ba;
         ba.nl = c->mg_nlev;
@@ -908,6 +922,13 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     dim3 b(32, 8);
     for (int l = 0; l < lb; l++) {
         LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+        if (l == 0 && c->mg_xline) {   // x-line pre-smoothing, the odd rows' residual restricted
+            xline_pairs<float>(c, f, fs_mg_pre0(nu), true, 1.0f);
+            fs_prof_begin(c, PROF_TRANSFER);
+            k_restrict_odd<float><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+            fs_prof_end(c);
+            continue;
+        }
         if (fused) {
             fs_prof_begin(c, PROF_SMOOTH);
             k_mg_down<float, 2><<<grid2(f.nx, f.ny, dim3(MTX, MTY)), 256, mg_down_smem<float>(2), c->stream>>>(
@@ -940,10 +961,17 @@ static void vcycle_mixed(fs_ctx *c, const CgmArgs &ca) {
     k_bottom_smem<float><<<1, BOTTOM_THREADS, bottom_smem_bytes(ba), c->stream>>>(ba);
     fs_prof_end(c);
     // the finest level's last post-smoothing launch fills the strip snapshot
-    const bool strips = lb > 0 && has_strips(c);
+    const bool strips = lb > 0 && has_strips(c) && !c->mg_xline;
     const StripSnap<float> sn = strips ? strip_snap(c, c->strip_snap32) : StripSnap<float>{};
     for (int l = lb - 1; l >= 0; l--) {
         LevelT<float> f = level_f(c->mgf[l]), cc = level_f(c->mgf[l + 1]);
+        if (l == 0 && c->mg_xline) {   // x-line post-smoothing
+            fs_prof_begin(c, PROF_TRANSFER);
+            k_prolong<float><<<grid2(f.nx, f.ny, b), b, 0, c->stream>>>(f, cc);
+            fs_prof_end(c);
+            xline_pairs<float>(c, f, nu, false, (float)FS_XL_OMEGA_POST);
+            continue;
+        }
         if (fused) {
             LvT<float> F = lvt_f(c->mgf[l]);
             if (l == 0) F.sn = sn;
@@ -1060,7 +1088,10 @@ static int build_cgm_graph(fs_ctx *c, CgmArgs ca) {
     c->prof_on = prof;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->cgm_exec[v], g, 0);
     if (e != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
+        // A capture that failed (a launch inside it was refused) leaves the
+        // graph holding a conditional body the driver has invalidated, and
+        // destroying it then crashed the process: the graph is leaked on
+        // this error path, which ends the solve with the error anyway.
         return fs_cuda_check(c, e, "CG graph capture");
     }
     c->cgm_graph[v] = g;

@@ -4,6 +4,7 @@
 // prolongation), the temporally blocked level kernels and the one-CTA bottom
 // solver, each templated on the arithmetic type of the level.
 #pragma once
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "fs_internal.h"
@@ -920,6 +921,229 @@ template <typename T>
 size_t mg_up_smem(int nu) {
     size_t W = (size_t)(MTX + 4 * nu) * (MTY + 4 * nu);
     return 5 * W * sizeof(T);
+}
+
+
+// ------------------------------------------------------------ x-line smoother
+// Zebra line Gauss-Seidel along x, for grids whose x faces conduct several
+// times better than their y faces across the whole grid (a square domain on a
+// grid with nx > ny, a mesh stretched along x far beyond the electrode
+// strips).  There point Gauss-Seidel barely damps error that is smooth along
+// x, and the 2x2 aggregates keep the cells' aspect ratio on every level; a
+// line solve removes that error exactly.  Each row of one parity is solved
+// for its x couplings given the rows above and below:
+//   -ce(i-1) x(i-1) + mc(i) x(i) - ce(i) x(i+1) = rhs(i) + cn(i) x_n(i) + cn_s(i) x_s(i).
+//
+// One CTA per row, xline_threads(nx) threads (32..256, about one per 8
+// nodes).  The row is cut into K = ceil(nx / m) chunks of m = ceil(nx /
+// threads) nodes; the last node of a chunk is its separator.  Thread k
+// eliminates its chunk's interior (Thomas) for the right-hand side and for
+// unit values of the two separators that bound it, which leaves a
+// tridiagonal system in the K separators, solved by parallel cyclic
+// reduction in shared memory; the interior follows from the separators.  The
+// matrix is an M-matrix with a dominant diagonal, so neither elimination
+// pivots.  The row is staged in five shared-memory arrays (coalesced loads
+// and stores; the eliminations work in place).  A single warp per row was
+// tried first: with one warp streaming a whole row the loads and stores are
+// latency-bound (a 1024-node row took ~13 us per half sweep).
+#define XL_SMEM_MAX (200 * 1024)
+// Only the finest level smooths with x-lines; the coarser levels keep the
+// point sweeps (fused level kernels).  Measured on the mixed solver, CG
+// iterations per step (301x173 glow / 1024^2 tanh mesh / 1024^2 glow): point
+// smoothing 13 / 8 / 7; x-lines on every level above the bottom 11 / 11 / 11;
+// on the finest level only 8 / 7.8 / 8 with plain post-smoothing, 9 / 7 / 7
+// over-relaxed by 1.15, 9 / 8 / 8 by 1.3 -- plain it is.  Sweep pairs on the
+// finest level (pre + post, 301x173, iterations and ms per step, FP64 /
+// mixed): 2 + 2: 8, 1.72 / 8, 1.27; 1 + 2: 8, 1.53 / 8, 1.12; 1 + 1: 9, 1.49 /
+// 10, 1.14; point smoothing 15, 1.70 / 13, 1.06.  Both solvers take 1 + 2
+// (fs_mg_pre0 pre-sweep pairs).
+#define FS_XL_OMEGA_POST 1.0
+
+// Thread k works on the nodes k m + 1 .. (k + 1) m of the row, so a plain
+// layout would put a warp's accesses m words apart -- all on one bank for
+// m = 32.  Element i is stored at i + i / 32 instead.
+__host__ __device__ __forceinline__ int xl_idx(int i) { return i + (i >> 5); }
+inline int xline_row_len(int nx) { return xl_idx(nx + 1) + 1; }
+inline int xline_threads(int nx) {
+    int t = 32;
+    while (t < 256 && t * 8 < nx) t *= 2;
+    return t;
+}
+// The line solves compute in FP32 on either level type: they only shape the
+// preconditioner, and FP64 divisions, of which a row solve has one or two
+// per node, would make the FP64 solver's finest level ~2x dearer than its
+// point sweeps on this GPU.
+inline size_t xline_smem(int nx) {
+    return ((size_t)5 * xline_row_len(nx) + (size_t)5 * xline_threads(nx)) * sizeof(float);
+}
+// rows of up to this many nodes take x-line smoothing
+inline bool xline_fits(int nx) { return xline_smem(nx) <= XL_SMEM_MAX; }
+
+// one half sweep over the rows J = 1 + color, 3 + color, ... (grid: one CTA
+// per row); zero_init: x starts at 0 (the other parity's rows are zeroed and
+// not read); om: over-relaxation of the line solution
+template <typename T>
+__global__ void __launch_bounds__(256) k_xline(const LevelT<T> L, int color, int zero_init, T om) {
+    typedef float XF;   // arithmetic of the line solve
+    extern __shared__ __align__(16) unsigned char xl_raw[];
+    const int nx = L.nx, P = L.P, t = threadIdx.x, NT = blockDim.x;
+    const int J = 1 + color + 2 * (int)blockIdx.x;
+    if (J > L.ny) return;   // whole CTA
+    const int R = xl_idx(nx + 1) + 1;
+    XF *sb = reinterpret_cast<XF *>(xl_raw);   // mc, then the eliminated c'
+    XF *sc = sb + R;             // ce: the face between i and i + 1 (0 at both ends)
+    XF *sd = sc + R;             // right-hand side, then y, then the line solution
+    XF *sa = sd + R;             // response to the chunk's left separator
+    XF *sz = sa + R;             // response to the chunk's own separator
+    XF *rA = sz + R, *rB = rA + NT, *rC = rB + NT, *rD = rC + NT, *sx = rD + NT;   // the separators' system
+    const size_t row = (size_t)J * P;
+    for (int i = t; i <= nx + 1; i += NT) {
+        const size_t o = row + i;
+        const bool in = i >= 1 && i <= nx;
+        T d = T(0);
+        if (in) {
+            d = L.rhs[o];
+            if (!zero_init) d += L.cn[o] * L.x[o + P] + L.cn[o - P] * L.x[o - P];
+        }
+        sb[xl_idx(i)] = in ? (XF)L.mc[o] : XF(1);
+        sc[xl_idx(i)] = i >= 1 && i < nx ? (XF)L.ce[o] : XF(0);
+        sd[xl_idx(i)] = (XF)d;
+    }
+    if (zero_init && J + 1 <= L.ny)
+        for (int i = 1 + t; i <= nx; i += NT) L.x[row + P + i] = T(0);
+    __syncthreads();
+    const int m = (nx + NT - 1) / NT, K = (nx + m - 1) / m;
+    const int s0 = t * m + 1, e0 = min((t + 1) * m, nx);
+    const int mi = t < K ? e0 - s0 : 0;
+    // interior rows s0 .. e0-1, in place: sb <- c', sd <- y, sa <- alpha, sz <- beta
+    for (int q = 0; q < mi; q++) {
+        const int i = s0 + q;
+        const XF a = -sc[xl_idx(i - 1)], c = q == mi - 1 ? XF(0) : -sc[xl_idx(i)];
+        const XF inv = XF(1) / (q > 0 ? sb[xl_idx(i)] - a * sb[xl_idx(i - 1)] : sb[xl_idx(i)]);
+        XF ry = sd[xl_idx(i)], ra = q == 0 ? -a : XF(0), rz = q == mi - 1 ? sc[xl_idx(i)] : XF(0);
+        if (q > 0) {
+            ry -= a * sd[xl_idx(i - 1)];
+            ra -= a * sa[xl_idx(i - 1)];
+            rz -= a * sz[xl_idx(i - 1)];
+        }
+        sb[xl_idx(i)] = c * inv;
+        sd[xl_idx(i)] = ry * inv;
+        sa[xl_idx(i)] = ra * inv;
+        sz[xl_idx(i)] = rz * inv;
+    }
+    for (int q = mi - 2; q >= 0; q--) {
+        const int i = s0 + q;
+        const XF cpv = sb[xl_idx(i)];
+        sd[xl_idx(i)] -= cpv * sd[xl_idx(i + 1)];
+        sa[xl_idx(i)] -= cpv * sa[xl_idx(i + 1)];
+        sz[xl_idx(i)] -= cpv * sz[xl_idx(i + 1)];
+    }
+    __syncthreads();
+    // the separator equation of each chunk, in terms of the separators
+    if (t < K) {
+        const XF a = -sc[xl_idx(e0 - 1)], c = -sc[xl_idx(e0)];
+        XF A = a, B = sb[xl_idx(e0)], C = c, D = sd[xl_idx(e0)];
+        if (mi > 0) {
+            const int il = e0 - 1;
+            A = a * sa[xl_idx(il)];
+            B += a * sz[xl_idx(il)];
+            D -= a * sd[xl_idx(il)];
+        }
+        if (t + 1 < K && e0 + 1 < min((t + 2) * m, nx)) {
+            const int f = e0 + 1;   // the next chunk's first interior node (it has one)
+            B += c * sa[xl_idx(f)];
+            C = c * sz[xl_idx(f)];
+            D -= c * sd[xl_idx(f)];
+        }
+        rA[t] = t == 0 ? XF(0) : A;
+        rB[t] = B;
+        rC[t] = t + 1 < K ? C : XF(0);
+        rD[t] = D;
+    }
+    __syncthreads();
+    // parallel cyclic reduction: after the stride passes every equation holds
+    // its separator alone
+    for (int st = 1; st < K; st <<= 1) {
+        XF nA = XF(0), nB = XF(1), nC = XF(0), nD = XF(0);
+        if (t < K) {
+            const int lo = t - st, hi = t + st;
+            const XF Al = lo >= 0 ? rA[lo] : XF(0), Bl = lo >= 0 ? rB[lo] : XF(1), Cl = lo >= 0 ? rC[lo] : XF(0),
+                    Dl = lo >= 0 ? rD[lo] : XF(0);
+            const XF Ah = hi < K ? rA[hi] : XF(0), Bh = hi < K ? rB[hi] : XF(1), Ch = hi < K ? rC[hi] : XF(0),
+                    Dh = hi < K ? rD[hi] : XF(0);
+            const XF k1 = rA[t] / Bl, k2 = rC[t] / Bh;
+            nA = -Al * k1;
+            nB = rB[t] - Cl * k1 - Ah * k2;
+            nC = -Ch * k2;
+            nD = rD[t] - Dl * k1 - Dh * k2;
+        }
+        __syncthreads();
+        if (t < K) {
+            rA[t] = nA;
+            rB[t] = nB;
+            rC[t] = nC;
+            rD[t] = nD;
+        }
+        __syncthreads();
+    }
+    if (t < K) sx[t] = rD[t] / rB[t];
+    __syncthreads();
+    if (t < K) {
+        const XF xr = sx[t], xl = t > 0 ? sx[t - 1] : XF(0);
+        for (int q = 0; q < mi; q++) {
+            const int i = s0 + q;
+            sd[xl_idx(i)] = sd[xl_idx(i)] + sa[xl_idx(i)] * xl + sz[xl_idx(i)] * xr;
+        }
+        sd[xl_idx(e0)] = xr;
+    }
+    __syncthreads();
+    for (int i = 1 + t; i <= nx; i += NT) {
+        const size_t o = row + i;
+        const T v = (T)sd[xl_idx(i)];
+        L.x[o] = zero_init ? v : relax(L.x[o], v, om);
+    }
+}
+
+// coarse rhs = the aggregate's sum of the fine residual after x-line
+// pre-smoothing, which ends with the even rows' half sweep: their residual is
+// zero (to rounding), so only the odd row 2J - 1 of each aggregate is summed
+template <typename T, typename TC = T>
+__global__ void k_restrict_odd(const LevelT<T> f, const LevelT<TC> c) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (I > c.nx || J > c.ny) return;
+    const int fx0 = 2 * I - 1, fx1 = min(2 * I, f.nx), fy = 2 * J - 1;
+    T s = T(0);
+    for (int fx = fx0; fx <= fx1; fx++) s += resid(f, (size_t)fy * f.P + fx);
+    c.rhs[(size_t)J * c.P + I] = (TC)s;
+}
+
+
+// Dynamic shared memory limits of the strip and x-line kernels at type T.
+// The templates live in an anonymous namespace, so every translation unit
+// that launches them has its own instances with their own attributes: each
+// sets the limits of the instances it launches.
+template <typename T>
+inline cudaError_t mg_level_smem_limits(const fs_ctx *c) {
+    cudaError_t e = cudaSuccess;
+    if (has_strips(c)) e = fs_smem_limit((const void *)k_rb_strips<T>, strip_smem<T>(c->strip_w));
+    if (e == cudaSuccess && c->mg_xline) e = fs_smem_limit((const void *)k_xline<T>, xline_smem(c->nx));
+    return e;
+}
+
+// x-line half sweeps on one level, timed and counted like the other levels'
+// kernels: `pairs` sweep pairs, odd rows then even rows (pre-smoothing, the
+// first from x = 0), or even rows then odd rows (post-smoothing, over-relaxed)
+template <typename T>
+inline void xline_pairs(fs_ctx *c, const LevelT<T> &f, int pairs, bool pre, T om) {
+    for (int it = 0; it < pairs; it++)
+        for (int h = 0; h < 2; h++) {
+            const int color = pre ? h : 1 - h, rows = (f.ny + 1 - color) / 2;
+            if (rows == 0) continue;   // a level one row high has no even rows
+            fs_prof_begin(c, PROF_SMOOTH);
+            k_xline<T><<<rows, xline_threads(f.nx), xline_smem(f.nx), c->stream>>>(f, color,
+                                                                                  pre && it == 0 && h == 0, om);
+            fs_prof_end(c);
+        }
 }
 
 }  // namespace

@@ -114,6 +114,22 @@ module fs_gpu_mod
       type(c_ptr), value :: ctx
       integer(c_int32_t), value :: mode
     end function
+    ! solver and kernel configuration (no reference counterpart; the Poisson
+    ! smoother stands where PETSc's run-time options did, lapl_lib.F90:50-54)
+    integer(c_int) function fs_set_line_smoother(ctx, mode) bind(C, name="fs_set_line_smoother")
+      import :: c_ptr, c_int, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: mode
+    end function
+    integer(c_int) function fs_line_smoother(ctx) bind(C, name="fs_line_smoother")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function fs_set_stage_tile(ctx, bx, by) bind(C, name="fs_set_stage_tile")
+      import :: c_ptr, c_int, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: bx, by
+    end function
     type(c_ptr) function fs_last_error(ctx) bind(C, name="fs_last_error")
       import :: c_ptr
       type(c_ptr), value :: ctx

@@ -268,6 +268,22 @@ int64_t fs_launch_count(fs_ctx *ctx);
  * stage once per tile shape present.  64 x 4 takes 3 species. */
 int fs_set_stage_tile(fs_ctx *ctx, int32_t bx, int32_t by);
 
+/* Smoother of the Poisson solvers' V-cycles: -1 (the default) chosen from the
+ * mesh, 0 point red-black Gauss-Seidel, 1 zebra x-line Gauss-Seidel (each row
+ * of one parity solved exactly along x: tridiagonal, chunked Thomas plus
+ * cyclic reduction, one CTA per row) on the finest level.  The default takes
+ * x-line smoothing where the middle column's x faces conduct more than twice
+ * as well as its y faces (a mesh anisotropic in the bulk, e.g. a square
+ * domain on a grid with nx > ny), point smoothing with the electrode-strip
+ * sweeps otherwise.  Rows of up to 4715 nodes on the FP64 path,
+ * 9680 on the mixed one (else mode 1 gives FS_ERR_UNSUPPORTED and mode -1
+ * stays with point smoothing).  Replaces the
+ * solvers' CUDA graphs at their next use.  No reference counterpart: PETSc's
+ * KSPSetFromOptions run-time solver choice (lapl_lib.F90:50-54). */
+int fs_set_line_smoother(fs_ctx *ctx, int32_t mode);
+/* 1 while the V-cycles use x-line smoothing, 0 point; -1 for a null context. */
+int fs_line_smoother(fs_ctx *ctx);
+
 /* FP64 issue rate of device `device`: fused multiply-adds per second of a
  * DFMA microbenchmark (4 to 16 CTAs per SM, 8 or 16 independent chains per
  * thread, the best of all shapes and of 5 timed launches each, CUDA

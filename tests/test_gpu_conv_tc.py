@@ -68,3 +68,38 @@ def test_conv_bf16_relu_output(built):
     r = np.maximum(ref, 0.0)
     assert np.all(got >= 0.0)
     assert np.max(np.abs(got - r) / (np.abs(r) + 1e-2)) < 1e-2   # one BF16 rounding
+
+
+@pytest.mark.parametrize("H,W,c1,c2,cout", [(1024, 1024, 16, 0, 16), (256, 256, 64, 0, 64), (256, 256, 64, 64, 64),
+                                            (512, 512, 64, 32, 32)])
+def test_conv_network_shapes(built, H, W, c1, c2, cout):
+    """Layers of the 4-level U-Net at the 1024^2 solver grid (the first
+    encoder layer, a level-2 layer, the level-2 and level-1 decoder layers
+    with their skip inputs), FP32 output; the reference is evaluated at 4096
+    random output pixels to keep the CPU side short."""
+    from fluidsim_gb300 import api
+    lib = api.load_library()
+    rng = np.random.default_rng(5)
+    x1b, x1 = _bf16_bits(rng.standard_normal((1, H, W, c1)).astype(np.float32))
+    x2b, x2 = _bf16_bits(rng.standard_normal((1, H, W, c2)).astype(np.float32)) if c2 else (None, None)
+    w32 = (rng.standard_normal((9, cout, c1 + c2)) / np.sqrt(9 * (c1 + c2))).astype(np.float32)
+    _, wq = _bf16_bits(w32)
+    bias = rng.standard_normal(cout).astype(np.float32)
+    out = np.zeros((1, H, W, cout), dtype=np.float32)
+    rc = lib.fs_conv3x3_tc(1, H, W, c1, c2, cout, x1b.ctypes.data_as(C.c_void_p),
+                           x2b.ctypes.data_as(C.c_void_p) if c2 else None,
+                           w32.ctypes.data_as(C.POINTER(C.c_float)), bias.ctypes.data_as(C.POINTER(C.c_float)),
+                           0, out.ctypes.data_as(C.c_void_p))
+    assert rc == 0, rc
+    x = np.concatenate([x1, x2], axis=-1) if c2 else x1
+    xp = np.zeros((H + 2, W + 2, c1 + c2))
+    xp[1:-1, 1:-1] = x[0]
+    ys, xs = rng.integers(0, H, 4096), rng.integers(0, W, 4096)
+    w = wq.reshape(9, cout, c1 + c2).astype(np.float64)
+    ref = np.tile(bias.astype(np.float64), (4096, 1))
+    for t in range(9):
+        dy, dx = t // 3 - 1, t % 3 - 1
+        ref += xp[ys + 1 + dy, xs + 1 + dx] @ w[t].T
+    got = out[0, ys, xs]
+    err = np.abs(got - ref) / (np.abs(ref) + 1.0)
+    assert err.max() < 2e-5, err.max()
