@@ -35,6 +35,11 @@ namespace {
 
 constexpr int kMaxStages = 32;             // A ring depth at most
 constexpr int kRingBudget = 96 * 1024;     // shared memory the A ring may take
+// epilogue staging: per epilogue warp 32 pixels x 16 channels in FP32, rows
+// of kEpiRow floats (80 bytes: the lanes' 16-byte accesses fall on distinct
+// banks), then the bias (up to 128 channels)
+constexpr int kEpiRow = 20;
+constexpr int kEpiBytes = 4 * 32 * kEpiRow * 4 + 128 * 4 + 16;
 constexpr long kSpinLimit = 1L << 20;      // bounded waits (each try_wait may sleep ~us)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -147,6 +152,8 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
     uint64_t *wbar = tempty + 2;
     uint64_t *fin = wbar + 1;                         // every MMA of this CTA complete
     uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
+    float *sstage = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tslot + 1) + 15) & ~(uintptr_t)15);
+    float *sbias = sstage + 4 * 32 * kEpiRow;
     __shared__ int s_fail;
     volatile int *vfail = &s_fail;   // raised by any role whose wait ran out
 
@@ -162,6 +169,9 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
         for (int s = 0; s < 2; ++s) { mbar_init(tfull + s, 1); mbar_init(tempty + s, 4); }
         mbar_init(wbar, 1);
         mbar_init(fin, 1);
+    }
+    for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sbias[i] = a.bias ? a.bias[i] : 0.0f;
+    if (threadIdx.x == 0) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -253,15 +263,43 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
             const bool in = px < a.W && py < a.H;
             const long pix = ((long)b * a.H + py) * a.W + px;
             const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(bs * a.tmem_cols);
+            float *st = sstage + warp * 32 * kEpiRow;   // this warp's staging rows
+            const int q0 = warp * 32;                    // first tile pixel of the warp
             for (int c0 = 0; c0 < a.cout; c0 += 16) {
                 float v[16];
                 __syncwarp();
                 tmem_ld16(acc + (uint32_t)c0, v);
-                if (!in) continue;
-                if (a.out32) {
+                const bool vec32 = a.out32 && (a.out32_ch & 3) == 0 && c0 + 16 <= a.out32_ch;
+                if (a.out32 && !vec32) {   // a narrow FP32 output (the prediction channel)
+                    if (in) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i)
-                        if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + a.bias[c0 + i];
+                        for (int i = 0; i < 16; ++i)
+                            if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + sbias[c0 + i];
+                    }
+                    continue;
+                }
+                // bias and ReLU on this lane's pixel, staged; then the warp
+                // writes its 32 pixels with 16-byte stores, consecutive lanes
+                // on consecutive addresses
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    float u = v[i] + sbias[c0 + i];
+                    if (a.relu && !a.out32) u = fmaxf(u, 0.0f);
+                    v[i] = u;
+                }
+                float4 *row = reinterpret_cast<float4 *>(st + lane * kEpiRow);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) row[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                __syncwarp();
+                if (a.out32) {
+                    for (int j = lane; j < 32 * 4; j += 32) {
+                        const int q = j >> 2, part = j & 3;
+                        const int pq = q0 + q, qx = tx * a.TW + pq % a.TW, qy = ty * a.TH + pq / a.TW;
+                        if (qx >= a.W || qy >= a.H) continue;
+                        const long qpix = ((long)b * a.H + qy) * a.W + qx;
+                        *reinterpret_cast<float4 *>(a.out32 + qpix * a.out32_ch + c0 + 4 * part) =
+                            reinterpret_cast<const float4 *>(st + q * kEpiRow)[part];
+                    }
                     continue;
                 }
                 // BF16 output, split over up to two tensors (the backward pass's
@@ -271,23 +309,32 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
                 const __nv_bfloat16 *msk;
                 if (c0 < a.split) { dst = a.out; cc = c0; cs = a.split; msk = a.mask; }
                 else { dst = a.out2; cc = c0 - a.split; cs = a.cout - a.split; msk = a.mask2; }
-                uint32_t pk[8];
+                for (int j = lane; j < 32 * 2; j += 32) {
+                    const int q = j >> 1, half = j & 1;
+                    const int pq = q0 + q, qx = tx * a.TW + pq % a.TW, qy = ty * a.TH + pq / a.TW;
+                    if (qx >= a.W || qy >= a.H) continue;
+                    const long qpix = ((long)b * a.H + qy) * a.W + qx;
+                    const float *f = st + q * kEpiRow + 8 * half;
+                    float w[8];
 #pragma unroll
-                for (int i = 0; i < 16; i += 2) {
-                    float u0 = v[i] + (a.bias ? a.bias[c0 + i] : 0.0f);
-                    float u1 = v[i + 1] + (a.bias ? a.bias[c0 + i + 1] : 0.0f);
-                    if (a.relu) { u0 = fmaxf(u0, 0.0f); u1 = fmaxf(u1, 0.0f); }
-                    if (msk) {
-                        const __nv_bfloat16 *m = msk + pix * cs + cc + i;
-                        if (!(__bfloat162float(m[0]) > 0.0f)) u0 = 0.0f;
-                        if (!(__bfloat162float(m[1]) > 0.0f)) u1 = 0.0f;
+                    for (int i = 0; i < 8; ++i) w[i] = f[i];
+                    if (msk) {   // ReLU mask of the backward pass: 8 BF16 values in one load
+                        const uint4 mk = *reinterpret_cast<const uint4 *>(msk + qpix * cs + cc + 8 * half);
+                        const uint32_t mw[4] = {mk.x, mk.y, mk.z, mk.w};
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const uint16_t hb = (uint16_t)(mw[i >> 1] >> (16 * (i & 1)));
+                            if (!(__bfloat162float(__ushort_as_bfloat16(hb)) > 0.0f)) w[i] = 0.0f;
+                        }
                     }
-                    const __nv_bfloat162 h = __floats2bfloat162_rn(u0, u1);
-                    pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int i = 0; i < 8; i += 2) {
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(w[i], w[i + 1]);
+                        pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                    }
+                    *reinterpret_cast<uint4 *>(dst + qpix * cs + cc + 8 * half) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 }
-                uint4 *o = reinterpret_cast<uint4 *>(dst + pix * cs + cc);
-                o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
             }
             // this warp's lanes of accumulator bs are read: hand it back
             tc_fence_before();
@@ -424,7 +471,7 @@ static void ring_shape(const TcConvArgs &a, size_t limit, int &nst, int &stage_b
     const int kcmax = a.kc[0] > a.kc[1] ? a.kc[0] : a.kc[1];
     stage_bytes = 128 * kcmax * 2;
     const int nk = 9 * (a.nchunk[0] + a.nchunk[1]);
-    long room = (long)limit - 1024 - a.wbytes - 256;
+    long room = (long)limit - 1024 - a.wbytes - 256 - kEpiBytes;
     if (room > kRingBudget) room = kRingBudget;
     nst = (int)(room / stage_bytes);
     if (nst > kMaxStages) nst = kMaxStages;
@@ -433,7 +480,7 @@ static void ring_shape(const TcConvArgs &a, size_t limit, int &nst, int &stage_b
 }
 
 size_t tc_smem_bytes(int wbytes, int nst, int stage_bytes) {
-    return 1024 + (size_t)wbytes + (size_t)nst * stage_bytes + 8 * (2 * (size_t)nst + 6) + 16;
+    return 1024 + (size_t)wbytes + (size_t)nst * stage_bytes + 8 * (2 * (size_t)nst + 6) + 16 + kEpiBytes;
 }
 
 namespace {
