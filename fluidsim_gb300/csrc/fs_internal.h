@@ -188,9 +188,9 @@ struct fs_ctx {
     int mg_aniso;                // the mesh is anisotropic beyond the electrode strips
     int mg_xline_mode;           // 0: chosen from the mesh (fs_mg_strips), 1: point, 2: x-line
     double *strip_snap64;        // the snapshot, FP64 solver
-    float *strip_snap32;         // the snapshot, mixed solver
+    float *strip_snap32;         // the snapshot, FP32 finest level (mixed solver, FP64 solver with mg_lf = 0)
     // FP64 solver: levels mg_lf.. of its preconditioner run in FP32 (mg_lf =
-    // mg_nlev: none), on these arrays, with the FP32 dense inverse d_ainvc
+    // mg_nlev: none; 0: all), on these arrays, with the FP32 dense inverse d_ainvc
     int mg_lf;
     MGLevelF mgc[FS_MG_MAX_LEVELS];
     float *d_ainvc;

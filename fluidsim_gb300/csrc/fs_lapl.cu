@@ -52,6 +52,7 @@ struct AsmArgs {
     Ctrl *ctrl_w;
     const double *sig;   // sig_pl of the dielectric wall, nx+2
     double *mc, *ce, *cn, *extra, *inv_mc, *rhs, *dinv;
+    float *mc32, *ce32, *cn32, *extra32, *inv_mc32;   // FP32 copy of the operator (the FP32 finest level), or null
 };
 
 __device__ __forceinline__ void tab_index(const PhysParams &pp, double T, int &k, double &w) {
@@ -364,6 +365,13 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         a.mc[o] = mc;
         a.inv_mc[o] = 1.0 / mc;
         a.extra[o] = extra;
+        if (a.mc32) {
+            a.mc32[o] = (float)mc;
+            a.inv_mc32[o] = (float)(1.0 / mc);
+            a.extra32[o] = (float)extra;
+            a.ce32[o] = (float)(offe * sx);
+            a.cn32[o] = (float)(offn * wn * dlx);
+        }
         a.ce[o] = offe * sx;
         a.cn[o] = offn * wn * dlx;
         a.rhs[o] = b * D;
@@ -379,6 +387,8 @@ struct CgArgs {
     dim3 grid;                             // nblk CTAs of 256 threads, grid-stride over nodes
     double *x, *r, *z, *p, *q, *rhs, *dinv, *part;
     const double *mc, *ce, *cn;
+    float *r32;                            // FP32 finest level: its right-hand side, a copy of r (or null)
+    const float *x32;                      // ... and its iterate, z in FP32
     Ctrl *ctrl;
     double rtol;
     int maxit;
@@ -391,6 +401,7 @@ __global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
     CG_NODES(a, {
         a.x[o] = 0.0;
         a.r[o] = a.rhs[o];
+        if (a.r32) a.r32[o] = (float)a.rhs[o];
         a.p[o] = 0.0;
         a.q[o] = 0.0;
         double u = a.rhs[o] * a.dinv[o];
@@ -418,6 +429,21 @@ __device__ __forceinline__ void cg_beta(Ctrl *c, double rz, double zq) {
     c->rz_old = c->rz;
     c->rz = rz;
     c->beta = c->cg_iters == 0 ? 0.0 : -zq / c->pq;
+}
+
+// z = the FP32 finest level's iterate, with rz = r.z and zq = z.q in FP64.
+// (k_cg_pq reading z from the FP32 iterate instead, its five conversions
+// per node on the FP64 pipe, was slower than this write and read of z.)
+__global__ void __launch_bounds__(256) k_cg_rz32(const CgArgs a) {
+    double v = 0.0, u = 0.0;
+    CG_NODES(a, {
+        const double z = (double)a.x32[o];
+        a.z[o] = z;
+        v += a.r[o] * z;
+        u += z * a.q[o];
+    })
+    double sv, su;
+    if (grid_sum2(v, u, a.part, &a.ctrl->counter[1], a.nblk, sv, su) && threadIdx.x == 0) cg_beta(a.ctrl, sv, su);
 }
 
 __global__ void __launch_bounds__(256) k_cg_rz(const CgArgs a) {
@@ -479,6 +505,7 @@ __global__ void __launch_bounds__(256) k_cg_xr(const CgArgs a) {
         a.x[o] += al * a.p[o];
         double rr = a.r[o] - al * a.q[o];
         a.r[o] = rr;
+        if (a.r32) a.r32[o] = (float)rr;
         double u = rr * a.dinv[o];
         v += u * u;
     })
@@ -648,11 +675,11 @@ int fs_lapl_alloc(fs_ctx *c) {
         if ((e = cudaMalloc(&c->d_ainv64, 64 * 64 * sizeof(double))) != cudaSuccess)
             return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
     }
-    // FP32 levels 1.. of the preconditioner (see vcycle): with the fused
-    // smoother and at least two levels above the bottom solver
+    // the preconditioner's levels in FP32 (see vcycle): all of them with the
+    // fused smoother and at least two levels above the bottom solver
     c->mg_lf = nl;
     if (!c->mixed && c->mg_fused && c->mg_lb >= 2) {
-        c->mg_lf = 1;
+        c->mg_lf = 0;
         for (int l = c->mg_lf; l < nl; l++) {
             MGLevelF &m = c->mgc[l];
             m.nx = c->mg[l].nx;
@@ -669,6 +696,12 @@ int fs_lapl_alloc(fs_ctx *c) {
         }
         cudaError_t e = cudaMalloc(&c->d_ainvc, 64 * 64 * sizeof(float));
         if (e != cudaSuccess) return fs_cuda_check(c, e, "cudaMalloc (dense inverse)");
+        if (has_strips(c)) {   // the FP32 finest level's strip snapshot
+            const size_t ns = (size_t)2 * (c->ny + 2) * c->strip_w;
+            e = cudaMalloc(&c->strip_snap32, ns * sizeof(float));
+            if (e == cudaSuccess) e = cudaMemset(c->strip_snap32, 0, ns * sizeof(float));
+            if (e != cudaSuccess) return fs_cuda_check(c, e, "strip snapshot");
+        }
         cudaFuncSetAttribute(k_mg_down<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)mg_down_smem<float>(2));
         cudaFuncSetAttribute(k_mg_up<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg_up_smem<float>(2));
@@ -723,13 +756,18 @@ void fs_lapl_free(fs_ctx *c) {
     c->mg_nlev = 0;
 }
 
-// The V-cycle of the FP64 solver's preconditioner.  Levels mg_lf.. (level 1
-// and coarser on grids with at least two levels above the bottom solver) run
-// in FP32 with the mixed solver's fused level kernels and bottom solver: they
-// are latency- and FP64-issue-bound on this GPU (the FP64 fused levels and
-// bottom solve took ~2.5x their FP32 time) and only shape the preconditioner
-// of the FP64 CG, whose iterate, residual and convergence test stay FP64.
-// Level 0 restricts into and prolongs from the FP32 level 1 in FP64.
+// The V-cycle of the FP64 solver's preconditioner.  Levels mg_lf.. run in
+// FP32 with the mixed solver's fused level kernels, strip sweeps and bottom
+// solver -- on grids with at least two levels above the bottom solver all of
+// them (mg_lf = 0): the V-cycle only shapes the preconditioner of the FP64
+// CG, whose iterate, residual, operator product and convergence test stay
+// FP64, and its FP64 kernels were FP64-issue-bound on this GPU (the FP64
+// fused levels and bottom solve took ~2.5x their FP32 time, the FP64
+// finest-level sweeps ~1.4x).  The finest level's operator is the FP64
+// assembly's, rounded to FP32 as the assembly writes it; its right-hand
+// side is r rounded by the CG kernels that update r, and z comes back in
+// FP64 with r.z (k_cg_rz32).  On smaller grids (mg_lf = mg_nlev) every
+// level runs in FP64.
 static void vcycle(fs_ctx *c, const CgArgs *ca) {
     const int nl = c->mg_nlev, nu = c->cfg.mg_smooth, lf = c->mg_lf;
     int lb = 0;
@@ -737,6 +775,14 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     dim3 b(32, 8);
     for (int l = 0; l < lb; l++) {
         if (l >= lf) {
+            if (l == 0 && c->mg_xline) {   // x-line pre-smoothing, the odd rows' residual restricted
+                const LevelT<float> f = level_f(c->mgc[0]), cc = level_f(c->mgc[1]);
+                xline_pairs<float>(c, f, fs_mg_pre0(nu), true, 1.0f);
+                fs_prof_begin(c, PROF_TRANSFER);
+                k_restrict_odd<float><<<grid2(cc.nx, cc.ny, b), b, 0, c->stream>>>(f, cc);
+                fs_prof_end(c);
+                continue;
+            }
             fs_prof_begin(c, PROF_SMOOTH);
             k_mg_down<float, 2><<<grid2(c->mgc[l].nx, c->mgc[l].ny, dim3(MTX, MTY)), 256, mg_down_smem<float>(2),
                                   c->stream>>>(lvt_f(c->mgc[l]), lvt_f(c->mgc[l + 1]));
@@ -807,10 +853,35 @@ static void vcycle(fs_ctx *c, const CgArgs *ca) {
     }
     for (int l = lb - 1; l >= 0; l--) {
         if (l >= lf) {
-            fs_prof_begin(c, PROF_SMOOTH);
-            k_mg_up<float, 2><<<grid2(c->mgc[l].nx, c->mgc[l].ny, dim3(MTX, MTY)), 256, mg_up_smem<float>(2),
-                                c->stream>>>(lvt_f(c->mgc[l]), lvt_f(c->mgc[l + 1]));
-            fs_prof_end(c);
+            if (l == 0 && c->mg_xline) {   // x-line post-smoothing
+                const LevelT<float> f = level_f(c->mgc[0]);
+                fs_prof_begin(c, PROF_TRANSFER);
+                k_prolong<float><<<grid2(f.nx, f.ny, b), b, 0, c->stream>>>(f, level_f(c->mgc[1]));
+                fs_prof_end(c);
+                xline_pairs<float>(c, f, nu, false, (float)FS_XL_OMEGA_POST);
+            } else {
+                // the finest level's post-smoothing fills the strip snapshot, and
+                // the strips get their extra sweep pairs after it
+                const bool strips = l == 0 && has_strips(c);
+                LvT<float> F = lvt_f(c->mgc[l]);
+                if (strips) F.sn = strip_snap(c, c->strip_snap32);
+                fs_prof_begin(c, PROF_SMOOTH);
+                k_mg_up<float, 2><<<grid2(c->mgc[l].nx, c->mgc[l].ny, dim3(MTX, MTY)), 256, mg_up_smem<float>(2),
+                                    c->stream>>>(F, lvt_f(c->mgc[l + 1]));
+                fs_prof_end(c);
+                if (strips) {
+                    fs_prof_begin(c, PROF_SMOOTH);
+                    k_rb_strips<float><<<dim3((c->ny + STRIP_ROWS - 1) / STRIP_ROWS, 2), 256,
+                                         strip_smem<float>(c->strip_w), c->stream>>>(
+                        level_f(c->mgc[0]), F.sn, 1, (float)FS_MG_OMEGA_POST);
+                    fs_prof_end(c);
+                }
+            }
+            if (l == 0) {   // z in FP64 from the FP32 iterate, r.z and z.q
+                fs_prof_begin(c, PROF_CG);
+                k_cg_rz32<<<ca->grid, 256, 0, c->stream>>>(*ca);
+                fs_prof_end(c);
+            }
             continue;
         }
         LevelDev f = level_dev(c->mg[l]), cc = level_dev(c->mg[l + 1]);
@@ -948,6 +1019,11 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.mc = m0.mc; a.ce = m0.ce; a.cn = m0.cn; a.extra = m0.extra; a.inv_mc = m0.inv_mc;
     a.rhs = c->bs;   // scaled right-hand side D b
     a.dinv = c->dinv;
+    a.mc32 = a.ce32 = a.cn32 = a.extra32 = a.inv_mc32 = nullptr;
+    if (c->mg_lf == 0) {   // the FP32 finest level of the preconditioner
+        MGLevelF &f0 = c->mgc[0];
+        a.mc32 = f0.mc; a.ce32 = f0.ce; a.cn32 = f0.cn; a.extra32 = f0.extra; a.inv_mc32 = f0.inv_mc;
+    }
     // status bits of the assembly
     cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);   // not a kernel
     dim3 g = grid2(c->nx, c->ny, dim3(LBX, LBY));
@@ -956,8 +1032,8 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     fs_prof_end(c);
     // coarse operators: one launch per large level, then one CTA for the
     // small levels and the dense inverse
-    if (c->mg_lf < c->mg_nlev) {   // FP32 levels lf.. (lf = 1): level 1 from the FP64 level 0
-        const int lf = c->mg_lf;
+    if (c->mg_lf < c->mg_nlev) {   // FP32 levels: level 1 from the FP64 level 0 (level 0 came with the assembly)
+        const int lf = std::max(c->mg_lf, 1);
         CoarsenTail<float> ct;
         for (int l = 0; l < c->mg_nlev; l++) {
             ct.L[l] = level_f(c->mgc[l]);
@@ -1009,6 +1085,8 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.x = c->xs; ca.r = c->r; ca.z = c->z; ca.p = c->p; ca.q = c->q;
     ca.rhs = c->bs; ca.dinv = c->dinv; ca.part = c->d_cg_part;
     ca.mc = m0.mc; ca.ce = m0.ce; ca.cn = m0.cn;
+    ca.r32 = c->mg_lf == 0 ? c->mgc[0].rhs : nullptr;
+    ca.x32 = c->mg_lf == 0 ? c->mgc[0].x : nullptr;
     ca.ctrl = c->d_ctrl;
     ca.rtol = c->cfg.lapl_rtol;
     ca.maxit = c->cfg.lapl_maxit;
