@@ -91,3 +91,18 @@ def test_invalid_config_rejected_before_device(built):
         with pytest.raises(api.FluidsimError) as ei:
             api.Discharge(cfg)
         assert ei.value.code == code, bad
+
+
+def test_null_context_rejected(built):
+    """The configuration and driver entry points refuse a null context (or
+    context array) with FS_ERR_INVALID before touching a device."""
+    lib = api.load_library()
+    assert lib.fs_set_line_smoother(None, 0) == abi.FS_ERR_INVALID
+    assert lib.fs_line_smoother(None) == -1
+    assert lib.fs_set_stage_tile(None, 32, 8) == abi.FS_ERR_INVALID
+    st = (abi.FsStats * 1)()
+    rc = (C.c_int32 * 1)()
+    assert lib.fs_batch_run(None, 1, 1, 0.0, 1, st, rc) == abi.FS_ERR_INVALID
+    assert lib.fs_batch_run_fused(None, 1, 1, 0.0, 1, st, rc) == abi.FS_ERR_INVALID
+    arr = (C.c_void_p * 1)(None)
+    assert lib.fs_batch_run_fused(arr, 1, 1, 0.0, 1, st, rc) == abi.FS_ERR_INVALID
