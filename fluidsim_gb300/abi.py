@@ -128,8 +128,19 @@ def declare_api(lib, prefix):
         "get_circuit": ([vp, dp], C.c_int),
         "set_circuit": ([vp, dp], C.c_int),
     }
+    # the Poisson warm-start vector: the GPU library only (the oracle's
+    # solvers start from zero)
+    optional = {
+        "get_lapl_guess": ([vp, dp, C.c_int32], C.c_int),
+        "set_lapl_guess": ([vp, dp, C.c_int32], C.c_int),
+    }
     for name, (args, res) in sig.items():
         f = getattr(lib, prefix + name)
         f.argtypes = args
         f.restype = res
+    for name, (args, res) in optional.items():
+        if hasattr(lib, prefix + name):
+            f = getattr(lib, prefix + name)
+            f.argtypes = args
+            f.restype = res
     return lib

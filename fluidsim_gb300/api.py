@@ -212,9 +212,10 @@ class Handle:
 
     def checkpoint(self):
         """Everything a restart needs: the three-level state, phi, time, dt,
-        the controller, the circuit and the wall charge (host copies)."""
+        the controller, the circuit, the wall charge and the Poisson solver's
+        warm-start vector (host copies)."""
         return dict(state=self.download(nlev=3), t=self.t, dt=self.dt, controller=self.controller(),
-                    circuit=self.circuit(), surface_charge=self.surface_charge())
+                    circuit=self.circuit(), surface_charge=self.surface_charge(), lapl_guess=self.lapl_guess())
 
     def restore(self, ck):
         self.upload(ck["state"])
@@ -224,6 +225,23 @@ class Handle:
         self.set_circuit(c["vd_pl"], c["vd_mi"], c["vd_or"])
         sc = ck["surface_charge"]
         self.set_surface_charge(sc["sig_pl"], sc["sig_mi"], sc["sig_or"])
+        if "lapl_guess" in ck:
+            self.set_lapl_guess(ck["lapl_guess"])
+
+    def lapl_guess(self):
+        """The Poisson solver's warm-start vector, (nx+2, ny+2) Fortran-ordered
+        (None for a library without one: the oracle starts from zero)."""
+        if not hasattr(self._lib, self.prefix + "get_lapl_guess"):
+            return None
+        d = np.zeros((self.nx + 2, self.ny + 2), order="F")
+        self.check(self._f("get_lapl_guess")(self.ctx, abi.dptr(d), self.nx + 2))
+        return d
+
+    def set_lapl_guess(self, d):
+        if d is None or not hasattr(self._lib, self.prefix + "set_lapl_guess"):
+            return
+        d = np.asfortranarray(d, dtype=np.float64)
+        self.check(self._f("set_lapl_guess")(self.ctx, abi.dptr(d), self.nx + 2))
 
     def circuit(self):
         """circ_lib's Vd_pl, Vd_mi, Vd_or and the last source voltage Vsrc."""

@@ -513,6 +513,33 @@ int fs_download_state(fs_ctx *c, double *ni, double *ne, double *nt, double *nm,
     return fs_cuda_check(c, e, "download_state");
 }
 
+int fs_get_lapl_guess(fs_ctx *c, double *d, int32_t ld) {
+    if (!c || !d) return FS_ERR_INVALID;
+    if (ld < c->nx + 2) return fs_set_error(c, FS_ERR_INVALID, "lapl guess: ld %d < nx+2", ld);
+    const int rows = c->ny + 2;
+    if (c->mixed) {   // the mixed solver starts every solve from zero
+        for (int j = 0; j < rows; j++)
+            for (int i = 0; i < c->nx + 2; i++) d[(size_t)j * ld + i] = 0.0;
+        return FS_OK;
+    }
+    cudaError_t e = cudaMemcpy2DAsync(d, (size_t)ld * sizeof(double), c->xs, (size_t)c->pitch * sizeof(double),
+                                      (size_t)(c->nx + 2) * sizeof(double), rows, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "get_lapl_guess");
+}
+
+int fs_set_lapl_guess(fs_ctx *c, const double *d, int32_t ld) {
+    if (!c || !d) return FS_ERR_INVALID;
+    if (ld < c->nx + 2) return fs_set_error(c, FS_ERR_INVALID, "lapl guess: ld %d < nx+2", ld);
+    if (c->mixed) return FS_OK;
+    // interior only: the ghost ring of the iterate stays zero
+    cudaError_t e = cudaMemcpy2DAsync(c->xs + c->pitch + 1, (size_t)c->pitch * sizeof(double), d + ld + 1,
+                                      (size_t)ld * sizeof(double), (size_t)c->nx * sizeof(double), c->ny,
+                                      cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return fs_cuda_check(c, e, "set_lapl_guess");
+}
+
 int fs_ptcl_step(fs_ctx *c, double *dt_inout, double *t_m_out, double *ida_out, double *idc_out,
                  int32_t *attempts_out) {
     if (!c) return FS_ERR_INVALID;

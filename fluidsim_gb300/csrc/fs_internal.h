@@ -88,7 +88,7 @@ struct Ctrl {
     double r0in2;              // mixed solver: inner residual norm^2 at the last refinement
     int inner_it, refine;      // mixed solver: inner iterations since it, refinement due
     double rr_prev;            // mixed solver: previous inner residual norm^2
-    double spare[2];           // [0]: step length of the learned correction
+    double spare[2];           // [0]: step length of the learned correction; [1]: FP64 solver's warm-start scale
     int lpc_off;               // learned correction switched off for this solve (stall)
     int cgm_restarted;         // mixed solver: the last refinement restarted the search direction
     double vd_pl, vd_mi;       // electrode voltage of the RC circuit (AC source, circ_lib.F90:158-174)

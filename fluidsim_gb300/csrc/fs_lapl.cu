@@ -396,27 +396,55 @@ struct CgArgs {
     cudaGraphConditionalHandle cond;
 };
 
-__global__ void __launch_bounds__(256) k_cg_init(const CgArgs a) {
-    double v = 0.0;
+// Warm start.  The previous solve's correction d (still in x) scaled by the
+// alpha that minimises the D^-1-weighted norm of b - alpha M d -- the norm
+// the convergence test takes -- is the initial guess: never a larger initial
+// residual than the zero start, which it becomes when M d vanishes or the
+// sums are not finite.  The corrections of consecutive steps are alike (the
+// discharge moves little in one dt), so the CG starts from a residual
+// several times smaller.  Here M d (into q) and the three sums; alpha goes
+// to the control block (spare[1]).
+__global__ void __launch_bounds__(256) k_cg_init_warm(const CgArgs a) {
+    double v[3] = {0.0, 0.0, 0.0};
     CG_NODES(a, {
-        a.x[o] = 0.0;
-        a.r[o] = a.rhs[o];
-        if (a.r32) a.r32[o] = (float)a.rhs[o];
+        const double d = a.x[o];
+        const double md = a.mc[o] * d - a.ce[o] * a.x[o + 1] - a.ce[o - 1] * a.x[o - 1] - a.cn[o] * a.x[o + a.P]
+                        - a.cn[o - a.P] * a.x[o - a.P];
+        a.q[o] = md;
+        const double bw = a.rhs[o] * a.dinv[o], mw = md * a.dinv[o];
+        v[0] += bw * bw;
+        v[1] += bw * mw;
+        v[2] += mw * mw;
+    })
+    double s[3];
+    if (grid_sum3(v, a.part, &a.ctrl->counter[0], a.nblk, s) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        double al = s[2] > 0.0 ? s[1] / s[2] : 0.0;
+        if (!isfinite(al)) al = 0.0;
+        const double rr = al != 0.0 ? fmax(s[0] - al * s[1], 0.0) : s[0];
+        c->spare[1] = al;
+        c->bnorm2 = s[0];
+        c->rnorm2 = rr;
+        c->relres = s[0] > 0.0 ? sqrt(rr / s[0]) : 0.0;
+        c->cg_done = s[0] == 0.0 ? 1 : 0;
+        c->cg_iters = 0;
+        c->cg_fail = 0;
+        c->rz = 0.0;
+    }
+}
+
+// x = alpha d, r = b - alpha M d (or the zero start), p = q = 0
+__global__ void __launch_bounds__(256) k_cg_init_apply(const CgArgs a) {
+    const double al = a.ctrl->spare[1];
+    const bool warm = al != 0.0;
+    CG_NODES(a, {
+        const double r = warm ? a.rhs[o] - al * a.q[o] : a.rhs[o];
+        a.x[o] = warm ? al * a.x[o] : 0.0;
+        a.r[o] = r;
+        if (a.r32) a.r32[o] = (float)r;
         a.p[o] = 0.0;
         a.q[o] = 0.0;
-        double u = a.rhs[o] * a.dinv[o];
-        v += u * u;
     })
-    double out;
-    if (grid_sum<256>(v, a.part, &a.ctrl->counter[0], a.nblk, &out) && threadIdx.x == 0) {
-        a.ctrl->bnorm2 = out;
-        a.ctrl->rnorm2 = out;
-        a.ctrl->relres = out > 0.0 ? 1.0 : 0.0;
-        a.ctrl->cg_done = out == 0.0 ? 1 : 0;
-        a.ctrl->cg_iters = 0;
-        a.ctrl->cg_fail = 0;
-        a.ctrl->rz = 0.0;
-    }
 }
 
 // rz = r.z and zq = z.q (q = M p_old) of the preconditioned residual, then the
@@ -722,8 +750,8 @@ int fs_lapl_alloc(fs_ctx *c) {
     c->mg[0].rhs = c->r;
     c->mg[0].x = c->z;
     dim3 g = grid2(c->nx, c->ny, dim3(32, 8));
-    // partials of the CG reductions: two per CTA of the (<= 4 per SM) CG grids
-    c->cg_nblk = std::max((int)(g.x * g.y), 2 * 4 * c->nsm);
+    // partials of the CG reductions: three per CTA of the (<= 4 per SM) CG grids
+    c->cg_nblk = std::max((int)(g.x * g.y), 3 * 4 * c->nsm);
     return alloc_zero(c, &c->d_cg_part, (size_t)c->cg_nblk);
 }
 
@@ -1094,7 +1122,10 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     ca.cond = 0;
     dim3 gb = grid2(c->nx, c->ny, dim3(32, 8));
     fs_prof_begin(c, PROF_CG);
-    k_cg_init<<<ca.grid, 256, 0, c->stream>>>(ca);
+    k_cg_init_warm<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cg_init_apply<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     int rc = fs_sync_ctrl(c);
     if (rc) return rc;

@@ -131,6 +131,43 @@ __device__ bool grid_sum2(double v, double w, double *part, unsigned int *counte
     return true;
 }
 
+// Fixed-order sum of three per-thread values over the grid (256-thread CTAs);
+// true in the last CTA (thread 0 holds the sums).  part needs 3 * nblk entries.
+__device__ bool grid_sum3(double (&v)[3], double *part, unsigned int *counter, int nblk, double (&out)[3]) {
+    __shared__ double s_p[3][8];
+    __shared__ bool s_last;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 3; k++) s_p[k][wid] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; k++) {
+            double r = 0.0;
+            for (int w = 0; w < 8; w++) r += s_p[k][w];
+            part[(size_t)k * nblk + blockIdx.x] = r;
+        }
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == (unsigned int)nblk - 1u;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    __shared__ double s_r[3][256];
+    for (int k = 0; k < 3; k++) s_r[k][threadIdx.x] = strided_sum<256>(part + (size_t)k * nblk, nblk, threadIdx.x);
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h)
+            for (int k = 0; k < 3; k++) s_r[k][threadIdx.x] += s_r[k][threadIdx.x + h];
+        __syncthreads();
+    }
+    for (int k = 0; k < 3; k++) out[k] = s_r[k][0];
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
 // ---------------------------------------------------------------- multigrid
 template <typename T>
 struct LevelT {

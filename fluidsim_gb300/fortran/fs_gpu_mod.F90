@@ -114,6 +114,19 @@ module fs_gpu_mod
       type(c_ptr), value :: ctx
       integer(c_int32_t), value :: mode
     end function
+    ! the FP64 Poisson solver's warm-start vector, part of the restart state
+    integer(c_int) function fs_get_lapl_guess(ctx, d, ld) bind(C, name="fs_get_lapl_guess")
+      import :: c_ptr, c_int, c_int32_t, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: d(*)
+      integer(c_int32_t), value :: ld
+    end function
+    integer(c_int) function fs_set_lapl_guess(ctx, d, ld) bind(C, name="fs_set_lapl_guess")
+      import :: c_ptr, c_int, c_int32_t, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: d(*)
+      integer(c_int32_t), value :: ld
+    end function
     ! solver and kernel configuration (no reference counterpart; the Poisson
     ! smoother stands where PETSc's run-time options did, lapl_lib.F90:50-54)
     integer(c_int) function fs_set_line_smoother(ctx, mode) bind(C, name="fs_set_line_smoother")
