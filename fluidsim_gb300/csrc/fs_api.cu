@@ -516,14 +516,24 @@ int fs_download_state(fs_ctx *c, double *ni, double *ne, double *nt, double *nm,
 int fs_get_lapl_guess(fs_ctx *c, double *d, int32_t ld) {
     if (!c || !d) return FS_ERR_INVALID;
     if (ld < c->nx + 2) return fs_set_error(c, FS_ERR_INVALID, "lapl guess: ld %d < nx+2", ld);
-    const int rows = c->ny + 2;
-    if (c->mixed) {   // the mixed solver starts every solve from zero
-        for (int j = 0; j < rows; j++)
-            for (int i = 0; i < c->nx + 2; i++) d[(size_t)j * ld + i] = 0.0;
-        return FS_OK;
+    const int rows = c->ny + 2, w = c->nx + 2;
+    cudaError_t e;
+    if (c->mixed) {   // the mixed solver's iterate is the float-float pair xh + xl
+        std::vector<float> h((size_t)rows * w), l((size_t)rows * w);
+        e = cudaMemcpy2DAsync(h.data(), w * sizeof(float), c->xh32, (size_t)c->pitch * sizeof(float),
+                              w * sizeof(float), rows, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(l.data(), w * sizeof(float), c->xl32, (size_t)c->pitch * sizeof(float),
+                                  w * sizeof(float), rows, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess)
+            for (int j = 0; j < rows; j++)
+                for (int i = 0; i < w; i++)
+                    d[(size_t)j * ld + i] = (double)h[(size_t)j * w + i] + (double)l[(size_t)j * w + i];
+        return fs_cuda_check(c, e, "get_lapl_guess");
     }
-    cudaError_t e = cudaMemcpy2DAsync(d, (size_t)ld * sizeof(double), c->xs, (size_t)c->pitch * sizeof(double),
-                                      (size_t)(c->nx + 2) * sizeof(double), rows, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpy2DAsync(d, (size_t)ld * sizeof(double), c->xs, (size_t)c->pitch * sizeof(double),
+                          w * sizeof(double), rows, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return fs_cuda_check(c, e, "get_lapl_guess");
 }
@@ -531,11 +541,29 @@ int fs_get_lapl_guess(fs_ctx *c, double *d, int32_t ld) {
 int fs_set_lapl_guess(fs_ctx *c, const double *d, int32_t ld) {
     if (!c || !d) return FS_ERR_INVALID;
     if (ld < c->nx + 2) return fs_set_error(c, FS_ERR_INVALID, "lapl guess: ld %d < nx+2", ld);
-    if (c->mixed) return FS_OK;
+    cudaError_t e;
+    if (c->mixed) {   // split into the float-float pair, interior only
+        const int nx = c->nx, ny = c->ny;
+        std::vector<float> h((size_t)ny * nx), l((size_t)ny * nx);
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                const double v = d[(size_t)(j + 1) * ld + i + 1];
+                const float hv = (float)v;
+                h[(size_t)j * nx + i] = hv;
+                l[(size_t)j * nx + i] = (float)(v - (double)hv);
+            }
+        e = cudaMemcpy2DAsync(c->xh32 + c->pitch + 1, (size_t)c->pitch * sizeof(float), h.data(), nx * sizeof(float),
+                              nx * sizeof(float), ny, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(c->xl32 + c->pitch + 1, (size_t)c->pitch * sizeof(float), l.data(),
+                                  nx * sizeof(float), nx * sizeof(float), ny, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        return fs_cuda_check(c, e, "set_lapl_guess");
+    }
     // interior only: the ghost ring of the iterate stays zero
-    cudaError_t e = cudaMemcpy2DAsync(c->xs + c->pitch + 1, (size_t)c->pitch * sizeof(double), d + ld + 1,
-                                      (size_t)ld * sizeof(double), (size_t)c->nx * sizeof(double), c->ny,
-                                      cudaMemcpyHostToDevice, c->stream);
+    e = cudaMemcpy2DAsync(c->xs + c->pitch + 1, (size_t)c->pitch * sizeof(double), d + ld + 1,
+                          (size_t)ld * sizeof(double), (size_t)c->nx * sizeof(double), c->ny,
+                          cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return fs_cuda_check(c, e, "set_lapl_guess");
 }

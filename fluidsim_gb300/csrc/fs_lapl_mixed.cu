@@ -473,6 +473,63 @@ __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
     }
 }
 
+// Warm start, as in the FP64 solver: the previous solve's correction d (the
+// float-float iterate, still in xh + xl) scaled by the alpha that minimises
+// |D^-1 (D b - alpha M d)|, the norm the convergence test takes, is the
+// initial guess; the refinement kernel then forms its residual in
+// float-float arithmetic.  This kernel: M d in FP64 from the FP32 operator,
+// the three sums, alpha (spare[1]) and the control block reset of
+// k_cgm_init, with the refinement requested (relres starts infinite, so
+// that the refinement's "did the residual fall" holds).
+__global__ void __launch_bounds__(256) k_cgm_init_warm(const CgmArgs a) {
+    double v[3] = {0.0, 0.0, 0.0};
+    auto dv = [&](size_t i) { return (double)a.xh[i] + (double)a.xl[i]; };
+    CG_NODES(a, {
+        const double d0 = dv(o);
+        const double md = (double)a.ce[o] * (d0 - dv(o + 1)) + (double)a.ce[o - 1] * (d0 - dv(o - 1))
+                        + (double)a.cn[o] * (d0 - dv(o + a.P)) + (double)a.cn[o - a.P] * (d0 - dv(o - a.P))
+                        + (double)a.extra[o] * d0;
+        const double bw = a.rhs[o] * a.dinv[o], mw = md * a.dinv[o];
+        v[0] += bw * bw;
+        v[1] += bw * mw;
+        v[2] += mw * mw;
+    })
+    double s[3];
+    if (grid_sum3(v, a.part, &a.ctrl->counter[0], a.nblk, s) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        double al = s[2] > 0.0 ? s[1] / s[2] : 0.0;
+        if (!isfinite(al)) al = 0.0;
+        c->spare[1] = al;
+        c->bnorm2 = s[0];
+        c->rnorm2 = s[0];
+        c->relres = INFINITY;
+        c->cg_done = s[0] == 0.0 ? 1 : 0;
+        c->cg_iters = 0;
+        c->cg_fail = 0;
+        c->inner_it = 0;
+        c->refine = 1;
+        c->rz = 0.0;
+        c->alpha = 0.0;
+        c->pq = 0.0;
+        c->lpc_off = 0;
+        c->lpc_stalls = 0;
+        c->cgm_restarted = 1;
+    }
+}
+
+// x = alpha d as a float-float pair (0 for the zero start); p = q = 0
+__global__ void __launch_bounds__(256) k_cgm_init_apply(const CgmArgs a) {
+    const double al = a.ctrl->spare[1];
+    CG_NODES(a, {
+        const double x = al != 0.0 ? al * ((double)a.xh[o] + (double)a.xl[o]) : 0.0;
+        const float h = (float)x;
+        a.xh[o] = h;
+        a.xl[o] = (float)(x - (double)h);
+        a.p[o] = 0.0f;
+        a.q[o] = 0.0f;
+    })
+}
+
 __device__ __forceinline__ float4 ld4(const float *p, size_t o) { return *reinterpret_cast<const float4 *>(p + o); }
 __device__ __forceinline__ void st4(float *p, size_t o, float4 v) { *reinterpret_cast<float4 *>(p + o) = v; }
 __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
@@ -1215,8 +1272,16 @@ int fs_lapl_solve_mixed(fs_ctx *c, int *lerr, int *iters, double *relres) {
         fs_prof_end(c);
     }
     CgmArgs ca = cgm_args(c);
+    // warm start: scale the previous correction, then the refinement forms
+    // the initial residual
     fs_prof_begin(c, PROF_CG);
-    k_cgm_init<<<ca.grid, 256, 0, c->stream>>>(ca);
+    k_cgm_init_warm<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_init_apply<<<ca.grid, 256, 0, c->stream>>>(ca);
+    fs_prof_end(c);
+    fs_prof_begin(c, PROF_CG);
+    k_cgm_refine<<<ca.grid, 256, 0, c->stream>>>(ca);
     fs_prof_end(c);
     int rc = fs_sync_ctrl(c);
     if (rc) return rc;

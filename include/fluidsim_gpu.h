@@ -227,13 +227,13 @@ int fs_get_surface_charge(fs_ctx *ctx, double *sig_pl, double *sig_mi, double *s
 int fs_set_surface_charge(fs_ctx *ctx, const double *sig_pl, const double *sig_mi,
                           const double *sig_or);
 
-/* The FP64 Poisson solver's warm-start vector: the previous solve's
- * correction of phi, which (scaled by the factor that minimises the initial
- * residual) is the next solve's initial guess.  Part of the restart state, so
- * that a restored context continues bit for bit.  ld >= bx+2 doubles per row,
- * (by+2) rows, the reference's layout; the ghost ring is zero.  A mixed-
- * precision context starts every solve from zero: get returns zeros, set is
- * a no-op.  No reference counterpart (the reference's KSP starts from zero,
+/* The Poisson solver's warm-start vector: the previous solve's correction of
+ * phi, which (scaled by the factor that minimises the initial residual) is
+ * the next solve's initial guess.  Part of the restart state, so that a
+ * restored FP64 context continues bit for bit.  ld >= bx+2 doubles per row,
+ * (by+2) rows, the reference's layout; the ghost ring is zero.  In a mixed-
+ * precision context the vector is its float-float iterate (xh + xl).  No
+ * reference counterpart (the reference's KSP starts from zero,
  * lapl_lib.F90:52). */
 int fs_get_lapl_guess(fs_ctx *ctx, double *d, int32_t ld);
 int fs_set_lapl_guess(fs_ctx *ctx, const double *d, int32_t ld);
