@@ -473,63 +473,6 @@ __global__ void __launch_bounds__(256) k_cgm_init(const CgmArgs a) {
     }
 }
 
-// Warm start, as in the FP64 solver: the previous solve's correction d (the
-// float-float iterate, still in xh + xl) scaled by the alpha that minimises
-// |D^-1 (D b - alpha M d)|, the norm the convergence test takes, is the
-// initial guess; the refinement kernel then forms its residual in
-// float-float arithmetic.  This kernel: M d in FP64 from the FP32 operator,
-// the three sums, alpha (spare[1]) and the control block reset of
-// k_cgm_init, with the refinement requested (relres starts infinite, so
-// that the refinement's "did the residual fall" holds).
-__global__ void __launch_bounds__(256) k_cgm_init_warm(const CgmArgs a) {
-    double v[3] = {0.0, 0.0, 0.0};
-    auto dv = [&](size_t i) { return (double)a.xh[i] + (double)a.xl[i]; };
-    CG_NODES(a, {
-        const double d0 = dv(o);
-        const double md = (double)a.ce[o] * (d0 - dv(o + 1)) + (double)a.ce[o - 1] * (d0 - dv(o - 1))
-                        + (double)a.cn[o] * (d0 - dv(o + a.P)) + (double)a.cn[o - a.P] * (d0 - dv(o - a.P))
-                        + (double)a.extra[o] * d0;
-        const double bw = a.rhs[o] * a.dinv[o], mw = md * a.dinv[o];
-        v[0] += bw * bw;
-        v[1] += bw * mw;
-        v[2] += mw * mw;
-    })
-    double s[3];
-    if (grid_sum3(v, a.part, &a.ctrl->counter[0], a.nblk, s) && threadIdx.x == 0) {
-        Ctrl *c = a.ctrl;
-        double al = s[2] > 0.0 ? s[1] / s[2] : 0.0;
-        if (!isfinite(al)) al = 0.0;
-        c->spare[1] = al;
-        c->bnorm2 = s[0];
-        c->rnorm2 = s[0];
-        c->relres = INFINITY;
-        c->cg_done = s[0] == 0.0 ? 1 : 0;
-        c->cg_iters = 0;
-        c->cg_fail = 0;
-        c->inner_it = 0;
-        c->refine = 1;
-        c->rz = 0.0;
-        c->alpha = 0.0;
-        c->pq = 0.0;
-        c->lpc_off = 0;
-        c->lpc_stalls = 0;
-        c->cgm_restarted = 1;
-    }
-}
-
-// x = alpha d as a float-float pair (0 for the zero start); p = q = 0
-__global__ void __launch_bounds__(256) k_cgm_init_apply(const CgmArgs a) {
-    const double al = a.ctrl->spare[1];
-    CG_NODES(a, {
-        const double x = al != 0.0 ? al * ((double)a.xh[o] + (double)a.xl[o]) : 0.0;
-        const float h = (float)x;
-        a.xh[o] = h;
-        a.xl[o] = (float)(x - (double)h);
-        a.p[o] = 0.0f;
-        a.q[o] = 0.0f;
-    })
-}
-
 __device__ __forceinline__ float4 ld4(const float *p, size_t o) { return *reinterpret_cast<const float4 *>(p + o); }
 __device__ __forceinline__ void st4(float *p, size_t o, float4 v) { *reinterpret_cast<float4 *>(p + o) = v; }
 __device__ __forceinline__ float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
@@ -562,6 +505,79 @@ __device__ __forceinline__ FF ff_mulf(FF a, float c) {   // (a.h + a.l) c
 __device__ __forceinline__ FF ff_from(double d) {
     const float h = __double2float_rn(d);
     return {h, __double2float_rn(d - (double)h)};
+}
+
+// Warm start, as in the FP64 solver: the previous solve's correction d (the
+// float-float iterate, still in xh + xl) scaled by the alpha that minimises
+// |D^-1 (D b - alpha M d)|, the norm the convergence test takes, is the
+// initial guess; the refinement kernel then forms its residual in
+// float-float arithmetic, so alpha itself needs no more than FP32 accuracy
+// (M d of the leading part xh, FP32 sums; a sum that overflows or vanishes
+// gives alpha = 0, the zero start).  This kernel: the three sums, alpha
+// (spare[1]) and the control block reset of k_cgm_init, with the refinement
+// requested (relres starts infinite, so that the refinement's "did the
+// residual fall" holds).
+__global__ void __launch_bounds__(256) k_cgm_init_warm(const CgmArgs a) {
+    float v[3] = {0.0f, 0.0f, 0.0f};
+    CG_NODES(a, {
+        const float d0 = a.xh[o];
+        const float md = a.ce[o] * (d0 - a.xh[o + 1]) + a.ce[o - 1] * (d0 - a.xh[o - 1])
+                       + a.cn[o] * (d0 - a.xh[o + a.P]) + a.cn[o - a.P] * (d0 - a.xh[o - a.P]) + a.extra[o] * d0;
+        const float bw = (float)a.rhs[o] * a.dinv32[o], mw = md * a.dinv32[o];
+        v[0] += bw * bw;
+        v[1] += bw * mw;
+        v[2] += mw * mw;
+    })
+    double s[3];
+    if (grid_sumf<3>(v, reinterpret_cast<float *>(a.part), &a.ctrl->counter[0], a.nblk, s) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        double al = s[2] > 0.0 ? s[1] / s[2] : 0.0;
+        if (!isfinite(al)) al = 0.0;
+        c->spare[1] = al;
+        c->cg_done = 0;   // decided by the refinement on the exact |D b|
+        c->cg_iters = 0;
+        c->cg_fail = 0;
+        c->inner_it = 0;
+        c->refine = 1;
+        c->relres = INFINITY;
+        c->rz = 0.0;
+        c->alpha = 0.0;
+        c->pq = 0.0;
+        c->lpc_off = 0;
+        c->lpc_stalls = 0;
+        c->cgm_restarted = 1;
+    }
+}
+
+// x = alpha d in float-float arithmetic (0 for the zero start); p = q = 0;
+// |D b|^2 for the convergence test (FP64 sum), and a zero right-hand side
+// ends the solve here
+__global__ void __launch_bounds__(256) k_cgm_init_apply(const CgmArgs a) {
+    const double al = a.ctrl->spare[1];
+    const FF alf = ff_from(al);
+    double vb = 0.0;
+    CG_NODES(a, {
+        const float xh = a.xh[o], xl = a.xl[o];
+        const float pr = __fmul_rn(alf.h, xh);
+        const float t = __fmaf_rn(alf.h, xl, __fmaf_rn(alf.l, xh, __fmaf_rn(alf.h, xh, -pr)));
+        const FF x = ff_fast2(pr, t);
+        a.xh[o] = al != 0.0 ? x.h : 0.0f;
+        a.xl[o] = al != 0.0 ? x.l : 0.0f;
+        a.p[o] = 0.0f;
+        a.q[o] = 0.0f;
+        const double u = a.rhs[o] * a.dinv[o];
+        vb += u * u;
+    })
+    double sb;
+    if (grid_sum<256>(vb, a.part, &a.ctrl->counter[0], a.nblk, &sb) && threadIdx.x == 0) {
+        Ctrl *c = a.ctrl;
+        c->bnorm2 = sb;
+        c->rnorm2 = sb;
+        if (sb == 0.0) {
+            c->cg_done = 1;
+            c->relres = 0.0;
+        }
+    }
 }
 
 // M z at one node in float-float arithmetic: each face term c (z_i - z_j) is
