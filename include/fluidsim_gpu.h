@@ -197,9 +197,12 @@ int fs_ptcl_step(fs_ctx *ctx, double *dt_inout, double *t_m_out,
                  double *ida_out, double *idc_out, int32_t *attempts_out);
 
 /* lapl_solve(g, ne(:,:,1), ni(:,:,1), nt(:,:,1), sig, lerr): assemble the
- * semi-implicit correction system with g%dt = dt, solve it to cfg->lapl_rtol,
- * and on success ph += delta, ph_mi = ph.  lerr_out = 0 converged, 1 not
- * (the caller then rejects the step, main.F90:102-121). */
+ * semi-implicit correction system with g%dt = dt, solve it to cfg->lapl_rtol
+ * (relative to the right-hand side's norm, as the reference's KSP; the
+ * multigrid-preconditioned CG starts from the previous solve's correction
+ * scaled to minimise the initial residual, see fs_get_lapl_guess), and on
+ * success ph += delta, ph_mi = ph.  lerr_out = 0 converged, 1 not (the caller
+ * then rejects the step, main.F90:102-121). */
 int fs_lapl_solve(fs_ctx *ctx, double dt, int32_t *lerr_out,
                   int32_t *iters_out, double *relres_out);
 
