@@ -197,6 +197,7 @@ struct fs_ctx {
     double *d_ainv64;            // dense inverse of level mg_dl (FP64 solver)
     float *d_ainv32;             // dense inverse of level mg_dl (mixed solver)
     double *p, *q, *z, *r, *xs, *bs, *dinv;  // CG vectors: solution xs, rhs D*b, 1/D
+    int dinv_done;               // 1/D (a property of the mesh) has been written
     double *d_cg_part;
     int cg_nblk;
     // CG loop as a CUDA graph with a conditional WHILE node (built on first use)

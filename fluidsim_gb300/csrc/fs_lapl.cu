@@ -363,11 +363,12 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         const double mc = (offw + offe) * sx + (offs * ws + offn * wn) * dlx + extra;
         const double D = dlx * dly * wr;
         a.mc[o] = mc;
-        a.inv_mc[o] = 1.0 / mc;
+        if (a.inv_mc) a.inv_mc[o] = 1.0 / mc;   // the FP64 finest level's smoother only
         a.extra[o] = extra;
         if (a.mc32) {
-            a.mc32[o] = (float)mc;
-            a.inv_mc32[o] = (float)(1.0 / mc);
+            const float mc32 = (float)mc;
+            a.mc32[o] = mc32;
+            a.inv_mc32[o] = 1.0f / mc32;
             a.extra32[o] = (float)extra;
             a.ce32[o] = (float)(offe * sx);
             a.cn32[o] = (float)(offn * wn * dlx);
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(LNT, 2) k_assemble(const AsmArgs a) {
         a.ce[o] = offe * sx;
         a.cn[o] = offn * wn * dlx;
         a.rhs[o] = b * D;
-        a.dinv[o] = 1.0 / D;
+        if (a.dinv) a.dinv[o] = 1.0 / D;   // a property of the mesh: the first assembly writes it
     }
     if (st) atomicOr(&a.ctrl_w->status, st);
 }
@@ -1048,16 +1049,19 @@ int fs_lapl_solve_impl(fs_ctx *c, int *lerr, int *iters, double *relres) {
     a.rhs = c->bs;   // scaled right-hand side D b
     a.dinv = c->dinv;
     a.mc32 = a.ce32 = a.cn32 = a.extra32 = a.inv_mc32 = nullptr;
-    if (c->mg_lf == 0) {   // the FP32 finest level of the preconditioner
+    if (c->mg_lf == 0) {   // the FP32 finest level of the preconditioner (no FP64 smoothing there)
         MGLevelF &f0 = c->mgc[0];
         a.mc32 = f0.mc; a.ce32 = f0.ce; a.cn32 = f0.cn; a.extra32 = f0.extra; a.inv_mc32 = f0.inv_mc;
+        a.inv_mc = nullptr;
     }
+    if (c->dinv_done) a.dinv = nullptr;
     // status bits of the assembly
     cudaMemsetAsync(&c->d_ctrl->status, 0, sizeof(unsigned int), c->stream);   // not a kernel
     dim3 g = grid2(c->nx, c->ny, dim3(LBX, LBY));
     fs_prof_begin(c, PROF_ASSEMBLE);
     k_assemble<<<g, LNT, 0, c->stream>>>(a);
     fs_prof_end(c);
+    c->dinv_done = 1;
     // coarse operators: one launch per large level, then one CTA for the
     // small levels and the dense inverse
     if (c->mg_lf < c->mg_nlev) {   // FP32 levels: level 1 from the FP64 level 0 (level 0 came with the assembly)
