@@ -476,13 +476,13 @@ __global__ void k_faces(const PhysParams pp, const MeshDev m, const double *ph, 
     if (gi > nx || gj > ny) return;
     const size_t o = (size_t)gj * P + gi;
     if (gj >= 1) {
-        double E = -(ph[o + 1] - ph[o]) / m.dx[gi];
+        double E = -(ph[o + 1] - ph[o]) * m.inv_dx[gi];   // reciprocal product (<= 1 ulp from the division)
         double cl, cr, dl, dr;
         ion_face(pp, E, m.dx[gi], m.inv_dx[gi], cl, cr, dl, dr);
         f.fx_e[o] = E; f.fx_cl[o] = cl; f.fx_cr[o] = cr; f.fx_dl[o] = dl; f.fx_dr[o] = dr;
     }
     if (gi >= 1) {
-        double E = -(ph[o + P] - ph[o]) / m.dy[gj];
+        double E = -(ph[o + P] - ph[o]) * m.inv_dy[gj];
         double cl, cr, dl, dr;
         ion_face(pp, E, m.dy[gj], m.inv_dy[gj], cl, cr, dl, dr);
         f.fy_e[o] = E; f.fy_cl[o] = cl; f.fy_cr[o] = cr; f.fy_dl[o] = dl; f.fy_dr[o] = dr;
