@@ -21,6 +21,14 @@
 //   * four warps read the other accumulator (tcgen05.ld, one pixel per
 //     thread) and apply bias, ReLU (or the ReLU mask of the backward pass)
 //     and the BF16 store while the next tile's MMAs run.
+// Halo rows (grids at least 128 wide, when three row slots fit): a tile is
+// one 128-pixel row segment and each CTA takes a contiguous run of rows.  The
+// producer loads each input row once, 130 pixels wide (the segment and one
+// pixel either side), into a ring of row slots; the MMAs of output row y read
+// rows y - 1, y, y + 1, the three x taps of a row being the same slot at
+// start addresses one pixel (one swizzled K-major row) apart.  A row slot is
+// freed by the commit after its last output row, so an input row crosses
+// from L2 once per run instead of three times per tap row.
 // Every wait on an mbarrier is bounded: a wait that runs out sets *err and
 // the CTA skips the rest of its work (after a bounded wait for its own
 // copies and MMAs in flight) and frees its tensor memory.
@@ -98,6 +106,39 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo, uint3
     return d;
 }
 
+// Coordinates of the CTA's it-th tile.  Halo rows: contiguous runs of the
+// linear tile index with y fastest; otherwise tiles blockIdx.x + it * gridDim.x
+// with x fastest.
+__device__ __forceinline__ void tile_at(const TcConvArgs &a, int it, int &tx, int &ty, int &b) {
+    long t;
+    if (a.halo) {
+        t = (long)blockIdx.x * a.ntiles / gridDim.x + it;
+        ty = (int)(t % a.tiles_y);
+        t /= a.tiles_y;
+        tx = (int)(t % a.tiles_x);
+        b = (int)(t / a.tiles_x);
+    } else {
+        t = blockIdx.x + (long)it * gridDim.x;
+        tx = (int)(t % a.tiles_x);
+        t /= a.tiles_x;
+        ty = (int)(t % a.tiles_y);
+        b = (int)(t / a.tiles_y);
+    }
+}
+
+// halo rows: the run of consecutive output rows starting at the CTA's tile it
+// (same image and x segment), its first row y0 and x segment tx, b
+__device__ __forceinline__ int run_at(const TcConvArgs &a, int it, int ntile_cta, int &tx, int &y0, int &b) {
+    tile_at(a, it, tx, y0, b);
+    int n = 1;
+    for (; it + n < ntile_cta; ++n) {
+        int t2, y2, b2;
+        tile_at(a, it + n, t2, y2, b2);
+        if (y2 != y0 + n) break;
+    }
+    return n;
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accum) {
     asm volatile(
@@ -115,17 +156,24 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld16(uint32_t addr, float (&v)[16]) {
-    uint32_t r[16];
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane: the
+// load is issued here and its registers hold the values only after
+// tmem_wait_ld, which names them as operands so that no use moves above it
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t addr, uint32_t (&r)[16]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(addr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
 }
 
 // swizzle mode field and atom size of a K chunk of kc BF16 channels
@@ -138,7 +186,7 @@ __device__ __host__ __forceinline__ uint32_t swz_atom(int kc) { return 8u * 2u *
 // accumulators in tensor memory while warps 0-3 drain the other (TMEM lane
 // quarter w to warp w), so loads, MMAs and the epilogue of consecutive tiles
 // overlap.
-__global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUtensorMap tm0,
+__global__ void __launch_bounds__(192, 4) k_conv_tc(const __grid_constant__ CUtensorMap tm0,
                                                     const __grid_constant__ CUtensorMap tm1, const TcConvArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -160,7 +208,9 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nper = a.nchunk[0] + a.nchunk[1];       // K chunks per tap
     const int nk = 9 * nper;
-    const int ntile_cta = blockIdx.x < a.ntiles ? (a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int ntile_cta =
+        a.halo ? (int)((long)(blockIdx.x + 1) * a.ntiles / gridDim.x - (long)blockIdx.x * a.ntiles / gridDim.x)
+               : blockIdx.x < a.ntiles ? (a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     if (threadIdx.x == 0) {
         // a CTA of this launch whose wait ran out voids the result: skip the work
@@ -188,16 +238,91 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (warp == 4 && lane == 0) {
+    if (warp == 4 && lane == 0 && a.halo) {
+        // producer, halo rows: the weight image, then for each run of output
+        // rows y0 .. y0 + n - 1 the input rows y0 - 1 .. y0 + n, one slot each
+        // (all K chunks of the row; rows outside the grid read TMA's zero fill)
+        mbar_expect_tx(wbar, (uint32_t)a.wbytes);
+        bulk_copy(sw, a.wimg, (uint32_t)a.wbytes, wbar);
+        long g = 0;   // rows issued
+        bool go = true;
+        for (int it = 0; go && it < ntile_cta && !*vfail;) {
+            int tx, y0, b;
+            const int n = run_at(a, it, ntile_cta, tx, y0, b);
+            for (int r = y0 - 1; r <= y0 + n; ++r, ++g) {
+                const int s = (int)(g % nst);
+                const long u = g / nst;
+                if (u > 0 && !mbar_wait(empty + s, (uint32_t)((u - 1) & 1))) { atomicExch(&s_fail, 1); go = false; break; }
+                mbar_expect_tx(full + s, (uint32_t)a.row_tx);
+                uint8_t *dst = sa + (size_t)s * a.stage_bytes;
+                for (int q = 0; q < nper; ++q) {
+                    const int src = q < a.nchunk[0] ? 0 : 1, j = src ? q - a.nchunk[0] : q;
+                    tma_load_4d(dst + a.qoff[q], src ? &tm1 : &tm0, j * a.kc[src], tx * a.TW - 1, r, b, full + s);
+                }
+            }
+            it += n;
+        }
+        for (long h = g - nst > 0 ? g - nst : 0; h < g; ++h)
+            mbar_wait(full + (int)(h % nst), (uint32_t)((h / nst) & 1));
+    } else if (warp == 5 && lane == 0 && a.halo) {
+        // MMA issuer, halo rows: output row y of a run reads row slots of
+        // input rows y - 1, y, y + 1 (row loads g + k, g + k + 1, g + k + 2);
+        // tap (dy, dx) = that slot at dx pixels' offset
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.cout >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
+        bool ok = mbar_wait(wbar, 0);
+        long g = 0;   // row load of the current run's first input row
+        for (int it = 0; ok && it < ntile_cta;) {
+            int tx, y0, b;
+            const int n = run_at(a, it, ntile_cta, tx, y0, b);
+            for (int k = 0; ok && k < n; ++k, ++it) {
+                const int bs = it & 1, u = it >> 1;
+                if (u > 0 && !mbar_wait(tempty + bs, (uint32_t)((u - 1) & 1))) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(bs * a.tmem_cols);
+                uint32_t accum = 0;
+                for (int dr = 0; ok && dr < 3; ++dr) {
+                    const long L = g + k + dr;
+                    const int s = (int)(L % nst);
+                    if (!mbar_wait(full + s, (uint32_t)((L / nst) & 1)) || *vfail) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t rbase = smem_u32(sa + (size_t)s * a.stage_bytes);
+                    for (int q = 0; q < nper; ++q) {
+                        const int kcw = a.kc[q < a.nchunk[0] ? 0 : 1];
+                        const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
+                        for (int dx = 0; dx < 3; ++dx) {
+                            const uint32_t abase = rbase + (uint32_t)a.qoff[q] + (uint32_t)(dx * 2 * kcw);
+                            const uint32_t bbase = smem_u32(sw + a.boff[(dr * 3 + dx) * nper + q]);
+                            for (int kk = 0; kk < kcw / 16; ++kk) {
+                                mma_bf16(acc, smem_desc(abase + 32 * kk, atom, mode),
+                                         smem_desc(bbase + 32 * kk, atom, mode), idesc, accum);
+                                accum = 1;
+                            }
+                        }
+                    }
+                }
+                if (!ok) break;
+                mma_commit(tfull + bs);
+                // input row y - 1 has no later reader; at the run's end neither have y, y + 1
+                mma_commit(empty + (int)((g + k) % nst));
+                if (k == n - 1) {
+                    mma_commit(empty + (int)((g + k + 1) % nst));
+                    mma_commit(empty + (int)((g + k + 2) % nst));
+                }
+            }
+            g += n + 2;
+        }
+        if (!ok) atomicExch(&s_fail, 1);
+        mma_commit(fin);
+        mbar_wait(fin, 0);
+    } else if (warp == 4 && lane == 0) {
         // producer: the weight image, then the A chunks of each tile, tap by tap
         mbar_expect_tx(wbar, (uint32_t)a.wbytes);
         bulk_copy(sw, a.wimg, (uint32_t)a.wbytes, wbar);
         long g = 0;   // chunks issued
         for (int it = 0; it < ntile_cta && !*vfail; ++it) {
-            int tile = blockIdx.x + it * gridDim.x;
-            const int tx = tile % a.tiles_x;
-            tile /= a.tiles_x;
-            const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
+            int tx, ty, b;
+            tile_at(a, it, tx, ty, b);
             const int x0 = tx * a.TW, y0 = ty * a.TH;
             for (int kc = 0; kc < nk; ++kc, ++g) {
                 const int s = (int)(g % nst);
@@ -247,58 +372,82 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
         mma_commit(fin);
         mbar_wait(fin, 0);
     } else if (warp < 4) {
-        // epilogue: thread = one pixel of the tile (its TMEM lane)
+        // epilogue: thread = one pixel of the tile (its TMEM lane).  The
+        // accumulator is read 16 columns at a time, the next group's load in
+        // flight while the current one is written out.
         const int p = warp * 32 + lane;
+        const int lgw = __ffs(a.TW) - 1;                 // TW is a power of two
+        const int ps = a.out32 ? 2 : 1;                 // log2 lanes per pixel in the coalesced stores
+        const int sub = lane & ((1 << ps) - 1);          // the lane's 16-byte piece of a pixel's row
+        const int q0 = warp * 32;                        // first tile pixel of the warp
+        float *st = sstage + warp * 32 * kEpiRow;       // this warp's staging rows
+        const bool narrow = a.out32 && !((a.out32_ch & 3) == 0 && a.out32_ch >= 16);
         for (int it = 0; it < ntile_cta; ++it) {
             const int bs = it & 1, u = it >> 1;
             bool ok = mbar_wait(tfull + bs, (uint32_t)(u & 1));
             ok = __all_sync(0xffffffffu, ok);   // warp-uniform (tcgen05.ld is warp-collective)
             if (!ok) { atomicExch(&s_fail, 1); break; }
             tc_fence_after();
-            int tile = blockIdx.x + it * gridDim.x;
-            const int tx = tile % a.tiles_x;
-            tile /= a.tiles_x;
-            const int ty = tile % a.tiles_y, b = tile / a.tiles_y;
-            const int px = tx * a.TW + p % a.TW, py = ty * a.TH + p / a.TW;
+            int tx, ty, b;
+            tile_at(a, it, tx, ty, b);
+            const int xb = tx * a.TW, yb = ty * a.TH;
+            const int px = xb + (p & (a.TW - 1)), py = yb + (p >> lgw);
             const bool in = px < a.W && py < a.H;
             const long pix = ((long)b * a.H + py) * a.W + px;
+            // the pixels this lane stores in the coalesced passes (4 FP32 passes
+            // of 8 pixels, or 2 BF16 passes of 16), -1 outside the grid
+            long qp[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int pq = q0 + (lane >> ps) + i * (32 >> ps);
+                const int qx = xb + (pq & (a.TW - 1)), qy = yb + (pq >> lgw);
+                qp[i] = (i < (1 << ps) && qx < a.W && qy < a.H) ? ((long)b * a.H + qy) * a.W + qx : -1;
+            }
             const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(bs * a.tmem_cols);
-            float *st = sstage + warp * 32 * kEpiRow;   // this warp's staging rows
-            const int q0 = warp * 32;                    // first tile pixel of the warp
+            uint32_t r[16];
+            __syncwarp();
+            tmem_ld16_issue(acc, r);
             for (int c0 = 0; c0 < a.cout; c0 += 16) {
-                float v[16];
                 __syncwarp();
-                tmem_ld16(acc + (uint32_t)c0, v);
-                const bool vec32 = a.out32 && (a.out32_ch & 3) == 0 && c0 + 16 <= a.out32_ch;
-                if (a.out32 && !vec32) {   // a narrow FP32 output (the prediction channel)
+                tmem_wait_ld(r);
+                float v[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+                if (c0 + 16 < a.cout) tmem_ld16_issue(acc + (uint32_t)(c0 + 16), r);   // next group in flight
+                const float4 *b4 = reinterpret_cast<const float4 *>(sbias + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 bb = b4[j];
+                    v[4 * j] += bb.x; v[4 * j + 1] += bb.y; v[4 * j + 2] += bb.z; v[4 * j + 3] += bb.w;
+                }
+                if (a.out32 && !narrow && c0 + 16 > a.out32_ch) continue;   // past the output's channels
+                if (narrow) {   // a narrow FP32 output (the prediction channel)
                     if (in) {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
-                            if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i] + sbias[c0 + i];
+                            if (c0 + i < a.out32_ch) a.out32[pix * a.out32_ch + c0 + i] = v[i];
                     }
                     continue;
                 }
                 // bias and ReLU on this lane's pixel, staged; then the warp
                 // writes its 32 pixels with 16-byte stores, consecutive lanes
                 // on consecutive addresses
+                if (a.relu && !a.out32) {
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    float u = v[i] + sbias[c0 + i];
-                    if (a.relu && !a.out32) u = fmaxf(u, 0.0f);
-                    v[i] = u;
+                    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
                 }
+                __syncwarp();   // the previous group's staging rows are read
                 float4 *row = reinterpret_cast<float4 *>(st + lane * kEpiRow);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) row[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 __syncwarp();
                 if (a.out32) {
-                    for (int j = lane; j < 32 * 4; j += 32) {
-                        const int q = j >> 2, part = j & 3;
-                        const int pq = q0 + q, qx = tx * a.TW + pq % a.TW, qy = ty * a.TH + pq / a.TW;
-                        if (qx >= a.W || qy >= a.H) continue;
-                        const long qpix = ((long)b * a.H + qy) * a.W + qx;
-                        *reinterpret_cast<float4 *>(a.out32 + qpix * a.out32_ch + c0 + 4 * part) =
-                            reinterpret_cast<const float4 *>(st + q * kEpiRow)[part];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        if (qp[i] < 0) continue;
+                        const int q = (lane >> 2) + 8 * i;
+                        *reinterpret_cast<float4 *>(a.out32 + qp[i] * a.out32_ch + c0 + 4 * sub) =
+                            reinterpret_cast<const float4 *>(st + q * kEpiRow)[sub];
                     }
                     continue;
                 }
@@ -309,31 +458,31 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc(const __grid_constant__ CUte
                 const __nv_bfloat16 *msk;
                 if (c0 < a.split) { dst = a.out; cc = c0; cs = a.split; msk = a.mask; }
                 else { dst = a.out2; cc = c0 - a.split; cs = a.cout - a.split; msk = a.mask2; }
-                for (int j = lane; j < 32 * 2; j += 32) {
-                    const int q = j >> 1, half = j & 1;
-                    const int pq = q0 + q, qx = tx * a.TW + pq % a.TW, qy = ty * a.TH + pq / a.TW;
-                    if (qx >= a.W || qy >= a.H) continue;
-                    const long qpix = ((long)b * a.H + qy) * a.W + qx;
-                    const float *f = st + q * kEpiRow + 8 * half;
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    if (qp[i] < 0) continue;
+                    const int q = (lane >> 1) + 16 * i;
+                    const float *f = st + q * kEpiRow + 8 * sub;
                     float w[8];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) w[i] = f[i];
+                    for (int k = 0; k < 8; ++k) w[k] = f[k];
+                    const long off = qp[i] * cs + cc + 8 * sub;
                     if (msk) {   // ReLU mask of the backward pass: 8 BF16 values in one load
-                        const uint4 mk = *reinterpret_cast<const uint4 *>(msk + qpix * cs + cc + 8 * half);
+                        const uint4 mk = *reinterpret_cast<const uint4 *>(msk + off);
                         const uint32_t mw[4] = {mk.x, mk.y, mk.z, mk.w};
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            const uint16_t hb = (uint16_t)(mw[i >> 1] >> (16 * (i & 1)));
-                            if (!(__bfloat162float(__ushort_as_bfloat16(hb)) > 0.0f)) w[i] = 0.0f;
+                        for (int k = 0; k < 8; ++k) {
+                            const uint16_t hb = (uint16_t)(mw[k >> 1] >> (16 * (k & 1)));
+                            if (!(__bfloat162float(__ushort_as_bfloat16(hb)) > 0.0f)) w[k] = 0.0f;
                         }
                     }
                     uint32_t pk[4];
 #pragma unroll
-                    for (int i = 0; i < 8; i += 2) {
-                        const __nv_bfloat162 h = __floats2bfloat162_rn(w[i], w[i + 1]);
-                        pk[i / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                    for (int k = 0; k < 8; k += 2) {
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(w[k], w[k + 1]);
+                        pk[k / 2] = *reinterpret_cast<const uint32_t *>(&h);
                     }
-                    *reinterpret_cast<uint4 *>(dst + qpix * cs + cc + 8 * half) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    *reinterpret_cast<uint4 *>(dst + off) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 }
             }
             // this warp's lanes of accumulator bs are read: hand it back
@@ -412,11 +561,15 @@ void tc_tile_shape(int W, int &TW, int &TH) {
     TH = 128 / TW;
 }
 
-int tc_make_map(CUtensorMap *m, const void *base, int B, int H, int W, int C, int kc) {
+int tc_make_map(CUtensorMap *m, const void *base, int B, int H, int W, int C, int kc, int halo) {
     if (load_encoder()) return -1;
     if (!(kc == 16 || kc == 32 || kc == 64) || C % kc || (reinterpret_cast<uintptr_t>(base) & 15)) return -2;
     int TW, TH;
     tc_tile_shape(W, TW, TH);
+    if (halo) {   // one input row: the segment and one pixel either side
+        if (TH != 1) return -2;
+        TW += 2;
+    }
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
     const cuuint32_t box[4] = {(cuuint32_t)kc, (cuuint32_t)TW, (cuuint32_t)TH, 1};
@@ -445,6 +598,12 @@ int tc_weight_layout(int c1, int c2, int cout, int *boff, int *kc, int *nchunk) 
             off += (bytes + 1023) / 1024 * 1024;
         }
     return off;
+}
+
+void tc_set_tiles(TcConvArgs &a) {
+    tc_tile_shape(a.W, a.TW, a.TH);
+    a.tiles_x = (a.W + a.TW - 1) / a.TW;
+    a.tiles_y = (a.H + a.TH - 1) / a.TH;
 }
 
 static void build_image(const float *w, int c1, int c2, int cout, void *img, int transposed, cudaStream_t st) {
@@ -477,6 +636,21 @@ static void ring_shape(const TcConvArgs &a, size_t limit, int &nst, int &stage_b
     if (nst > kMaxStages) nst = kMaxStages;
     if (nst > nk) nst = nk;   // one tile ahead: a deeper ring costs CTAs per SM (measured slower)
     if (nst < 2) nst = 2;
+}
+
+// halo rows: a row slot holds each K chunk of one input row (130 pixels) in a
+// block of its own, 1024-aligned for the swizzle; fills qoff and row_tx
+static int halo_slot(TcConvArgs &a) {
+    const int nper = a.nchunk[0] + a.nchunk[1];
+    int off = 0, tx = 0;
+    for (int q = 0; q < nper && q < 4; ++q) {
+        const int kc = a.kc[q < a.nchunk[0] ? 0 : 1], bytes = 130 * kc * 2;
+        a.qoff[q] = off;
+        tx += bytes;
+        off += (bytes + 1023) / 1024 * 1024;
+    }
+    a.row_tx = tx;
+    return off;
 }
 
 size_t tc_smem_bytes(int wbytes, int nst, int stage_bytes) {
@@ -520,10 +694,26 @@ int tc_init() {
 
 size_t tc_smem_limit() { return g_smem_max; }
 
+int tc_halo_fits(const TcConvArgs &a0) {
+    if (!g_smem_max || a0.W < 128 || a0.nchunk[0] + a0.nchunk[1] > 4) return 0;
+    TcConvArgs a = a0;
+    const long room = (long)g_smem_max - 1024 - a.wbytes - 256 - kEpiBytes;
+    return room >= 3L * halo_slot(a) ? 1 : 0;
+}
+
 int tc_conv(const CUtensorMap *m0, const CUtensorMap *m1, const TcConvArgs &a0, cudaStream_t st) {
     if (!g_smem_max) return -2;
     TcConvArgs a = a0;
-    ring_shape(a, g_smem_max, a.nst, a.stage_bytes);
+    if (a.halo) {
+        // row slots: three in use and up to two loading ahead
+        if (!tc_halo_fits(a)) return -2;
+        a.stage_bytes = halo_slot(a);
+        const long room = (long)g_smem_max - 1024 - a.wbytes - 256 - kEpiBytes;
+        a.nst = (int)(room / a.stage_bytes);
+        if (a.nst > 5) a.nst = 5;
+    } else {
+        ring_shape(a, g_smem_max, a.nst, a.stage_bytes);
+    }
     const size_t smem = tc_smem_bytes(a.wbytes, a.nst, a.stage_bytes);
     if (smem > g_smem_max) return -2;
     a.ntiles = a.tiles_x * a.tiles_y * a.B;
@@ -576,17 +766,16 @@ extern "C" int fs_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t c1, int32_
     else cudaMemset(d + o_b, 0, cout * 4);
     cudaMemset(d + o_err, 0, 16);
     tc_build_weights(reinterpret_cast<float *>(d + o_w), c1, c2, cout, d + o_img, st);
+    a.cout = cout;
+    a.B = B; a.H = H; a.W = W;
+    a.halo = tc_halo_fits(a);
     CUtensorMap m0, m1;
-    if (tc_make_map(&m0, d + o_in1, B, H, W, c1, a.kc[0]) ||
-        (c2 && tc_make_map(&m1, d + o_in2, B, H, W, c2, a.kc[1])))
+    if (tc_make_map(&m0, d + o_in1, B, H, W, c1, a.kc[0], a.halo) ||
+        (c2 && tc_make_map(&m1, d + o_in2, B, H, W, c2, a.kc[1], a.halo)))
         rc = -3;
     if (!rc) {
-        a.cout = cout;
         a.tmem_cols = tc_tmem_cols(cout);
-        a.B = B; a.H = H; a.W = W;
-        tc_tile_shape(W, a.TW, a.TH);
-        a.tiles_x = (W + a.TW - 1) / a.TW;
-        a.tiles_y = (H + a.TH - 1) / a.TH;
+        tc_set_tiles(a);
         a.wimg = d + o_img;
         a.bias = reinterpret_cast<float *>(d + o_b);
         a.relu = mode == 1;

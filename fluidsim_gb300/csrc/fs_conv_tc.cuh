@@ -26,15 +26,26 @@ struct TcConvArgs {
     float *out32;              // FP32 output [pix][out32_ch] instead of BF16 (null: BF16)
     int out32_ch;
     int *err;                  // set to 1 if a wait ran out
+    int halo;                  // 1: halo-row tiles, 0: tap tiles (tc_halo_fits)
     int nst, stage_bytes, ntiles;   // A ring and tile count (set by tc_conv)
+    int qoff[4];               // halo rows: byte offset of each K chunk in a row slot (set by tc_conv)
+    int row_tx;                // halo rows: bytes one row slot receives (set by tc_conv)
 };
 
 // pixel tile of a grid W wide: TW = min(128, W) rounded up to a power of two
 // (at least 16), TH = 128 / TW
 void tc_tile_shape(int W, int &TW, int &TH);
 // TMA descriptor of an NHWC BF16 tensor [B][H][W][C] read in chunks of kc
-// channels over the tile box; 0 or a negative error
-int tc_make_map(CUtensorMap *m, const void *base, int B, int H, int W, int C, int kc);
+// channels over the tile box (halo = 0) or over one input row of TW + 2
+// pixels (halo = 1); 0 or a negative error
+int tc_make_map(CUtensorMap *m, const void *base, int B, int H, int W, int C, int kc, int halo);
+// 1 if a layer (kc, nchunk, wbytes, W set; after tc_init) runs with halo
+// rows: tiles of one 128-pixel row segment, each input row loaded once and
+// shared by the three output rows that read it; needs a grid at least 128
+// wide and three row slots beside the weight image
+int tc_halo_fits(const TcConvArgs &a);
+// tile geometry of a layer (W, H, halo set): TW, TH, tiles_x, tiles_y
+void tc_set_tiles(TcConvArgs &a);
 // block offsets of the weight image of a layer with sources of c1 and c2
 // channels and cout outputs; fills kc, nchunk; returns the image size in bytes
 int tc_weight_layout(int c1, int c2, int cout, int *boff, int *kc, int *nchunk);

@@ -321,15 +321,15 @@ int tc_layer(LpcState *L, int l, int bwd, int B, int H, int W, const bf16 *in1, 
     if (!bwd) { ci1 = Y.c1; ci2 = Y.c2; co = Y.cout; }
     else { ci1 = Y.cout; ci2 = 0; co = Y.c1 + Y.c2; }
     a.wbytes = tc_weight_layout(ci1, ci2, co, a.boff, a.kc, a.nchunk);
-    CUtensorMap m[2];
-    if (tc_make_map(&m[0], in1, B, H, W, ci1, a.kc[0]) || (ci2 && tc_make_map(&m[1], in2, B, H, W, ci2, a.kc[1])))
-        return -1;
     a.cout = co;
-    a.tmem_cols = tc_tmem_cols(co);
     a.B = B; a.H = H; a.W = W;
-    tc_tile_shape(W, a.TW, a.TH);
-    a.tiles_x = (W + a.TW - 1) / a.TW;
-    a.tiles_y = (H + a.TH - 1) / a.TH;
+    a.halo = tc_halo_fits(a);
+    CUtensorMap m[2];
+    if (tc_make_map(&m[0], in1, B, H, W, ci1, a.kc[0], a.halo) ||
+        (ci2 && tc_make_map(&m[1], in2, B, H, W, ci2, a.kc[1], a.halo)))
+        return -1;
+    a.tmem_cols = tc_tmem_cols(co);
+    tc_set_tiles(a);
     a.wimg = L->img + (bwd ? Y.img_b : Y.img_f);
     a.err = L->d_tc_err;
     if (!bwd) {

@@ -55,7 +55,7 @@ def _run(B, H, W, c1, c2, cout, mode, seed=0):
 @pytest.mark.parametrize("B,H,W,c1,c2,cout", [
     (1, 8, 128, 16, 0, 16), (1, 16, 256, 16, 0, 32), (2, 12, 64, 32, 0, 64), (1, 33, 47, 64, 0, 64),
     (1, 20, 128, 64, 64, 64), (1, 10, 96, 64, 32, 32), (2, 9, 40, 32, 16, 16), (1, 6, 200, 128, 0, 32),
-    (3, 4, 16, 16, 16, 16)])
+    (3, 4, 16, 16, 16, 16), (3, 7, 384, 32, 16, 48), (2, 1, 256, 64, 0, 16), (1, 3, 130, 16, 0, 128)])
 def test_conv_fp32_output(built, B, H, W, c1, c2, cout):
     out, ref = _run(B, H, W, c1, c2, cout, 0)
     err = np.abs(out - ref) / (np.abs(ref) + 1.0)
@@ -71,17 +71,18 @@ def test_conv_bf16_relu_output(built):
 
 
 @pytest.mark.parametrize("H,W,c1,c2,cout", [(1024, 1024, 16, 0, 16), (256, 256, 64, 0, 64), (256, 256, 64, 64, 64),
-                                            (512, 512, 64, 32, 32)])
+                                            (512, 512, 64, 32, 32), (1024, 1024, 64, 0, 64)])
 def test_conv_network_shapes(built, H, W, c1, c2, cout):
     """Layers of the 4-level U-Net at the 1024^2 solver grid (the first
     encoder layer, a level-2 layer, the level-2 and level-1 decoder layers
-    with their skip inputs), FP32 output; the reference is evaluated at 4096
-    random output pixels to keep the CPU side short."""
+    with their skip inputs) and a 64-channel layer at the full grid (77
+    GFLOP, the compute-bound case), FP32 output; the reference is evaluated
+    at 4096 random output pixels to keep the CPU side short."""
     from fluidsim_gb300 import api
     lib = api.load_library()
     rng = np.random.default_rng(5)
-    x1b, x1 = _bf16_bits(rng.standard_normal((1, H, W, c1)).astype(np.float32))
-    x2b, x2 = _bf16_bits(rng.standard_normal((1, H, W, c2)).astype(np.float32)) if c2 else (None, None)
+    x1b, x1 = _bf16_bits(rng.standard_normal((1, H, W, c1), dtype=np.float32))
+    x2b, x2 = _bf16_bits(rng.standard_normal((1, H, W, c2), dtype=np.float32)) if c2 else (None, None)
     w32 = (rng.standard_normal((9, cout, c1 + c2)) / np.sqrt(9 * (c1 + c2))).astype(np.float32)
     _, wq = _bf16_bits(w32)
     bias = rng.standard_normal(cout).astype(np.float32)
