@@ -584,6 +584,45 @@ def run_gpu(args):
     breakdown = d.profile_read()
     d.profile([])
 
+    # ---- optional: the reference's output files every K steps ---------------
+    # The same steps from the checkpoint with and without a record (the
+    # writeOut files) after every K steps; the writer thread's last record is
+    # on disk before the closing event.
+    output = None
+    if args.output_every > 0:
+        K = args.output_every
+        res = {}
+        with tempfile.TemporaryDirectory() as td:
+            for write in (False, True):
+                d.restore(ck)
+                d.ts = ck["controller"]["ts"]
+                if write:
+                    d.write_output(td, init=True)
+                    d.output_wait()
+                barrier()
+                torch.cuda.synchronize()
+                e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                call_s, done = 0.0, 0
+                e4.record(stream)
+                while done < args.steps:
+                    n = min(K, args.steps - done)
+                    d.run(n)
+                    done += n
+                    if write:
+                        t0 = time.perf_counter()
+                        d.write_output(td)
+                        call_s += time.perf_counter() - t0
+                if write:
+                    d.output_wait()
+                e5.record(stream)
+                torch.cuda.synchronize()
+                res[write] = (e4.elapsed_time(e5), call_s)
+        nrec = (args.steps + K - 1) // K
+        output = {"every": K, "records": nrec,
+                  "steps_per_s_without": args.steps / (res[False][0] * 1e-3),
+                  "steps_per_s_with": args.steps / (res[True][0] * 1e-3),
+                  "call_ms": 1e3 * res[True][1] / nrec}
+
     # ---- roofline of the dominant kernel (RK stage, FP64-issue-bound) -------
     hbm_peak, peak_kind = measured_peaks()
     fp64_peak = fp64_peak_tflops(local)
@@ -662,6 +701,8 @@ def run_gpu(args):
             "clocks": clocks,
             "gpu_launches": launches,
         }
+        if output is not None:
+            line["output"] = output
         print(json.dumps(line))
     d.close()
     if ws > 1:
@@ -686,6 +727,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the mixed-precision comparison run")
     ap.add_argument("--sweep", action="store_true", help="the batched uneven sweep instead")
+    ap.add_argument("--output-every", type=int, default=0,
+                    help="also time the steps with the reference's output files written every K steps")
     ap.add_argument("--accuracy", action="store_true",
                     help="per-field error of the mixed path against the FP64 path instead")
     ap.add_argument("--acc-steps", type=int, default=2000)

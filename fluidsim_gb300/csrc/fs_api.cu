@@ -1,6 +1,7 @@
 // fs_api.cu -- C ABI of the CUDA implementation (include/fluidsim_gpu.h):
 // context creation (lapl_init + ptcl_init + circ_init), state transfer, the
 // per-step entry points and the main-loop rotation of main.F90:83-121.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -117,6 +118,25 @@ __global__ void k_fill(double *p, size_t n, double v) {
 }
 
 __global__ void k_set_dt(Ctrl *c, double dt) { c->dt = dt; }
+
+// One writeOut record in the reference's units (main.F90:297-333), the
+// interior block of each field x fastest, as the files hold it: f1 = phi ph0,
+// f2 = n_e / x0^3, f3 = n_i / x0^3, f4 = n_eps / x0^3 ph0 / 1.5 (the same
+// operations in the same order as the host conversion, IEEE-rounded), f5 =
+// n_m / x0^3 or zeros with three species.
+__global__ void k_output_record(const double *ph, const double *ni, const double *ne, const double *nt,
+                                const double *nm, int nx, int ny, int P, double x03, double ph0, double *dst) {
+    const size_t n = (size_t)nx * ny;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nx), j = (int)(q / nx);
+        const size_t o = (size_t)(j + 1) * P + i + 1;
+        dst[q] = ph[o] * ph0;
+        dst[n + q] = ne[o] / x03;
+        dst[2 * n + q] = ni[o] / x03;
+        dst[3 * n + q] = nt[o] / x03 * ph0 / 1.5;
+        dst[4 * n + q] = nm ? nm[o] / x03 : 0.0;
+    }
+}
 
 // maxval over the three RK levels of one species, ghost ring included:
 // pass 1, CTA b takes elements [b*FS_MAX_PER_CTA, (b+1)*FS_MAX_PER_CTA) of
@@ -903,4 +923,16 @@ int fs_lpc_info(fs_ctx *c, int32_t *h, int32_t *w, int32_t *nsamples, int64_t *n
     if (solves) *solves = c->lpc_solves;
     if (nn_solves) *nn_solves = c->lpc_nn_solves;
     return FS_OK;
+}
+
+// The converted record of the level-1 fields into dev (5 nx ny doubles),
+// queued on the context's stream.
+cudaError_t fs_output_stage(fs_ctx *c, double *dev, double x03) {
+    const int ns = c->cfg.nspecies, lv = c->lev[0];
+    const size_t n = (size_t)c->nx * c->ny;
+    const int nb = (int)std::min<size_t>((n + 255) / 256, 4096);
+    k_output_record<<<nb, 256, 0, c->stream>>>(c->ph, c->sp[0].buf[lv], c->sp[1].buf[lv], c->sp[2].buf[lv],
+                                               ns == 4 ? c->sp[3].buf[lv] : nullptr, c->nx, c->ny, c->pitch, x03,
+                                               c->k.ph0, dev);
+    return cudaGetLastError();
 }

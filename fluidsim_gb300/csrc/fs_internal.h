@@ -298,6 +298,9 @@ int fs_lpc_grad_impl(fs_ctx *c, const float *feat, const float *tgt, const float
                      float *loss, float *pred);
 // output writer (fs_output.cpp): waits for the record in flight, stops the thread
 void fs_output_free(fs_ctx *c);
+// one output record converted on the device into dev, on the context's
+// stream (fs_api.cu)
+cudaError_t fs_output_stage(fs_ctx *c, double *dev, double x03);
 // misc device helpers (fs_api.cu)
 int fs_run(fs_ctx *c, int32_t nsteps, fs_stats *out);
 int fs_cuda_check(fs_ctx *c, cudaError_t e, const char *what);

@@ -10,13 +10,15 @@
 // t), vd.dat (V), ida.dat / idc.dat (A), dt.dat (nondimensional) and flx.dat
 // (the EM flux, zero: the EM module is not part of the path).
 //
-// A record is written asynchronously: fs_write_output queues a device-to-host
-// copy of the level-1 fields into a pinned staging buffer on the context's
-// stream, records an event and hands the record to the context's writer
-// thread, which waits for the event, converts and appends while the caller
-// keeps stepping (stream order makes the copy see the state as of the call).
-// One record is in flight at a time: the next call, fs_output_wait and
-// fs_destroy wait for it.
+// A record is written asynchronously: fs_write_output queues on the context's
+// stream a kernel that converts the level-1 fields into the files' units and
+// layout (fs_output_stage; stream order makes it see the state as of the
+// call), then on the writer's own copy stream, after that kernel, one
+// device-to-host copy of the result into a pinned block, so that the copy
+// overlaps the steps that follow; the writer thread waits for the copy and
+// appends the five blocks to their files, one thread per file, while the
+// caller keeps stepping.  One record is in flight at a time: the next call,
+// fs_output_wait and fs_destroy wait for it.
 #include <condition_variable>
 #include <cstdio>
 #include <mutex>
@@ -36,8 +38,11 @@ struct fs_output {
     // the record in flight
     std::string dir;
     double vals[6] = {0, 0, 0, 0, 0, 0};
-    double *stage = nullptr;     // pinned: ni, ne, nt, nm, ph at (nx+2, ny+2) each
-    cudaEvent_t ev = nullptr;
+    double *stage = nullptr;     // pinned: the f1..f5 blocks, nx ny values each
+    double *dstage = nullptr;    // device: the same blocks, converted by fs_output_stage
+    cudaEvent_t ev = nullptr;    // the record's copy is complete (copy stream)
+    cudaEvent_t conv = nullptr;  // the record's conversion is complete (context's stream)
+    cudaStream_t cs = nullptr;   // copy stream
     int nx = 0, ny = 0, ns = 3;
     int device = 0;
     double x0 = 0, ph0 = 0;
@@ -54,32 +59,29 @@ int put(std::string &err, const std::string &path, const double *v, size_t n, bo
     return FS_OK;
 }
 
-// writeOut for the staged record (runs on the writer thread)
+// writeOut for the staged record (runs on the writer thread): the five field
+// blocks, already in the files' units and layout, appended by one thread each,
+// then the six scalars
 int write_record(fs_output &o) {
-    const int nx = o.nx, ny = o.ny, ld = nx + 2;
-    const size_t ng = (size_t)ld * (ny + 2);
-    const double x03 = o.x0 * o.x0 * o.x0, ph0 = o.ph0;
+    const size_t n = (size_t)o.nx * o.ny;
     const std::string p = o.dir + "/";
-    std::vector<double> blk((size_t)nx * ny);
-    auto field = [&](int q) { return o.stage + (size_t)q * ng; };
-    // the interior block, each value converted as writeOut converts it
-    auto interior = [&](const double *a, auto conv) {
-        for (int j = 1; j <= ny; j++)
-            for (int i = 1; i <= nx; i++) blk[(size_t)(j - 1) * nx + (i - 1)] = conv(a[(size_t)j * ld + i]);
-    };
-    int rc;
-    interior(field(4), [&](double v) { return v * ph0; });
-    if ((rc = put(o.err, p + "f1.dat", blk.data(), blk.size(), true))) return rc;
-    interior(field(1), [&](double v) { return v / x03; });
-    if ((rc = put(o.err, p + "f2.dat", blk.data(), blk.size(), true))) return rc;
-    interior(field(0), [&](double v) { return v / x03; });
-    if ((rc = put(o.err, p + "f3.dat", blk.data(), blk.size(), true))) return rc;
-    interior(field(2), [&](double v) { return v / x03 * ph0 / 1.5; });
-    if ((rc = put(o.err, p + "f4.dat", blk.data(), blk.size(), true))) return rc;
-    if (o.ns == 4) interior(field(3), [&](double v) { return v / x03; });
-    else std::fill(blk.begin(), blk.end(), 0.0);
-    if ((rc = put(o.err, p + "f5.dat", blk.data(), blk.size(), true))) return rc;
+    static const char *fields[5] = {"f1.dat", "f2.dat", "f3.dat", "f4.dat", "f5.dat"};
+    int rcs[5] = {FS_OK, FS_OK, FS_OK, FS_OK, FS_OK};
+    std::string errs[5];
+    auto one = [&](int q) { rcs[q] = put(errs[q], p + fields[q], o.stage + q * n, n, true); };
+    std::thread th[4];
+    int started = 0;
+    try {
+        for (; started < 4; started++) th[started] = std::thread(one, started + 1);
+    } catch (...) {   // no thread to be had: the rest on this one
+    }
+    for (int q = started + 1; q < 5; q++) one(q);
+    one(0);
+    for (int t = 0; t < started; t++) th[t].join();
+    for (int q = 0; q < 5; q++)
+        if (rcs[q]) { o.err = errs[q]; return rcs[q]; }
     static const char *names[6] = {"time.dat", "vd.dat", "ida.dat", "idc.dat", "dt.dat", "flx.dat"};
+    int rc;
     for (int k = 0; k < 6; k++)
         if ((rc = put(o.err, p + names[k], &o.vals[k], 1, true))) return rc;
     return FS_OK;
@@ -131,11 +133,17 @@ int start(fs_ctx *c) {
     o->ns = c->cfg.nspecies;
     o->x0 = c->k.x0;
     o->ph0 = c->k.ph0;
-    const size_t ng = (size_t)(c->nx + 2) * (c->ny + 2);
-    cudaError_t e = cudaMallocHost(&o->stage, sizeof(double) * 5 * ng);
+    const size_t n = (size_t)c->nx * c->ny;
+    cudaError_t e = cudaMallocHost(&o->stage, sizeof(double) * 5 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&o->dstage, sizeof(double) * 5 * n);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&o->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&o->conv, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&o->cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         if (o->stage) cudaFreeHost(o->stage);
+        if (o->dstage) cudaFree(o->dstage);
+        if (o->ev) cudaEventDestroy(o->ev);
+        if (o->conv) cudaEventDestroy(o->conv);
         delete o;
         return fs_cuda_check(c, e, "output staging");
     }
@@ -156,8 +164,12 @@ void fs_output_free(fs_ctx *c) {
         o->cv.notify_all();
     }
     o->th.join();
+    cudaStreamSynchronize(o->cs);
+    cudaStreamDestroy(o->cs);
     cudaEventDestroy(o->ev);
+    cudaEventDestroy(o->conv);
     cudaFreeHost(o->stage);
+    cudaFree(o->dstage);
     delete o;
     c->out = nullptr;
 }
@@ -189,16 +201,15 @@ int fs_write_output(fs_ctx *c, const char *dir, int32_t init) {
     }
     if ((rc = start(c))) return rc;
     fs_output *o = c->out;
-    // stage the level-1 fields on the stream: ni, ne, nt, nm, ph
-    const size_t ld = (size_t)c->nx + 2, rows = (size_t)c->ny + 2, ng = ld * rows;
-    const size_t w = ld * sizeof(double), dp = (size_t)c->pitch * sizeof(double);
-    cudaError_t e = cudaSuccess;
-    for (int s = 0; s < c->cfg.nspecies && e == cudaSuccess; s++)
-        e = cudaMemcpy2DAsync(o->stage + (size_t)s * ng, w, c->sp[s].buf[c->lev[0]], dp, w, rows,
-                              cudaMemcpyDeviceToHost, c->stream);
+    // the level-1 fields converted on the device (context's stream), then
+    // copied to the pinned block on the copy stream
+    const size_t n = (size_t)c->nx * c->ny;
+    cudaError_t e = fs_output_stage(c, o->dstage, o->x0 * o->x0 * o->x0);
+    if (e == cudaSuccess) e = cudaEventRecord(o->conv, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(o->cs, o->conv, 0);
     if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(o->stage + 4 * ng, w, c->ph, dp, w, rows, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(o->ev, c->stream);
+        e = cudaMemcpyAsync(o->stage, o->dstage, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, o->cs);
+    if (e == cudaSuccess) e = cudaEventRecord(o->ev, o->cs);
     if (e != cudaSuccess) return fs_cuda_check(c, e, "output staging copy");
     std::lock_guard<std::mutex> lk(o->m);
     o->dir = dir;
