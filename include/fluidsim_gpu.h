@@ -344,9 +344,12 @@ int fs_max_ne_noalloc(fs_ctx *ctx, double *out);
  * idc.dat, dt.dat, flx.dat; init = 0 appends the current state -- raw native
  * FP64, same units and layout as the reference, so its save.py reads them.
  * With three species f5.dat gets zeros; flx.dat (the EM flux) gets 0.
- * init = 0 returns once the record's device-to-host copy is queued on the
- * context's stream: a writer thread appends it to the files while the caller
- * keeps stepping.  One record is in flight at a time; the next
+ * init = 0 returns once the record is queued: a kernel on the context's
+ * stream converts the fields (the state as of the call), a stream of the
+ * writer's own copies the result to pinned host memory, and a writer thread
+ * appends it to the files while the caller keeps stepping.  The first
+ * init = 0 call allocates 5 nx ny doubles on the device and as much pinned
+ * host memory.  One record is in flight at a time; the next
  * fs_write_output, fs_output_wait and fs_destroy wait for it, and a write
  * error surfaces from whichever of the first two comes next. */
 int fs_write_output(fs_ctx *ctx, const char *dir, int32_t init);
