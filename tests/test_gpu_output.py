@@ -10,12 +10,18 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_output_files_match_state(built, tmp_path):
+@pytest.mark.parametrize("species", [3, 4])
+def test_output_files_match_state(built, tmp_path, species):
+    """Three species (the glow workload; f5 zeros) and four (the reference's
+    defaults, fits; f5 the metastables in m^-3)."""
     from fluidsim_gb300 import api, config, grid
-    cfg = config.glow(40, ny=32)
+    cfg = config.glow(40, ny=32) if species == 3 else config.reference_defaults(40, 32)
     mesh = cfg.mesh()
     k = api.constants(cfg)
-    d = api.Discharge(cfg, mesh, grid.blob_state(mesh, k, noise=0.01, seed=2, vl=cfg.vl))
+    st = grid.blob_state(mesh, k, noise=0.01, seed=2, vl=cfg.vl if species == 3 else None)
+    if species == 4:
+        st["nm"] = np.asfortranarray(0.1 * st["ni"])
+    d = api.Discharge(cfg, mesh, st)
     d.write_output(str(tmp_path), init=True)
     states, times = [], []
     for _ in range(3):
@@ -37,12 +43,17 @@ def test_output_files_match_state(built, tmp_path):
     x03 = k["x0"] * k["x0"] * k["x0"]
     conv = {"f1.dat": ("ph", lambda v: v * k["ph0"]), "f2.dat": ("ne", lambda v: v / x03),
             "f3.dat": ("ni", lambda v: v / x03), "f4.dat": ("nt", lambda v: v / x03 * k["ph0"] / 1.5)}
+    if species == 4:
+        conv["f5.dat"] = ("nm", lambda v: v / x03)
     for fname, (field, f) in conv.items():
         data = rd(fname).reshape([nt, ny, nx])
         for r in range(nt):
             want = f(np.asarray(states[r][field])[1:-1, 1:-1]).T
             assert np.array_equal(data[r], want), (fname, r)
-    assert np.all(rd("f5.dat") == 0) and rd("f5.dat").size == nt * ny * nx
+    assert rd("f5.dat").size == nt * ny * nx
+    if species == 3:
+        assert np.all(rd("f5.dat") == 0)
     for n in ("vd.dat", "ida.dat", "idc.dat", "dt.dat", "flx.dat"):
         assert rd(n).size == nt
-    assert np.allclose(rd("vd.dat"), cfg.vl * k["ph0"])
+    if species == 3:
+        assert np.allclose(rd("vd.dat"), cfg.vl * k["ph0"])
