@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(192, 4) k_conv_tc(const __grid_constant__ CUte
     float *sstage = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tslot + 1) + 15) & ~(uintptr_t)15);
     float *sbias = sstage + 4 * 32 * kEpiRow;
     __shared__ int s_fail;
+    __shared__ uint64_t s_bdesc[TC_MAX_CHUNKS];      // B descriptor of each (tap, chunk) weight block
     volatile int *vfail = &s_fail;   // raised by any role whose wait ran out
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -221,6 +222,13 @@ __global__ void __launch_bounds__(192, 4) k_conv_tc(const __grid_constant__ CUte
         mbar_init(fin, 1);
     }
     for (int i = threadIdx.x; i < a.cout; i += blockDim.x) sbias[i] = a.bias ? a.bias[i] : 0.0f;
+    // the MMA descriptors of the weight blocks, once per CTA: the issuing
+    // thread then adds offsets to precomputed descriptors (a descriptor's
+    // start field is the address / 16, so address + 32 k is descriptor + 2 k)
+    for (int i = threadIdx.x; i < 9 * (a.nchunk[0] + a.nchunk[1]); i += blockDim.x) {
+        const int q = i % (a.nchunk[0] + a.nchunk[1]), kcw = a.kc[q < a.nchunk[0] ? 0 : 1];
+        s_bdesc[i] = smem_desc(smem_u32(sw + a.boff[i]), swz_atom(kcw), swz_mode(kcw));
+    }
     if (threadIdx.x == 0) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -288,14 +296,14 @@ __global__ void __launch_bounds__(192, 4) k_conv_tc(const __grid_constant__ CUte
                     tc_fence_after();
                     const uint32_t rbase = smem_u32(sa + (size_t)s * a.stage_bytes);
                     for (int q = 0; q < nper; ++q) {
-                        const int kcw = a.kc[q < a.nchunk[0] ? 0 : 1];
-                        const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
+                        const int kcw = a.kc[q < a.nchunk[0] ? 0 : 1], nk16 = kcw / 16;
+                        // the chunk's A descriptor at dx = 0; each dx one pixel row (2 kcw bytes) on
+                        const uint64_t a0 = smem_desc(rbase + (uint32_t)a.qoff[q], swz_atom(kcw), swz_mode(kcw));
+                        const uint64_t *bd = s_bdesc + dr * 3 * nper + q;
                         for (int dx = 0; dx < 3; ++dx) {
-                            const uint32_t abase = rbase + (uint32_t)a.qoff[q] + (uint32_t)(dx * 2 * kcw);
-                            const uint32_t bbase = smem_u32(sw + a.boff[(dr * 3 + dx) * nper + q]);
-                            for (int kk = 0; kk < kcw / 16; ++kk) {
-                                mma_bf16(acc, smem_desc(abase + 32 * kk, atom, mode),
-                                         smem_desc(bbase + 32 * kk, atom, mode), idesc, accum);
+                            const uint64_t ad = a0 + (uint64_t)(dx * kcw / 8), bdx = bd[dx * nper];
+                            for (int kk = 0; kk < nk16; ++kk) {
+                                mma_bf16(acc, ad + 2 * kk, bdx + 2 * kk, idesc, accum);
                                 accum = 1;
                             }
                         }
@@ -357,12 +365,10 @@ __global__ void __launch_bounds__(192, 4) k_conv_tc(const __grid_constant__ CUte
                 const int t = kc / nper, q = kc - t * nper;
                 const int src = q < a.nchunk[0] ? 0 : 1;
                 const int kcw = a.kc[src];
-                const uint32_t mode = swz_mode(kcw), atom = swz_atom(kcw);
-                const uint32_t abase = smem_u32(sa + (size_t)s * a.stage_bytes);
-                const uint32_t bbase = smem_u32(sw + a.boff[t * nper + q]);
+                const uint64_t ad = smem_desc(smem_u32(sa + (size_t)s * a.stage_bytes), swz_atom(kcw), swz_mode(kcw));
+                const uint64_t bd = s_bdesc[t * nper + q];
                 for (int k = 0; k < kcw / 16; ++k)
-                    mma_bf16(acc, smem_desc(abase + 32 * k, atom, mode), smem_desc(bbase + 32 * k, atom, mode),
-                             idesc, (kc > 0 || k > 0) ? 1u : 0u);
+                    mma_bf16(acc, ad + 2 * k, bd + 2 * k, idesc, (kc > 0 || k > 0) ? 1u : 0u);
                 mma_commit(empty + s);
             }
             if (ok) mma_commit(tfull + bs);
@@ -527,7 +533,77 @@ __global__ void k_tc_weights(const float *w, int c1, int c2, int cout, TcConvArg
     }
 }
 
+// tcgen05.mma issue rate, the bound of the convolutions: one thread issues
+// nmma MMAs (M = 128, N = n, K = 16, BF16 x BF16 -> FP32, both operands in
+// zeroed shared memory with the 128-byte swizzle) into one accumulator;
+// out = SM cycles from the first issue to the completion of the last.
+__global__ void __launch_bounds__(128) k_mma_rate(int nmma, int n, unsigned long long *out, int *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t bar;
+    __shared__ uint32_t slot;
+    for (int i = threadIdx.x; i < 48 * 1024 / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(sm)[i] = 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = slot;
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
+        const uint32_t a = smem_u32(sm), b = smem_u32(sm + 16384);   // 128 rows of A, up to 256 of B
+        const long long t0 = clock64();
+        for (int i = 0; i < nmma; ++i)
+            mma_bf16(tmem, smem_desc(a + 32 * (i & 3), 1024, 2), smem_desc(b + 32 * (i & 3), 1024, 2), idesc,
+                     i > 0 ? 1u : 0u);
+        mma_commit(&bar);
+        const bool ok = mbar_wait(&bar, 0);
+        out[0] = (unsigned long long)(clock64() - t0);
+        if (!ok) atomicExch(err, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+}
+
 }  // namespace
+
+// SM cycles per tcgen05.mma (M = 128, N = n, K = 16, BF16) issued back to back
+// by one thread, on the current device: 2048 instructions after a warm-up
+// launch, one CTA, timed with clock64 (no clocks or settings touched).
+extern "C" int fs_mma_rate(int32_t n, double *cycles_per_mma) {
+    if (!cycles_per_mma || n < 16 || n > 256 || n % 16) return -1;
+    const int smem = 49 * 1024 + 1024;
+    if (cudaFuncSetAttribute(k_mma_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return -2;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return -2;
+    int *err = reinterpret_cast<int *>(d + 1);
+    int rc = cudaMemset(d, 0, 16) == cudaSuccess ? 0 : -2;
+    const int nmma = 2048;
+    for (int rep = 0; rep < 2 && !rc; ++rep) {
+        k_mma_rate<<<1, 128, smem>>>(nmma, n, d, err);
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = -3;
+    }
+    unsigned long long h[2] = {0, 0};
+    if (!rc && cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost) != cudaSuccess) rc = -3;
+    if (!rc && (int)h[1]) rc = -6;   // the wait for the MMAs ran out
+    if (!rc) *cycles_per_mma = (double)h[0] / nmma;
+    cudaFree(d);
+    return rc;
+}
 
 // ----------------------------------------------------------------------- host
 namespace {

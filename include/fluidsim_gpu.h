@@ -327,6 +327,14 @@ int fs_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t c1, int32_t c2, int32
                   const uint16_t *in1, const uint16_t *in2, const float *w, const float *bias,
                   int32_t mode, void *out);
 
+/* Measurement of the bound of those convolutions (no counterpart in the
+ * reference): SM cycles per tcgen05.mma instruction (M = 128, N = n, K = 16,
+ * BF16 -> FP32, operands in shared memory) issued back to back by one
+ * thread, on the current device, clock64-timed, no clocks or settings
+ * touched.  n a multiple of 16 in 16..256.  Returns 0, -1 bad arguments, -2
+ * set-up failed, -3 launch failed, -6 the bounded wait ran out. */
+int fs_mma_rate(int32_t n, double *cycles_per_mma);
+
 /* fs_max_ne for callers that may not allocate device memory after set-up
  * (this entry point has no counterpart in the reference): same result as
  * fs_max_ne, with its scratch in a fixed device array of the library instead

@@ -104,3 +104,21 @@ def test_conv_network_shapes(built, H, W, c1, c2, cout):
     got = out[0, ys, xs]
     err = np.abs(got - ref) / (np.abs(ref) + 1.0)
     assert err.max() < 2e-5, err.max()
+
+
+def test_mma_issue_rate(built):
+    """fs_mma_rate, the measurement behind the convolution's roofline: SM
+    cycles per back-to-back tcgen05.mma (M = 128, K = 16, BF16).  An N = 256
+    instruction cannot beat the tensor peak (8192 FLOP per cycle and SM: 128
+    cycles); every N gives a positive, bounded figure."""
+    from fluidsim_gb300 import api
+    lib = api.load_library()
+    got = {}
+    for n in (16, 64, 256):
+        v = C.c_double()
+        rc = lib.fs_mma_rate(n, C.byref(v))
+        assert rc == 0, (n, rc)
+        got[n] = v.value
+    print("cycles per tcgen05.mma (M=128, K=16) by N:", got)
+    assert all(0.0 < c < 5000.0 for c in got.values()), got
+    assert got[256] >= 0.9 * 128.0, got
