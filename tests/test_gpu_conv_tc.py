@@ -3,7 +3,9 @@
 memory) against a float64 numpy convolution of the same BF16-rounded inputs
 and weights (needs a GB300).  Covers every channel shape the network uses
 (one and two sources, 16/32/64-channel chunks, multi-chunk sources), grids
-narrower and wider than the 128-pixel tile, ragged edges and batches."""
+narrower than the 128-pixel tile (tap tiles) and wider (halo rows, one-row
+images and runs split across CTAs included), layers whose weights leave no
+room for halo rows, ragged edges and batches; and the MMA-rate probe."""
 import ctypes as C
 
 import numpy as np
